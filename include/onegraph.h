@@ -1,0 +1,215 @@
+/*
+ * onegraph.h — C ABI of the GB300 out-of-memory graph engine (libog.so).
+ *
+ * Drop-in for OneGraph's Ascetic path: the C++ entry points bfs_opt / sssp_opt /
+ * cc_opt / pr_opt (BFS/oneGraph_BFS/CalculateOpt.h:9, SSSP/oneGraph/CalculateOpt.h:12,
+ * CC/onegraph/CalculateOpt.h:6, PR/OneGraph/CalculateOpt.h:13) and the
+ * GraphMeta loader/planner they drive (BFS/oneGraph_BFS/GraphMeta.h:31-557).
+ *
+ * Conventions
+ *  - Every call returns an og_status; on failure og_last_error() gives a message
+ *    (thread-local).  No C++ exception crosses this boundary.
+ *  - The engine owns its device and pinned buffers; the caller owns every output
+ *    array it passes in.  An output pointer may be NULL: the result then stays
+ *    in device memory (used to time the device-resident path).
+ *  - Vertex values follow the reference: BFS depth(src) = 1 and unreached = V+1
+ *    (GraphMeta.h:376-381); SSSP dist(src) = 1 and unreached = 0xFFFFFFFF
+ *    (SSSP/oneGraph/GraphMeta.h:376-381); CC label = minimum vertex id that
+ *    reaches the vertex (CC/onegraph/GraphMeta.h:341-345 init value = id).
+ *  - One host thread per engine at a time.  Engines are independent.
+ */
+#ifndef ONEGRAPH_H
+#define ONEGRAPH_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define OG_ABI_VERSION 1
+
+typedef enum og_status {
+  OG_OK = 0,
+  OG_E_ARG = 1,         /* invalid argument */
+  OG_E_IO = 2,          /* file could not be opened / read / written */
+  OG_E_FORMAT = 3,      /* CSR file is malformed (short, non-monotone, dst >= V) */
+  OG_E_BUDGET = 4,      /* device budget cannot hold the per-vertex state */
+  OG_E_CUDA = 5,        /* a CUDA call failed */
+  OG_E_TIMEOUT = 6,     /* a bounded device-side wait gave up */
+  OG_E_NOMEM = 7,       /* host allocation failed */
+  OG_E_STATE = 8,       /* call not valid in the current state */
+  OG_E_UNSUPPORTED = 9, /* algorithm not available for this graph kind */
+  OG_E_DEVICE = 10      /* a kernel reported an out-of-range index */
+} og_status;
+
+/* Edge layout of a CSR file (GraphMeta.h:126-145 readDataFromFile):
+ *   u64 V, u64 E, [u32 outDegree[V] for PR], u64 offsets[V] (no sentinel),
+ *   Edge[E] with Edge = u32 (BFS/CC/PR; PR lists IN-neighbours) or
+ *   {u32 toNode, u32 weight} (SSSP, globals.h:18-21 EdgeWithWeight). */
+typedef enum og_graph_kind {
+  OG_GRAPH_PLAIN = 0,    /* u32 columns                          */
+  OG_GRAPH_WEIGHTED = 1, /* {u32 dst, u32 weight} pairs           */
+  OG_GRAPH_PR = 2        /* u32 outDegree[V] block + u32 in-edges */
+} og_graph_kind;
+
+typedef enum og_algo {
+  OG_ALGO_BFS = 0,
+  OG_ALGO_SSSP = 1,
+  OG_ALGO_CC = 2,
+  OG_ALGO_PR = 3
+} og_algo;
+
+typedef struct og_graph og_graph;
+typedef struct og_engine og_engine;
+
+/* ---------------------------------------------------------------- graphs */
+
+/* GraphMeta::readDataFromFile (BFS/oneGraph_BFS/GraphMeta.h:126-145, PR variant
+ * PR/OneGraph/GraphMeta.h:131-149).  Validates the header, monotone offsets,
+ * offsets <= E and every column < V. */
+int og_graph_load(const char *path, int kind, og_graph **out);
+
+/* Builds a graph from caller arrays (copied).  offsets has V entries (the file
+ * layout) or V+1 when with_sentinel != 0; outdeg only for OG_GRAPH_PR. */
+int og_graph_from_arrays(uint64_t V, uint64_t E, const uint64_t *offsets,
+                         int with_sentinel, const void *edges,
+                         const uint32_t *outdeg, int kind, og_graph **out);
+
+/* Writes the graph in the reference's file layout (inverse of readDataFromFile). */
+int og_graph_save(const og_graph *g, const char *path);
+
+/* V, E, kind, and borrowed pointers to the host arrays (offsets with the V+1
+ * sentinel; outdeg NULL unless OG_GRAPH_PR).  Any out pointer may be NULL. */
+int og_graph_info(const og_graph *g, uint64_t *V, uint64_t *E, int *kind,
+                  const uint64_t **offsets, const void **edges,
+                  const uint32_t **outdeg);
+
+void og_graph_free(og_graph *g);
+
+/* GraphMeta::findbignode (GraphMeta.h:150-165): first vertex after `last`
+ * whose degree exceeds 3000, or `last` when there is none. */
+uint32_t og_graph_findbignode(const og_graph *g, uint32_t last);
+
+/* Seeded R-MAT generator (no reference counterpart: the reference points at
+ * an external converter, README.md:8).  Deterministic on every platform. */
+typedef struct og_rmat_params {
+  uint32_t scale;       /* V = 2^scale                                    */
+  uint32_t edge_factor; /* edge_factor * V tuples are drawn               */
+  double a, b, c;       /* quadrant probabilities; d = 1 - a - b - c      */
+  uint64_t seed;        /* tuple seed                                      */
+  uint64_t weight_seed; /* seed of the per-edge weights                    */
+  uint32_t wmin, wmax;  /* weights uniform in [wmin, wmax] (weighted only) */
+  uint32_t flags;       /* OG_RMAT_* below                                 */
+  uint32_t threads;     /* host threads (0 = all)                          */
+} og_rmat_params;
+
+#define OG_RMAT_SYMMETRIC 1u /* add the reverse of every edge            */
+#define OG_RMAT_PERMUTE 2u   /* seeded bijective relabelling of vertex ids */
+#define OG_RMAT_WEIGHTED 4u  /* {dst, w} edges (OG_GRAPH_WEIGHTED)       */
+#define OG_RMAT_PR 8u        /* directed in-edge CSR + outDegree (OG_GRAPH_PR) */
+#define OG_RMAT_ON_GPU 16u   /* draw, sort and dedup on cuda device 0     */
+
+/* Self-loops and duplicate edges are always removed. */
+int og_rmat_generate(const og_rmat_params *p, og_graph **out);
+
+/* ---------------------------------------------------------------- planner */
+
+/* Result of the region planner (GraphMeta.h:300-360 getMaxPartitionSize). */
+typedef struct og_plan {
+  uint64_t budget_bytes;     /* device budget the plan was made for          */
+  uint64_t vertex_bytes;     /* bytes of per-vertex device state             */
+  uint64_t fixed_bytes;      /* scratch independent of V and E               */
+  uint64_t edge_capacity;    /* T: edges the remaining budget holds          */
+  double advisek;            /* static share of T actually used              */
+  double advisek_auto;       /* the reference's (10 - E/T)/9 heuristic       */
+  uint64_t max_partition;    /* floor(advisek * T) clamped to E              */
+  uint32_t static_vertices;  /* Vs: vertices [0, Vs) are static              */
+  uint64_t static_edges;     /* off[Vs]: edges preloaded once                */
+  uint64_t dynamic_edges;    /* E - static_edges                             */
+  uint64_t chunk_edges;      /* staging capacity per buffer (two buffers)    */
+  uint32_t edge_bytes;       /* 4 or 8                                       */
+  uint32_t reserved;
+} og_plan;
+
+/* Pure host computation, no device needed.  `offsets` has V+1 entries.
+ * budget_bytes == 0 selects the reference's 12 GiB (GraphMeta.h:305);
+ * advisek <= 0 selects the heuristic (GraphMeta.h:311-324). */
+int og_plan_compute(uint64_t V, uint64_t E, const uint64_t *offsets, int kind,
+                    uint64_t budget_bytes, double advisek, uint32_t flags,
+                    og_plan *out);
+
+/* ---------------------------------------------------------------- engine */
+
+typedef struct og_config {
+  uint64_t budget_bytes; /* 0 = 12 GiB (GraphMeta.h:305)                  */
+  double advisek;        /* <= 0 = heuristic; the CLI's --advisek          */
+  uint32_t flags;        /* OG_CFG_* below                                 */
+  int32_t device;        /* CUDA device ordinal                            */
+} og_config;
+
+#define OG_CFG_DIRECT 1u  /* dynamic region relaxed straight from pinned host
+                             memory instead of through device staging buffers */
+#define OG_CFG_NO_PIN 2u  /* do not page-lock the host CSR (ATS access only)  */
+#define OG_CFG_PR 4u      /* also hold PageRank state for a PLAIN/WEIGHTED
+                             graph, read as symmetric (in-edges = out-edges,
+                             outDegree = degree); implied for OG_GRAPH_PR    */
+
+/* Per-query counters (what CalculateOpt.h:193-208 prints, plus rooflines). */
+typedef struct og_stats {
+  uint32_t iterations;       /* rounds of the hot loop                      */
+  uint32_t chunks;           /* dynamic chunks moved                        */
+  uint64_t frontier_sum;     /* "nodeSum": vertices expanded over all rounds */
+  uint64_t static_vertices;  /* expanded in the static region               */
+  uint64_t edges_static;     /* edges relaxed from the resident prefix      */
+  uint64_t edges_dynamic;    /* edges gathered from host memory and relaxed */
+  uint64_t link_bytes;       /* bytes read over the host link               */
+  double ms_total;           /* host wall time of the query                 */
+  double ms_static;          /* device time of static relax kernels         */
+  double ms_dynamic;         /* device time of dynamic gather+relax         */
+  double ms_compact;         /* device time of frontier compaction          */
+  double residual;           /* PR: last L1 delta; otherwise 0              */
+  uint64_t launches;         /* kernels launched for the query              */
+} og_stats;
+
+/* initGraphHost + getMaxPartitionSize + initGraphDevice
+ * (GraphMeta.h:204-291): plans the regions and preloads the static prefix. */
+int og_engine_create(og_graph *g, const og_config *cfg, og_engine **out);
+int og_engine_plan(const og_engine *e, og_plan *out);
+void og_engine_destroy(og_engine *e);
+
+/* bfs_opt loop body for one source (BFS/oneGraph_BFS/CalculateOpt.h:55-209).
+ * out_depth: V entries or NULL. */
+int og_bfs(og_engine *e, uint32_t src, uint32_t *out_depth, og_stats *st);
+
+/* sssp_opt (SSSP/oneGraph/CalculateOpt.h:12-192); OG_GRAPH_WEIGHTED only. */
+int og_sssp(og_engine *e, uint32_t src, uint32_t *out_dist, og_stats *st);
+
+/* cc_opt (CC/onegraph/CalculateOpt.h:6-144). */
+int og_cc(og_engine *e, uint32_t *out_label, og_stats *st);
+
+/* pr_opt (PR/OneGraph/CalculateOpt.h:13-185): ranks start at 1.0, a vertex
+ * keeps iterating while |new - old| > threshold (0.001 in the reference,
+ * gpu_kernels.h:307).  Values are FP32.  max_rounds <= 0 means unbounded. */
+int og_pr(og_engine *e, float *out_rank, double threshold, int max_rounds,
+          og_stats *st);
+
+/* Precision-study PageRank: normalised ranks (sum 1), FP32 values and FP32
+ * accumulation, every vertex every iteration, stop when the FP64 L1 delta
+ * (reduced on the GPU) drops below tol or after max_iter iterations.
+ * No reference counterpart beyond the pr_cal_cpu formula (PR/usm/pr.cpp:149-187). */
+int og_pr_l1(og_engine *e, float *out_rank, double damping, double tol,
+             int max_iter, og_stats *st);
+
+/* Copies the last result of the given algorithm from device memory into out
+ * (V entries: u32 for BFS/SSSP/CC, float for PR). */
+int og_result_fetch(og_engine *e, int algo, void *out);
+
+const char *og_last_error(void);
+int og_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* ONEGRAPH_H */

@@ -1,0 +1,353 @@
+"""Python mirror of the GB300 OneGraph engine's C ABI (include/onegraph.h).
+
+The compute path is libog.so (hand-written sm_103a CUDA + C++ host code); this
+module only binds it with ctypes and mirrors the reference's driver entry
+points (``bfs_opt`` / ``sssp_opt`` / ``cc_opt`` / ``pr_opt``,
+BFS/oneGraph_BFS/CalculateOpt.h:9, SSSP/oneGraph/CalculateOpt.h:12,
+CC/onegraph/CalculateOpt.h:6, PR/OneGraph/CalculateOpt.h:13).  There is no
+fallback: if libog.so is missing, importing the library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+_PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_PKG, "libog.so")
+BIN_DIR = os.path.join(_PKG, "bin")
+
+OG_OK = 0
+STATUS = {0: "OG_OK", 1: "OG_E_ARG", 2: "OG_E_IO", 3: "OG_E_FORMAT", 4: "OG_E_BUDGET",
+          5: "OG_E_CUDA", 6: "OG_E_TIMEOUT", 7: "OG_E_NOMEM", 8: "OG_E_STATE",
+          9: "OG_E_UNSUPPORTED", 10: "OG_E_DEVICE"}
+PLAIN, WEIGHTED, PR = 0, 1, 2
+ALGO_BFS, ALGO_SSSP, ALGO_CC, ALGO_PR = 0, 1, 2, 3
+RMAT_SYMMETRIC, RMAT_PERMUTE, RMAT_WEIGHTED, RMAT_PR, RMAT_ON_GPU = 1, 2, 4, 8, 16
+CFG_DIRECT, CFG_NO_PIN, CFG_PR = 1, 2, 4
+# R-MAT quadrant probabilities of the benchmark graphs
+RMAT_ABC = (0.57, 0.19, 0.19)
+
+
+class OGError(RuntimeError):
+    def __init__(self, status: int, where: str, msg: str):
+        super().__init__("%s: %s (%s)" % (where, msg, STATUS.get(status, status)))
+        self.status = status
+
+
+class RmatParams(C.Structure):
+    _fields_ = [("scale", C.c_uint32), ("edge_factor", C.c_uint32), ("a", C.c_double),
+                ("b", C.c_double), ("c", C.c_double), ("seed", C.c_uint64),
+                ("weight_seed", C.c_uint64), ("wmin", C.c_uint32), ("wmax", C.c_uint32),
+                ("flags", C.c_uint32), ("threads", C.c_uint32)]
+
+
+class Plan(C.Structure):
+    _fields_ = [("budget_bytes", C.c_uint64), ("vertex_bytes", C.c_uint64),
+                ("fixed_bytes", C.c_uint64), ("edge_capacity", C.c_uint64),
+                ("advisek", C.c_double), ("advisek_auto", C.c_double),
+                ("max_partition", C.c_uint64), ("static_vertices", C.c_uint32),
+                ("static_edges", C.c_uint64), ("dynamic_edges", C.c_uint64),
+                ("chunk_edges", C.c_uint64), ("edge_bytes", C.c_uint32), ("reserved", C.c_uint32)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
+class Config(C.Structure):
+    _fields_ = [("budget_bytes", C.c_uint64), ("advisek", C.c_double), ("flags", C.c_uint32),
+                ("device", C.c_int32)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("iterations", C.c_uint32), ("chunks", C.c_uint32), ("frontier_sum", C.c_uint64),
+                ("static_vertices", C.c_uint64), ("edges_static", C.c_uint64),
+                ("edges_dynamic", C.c_uint64), ("link_bytes", C.c_uint64),
+                ("ms_total", C.c_double), ("ms_static", C.c_double), ("ms_dynamic", C.c_double),
+                ("ms_compact", C.c_double), ("residual", C.c_double), ("launches", C.c_uint64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_lib = None
+
+# (name, restype, argtypes) for every symbol declared in include/onegraph.h
+_P = C.c_void_p
+SIGNATURES = [
+    ("og_graph_load", C.c_int, [C.c_char_p, C.c_int, C.POINTER(_P)]),
+    ("og_graph_from_arrays", C.c_int, [C.c_uint64, C.c_uint64, _P, C.c_int, _P, _P, C.c_int,
+                                       C.POINTER(_P)]),
+    ("og_graph_save", C.c_int, [_P, C.c_char_p]),
+    ("og_graph_info", C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64),
+                                C.POINTER(C.c_int), C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
+    ("og_graph_free", None, [_P]),
+    ("og_graph_findbignode", C.c_uint32, [_P, C.c_uint32]),
+    ("og_rmat_generate", C.c_int, [C.POINTER(RmatParams), C.POINTER(_P)]),
+    ("og_plan_compute", C.c_int, [C.c_uint64, C.c_uint64, _P, C.c_int, C.c_uint64, C.c_double,
+                                  C.c_uint32, C.POINTER(Plan)]),
+    ("og_engine_create", C.c_int, [_P, C.POINTER(Config), C.POINTER(_P)]),
+    ("og_engine_plan", C.c_int, [_P, C.POINTER(Plan)]),
+    ("og_engine_destroy", None, [_P]),
+    ("og_bfs", C.c_int, [_P, C.c_uint32, _P, C.POINTER(Stats)]),
+    ("og_sssp", C.c_int, [_P, C.c_uint32, _P, C.POINTER(Stats)]),
+    ("og_cc", C.c_int, [_P, _P, C.POINTER(Stats)]),
+    ("og_pr", C.c_int, [_P, _P, C.c_double, C.c_int, C.POINTER(Stats)]),
+    ("og_pr_l1", C.c_int, [_P, _P, C.c_double, C.c_double, C.c_int, C.POINTER(Stats)]),
+    ("og_result_fetch", C.c_int, [_P, C.c_int, _P]),
+    ("og_last_error", C.c_char_p, []),
+    ("og_abi_version", C.c_int, []),
+]
+
+
+def lib():
+    """Loads libog.so (built by onegraph_gb300.build / __graft_entry__.build)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise OSError("libog.so not built: run `python -c 'import __graft_entry__ as g; g.build()'`")
+        L = C.CDLL(LIB_PATH)
+        for name, res, args in SIGNATURES:
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _check(rc: int, where: str):
+    if rc != OG_OK:
+        raise OGError(rc, where, lib().og_last_error().decode(errors="replace"))
+
+
+def _ptr(a: np.ndarray | None):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+class Graph:
+    """Host CSR in the reference layout (GraphMeta.h:126-145) owned by libog."""
+
+    def __init__(self, handle):
+        self._h = handle
+        V, E, kind = C.c_uint64(), C.c_uint64(), C.c_int()
+        off, edges, outdeg = _P(), _P(), _P()
+        _check(lib().og_graph_info(handle, C.byref(V), C.byref(E), C.byref(kind), C.byref(off),
+                                   C.byref(edges), C.byref(outdeg)), "og_graph_info")
+        self.V, self.E, self.kind = V.value, E.value, kind.value
+        self._off_p, self._edges_p, self._outdeg_p = off.value, edges.value, outdeg.value
+
+    @classmethod
+    def load(cls, path: str, kind: int = PLAIN) -> "Graph":
+        h = _P()
+        _check(lib().og_graph_load(path.encode(), kind, C.byref(h)), "og_graph_load")
+        return cls(h)
+
+    @classmethod
+    def from_arrays(cls, offsets, edges, outdeg=None, kind: int = PLAIN,
+                    with_sentinel: bool = True) -> "Graph":
+        """offsets: V+1 entries (with_sentinel) or the file's V entries."""
+        off = np.ascontiguousarray(offsets, dtype=np.uint64)
+        ed = np.ascontiguousarray(edges, dtype=np.uint32)
+        od = None if outdeg is None else np.ascontiguousarray(outdeg, dtype=np.uint32)
+        E = ed.size // (2 if kind == WEIGHTED else 1)
+        V = off.size - (1 if with_sentinel else 0)
+        h = _P()
+        _check(lib().og_graph_from_arrays(V, E, _ptr(off), 1 if with_sentinel else 0,
+                                          _ptr(ed) if E else None, _ptr(od), kind, C.byref(h)),
+               "og_graph_from_arrays")
+        return cls(h)
+
+    @classmethod
+    def rmat(cls, scale: int, edge_factor: int = 16, seed: int = 1, weight_seed: int = 2,
+             symmetric: bool = True, permute: bool = True, weighted: bool = False,
+             pagerank: bool = False, on_gpu: bool = False, wmin: int = 1, wmax: int = 64,
+             abc=RMAT_ABC, threads: int = 0) -> "Graph":
+        flags = ((RMAT_SYMMETRIC if symmetric else 0) | (RMAT_PERMUTE if permute else 0) |
+                 (RMAT_WEIGHTED if weighted else 0) | (RMAT_PR if pagerank else 0) |
+                 (RMAT_ON_GPU if on_gpu else 0))
+        p = RmatParams(scale, edge_factor, abc[0], abc[1], abc[2], seed, weight_seed, wmin, wmax,
+                       flags, threads)
+        h = _P()
+        _check(lib().og_rmat_generate(C.byref(p), C.byref(h)), "og_rmat_generate")
+        return cls(h)
+
+    def save(self, path: str):
+        _check(lib().og_graph_save(self._h, path.encode()), "og_graph_save")
+
+    @property
+    def offsets(self) -> np.ndarray:
+        """V+1 offsets (borrowed view, valid while the graph lives)."""
+        return np.ctypeslib.as_array(C.cast(self._off_p, C.POINTER(C.c_uint64)), (self.V + 1,))
+
+    @property
+    def edges(self) -> np.ndarray:
+        """u32 columns, or an (E, 2) array of {dst, weight} for weighted graphs."""
+        n = self.E * (2 if self.kind == WEIGHTED else 1)
+        if n == 0:
+            return np.zeros((0, 2) if self.kind == WEIGHTED else 0, np.uint32)
+        a = np.ctypeslib.as_array(C.cast(self._edges_p, C.POINTER(C.c_uint32)), (n,))
+        return a.reshape(-1, 2) if self.kind == WEIGHTED else a
+
+    @property
+    def columns(self) -> np.ndarray:
+        e = self.edges
+        return e[:, 0] if self.kind == WEIGHTED else e
+
+    @property
+    def outdeg(self) -> np.ndarray | None:
+        if not self._outdeg_p:
+            return None
+        return np.ctypeslib.as_array(C.cast(self._outdeg_p, C.POINTER(C.c_uint32)), (self.V,))
+
+    def degrees(self) -> np.ndarray:
+        return np.diff(self.offsets).astype(np.uint32)
+
+    def findbignode(self, last: int) -> int:
+        return int(lib().og_graph_findbignode(self._h, last))
+
+    def close(self):
+        if self._h:
+            lib().og_graph_free(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def plan(V: int, E: int, offsets: np.ndarray, kind: int = PLAIN, budget: int = 0,
+         advisek: float = 0.0, flags: int = 0) -> dict:
+    off = np.ascontiguousarray(offsets, dtype=np.uint64)
+    assert off.size == V + 1
+    p = Plan()
+    _check(lib().og_plan_compute(V, E, _ptr(off), kind, budget, advisek, flags, C.byref(p)),
+           "og_plan_compute")
+    return p.as_dict()
+
+
+class Engine:
+    """og_engine: a graph planned against a device budget, static prefix resident."""
+
+    def __init__(self, graph: Graph, budget: int = 0, advisek: float = 0.0, direct: bool = False,
+                 pagerank: bool = False, no_pin: bool = False, device: int = 0):
+        self.graph = graph
+        cfg = Config(budget, advisek, (CFG_DIRECT if direct else 0) | (CFG_PR if pagerank else 0) |
+                     (CFG_NO_PIN if no_pin else 0), device)
+        h = _P()
+        _check(lib().og_engine_create(graph._h, C.byref(cfg), C.byref(h)), "og_engine_create")
+        self._h = h
+        p = Plan()
+        _check(lib().og_engine_plan(h, C.byref(p)), "og_engine_plan")
+        self.plan = p.as_dict()
+        self.stats: dict = {}
+
+    def _out(self, out, dtype):
+        if out is False:
+            return None
+        if out is None:
+            return np.empty(self.graph.V, dtype)
+        assert out.dtype == dtype and out.size >= self.graph.V and out.flags.c_contiguous
+        return out
+
+    def bfs(self, src: int, out=None) -> np.ndarray | None:
+        """Depths, depth(src) = 1, unreached = V+1.  out=False keeps them on the device."""
+        o = self._out(out, np.uint32)
+        st = Stats()
+        _check(lib().og_bfs(self._h, src, _ptr(o), C.byref(st)), "og_bfs")
+        self.stats = st.as_dict()
+        return o
+
+    def sssp(self, src: int, out=None) -> np.ndarray | None:
+        o = self._out(out, np.uint32)
+        st = Stats()
+        _check(lib().og_sssp(self._h, src, _ptr(o), C.byref(st)), "og_sssp")
+        self.stats = st.as_dict()
+        return o
+
+    def cc(self, out=None) -> np.ndarray | None:
+        o = self._out(out, np.uint32)
+        st = Stats()
+        _check(lib().og_cc(self._h, _ptr(o), C.byref(st)), "og_cc")
+        self.stats = st.as_dict()
+        return o
+
+    def pr(self, threshold: float = 0.001, max_rounds: int = 0, out=None) -> np.ndarray | None:
+        o = self._out(out, np.float32)
+        st = Stats()
+        _check(lib().og_pr(self._h, _ptr(o), threshold, max_rounds, C.byref(st)), "og_pr")
+        self.stats = st.as_dict()
+        return o
+
+    def pr_l1(self, damping: float = 0.85, tol: float = 1e-6, max_iter: int = 200,
+              out=None) -> np.ndarray | None:
+        o = self._out(out, np.float32)
+        st = Stats()
+        _check(lib().og_pr_l1(self._h, _ptr(o), damping, tol, max_iter, C.byref(st)), "og_pr_l1")
+        self.stats = st.as_dict()
+        return o
+
+    def fetch(self, algo: int, dtype=np.uint32) -> np.ndarray:
+        o = np.empty(self.graph.V, dtype)
+        _check(lib().og_result_fetch(self._h, algo, _ptr(o)), "og_result_fetch")
+        return o
+
+    def close(self):
+        if getattr(self, "_h", None):
+            lib().og_engine_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+# ------------------------------------------------------- reference-named drivers
+
+def bfs_opt(path: str, sourceNode: int | None = None, adviseRate: float = 0.0, budget: int = 0,
+            testTimes: int = 5):
+    """bfs_opt (BFS/oneGraph_BFS/CalculateOpt.h:9): without a source, the
+    reference's five findbignode sources.  Returns [(source, depths, stats)]."""
+    g = Graph.load(path, PLAIN)
+    eng = Engine(g, budget=budget, advisek=adviseRate)
+    if sourceNode is None:
+        srcs, last = [], 0
+        for _ in range(testTimes):
+            last = g.findbignode(last)
+            srcs.append(last)
+    else:
+        srcs = [sourceNode]
+    res = [(s, eng.bfs(s), dict(eng.stats)) for s in srcs]
+    eng.close()
+    return res
+
+
+def sssp_opt(path: str, sourceNode: int = 0, adviseRate: float = 0.0, budget: int = 0):
+    g = Graph.load(path, WEIGHTED)
+    eng = Engine(g, budget=budget, advisek=adviseRate)
+    d = eng.sssp(sourceNode)
+    st = dict(eng.stats)
+    eng.close()
+    return d, st
+
+
+def cc_opt(path: str, adviseRate: float = 0.0, budget: int = 0):
+    g = Graph.load(path, PLAIN)
+    eng = Engine(g, budget=budget, advisek=adviseRate)
+    lab = eng.cc()
+    st = dict(eng.stats)
+    eng.close()
+    return lab, st
+
+
+def pr_opt(path: str, adviseRate: float = 0.0, budget: int = 0, threshold: float = 0.001):
+    g = Graph.load(path, PR)
+    eng = Engine(g, budget=budget, advisek=adviseRate)
+    r = eng.pr(threshold)
+    st = dict(eng.stats)
+    eng.close()
+    return r, st

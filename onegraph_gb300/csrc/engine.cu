@@ -1,0 +1,731 @@
+// engine.cu — the out-of-memory engine behind og_engine_* / og_bfs / og_sssp /
+// og_cc / og_pr (onegraph.h).
+//
+// One engine = one graph on one GB300, planned against a device budget:
+//  * static region: vertices [0, Vs) whose whole adjacency lies in the edge
+//    prefix [0, off[Vs]); that prefix is copied to HBM once
+//    (GraphMeta.h:234-291 initGraphDevice, 300-360 getMaxPartitionSize);
+//  * dynamic region: vertices [Vs, V); their edges stay in page-locked host
+//    memory and every round the active ones are gathered by a kernel over the
+//    host link into one of two device staging buffers (side stream), while the
+//    previous buffer is relaxed and the static region is relaxed on the main
+//    stream (CalculateOpt.h:75-188, GraphMeta.h:471-557).
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <new>
+#include <vector>
+
+#include "kernels.cuh"
+#include "og_internal.hpp"
+
+using namespace og;
+
+#define CK(x)                                                                          \
+  do {                                                                                 \
+    cudaError_t e_ = (x);                                                              \
+    if (e_ != cudaSuccess)                                                             \
+      return og::fail(OG_E_CUDA, "%s: %s (%s:%d)", #x, cudaGetErrorString(e_), __FILE__, \
+                      __LINE__);                                                       \
+  } while (0)
+
+#define RC(x)                    \
+  do {                           \
+    int r_ = (x);                \
+    if (r_ != OG_OK) return r_;  \
+  } while (0)
+
+struct og_engine {
+  og_graph *g = nullptr;
+  og_config cfg{};
+  og_plan plan{};
+  int dev = 0;
+  int sms = 0;
+  bool pr_enabled = false;
+  bool registered = false;
+  uint32_t V = 0, Vs = 0;
+  uint64_t nwords = 0;
+  uint32_t eb = 4;
+
+  cudaStream_t s_main = nullptr, s_dyn = nullptr, s_gat = nullptr;
+  cudaEvent_t ev_round = nullptr, ev_cs = nullptr, ev_cd = nullptr, ev_dyn_done = nullptr;
+  cudaEvent_t ev_gat[2] = {nullptr, nullptr}, ev_rel[2] = {nullptr, nullptr};
+  cudaEvent_t t_s0 = nullptr, t_s1 = nullptr, t_d0 = nullptr;
+
+  uint64_t *off_d = nullptr;
+  void *sedges_d = nullptr;
+  void *stage_d[2] = {nullptr, nullptr};
+  const void *hedges_d = nullptr;
+  uint32_t *value_d = nullptr;
+  uint32_t *bm[3] = {nullptr, nullptr, nullptr};
+  uint32_t *list_d[2] = {nullptr, nullptr};
+  uint64_t *pref_d[2] = {nullptr, nullptr};
+  uint32_t *tile_d[2] = {nullptr, nullptr};
+  uint64_t list_cap[2] = {0, 0}, tile_cap[2] = {0, 0};
+  Lookback lb[2]{};
+  uint32_t lb_tiles = 0;
+  Counts *counts_d = nullptr, *counts_h = nullptr;
+  uint32_t *err_d = nullptr, *err_h = nullptr;
+  uint32_t *active_d = nullptr;
+
+  // PageRank state
+  float *contrib_d = nullptr, *sum_d = nullptr, *cont_d = nullptr, *carry_d = nullptr;
+  uint32_t *outdeg_d = nullptr, *carry_idx_d = nullptr;
+  double *part_d = nullptr, *l1_d = nullptr, *l1_h = nullptr;
+  uint32_t part_n = 0;
+  uint64_t pr_tiles = 0;
+
+  int last_algo = -1;
+  uint64_t launches = 0;  // kernels launched since the query began
+  std::vector<void *> dallocs;
+  uint64_t dbytes = 0;
+};
+
+namespace {
+
+template <class T>
+int dalloc(og_engine *e, T **p, uint64_t count) {
+  const uint64_t bytes = std::max<uint64_t>(count * sizeof(T), 256);
+  void *q = nullptr;
+  cudaError_t err = cudaMalloc(&q, bytes);
+  if (err != cudaSuccess)
+    return fail(OG_E_CUDA, "cudaMalloc(%llu B) failed: %s (engine holds %llu B)",
+                (unsigned long long)bytes, cudaGetErrorString(err), (unsigned long long)e->dbytes);
+  e->dallocs.push_back(q);
+  e->dbytes += bytes;
+  *p = (T *)q;
+  return OG_OK;
+}
+
+int grid_for(uint64_t n, int sms) {
+  const uint64_t g = (n + kThreads - 1) / kThreads;
+  return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, (uint64_t)sms * 8));
+}
+
+void destroy(og_engine *e) {
+  if (!e) return;
+  cudaSetDevice(e->dev);
+  if (e->s_main) cudaStreamSynchronize(e->s_main);
+  if (e->s_dyn) cudaStreamSynchronize(e->s_dyn);
+  if (e->s_gat) cudaStreamSynchronize(e->s_gat);
+  for (void *p : e->dallocs) cudaFree(p);
+  if (e->counts_h) cudaFreeHost(e->counts_h);
+  if (e->err_h) cudaFreeHost(e->err_h);
+  if (e->l1_h) cudaFreeHost(e->l1_h);
+  cudaEvent_t evs[] = {e->ev_round, e->ev_cs, e->ev_cd, e->ev_dyn_done, e->ev_gat[0], e->ev_gat[1],
+                       e->ev_rel[0], e->ev_rel[1], e->t_s0, e->t_s1, e->t_d0};
+  for (auto ev : evs)
+    if (ev) cudaEventDestroy(ev);
+  if (e->s_main) cudaStreamDestroy(e->s_main);
+  if (e->s_dyn) cudaStreamDestroy(e->s_dyn);
+  if (e->s_gat) cudaStreamDestroy(e->s_gat);
+  if (e->registered && e->g) {
+    if (--e->g->registered == 0) cudaHostUnregister(e->g->edges);
+  }
+  delete e;
+}
+
+int create(og_graph *g, const og_config *cfg, og_engine *e) {
+  e->g = g;
+  e->cfg = *cfg;
+  e->dev = cfg->device;
+  e->V = g->V;
+  e->eb = g->edge_bytes();
+  e->pr_enabled = g->kind == OG_GRAPH_PR || (cfg->flags & OG_CFG_PR);
+  CK(cudaSetDevice(e->dev));
+  CK(cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, e->dev));
+  uint32_t pflags = cfg->flags;
+  RC(plan_compute(g->V, g->E, g->off, g->kind, cfg->budget_bytes, cfg->advisek, pflags, &e->plan));
+  const og_plan &P = e->plan;
+  size_t free_b = 0, total_b = 0;
+  CK(cudaMemGetInfo(&free_b, &total_b));
+  if (P.budget_bytes > free_b)
+    return fail(OG_E_BUDGET, "budget %llu B exceeds free device memory %llu B",
+                (unsigned long long)P.budget_bytes, (unsigned long long)free_b);
+  e->Vs = P.static_vertices;
+  e->nwords = ((uint64_t)g->V + 31) / 32 + 2 * kWordsPerCompactTile;
+
+  CK(cudaStreamCreateWithFlags(&e->s_main, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&e->s_dyn, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&e->s_gat, cudaStreamNonBlocking));
+  cudaEvent_t *evs[] = {&e->ev_round, &e->ev_cs, &e->ev_cd, &e->ev_dyn_done, &e->ev_gat[0],
+                        &e->ev_gat[1], &e->ev_rel[0], &e->ev_rel[1], &e->t_s0, &e->t_s1, &e->t_d0};
+  for (auto ev : evs) CK(cudaEventCreate(ev));
+
+  // host CSR: page-lock so kernels can gather from it over the link
+  if (P.dynamic_edges > 0) {
+    if (cfg->flags & OG_CFG_NO_PIN) {
+      int pageable = 0;
+      CK(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, e->dev));
+      if (!pageable) return fail(OG_E_UNSUPPORTED, "device cannot read pageable host memory");
+      e->hedges_d = g->edges;
+    } else {
+      if (g->registered == 0) {
+        int ro = 0;
+        cudaDeviceGetAttribute(&ro, cudaDevAttrHostRegisterReadOnlySupported, e->dev);
+        CK(cudaHostRegister(g->edges, g->E * e->eb,
+                            cudaHostRegisterMapped | (ro ? cudaHostRegisterReadOnly : 0)));
+      }
+      g->registered++;
+      e->registered = true;
+      void *dp = nullptr;
+      CK(cudaHostGetDevicePointer(&dp, g->edges, 0));
+      e->hedges_d = dp;
+    }
+  }
+
+  const uint64_t V = g->V;
+  RC(dalloc(e, &e->off_d, V + 1));
+  RC(dalloc(e, &e->value_d, V + 1));
+  for (int i = 0; i < 3; i++) RC(dalloc(e, &e->bm[i], e->nwords));
+  e->list_cap[0] = std::max<uint64_t>(e->Vs, 1);
+  e->list_cap[1] = std::max<uint64_t>(V - e->Vs, 1);
+  e->tile_cap[0] = P.static_edges / kTile + 2;
+  e->tile_cap[1] = P.dynamic_edges / kTile + 2;
+  for (int r = 0; r < 2; r++) {
+    RC(dalloc(e, &e->list_d[r], e->list_cap[r]));
+    RC(dalloc(e, &e->pref_d[r], e->list_cap[r] + 1));
+    RC(dalloc(e, &e->tile_d[r], e->tile_cap[r]));
+  }
+  e->lb_tiles = (uint32_t)((e->nwords + kWordsPerCompactTile - 1) / kWordsPerCompactTile + 1);
+  for (int r = 0; r < 2; r++) {
+    RC(dalloc(e, &e->lb[r].status, e->lb_tiles + 1));
+    e->lb[r].ticket = e->lb[r].status + e->lb_tiles;
+    RC(dalloc(e, &e->lb[r].agg_n, e->lb_tiles));
+    RC(dalloc(e, &e->lb[r].agg_e, e->lb_tiles));
+    RC(dalloc(e, &e->lb[r].inc_n, e->lb_tiles));
+    RC(dalloc(e, &e->lb[r].inc_e, e->lb_tiles));
+  }
+  RC(dalloc(e, &e->counts_d, 2));
+  RC(dalloc(e, &e->err_d, 4));
+  e->active_d = e->err_d + 1;
+  CK(cudaMallocHost(&e->counts_h, 2 * sizeof(Counts)));
+  CK(cudaMallocHost(&e->err_h, 4 * sizeof(uint32_t)));
+  CK(cudaMallocHost(&e->l1_h, sizeof(double)));
+
+  if (P.static_edges) {
+    RC(dalloc(e, (char **)&e->sedges_d, P.static_edges * e->eb));
+  }
+  if (P.chunk_edges) {
+    RC(dalloc(e, (char **)&e->stage_d[0], P.chunk_edges * e->eb));
+    RC(dalloc(e, (char **)&e->stage_d[1], P.chunk_edges * e->eb));
+  }
+  if (e->pr_enabled) {
+    RC(dalloc(e, &e->contrib_d, V + 1));
+    RC(dalloc(e, &e->sum_d, V + 1));
+    RC(dalloc(e, &e->outdeg_d, V + 1));
+    e->pr_tiles = e->tile_cap[0] + e->tile_cap[1];
+    RC(dalloc(e, &e->cont_d, e->pr_tiles));
+    RC(dalloc(e, &e->carry_d, e->pr_tiles));
+    RC(dalloc(e, &e->carry_idx_d, e->pr_tiles));
+    e->part_n = (uint32_t)e->sms * 8;
+    RC(dalloc(e, &e->part_d, e->part_n));
+    RC(dalloc(e, &e->l1_d, 1));
+  }
+  if (e->dbytes > P.budget_bytes)
+    return fail(OG_E_BUDGET, "engine allocated %llu B, above the %llu B budget",
+                (unsigned long long)e->dbytes, (unsigned long long)P.budget_bytes);
+
+  // initGraphDevice: offsets, the static edge prefix, PageRank out-degrees
+  CK(cudaMemcpyAsync(e->off_d, g->off, 8 * (V + 1), cudaMemcpyHostToDevice, e->s_main));
+  if (P.static_edges)
+    CK(cudaMemcpyAsync(e->sedges_d, g->edges, P.static_edges * e->eb, cudaMemcpyHostToDevice,
+                       e->s_main));
+  if (e->pr_enabled) {
+    if (g->kind == OG_GRAPH_PR)
+      CK(cudaMemcpyAsync(e->outdeg_d, g->outdeg, 4 * V, cudaMemcpyHostToDevice, e->s_main));
+    else
+      k_degree_from_offsets<<<grid_for(V, e->sms), kThreads, 0, e->s_main>>>(V, e->off_d, e->outdeg_d);
+      e->launches++;
+  }
+  CK(cudaMemsetAsync(e->err_d, 0, 16, e->s_main));
+  CK(cudaStreamSynchronize(e->s_main));
+  CK(cudaGetLastError());
+  return OG_OK;
+}
+
+// ------------------------------------------------------------------ rounds
+
+int launch_compact(og_engine *e, int r, const uint32_t *bits, uint32_t vb, uint32_t ve,
+                   cudaStream_t s) {
+  CK(cudaMemsetAsync(e->counts_d + r, 0, sizeof(Counts), s));
+  if (ve <= vb) return OG_OK;
+  CompactArgs a;
+  a.bits = bits;
+  a.v_begin = vb;
+  a.v_end = ve;
+  a.w_begin = vb / 32;
+  a.w_end = (uint32_t)(((uint64_t)ve + 31) / 32);
+  a.ntiles = (a.w_end - a.w_begin + kWordsPerCompactTile - 1) / kWordsPerCompactTile;
+  a.off = e->off_d;
+  a.list = e->list_d[r];
+  a.pref = e->pref_d[r];
+  a.tile_first = e->tile_d[r];
+  a.counts = e->counts_d + r;
+  a.lb = e->lb[r];
+  a.err = e->err_d;
+  a.list_cap = e->list_cap[r];
+  a.tile_cap = e->tile_cap[r];
+  if (a.ntiles + 1 > e->lb_tiles) return fail(OG_E_STATE, "compaction scratch too small");
+  CK(cudaMemsetAsync(e->lb[r].status, 0, sizeof(uint32_t) * (e->lb_tiles + 1), s));
+  k_compact<<<a.ntiles, kThreads, 0, s>>>(a);
+  e->launches++;
+  return OG_OK;
+}
+
+LbsArgs lbs_args(og_engine *e, int r, uint64_t pos_begin, uint64_t pos_end, bool csr,
+                 uint64_t edge_bound) {
+  LbsArgs a;
+  a.list = e->list_d[r];
+  a.pref = e->pref_d[r];
+  a.tile_first = e->tile_d[r];
+  a.n = e->counts_h[r].n;
+  a.total = e->counts_h[r].total;
+  a.pos_begin = pos_begin;
+  a.pos_end = pos_end;
+  a.off = csr ? e->off_d : nullptr;
+  a.stage_base = pos_begin;
+  a.edge_bound = edge_bound;
+  a.err = e->err_d;
+  return a;
+}
+
+unsigned lbs_grid(uint64_t pb, uint64_t pe) { return (unsigned)((pe - pb + kTile - 1) / kTile); }
+
+int check_device_error(og_engine *e) {
+  const uint32_t err = *e->err_h;
+  if (!err) return OG_OK;
+  if (err & kErrLookback) return fail(OG_E_TIMEOUT, "frontier compaction look-back wait gave up");
+  return fail(OG_E_DEVICE, "kernel reported an out-of-range index (flags 0x%x)", err);
+}
+
+// Relax op factory per algorithm; `level` is the BFS depth of the frontier.
+struct RoundOps {
+  int algo;
+  uint32_t level;
+};
+
+template <class Edge>
+int launch_relax(og_engine *e, const RoundOps &ro, const LbsArgs &a, const Edge *edges,
+                 uint32_t *next, cudaStream_t s) {
+  const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
+  if (grid == 0) return OG_OK;
+  if (ro.algo == OG_ALGO_BFS) {
+    BfsOp op{e->bm[2], next, e->value_d, e->err_d, e->V, ro.level + 1};
+    k_lbs<Edge, BfsOp><<<grid, kThreads, 0, s>>>(a, edges, op);
+    e->launches++;
+  } else if (ro.algo == OG_ALGO_SSSP) {
+    MinOp<true> op{e->value_d, next, e->err_d, e->V};
+    k_lbs<Edge, MinOp<true>><<<grid, kThreads, 0, s>>>(a, edges, op);
+    e->launches++;
+  } else {
+    MinOp<false> op{e->value_d, next, e->err_d, e->V};
+    k_lbs<Edge, MinOp<false>><<<grid, kThreads, 0, s>>>(a, edges, op);
+    e->launches++;
+  }
+  return OG_OK;
+}
+
+template <class Edge>
+int launch_gather(og_engine *e, const LbsArgs &a, Edge *stage, cudaStream_t s) {
+  const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
+  if (grid == 0) return OG_OK;
+  GatherOp<Edge> op{stage, a.pos_begin};
+  k_lbs<Edge, GatherOp<Edge>><<<grid, kThreads, 0, s>>>(a, (const Edge *)e->hedges_d, op);
+  e->launches++;
+  return OG_OK;
+}
+
+struct Timing {
+  bool pend_s = false, pend_d = false;
+};
+
+void collect_timing(og_engine *e, Timing &t, og_stats *st) {
+  float ms;
+  if (t.pend_s && cudaEventElapsedTime(&ms, e->t_s0, e->t_s1) == cudaSuccess) st->ms_static += ms;
+  if (t.pend_d && cudaEventElapsedTime(&ms, e->t_d0, e->ev_dyn_done) == cudaSuccess)
+    st->ms_dynamic += ms;
+  t.pend_s = t.pend_d = false;
+}
+
+// One round's region work given the compaction counts (already on the host).
+// `body_static(a)` / `body_dyn(a, edges, ...)` launch the per-region kernel.
+template <class Edge, class StaticFn, class DynFn>
+int run_regions(og_engine *e, og_stats &st, Timing &tm, StaticFn static_fn, DynFn dyn_fn) {
+  const Counts cs = e->counts_h[0], cd = e->counts_h[1];
+  if (cs.n) {
+    CK(cudaEventRecord(e->t_s0, e->s_main));
+    RC(static_fn(lbs_args(e, 0, 0, cs.total, true, e->plan.static_edges)));
+    CK(cudaEventRecord(e->t_s1, e->s_main));
+    tm.pend_s = true;
+    st.edges_static += cs.total;
+  }
+  if (cd.n) {
+    CK(cudaEventRecord(e->t_d0, e->s_dyn));
+    if (e->cfg.flags & OG_CFG_DIRECT) {
+      RC(dyn_fn(lbs_args(e, 1, 0, cd.total, true, e->g->E), (const Edge *)e->hedges_d, e->s_dyn));
+      st.chunks += 1;
+    } else {
+      const uint64_t C = e->plan.chunk_edges;
+      const uint64_t nch = (cd.total + C - 1) / C;
+      for (uint64_t c = 0; c < nch; c++) {
+        const int buf = (int)(c & 1);
+        const uint64_t b = c * C, en = std::min(b + C, cd.total);
+        CK(cudaStreamWaitEvent(e->s_gat, e->ev_cd, 0));
+        if (c >= 2) CK(cudaStreamWaitEvent(e->s_gat, e->ev_rel[buf], 0));
+        RC(launch_gather<Edge>(e, lbs_args(e, 1, b, en, true, e->g->E), (Edge *)e->stage_d[buf],
+                               e->s_gat));
+        CK(cudaEventRecord(e->ev_gat[buf], e->s_gat));
+        CK(cudaStreamWaitEvent(e->s_dyn, e->ev_gat[buf], 0));
+        RC(dyn_fn(lbs_args(e, 1, b, en, false, C), (const Edge *)e->stage_d[buf], e->s_dyn));
+        CK(cudaEventRecord(e->ev_rel[buf], e->s_dyn));
+      }
+      st.chunks += (uint32_t)nch;
+    }
+    CK(cudaEventRecord(e->ev_dyn_done, e->s_dyn));
+    CK(cudaStreamWaitEvent(e->s_main, e->ev_dyn_done, 0));
+    tm.pend_d = true;
+    st.edges_dynamic += cd.total;
+    st.link_bytes += cd.total * e->eb;
+  }
+  return OG_OK;
+}
+
+// Compacts both regions of `cur` and brings the counts (and the error word) to
+// the host.  Returns the number of listed vertices through *n.
+int compact_round(og_engine *e, const uint32_t *cur, og_stats &st, Timing &tm, uint64_t *n) {
+  CK(cudaEventRecord(e->ev_round, e->s_main));
+  RC(launch_compact(e, 0, cur, 0, e->Vs, e->s_main));
+  CK(cudaEventRecord(e->ev_cs, e->s_main));
+  CK(cudaStreamWaitEvent(e->s_dyn, e->ev_round, 0));
+  RC(launch_compact(e, 1, cur, e->Vs, e->V, e->s_dyn));
+  CK(cudaEventRecord(e->ev_cd, e->s_dyn));
+  CK(cudaStreamWaitEvent(e->s_dyn, e->ev_cs, 0));
+  CK(cudaMemcpyAsync(e->counts_h, e->counts_d, 2 * sizeof(Counts), cudaMemcpyDeviceToHost, e->s_dyn));
+  CK(cudaMemcpyAsync(e->err_h, e->err_d, 4, cudaMemcpyDeviceToHost, e->s_dyn));
+  CK(cudaStreamSynchronize(e->s_dyn));
+  collect_timing(e, tm, &st);
+  float ms;
+  if (cudaEventElapsedTime(&ms, e->ev_round, e->ev_cd) == cudaSuccess) st.ms_compact += ms;
+  RC(check_device_error(e));
+  *n = (uint64_t)e->counts_h[0].n + e->counts_h[1].n;
+  return OG_OK;
+}
+
+template <class Edge>
+int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
+  const uint64_t V = e->V;
+  uint32_t *cur = e->bm[0], *next = e->bm[1];
+  cudaStream_t s = e->s_main;
+  const int g = grid_for(V, e->sms);
+  CK(cudaMemsetAsync(e->err_d, 0, 16, s));
+  CK(cudaMemsetAsync(cur, 0, 4 * e->nwords, s));
+  CK(cudaMemsetAsync(next, 0, 4 * e->nwords, s));
+  if (algo == OG_ALGO_BFS) {
+    CK(cudaMemsetAsync(e->bm[2], 0, 4 * e->nwords, s));
+    k_fill_u32<<<g, kThreads, 0, s>>>(e->value_d, V, (uint32_t)(V + 1));  // GraphMeta.h:378
+    k_set_source<<<1, 1, 0, s>>>(e->value_d, src, 1u, cur, e->bm[2]);
+    e->launches += 2;
+  } else if (algo == OG_ALGO_SSSP) {
+    k_fill_u32<<<g, kThreads, 0, s>>>(e->value_d, V, 0xFFFFFFFFu);  // SSSP GraphMeta.h:377
+    k_set_source<<<1, 1, 0, s>>>(e->value_d, src, 1u, cur, nullptr);
+    e->launches += 2;
+  } else {
+    k_iota_u32<<<g, kThreads, 0, s>>>(e->value_d, V);  // CC GraphMeta.h:341-345
+    k_fill_bits<<<g, kThreads, 0, s>>>(cur, e->nwords, V);
+    e->launches += 2;
+  }
+  CK(cudaGetLastError());
+  Timing tm;
+  RoundOps ro{algo, 1};
+  for (;;) {
+    uint64_t n = 0;
+    RC(compact_round(e, cur, st, tm, &n));
+    if (n == 0) break;
+    st.iterations++;
+    st.frontier_sum += n;
+    st.static_vertices += e->counts_h[0].n;
+    auto sfn = [&](const LbsArgs &a) { return launch_relax<Edge>(e, ro, a, (const Edge *)e->sedges_d, next, e->s_main); };
+    auto dfn = [&](const LbsArgs &a, const Edge *edges, cudaStream_t ds) {
+      return launch_relax<Edge>(e, ro, a, edges, next, ds);
+    };
+    RC((run_regions<Edge>(e, st, tm, sfn, dfn)));
+    CK(cudaStreamWaitEvent(e->s_main, e->ev_cd, 0));
+    CK(cudaMemsetAsync(cur, 0, 4 * e->nwords, e->s_main));
+    std::swap(cur, next);
+    ro.level++;
+    CK(cudaGetLastError());
+  }
+  CK(cudaStreamSynchronize(e->s_main));
+  CK(cudaMemcpy(e->err_h, e->err_d, 4, cudaMemcpyDeviceToHost));
+  RC(check_device_error(e));
+  e->last_algo = algo;
+  return OG_OK;
+}
+
+// ------------------------------------------------------------------ PageRank
+
+template <class Edge>
+int pr_sums(og_engine *e, og_stats &st, Timing &tm) {
+  PrArgs p;
+  p.contrib = e->contrib_d;
+  p.sum = e->sum_d;
+  p.V = e->V;
+  // static tiles use [0, tile_cap0), dynamic tiles [tile_cap0, ...)
+  const uint64_t toff[2] = {0, e->tile_cap[0]};
+  CK(cudaMemsetAsync(e->carry_idx_d, 0xff, 4 * e->pr_tiles, e->s_main));
+  CK(cudaEventRecord(e->ev_round, e->s_main));
+  CK(cudaStreamWaitEvent(e->s_dyn, e->ev_round, 0));
+  CK(cudaStreamWaitEvent(e->s_gat, e->ev_round, 0));
+  auto args_for = [&](int r) {
+    PrArgs q = p;
+    q.cont = e->cont_d + toff[r];
+    q.carry = e->carry_d + toff[r];
+    q.carry_idx = e->carry_idx_d + toff[r];
+    return q;
+  };
+  auto sfn = [&](const LbsArgs &a) {
+    const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
+    if (grid) {
+      k_pr_pull<Edge><<<grid, kThreads, 0, e->s_main>>>(a, (const Edge *)e->sedges_d, args_for(0));
+      e->launches++;
+    }
+    return (int)OG_OK;
+  };
+  auto dfn = [&](const LbsArgs &a, const Edge *edges, cudaStream_t ds) {
+    const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
+    if (grid) {
+      k_pr_pull<Edge><<<grid, kThreads, 0, ds>>>(a, edges, args_for(1));
+      e->launches++;
+    }
+    return (int)OG_OK;
+  };
+  RC((run_regions<Edge>(e, st, tm, sfn, dfn)));
+  for (int r = 0; r < 2; r++) {
+    const Counts c = e->counts_h[r];
+    if (!c.n) continue;
+    const uint64_t nt = (c.total + kTile - 1) / kTile;
+    k_pr_fixup<<<(unsigned)((nt + kThreads - 1) / kThreads), kThreads, 0, e->s_main>>>(
+        e->list_d[r], e->pref_d[r], 0, nt, args_for(r));
+    e->launches++;
+  }
+  CK(cudaGetLastError());
+  return OG_OK;
+}
+
+template <class Edge>
+int run_pr_delta(og_engine *e, float thresh, int max_rounds, og_stats &st) {
+  const uint64_t V = e->V;
+  uint32_t *cur = e->bm[0], *next = e->bm[1];
+  cudaStream_t s = e->s_main;
+  const int g = grid_for(V, e->sms);
+  CK(cudaMemsetAsync(e->err_d, 0, 16, s));
+  k_pr_init<<<g, kThreads, 0, s>>>(V, (float *)e->value_d, e->contrib_d, e->sum_d, e->outdeg_d,
+                                   1.0f);  // PR/OneGraph/GraphMeta.h:354-357
+  k_fill_bits<<<g, kThreads, 0, s>>>(cur, e->nwords, V);
+  e->launches += 2;
+  CK(cudaGetLastError());
+  Timing tm;
+  for (int round = 0; max_rounds <= 0 || round < max_rounds; round++) {
+    uint64_t n = 0;
+    RC(compact_round(e, cur, st, tm, &n));
+    st.iterations++;
+    st.frontier_sum += n;
+    st.static_vertices += e->counts_h[0].n;
+    RC(pr_sums<Edge>(e, st, tm));
+    CK(cudaMemsetAsync(e->active_d, 0, 4, s));
+    k_pr_update_delta<<<grid_for(e->nwords, e->sms), kThreads, 0, s>>>(
+        cur, next, e->nwords, (float *)e->value_d, e->contrib_d, e->sum_d, e->outdeg_d, thresh,
+        e->active_d);
+    e->launches++;
+    CK(cudaMemcpyAsync(e->err_h, e->err_d, 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    RC(check_device_error(e));
+    std::swap(cur, next);
+    if (e->err_h[1] == 0) break;
+  }
+  CK(cudaStreamSynchronize(s));
+  collect_timing(e, tm, &st);
+  e->last_algo = OG_ALGO_PR;
+  return OG_OK;
+}
+
+template <class Edge>
+int run_pr_l1(og_engine *e, float damping, double tol, int max_iter, og_stats &st) {
+  const uint64_t V = e->V;
+  uint32_t *cur = e->bm[0];
+  cudaStream_t s = e->s_main;
+  const int g = grid_for(V, e->sms);
+  CK(cudaMemsetAsync(e->err_d, 0, 16, s));
+  k_pr_init<<<g, kThreads, 0, s>>>(V, (float *)e->value_d, e->contrib_d, e->sum_d, e->outdeg_d,
+                                   (float)(1.0 / (double)V));
+  e->launches++;
+  k_fill_bits<<<g, kThreads, 0, s>>>(cur, e->nwords, V);
+  e->launches++;
+  CK(cudaGetLastError());
+  Timing tm;
+  uint64_t n = 0;
+  RC(compact_round(e, cur, st, tm, &n));  // every vertex with in-edges, once
+  const float teleport = (float)((1.0 - (double)damping) / (double)V);
+  for (int it = 0; it < max_iter; it++) {
+    st.iterations++;
+    st.frontier_sum += n;
+    st.static_vertices += e->counts_h[0].n;
+    RC(pr_sums<Edge>(e, st, tm));
+    k_pr_update_l1<<<e->part_n, kThreads, 0, s>>>(V, (float *)e->value_d, e->contrib_d, e->sum_d,
+                                                  e->outdeg_d, teleport, damping, e->part_d);
+    e->launches++;
+    k_reduce_f64<<<1, kThreads, 0, s>>>(e->part_d, e->part_n, e->l1_d);
+    e->launches++;
+    CK(cudaMemcpyAsync(e->l1_h, e->l1_d, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(e->err_h, e->err_d, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    RC(check_device_error(e));
+    collect_timing(e, tm, &st);
+    st.residual = *e->l1_h;
+    if (*e->l1_h < tol) break;
+  }
+  e->last_algo = OG_ALGO_PR;
+  return OG_OK;
+}
+
+double now_ms() {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch())
+      .count();
+}
+
+int fetch(og_engine *e, void *out) {
+  CK(cudaSetDevice(e->dev));
+  CK(cudaMemcpyAsync(out, e->value_d, 4ull * e->V, cudaMemcpyDeviceToHost, e->s_main));
+  CK(cudaStreamSynchronize(e->s_main));
+  return OG_OK;
+}
+
+template <class F>
+int guarded(F f) {
+  try {
+    return f();
+  } catch (const std::bad_alloc &) {
+    return fail(OG_E_NOMEM, "host allocation failed");
+  } catch (...) {
+    return fail(OG_E_STATE, "unexpected exception");
+  }
+}
+
+int query_common(og_engine *e, int algo, og_stats *st_out, void *out,
+                 int (*body)(og_engine *, og_stats &, void *), void *ctx) {
+  if (!e) return fail(OG_E_ARG, "null engine");
+  return guarded([&]() -> int {
+    clear_error();
+    CK(cudaSetDevice(e->dev));
+    og_stats st;
+    memset(&st, 0, sizeof st);
+    e->launches = 0;
+    const double t0 = now_ms();
+    RC(body(e, st, ctx));
+    st.launches = e->launches;
+    if (out) RC(fetch(e, out));
+    st.ms_total = now_ms() - t0;
+    if (st_out) *st_out = st;
+    (void)algo;
+    return OG_OK;
+  });
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+
+extern "C" int og_engine_create(og_graph *g, const og_config *cfg, og_engine **out) {
+  clear_error();
+  if (!g || !out) return fail(OG_E_ARG, "og_engine_create: null argument");
+  *out = nullptr;
+  og_config c;
+  memset(&c, 0, sizeof c);
+  if (cfg) c = *cfg;
+  return guarded([&]() -> int {
+    og_engine *e = new og_engine;
+    int rc = create(g, &c, e);
+    if (rc != OG_OK) {
+      std::string keep = og_last_error();
+      destroy(e);
+      return fail(rc, "%s", keep.c_str());
+    }
+    *out = e;
+    return OG_OK;
+  });
+}
+
+extern "C" int og_engine_plan(const og_engine *e, og_plan *out) {
+  if (!e || !out) return fail(OG_E_ARG, "og_engine_plan: null argument");
+  *out = e->plan;
+  return OG_OK;
+}
+
+extern "C" void og_engine_destroy(og_engine *e) { destroy(e); }
+
+extern "C" int og_bfs(og_engine *e, uint32_t src, uint32_t *out_depth, og_stats *st) {
+  if (e && src >= e->V) return fail(OG_E_ARG, "source %u >= V %u", src, e->V);
+  return query_common(e, OG_ALGO_BFS, st, out_depth, [](og_engine *en, og_stats &s, void *c) {
+    const uint32_t src_ = *(uint32_t *)c;
+    return en->g->kind == OG_GRAPH_WEIGHTED ? run_frontier<uint2>(en, OG_ALGO_BFS, src_, s)
+                                            : run_frontier<uint32_t>(en, OG_ALGO_BFS, src_, s);
+  }, &src);
+}
+
+extern "C" int og_sssp(og_engine *e, uint32_t src, uint32_t *out_dist, og_stats *st) {
+  if (e && src >= e->V) return fail(OG_E_ARG, "source %u >= V %u", src, e->V);
+  if (e && e->g->kind != OG_GRAPH_WEIGHTED) return fail(OG_E_UNSUPPORTED, "SSSP needs a weighted graph");
+  return query_common(e, OG_ALGO_SSSP, st, out_dist, [](og_engine *en, og_stats &s, void *c) {
+    return run_frontier<uint2>(en, OG_ALGO_SSSP, *(uint32_t *)c, s);
+  }, &src);
+}
+
+extern "C" int og_cc(og_engine *e, uint32_t *out_label, og_stats *st) {
+  uint32_t dummy = 0;
+  return query_common(e, OG_ALGO_CC, st, out_label, [](og_engine *en, og_stats &s, void *) {
+    return en->g->kind == OG_GRAPH_WEIGHTED ? run_frontier<uint2>(en, OG_ALGO_CC, 0, s)
+                                            : run_frontier<uint32_t>(en, OG_ALGO_CC, 0, s);
+  }, &dummy);
+}
+
+namespace {
+struct PrCtx {
+  double a, b;
+  int n;
+};
+}  // namespace
+
+extern "C" int og_pr(og_engine *e, float *out_rank, double threshold, int max_rounds, og_stats *st) {
+  if (e && !e->pr_enabled) return fail(OG_E_UNSUPPORTED, "engine has no PageRank state (OG_CFG_PR)");
+  PrCtx c{threshold, 0, max_rounds};
+  return query_common(e, OG_ALGO_PR, st, out_rank, [](og_engine *en, og_stats &s, void *cx) {
+    const PrCtx &p = *(PrCtx *)cx;
+    return en->g->kind == OG_GRAPH_WEIGHTED ? run_pr_delta<uint2>(en, (float)p.a, p.n, s)
+                                            : run_pr_delta<uint32_t>(en, (float)p.a, p.n, s);
+  }, &c);
+}
+
+extern "C" int og_pr_l1(og_engine *e, float *out_rank, double damping, double tol, int max_iter,
+                        og_stats *st) {
+  if (e && !e->pr_enabled) return fail(OG_E_UNSUPPORTED, "engine has no PageRank state (OG_CFG_PR)");
+  if (max_iter <= 0) return fail(OG_E_ARG, "max_iter must be positive");
+  PrCtx c{damping, tol, max_iter};
+  return query_common(e, OG_ALGO_PR, st, out_rank, [](og_engine *en, og_stats &s, void *cx) {
+    const PrCtx &p = *(PrCtx *)cx;
+    return en->g->kind == OG_GRAPH_WEIGHTED ? run_pr_l1<uint2>(en, (float)p.a, p.b, p.n, s)
+                                            : run_pr_l1<uint32_t>(en, (float)p.a, p.b, p.n, s);
+  }, &c);
+}
+
+extern "C" int og_result_fetch(og_engine *e, int algo, void *out) {
+  if (!e || !out) return fail(OG_E_ARG, "og_result_fetch: null argument");
+  if (e->last_algo != algo) return fail(OG_E_STATE, "no result of algorithm %d on the device", algo);
+  return guarded([&]() { return fetch(e, out); });
+}
+
+extern "C" void og_graph_free(og_graph *g) {
+  if (!g) return;
+  if (g->registered) cudaHostUnregister(g->edges);
+  og::graph_delete(g);
+}

@@ -1,0 +1,340 @@
+// graph_host.cpp — host side of libog.so: errors, CSR file I/O, validation,
+// the region planner and the seeded R-MAT generator.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdarg>
+#include <cstdlib>
+#include <cstring>
+#include <thread>
+
+#include "og_internal.hpp"
+
+namespace og {
+
+static thread_local std::string t_err;
+
+int fail(int status, const char *fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  t_err = buf;
+  return status;
+}
+
+void clear_error() { t_err.clear(); }
+
+// Host CSR arrays start on a 64 KiB boundary and fill whole 64 KiB pages, so
+// two graphs never share a page and each can be page-locked on its own
+// (cudaHostRegister rejects ranges that overlap an earlier registration).
+void *host_alloc(size_t bytes) {
+  constexpr size_t kPage = 64 << 10;
+  const size_t n = (bytes + kPage - 1) / kPage * kPage;
+  void *p = nullptr;
+  if (posix_memalign(&p, kPage, n ? n : kPage) != 0) return nullptr;
+  return p;
+}
+
+void host_free(void *p) { free(p); }
+
+unsigned hw_threads(unsigned requested) {
+  unsigned n = std::thread::hardware_concurrency();
+  if (n == 0) n = 1;
+  if (requested && requested < n) n = requested;
+  return n;
+}
+
+og_graph *graph_new(uint32_t V, uint64_t E, int kind) {
+  og_graph *g = new (std::nothrow) og_graph;
+  if (!g) return nullptr;
+  g->V = V;
+  g->E = E;
+  g->kind = kind;
+  g->off = (uint64_t *)host_alloc(sizeof(uint64_t) * ((size_t)V + 1));
+  g->edges = host_alloc((size_t)E * g->edge_bytes());
+  if (kind == OG_GRAPH_PR) g->outdeg = (uint32_t *)host_alloc(sizeof(uint32_t) * (size_t)(V ? V : 1));
+  if (!g->off || !g->edges || (kind == OG_GRAPH_PR && !g->outdeg)) {
+    graph_delete(g);
+    return nullptr;
+  }
+  return g;
+}
+
+void graph_delete(og_graph *g) {
+  if (!g) return;
+  host_free(g->off);
+  host_free(g->edges);
+  host_free(g->outdeg);
+  delete g;
+}
+
+int graph_validate(const og_graph *g) {
+  const uint32_t V = g->V;
+  if (V == 0) return fail(OG_E_FORMAT, "graph has no vertices");
+  if (g->off[0] != 0) return fail(OG_E_FORMAT, "offsets[0] = %llu, expected 0", (unsigned long long)g->off[0]);
+  if (g->off[V] != g->E) return fail(OG_E_FORMAT, "offset sentinel %llu != E %llu", (unsigned long long)g->off[V], (unsigned long long)g->E);
+  const unsigned nt = hw_threads(0);
+  std::atomic<uint64_t> bad_off{UINT64_MAX}, bad_col{UINT64_MAX};
+  parallel_for_threads(nt, [&](unsigned t, unsigned n) {
+    const uint64_t vb = (uint64_t)V * t / n, ve = (uint64_t)V * (t + 1) / n;
+    for (uint64_t v = vb; v < ve; v++)
+      if (g->off[v + 1] < g->off[v]) {
+        uint64_t cur = bad_off.load();
+        while (v < cur && !bad_off.compare_exchange_weak(cur, v)) {}
+        break;
+      }
+    const uint64_t eb = g->E * t / n, ee = g->E * (t + 1) / n;
+    const uint32_t *c = (const uint32_t *)g->edges;
+    const uint64_t stride = g->kind == OG_GRAPH_WEIGHTED ? 2 : 1;
+    for (uint64_t e = eb; e < ee; e++)
+      if (c[e * stride] >= V) {
+        uint64_t cur = bad_col.load();
+        while (e < cur && !bad_col.compare_exchange_weak(cur, e)) {}
+        break;
+      }
+  });
+  if (bad_off.load() != UINT64_MAX)
+    return fail(OG_E_FORMAT, "offsets decrease at vertex %llu", (unsigned long long)bad_off.load());
+  if (bad_col.load() != UINT64_MAX)
+    return fail(OG_E_FORMAT, "edge %llu has a column >= V", (unsigned long long)bad_col.load());
+  return OG_OK;
+}
+
+// ------------------------------------------------------------------ planner
+
+uint64_t engine_vertex_bytes(int kind, uint32_t flags) {
+  // off_d u64 (8) + value u32 (4, also the f32 rank) + static/dynamic
+  // compacted list u32 (4) + their u64 degree prefixes (8); the three frontier
+  // bitmaps are counted in engine_fixed_bytes.  PageRank adds contrib f32,
+  // sum f32 and outdeg u32.
+  uint64_t b = 8 + 4 + 4 + 8;
+  if (kind == OG_GRAPH_PR || (flags & OG_CFG_PR)) b += 12;
+  return b;
+}
+
+uint64_t engine_fixed_bytes(uint32_t V, uint64_t E) {
+  const uint64_t words = ((uint64_t)V + 31) / 32 + 2 * kCompactWords;
+  const uint64_t bitmaps = 3 * 4 * words;
+  const uint64_t ctiles = words / kCompactWords + 2;
+  const uint64_t lookback = 2 * ctiles * 32;           // two scans in flight
+  const uint64_t lbs_tiles = (E / kLbsTile + 8) * 16;  // tile maps + PR carries
+  // 64 KiB covers the counters, the FP64 partials and the 256 B allocation floor
+  return bitmaps + lookback + lbs_tiles + (64u << 10);
+}
+
+int plan_compute(uint32_t V, uint64_t E, const uint64_t *off, int kind,
+                 uint64_t budget, double advisek, uint32_t flags, og_plan *out) {
+  if (!out || !off) return fail(OG_E_ARG, "plan_compute: null argument");
+  if (kind < OG_GRAPH_PLAIN || kind > OG_GRAPH_PR) return fail(OG_E_ARG, "bad graph kind %d", kind);
+  if (budget == 0) budget = kDefaultBudget;
+  og_plan p;
+  memset(&p, 0, sizeof p);
+  p.budget_bytes = budget;
+  p.edge_bytes = kind == OG_GRAPH_WEIGHTED ? 8 : 4;
+  p.vertex_bytes = engine_vertex_bytes(kind, flags) * ((uint64_t)V + 1);
+  p.fixed_bytes = engine_fixed_bytes(V, E);
+  if (budget <= p.vertex_bytes + p.fixed_bytes)
+    return fail(OG_E_BUDGET,
+                "budget %llu B cannot hold the per-vertex state (%llu B) and scratch (%llu B)",
+                (unsigned long long)budget, (unsigned long long)p.vertex_bytes,
+                (unsigned long long)p.fixed_bytes);
+  const uint64_t T = (budget - p.vertex_bytes - p.fixed_bytes) / p.edge_bytes;
+  p.edge_capacity = T;
+  // GraphMeta.h:311-324: adviseK = (10 - E/T)/9, <0 -> 0.5, >1 -> 1, a positive
+  // user value overrides it.  A user value above 1 is clamped to 1 here (the
+  // reference would make partOverloadSize negative, GraphMeta.h:357).
+  float ak = (10.0f - (float)E / (float)(T ? T : 1)) / 9.0f;
+  if (ak < 0) ak = 0.5f;
+  if (ak > 1) ak = 1.0f;
+  p.advisek_auto = ak;
+  double use = advisek > 0 ? std::min(advisek, 1.0) : (double)ak;
+  p.advisek = use;
+  uint64_t mps = (uint64_t)(use * (double)T);
+  if (mps > E) mps = E;
+  const bool direct = (flags & OG_CFG_DIRECT) != 0;
+  auto prefix_for = [&](uint64_t limit) -> uint32_t {
+    // largest Vs with off[Vs] <= limit (off is monotone, off[0] == 0)
+    const uint64_t *it = std::upper_bound(off, off + (size_t)V + 1, limit);
+    return (uint32_t)((it - off) - 1);
+  };
+  uint32_t Vs = prefix_for(mps);
+  uint64_t st = off[Vs];
+  uint64_t dyn = E - st;
+  uint64_t chunk = 0;
+  if (dyn > 0 && !direct) {
+    // smallest acceptable staging buffer: 1M edges, or an eighth of the edge
+    // budget when that is smaller (small budgets used to force many chunks),
+    // never below one LBS tile and never above the dynamic region itself
+    const uint64_t eighth = std::max<uint64_t>(kLbsTile, T / 8 / kLbsTile * kLbsTile);
+    const uint64_t need = std::min<uint64_t>(
+        std::min<uint64_t>(kMinChunkEdges, eighth), (dyn + kLbsTile - 1) / kLbsTile * kLbsTile);
+    uint64_t room = (T - st) / 2 / kLbsTile * kLbsTile;
+    if (room < need) {
+      // leave room for two staging buffers by shrinking the static prefix
+      if (T < 2 * need)
+        return fail(OG_E_BUDGET, "budget leaves no room for the dynamic staging buffers");
+      mps = std::min(mps, T - 2 * need);
+      Vs = prefix_for(mps);
+      st = off[Vs];
+      dyn = E - st;
+      room = (T - st) / 2 / kLbsTile * kLbsTile;
+    }
+    chunk = std::min(room, (dyn + kLbsTile - 1) / kLbsTile * kLbsTile);
+  }
+  p.max_partition = mps;
+  p.static_vertices = Vs;
+  p.static_edges = st;
+  p.dynamic_edges = dyn;
+  p.chunk_edges = chunk;
+  *out = p;
+  return OG_OK;
+}
+
+}  // namespace og
+
+// ====================================================================== C ABI
+
+using namespace og;
+
+extern "C" const char *og_last_error(void) { return t_err.c_str(); }
+extern "C" int og_abi_version(void) { return OG_ABI_VERSION; }
+
+static bool read_exact(FILE *f, void *p, size_t n) {
+  // large reads in pieces so that a short read is detected early
+  char *c = (char *)p;
+  while (n) {
+    size_t k = std::min<size_t>(n, (size_t)1 << 30);
+    if (fread(c, 1, k, f) != k) return false;
+    c += k;
+    n -= k;
+  }
+  return true;
+}
+
+extern "C" int og_graph_load(const char *path, int kind, og_graph **out) {
+  clear_error();
+  if (!path || !out) return fail(OG_E_ARG, "og_graph_load: null argument");
+  if (kind < OG_GRAPH_PLAIN || kind > OG_GRAPH_PR) return fail(OG_E_ARG, "bad graph kind %d", kind);
+  *out = nullptr;
+  FILE *f = fopen(path, "rb");
+  if (!f) return fail(OG_E_IO, "cannot open %s", path);
+  uint64_t hdr[2];
+  if (fread(hdr, 8, 2, f) != 2) {
+    fclose(f);
+    return fail(OG_E_FORMAT, "%s: short header", path);
+  }
+  // GraphMeta.h:130 reads the u64 V into a 32-bit field; V must fit in 32 bits.
+  if (hdr[0] == 0 || hdr[0] > 0xFFFFFFFFull) {
+    fclose(f);
+    return fail(OG_E_FORMAT, "%s: vertex count %llu out of range", path, (unsigned long long)hdr[0]);
+  }
+  const uint32_t V = (uint32_t)hdr[0];
+  const uint64_t E = hdr[1];
+  const uint64_t eb = kind == OG_GRAPH_WEIGHTED ? 8 : 4;
+  fseeko(f, 0, SEEK_END);
+  const uint64_t size = (uint64_t)ftello(f);
+  const uint64_t want = 16 + (kind == OG_GRAPH_PR ? 4ull * V : 0) + 8ull * V + E * eb;
+  if (E > (1ull << 40) || size != want) {
+    fclose(f);
+    return fail(OG_E_FORMAT, "%s: file has %llu bytes, header implies %llu", path,
+                (unsigned long long)size, (unsigned long long)want);
+  }
+  fseeko(f, 16, SEEK_SET);
+  og_graph *g = graph_new(V, E, kind);
+  if (!g) {
+    fclose(f);
+    return fail(OG_E_NOMEM, "cannot allocate host CSR (%llu edges)", (unsigned long long)E);
+  }
+  bool ok = true;
+  if (kind == OG_GRAPH_PR) ok = read_exact(f, g->outdeg, 4ull * V);
+  ok = ok && read_exact(f, g->off, 8ull * V) && read_exact(f, g->edges, E * eb);
+  fclose(f);
+  if (!ok) {
+    graph_delete(g);
+    return fail(OG_E_IO, "%s: read failed", path);
+  }
+  g->off[V] = E;
+  int rc = graph_validate(g);
+  if (rc != OG_OK) {
+    graph_delete(g);
+    return rc;
+  }
+  *out = g;
+  return OG_OK;
+}
+
+extern "C" int og_graph_from_arrays(uint64_t V, uint64_t E, const uint64_t *offsets,
+                                    int with_sentinel, const void *edges,
+                                    const uint32_t *outdeg, int kind, og_graph **out) {
+  clear_error();
+  if (!out || !offsets || (E && !edges)) return fail(OG_E_ARG, "og_graph_from_arrays: null argument");
+  if (V == 0 || V > 0xFFFFFFFFull) return fail(OG_E_ARG, "vertex count out of range");
+  if (kind < OG_GRAPH_PLAIN || kind > OG_GRAPH_PR) return fail(OG_E_ARG, "bad graph kind %d", kind);
+  if (kind == OG_GRAPH_PR && !outdeg) return fail(OG_E_ARG, "PR graph needs outdeg");
+  *out = nullptr;
+  og_graph *g = graph_new((uint32_t)V, E, kind);
+  if (!g) return fail(OG_E_NOMEM, "cannot allocate host CSR");
+  memcpy(g->off, offsets, 8 * V);
+  g->off[V] = with_sentinel ? offsets[V] : E;
+  if (E) memcpy(g->edges, edges, E * g->edge_bytes());
+  if (kind == OG_GRAPH_PR) memcpy(g->outdeg, outdeg, 4 * V);
+  int rc = graph_validate(g);
+  if (rc != OG_OK) {
+    graph_delete(g);
+    return rc;
+  }
+  *out = g;
+  return OG_OK;
+}
+
+extern "C" int og_graph_save(const og_graph *g, const char *path) {
+  clear_error();
+  if (!g || !path) return fail(OG_E_ARG, "og_graph_save: null argument");
+  FILE *f = fopen(path, "wb");
+  if (!f) return fail(OG_E_IO, "cannot create %s", path);
+  uint64_t hdr[2] = {g->V, g->E};
+  bool ok = fwrite(hdr, 8, 2, f) == 2;
+  if (ok && g->kind == OG_GRAPH_PR) ok = fwrite(g->outdeg, 4, g->V, f) == g->V;
+  ok = ok && fwrite(g->off, 8, g->V, f) == g->V;
+  const char *c = (const char *)g->edges;
+  uint64_t left = g->E * g->edge_bytes();
+  while (ok && left) {
+    size_t k = (size_t)std::min<uint64_t>(left, 1ull << 30);
+    ok = fwrite(c, 1, k, f) == k;
+    c += k;
+    left -= k;
+  }
+  ok = (fclose(f) == 0) && ok;
+  return ok ? OG_OK : fail(OG_E_IO, "write to %s failed", path);
+}
+
+extern "C" int og_graph_info(const og_graph *g, uint64_t *V, uint64_t *E, int *kind,
+                             const uint64_t **offsets, const void **edges,
+                             const uint32_t **outdeg) {
+  if (!g) return fail(OG_E_ARG, "og_graph_info: null graph");
+  if (V) *V = g->V;
+  if (E) *E = g->E;
+  if (kind) *kind = g->kind;
+  if (offsets) *offsets = g->off;
+  if (edges) *edges = g->edges;
+  if (outdeg) *outdeg = g->outdeg;
+  return OG_OK;
+}
+
+extern "C" uint32_t og_graph_findbignode(const og_graph *g, uint32_t last) {
+  // GraphMeta.h:150-165
+  if (!g || g->V < 2) return last;
+  for (uint64_t i = (uint64_t)last + 1; i < (uint64_t)g->V - 1; i++)
+    if (g->off[i + 1] - g->off[i] > 3000) return (uint32_t)i;
+  return last;
+}
+
+extern "C" int og_plan_compute(uint64_t V, uint64_t E, const uint64_t *offsets, int kind,
+                               uint64_t budget_bytes, double advisek, uint32_t flags,
+                               og_plan *out) {
+  clear_error();
+  if (V == 0 || V > 0xFFFFFFFFull) return fail(OG_E_ARG, "vertex count out of range");
+  return plan_compute((uint32_t)V, E, offsets, kind, budget_bytes, advisek, flags, out);
+}

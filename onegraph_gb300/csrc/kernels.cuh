@@ -1,0 +1,613 @@
+// kernels.cuh — sm_103a kernels of the out-of-memory engine.
+//
+//  k_compact   frontier bitmap -> compacted vertex list + u64 degree prefix +
+//              LBS tile map, one pass with a decoupled look-back scan.  Replaces
+//              setStaticAndOverloadLabelBool / myReduction / myExclusive_scan /
+//              setStaticActiveNodeArray / setOverloadNodePointerSwap and the
+//              host degree scan (BFS/oneGraph_BFS/gpu_kernels.h:243-379,
+//              CalculateOpt.h:78-124) and the Subway generator's
+//              flag/scan/queue/pointer steps (PR/sbw/subgraph_generator.h:57-234).
+//  k_lbs<Op>   edge-balanced ("load-balanced search") expansion: every CTA owns
+//              2048 consecutive edge positions of the compacted list, whatever
+//              the degrees; columns are read coalesced.  Op = BFS / SSSP / CC
+//              relax (gpu_kernels.h:180-241, SSSP :106-203, CC :105-157) or
+//              the dynamic-region gather from page-locked host memory
+//              (GraphMeta.h:471-506 fillEdgeArrByMultiThread).
+//  k_pr_*      PageRank pull sum with a deterministic segmented reduction
+//              (PR/OneGraph/gpu_kernels.h:107-158) and the rank update with an
+//              FP64 L1 reduction (gpu_kernels.h:295-319).
+#pragma once
+#include <cuda/atomic>
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+namespace og {
+
+constexpr int kThreads = 256;
+constexpr uint32_t kTile = 2048;             // LBS edge positions per CTA
+constexpr uint32_t kItems = kTile / kThreads;  // 8
+constexpr uint32_t kWordsPerCompactTile = 256;
+
+// device error bits (OR-ed into the engine's error word)
+constexpr uint32_t kErrLookback = 1u;    // look-back wait gave up
+constexpr uint32_t kErrEdgeIndex = 2u;   // edge index outside the array
+constexpr uint32_t kErrVertex = 4u;      // column >= V
+constexpr uint32_t kErrTileMap = 8u;     // LBS tile map inconsistent
+
+constexpr uint32_t kSpinLimit = 1u << 24;
+
+struct Counts {
+  uint32_t n;      // compacted vertices
+  uint32_t pad;
+  uint64_t total;  // sum of their degrees (edge positions)
+};
+
+struct Lookback {
+  uint32_t *status;  // 0 empty, 1 aggregate, 2 inclusive prefix
+  uint32_t *agg_n;
+  unsigned long long *agg_e;
+  uint32_t *inc_n;
+  unsigned long long *inc_e;
+  uint32_t *ticket;
+};
+
+struct CompactArgs {
+  const uint32_t *bits;  // frontier bitmap
+  uint32_t v_begin, v_end;
+  uint32_t w_begin, w_end, ntiles;
+  const uint64_t *off;   // CSR offsets (V+1) on the device
+  uint32_t *list;
+  uint64_t *pref;        // exclusive degree prefix, pref[n] = total
+  uint32_t *tile_first;  // LBS tile -> list index of the vertex holding its first position
+  Counts *counts;
+  Lookback lb;
+  uint32_t *err;
+  uint64_t list_cap;     // entries of list (pref has list_cap + 1)
+  uint64_t tile_cap;     // entries of tile_first
+};
+
+__device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
+  return cuda::atomic_ref<const uint32_t, cuda::thread_scope_device>(*p).load(
+      cuda::memory_order_acquire);
+}
+__device__ __forceinline__ void st_release(uint32_t *p, uint32_t v) {
+  cuda::atomic_ref<uint32_t, cuda::thread_scope_device>(*p).store(v, cuda::memory_order_release);
+}
+
+// Block-wide exclusive scan of (u32, u64) pairs; returns the block totals.
+__device__ __forceinline__ void block_scan_pair(uint32_t cnt, uint64_t sum, uint32_t &ex_cnt,
+                                                uint64_t &ex_sum, uint32_t &tot_cnt,
+                                                uint64_t &tot_sum) {
+  __shared__ uint32_t s_wc[kThreads / 32];
+  __shared__ uint64_t s_ws[kThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t ic = cnt;
+  uint64_t is = sum;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t c = __shfl_up_sync(0xffffffffu, ic, d);
+    const uint64_t s = __shfl_up_sync(0xffffffffu, is, d);
+    if (lane >= d) {
+      ic += c;
+      is += s;
+    }
+  }
+  if (lane == 31) {
+    s_wc[warp] = ic;
+    s_ws[warp] = is;
+  }
+  __syncthreads();
+  if (warp == 0) {
+    uint32_t wc = lane < kThreads / 32 ? s_wc[lane] : 0;
+    uint64_t ws = lane < kThreads / 32 ? s_ws[lane] : 0;
+#pragma unroll
+    for (int d = 1; d < kThreads / 32; d <<= 1) {
+      const uint32_t c = __shfl_up_sync(0xffffffffu, wc, d);
+      const uint64_t s = __shfl_up_sync(0xffffffffu, ws, d);
+      if (lane >= d) {
+        wc += c;
+        ws += s;
+      }
+    }
+    if (lane < kThreads / 32) {
+      s_wc[lane] = wc;  // inclusive warp prefixes
+      s_ws[lane] = ws;
+    }
+  }
+  __syncthreads();
+  const uint32_t wpc = warp ? s_wc[warp - 1] : 0;
+  const uint64_t wps = warp ? s_ws[warp - 1] : 0;
+  ex_cnt = wpc + ic - cnt;
+  ex_sum = wps + is - sum;
+  tot_cnt = s_wc[kThreads / 32 - 1];
+  tot_sum = s_ws[kThreads / 32 - 1];
+  __syncthreads();  // shared arrays are reused by the next call
+}
+
+// Frontier compaction for the vertex range [v_begin, v_end).  One thread per
+// bitmap word (32 vertices), 256 words per CTA tile, tiles ordered by a ticket
+// so that every predecessor a tile waits for is already running.
+__global__ void __launch_bounds__(kThreads) k_compact(CompactArgs a) {
+  __shared__ uint32_t s_tile;
+  __shared__ uint32_t s_excl_n;
+  __shared__ uint64_t s_excl_e;
+  __shared__ int s_bad;
+  if (threadIdx.x == 0) s_tile = atomicAdd(a.lb.ticket, 1u);
+  __syncthreads();
+  const uint32_t tile = s_tile;
+  const uint32_t w = a.w_begin + tile * kWordsPerCompactTile + threadIdx.x;
+  const uint64_t vbase = (uint64_t)w * 32;
+  uint32_t word = 0;
+  if (w < a.w_end) {
+    word = a.bits[w];
+    if (vbase < a.v_begin) {
+      const uint32_t sh = a.v_begin - (uint32_t)vbase;
+      word = sh >= 32 ? 0 : word & (0xffffffffu << sh);
+    }
+    if (vbase + 32 > a.v_end) {
+      const uint64_t keep = a.v_end > vbase ? a.v_end - vbase : 0;
+      word = keep >= 32 ? word : word & ((1u << keep) - 1u);
+    }
+  }
+  // drop vertices without edges: nothing to expand
+  uint32_t keep = 0, cnt = 0;
+  uint64_t sum = 0;
+  for (uint32_t m = word; m; m &= m - 1) {
+    const uint32_t b = __ffs(m) - 1;
+    const uint64_t v = vbase + b;
+    const uint64_t d = a.off[v + 1] - a.off[v];
+    if (d) {
+      keep |= 1u << b;
+      cnt++;
+      sum += d;
+    }
+  }
+  uint32_t ex_n, tot_n;
+  uint64_t ex_e, tot_e;
+  block_scan_pair(cnt, sum, ex_n, ex_e, tot_n, tot_e);
+  if (threadIdx.x == 0) {
+    uint32_t pn = 0;
+    uint64_t pe = 0;
+    int bad = 0;
+    if (tile == 0) {
+      a.lb.inc_n[0] = tot_n;
+      a.lb.inc_e[0] = tot_e;
+      __threadfence();
+      st_release(&a.lb.status[0], 2u);
+    } else {
+      a.lb.agg_n[tile] = tot_n;
+      a.lb.agg_e[tile] = tot_e;
+      __threadfence();
+      st_release(&a.lb.status[tile], 1u);
+      for (int p = (int)tile - 1; p >= 0;) {
+        uint32_t st;
+        uint32_t spins = 0;
+        while ((st = ld_acquire(&a.lb.status[p])) == 0u) {
+          if (++spins > kSpinLimit) break;
+          __nanosleep(64);
+        }
+        if (st == 0u) {  // bounded wait expired: report, never hang
+          atomicOr(a.err, kErrLookback);
+          bad = 1;
+          break;
+        }
+        if (st == 2u) {
+          pn += __ldcg(&a.lb.inc_n[p]);
+          pe += __ldcg(&a.lb.inc_e[p]);
+          break;
+        }
+        pn += __ldcg(&a.lb.agg_n[p]);
+        pe += __ldcg(&a.lb.agg_e[p]);
+        p--;
+      }
+      a.lb.inc_n[tile] = pn + tot_n;
+      a.lb.inc_e[tile] = pe + tot_e;
+      __threadfence();
+      st_release(&a.lb.status[tile], 2u);
+    }
+    if (!bad && (uint64_t)pn + tot_n > a.list_cap) {
+      atomicOr(a.err, kErrTileMap);
+      bad = 1;
+    }
+    s_excl_n = pn;
+    s_excl_e = pe;
+    s_bad = bad;
+    if (!bad && tile == a.ntiles - 1) {
+      a.counts->n = pn + tot_n;
+      a.counts->total = pe + tot_e;
+      a.pref[pn + tot_n] = pe + tot_e;
+    }
+  }
+  __syncthreads();
+  if (s_bad) return;  // positions unknown: write nothing
+  uint32_t pos = s_excl_n + ex_n;
+  uint64_t ep = s_excl_e + ex_e;
+  for (uint32_t m = keep; m; m &= m - 1) {
+    const uint32_t b = __ffs(m) - 1;
+    const uint64_t v = vbase + b;
+    const uint64_t d = a.off[v + 1] - a.off[v];
+    a.list[pos] = (uint32_t)v;
+    a.pref[pos] = ep;
+    for (uint64_t t = (ep + kTile - 1) / kTile; t * kTile < ep + d; t++) {
+      if (t >= a.tile_cap) {
+        atomicOr(a.err, kErrTileMap);
+        break;
+      }
+      a.tile_first[t] = pos;
+    }
+    pos++;
+    ep += d;
+  }
+}
+
+// ------------------------------------------------------------------ LBS
+
+struct LbsArgs {
+  const uint32_t *list;
+  const uint64_t *pref;
+  const uint32_t *tile_first;
+  uint32_t n;            // list length
+  uint64_t total;        // pref[n]
+  uint64_t pos_begin;    // multiple of kTile
+  uint64_t pos_end;
+  const uint64_t *off;   // CSR mode: edge index = off[v] - pref[i] + q
+  uint64_t stage_base;   // staging mode (off == nullptr): index = q - stage_base
+  uint64_t edge_bound;   // entries addressable through the edge pointer
+  uint32_t *err;
+};
+
+struct LbsShared {
+  uint32_t rs[kTile + 2];      // tile-relative start of each local vertex
+  unsigned long long cb[kTile + 1];  // edge index of tile position 0 for the vertex
+  uint32_t val[kTile + 1];     // source value of each local vertex
+  unsigned short map[kTile];   // tile position -> local vertex
+};
+
+// Builds the local-vertex tables of tile k; returns the local count (0 on error).
+template <bool kNeedVal, class Op>
+__device__ __forceinline__ uint32_t lbs_setup(const LbsArgs &a, const Op &op, LbsShared &sh,
+                                              uint64_t k, uint64_t pos0, uint32_t &i0_out) {
+  const uint64_t ntiles_total = (a.total + kTile - 1) / kTile;
+  const uint32_t i0 = a.tile_first[k];
+  const uint32_t i1 = (k + 1 < ntiles_total) ? a.tile_first[k + 1] : a.n - 1;
+  i0_out = i0;
+  if (i1 < i0 || i1 - i0 > kTile || i1 >= a.n) {
+    if (threadIdx.x == 0) atomicOr(a.err, kErrTileMap);
+    return 0;
+  }
+  const uint32_t nl = i1 - i0 + 1;
+  for (uint32_t j = threadIdx.x; j < nl; j += kThreads) {
+    const uint32_t i = i0 + j;
+    const uint32_t v = a.list[i];
+    const uint64_t p = a.pref[i];
+    sh.rs[j] = p > pos0 ? (uint32_t)min(p - pos0, (uint64_t)kTile) : 0u;
+    const uint64_t src = a.off ? a.off[v] - p : (0ull - a.stage_base);
+    sh.cb[j] = src + pos0;
+    if (kNeedVal) sh.val[j] = op.src_val(v);
+  }
+  for (uint32_t x = threadIdx.x; x < kTile; x += kThreads) sh.map[x] = 0;
+  __syncthreads();
+  // Head flags.  Compacted lists hold no zero-degree vertex, so for j >= 1 the
+  // starts rs[j] are distinct and strictly increasing (rs[0] = 0).
+  for (uint32_t j = 1 + threadIdx.x; j < nl; j += kThreads) {
+    const uint32_t r = sh.rs[j];
+    if (r < kTile) sh.map[r] = (unsigned short)1;
+  }
+  __syncthreads();
+  // inclusive scan of the head flags (blocked: thread t owns 8 positions)
+  {
+    uint32_t f[kItems];
+    uint32_t s = 0;
+#pragma unroll
+    for (int i = 0; i < (int)kItems; i++) {
+      f[i] = sh.map[threadIdx.x * kItems + i];
+      s += f[i];
+    }
+    uint32_t ex, tot;
+    uint64_t ex64, tot64;
+    block_scan_pair(s, 0, ex, ex64, tot, tot64);
+    uint32_t run = ex;
+#pragma unroll
+    for (int i = 0; i < (int)kItems; i++) {
+      run += f[i];
+      sh.map[threadIdx.x * kItems + i] = (unsigned short)run;
+    }
+  }
+  __syncthreads();
+  return nl;
+}
+
+template <class Edge, class Op>
+__global__ void __launch_bounds__(kThreads) k_lbs(LbsArgs a, const Edge *__restrict__ edges, Op op) {
+  __shared__ LbsShared sh;
+  const uint64_t k = a.pos_begin / kTile + blockIdx.x;
+  const uint64_t pos0 = k * kTile;
+  if (pos0 >= a.pos_end) return;
+  const uint64_t pend = min(pos0 + kTile, a.pos_end);
+  uint32_t i0;
+  const uint32_t nl = lbs_setup<Op::kNeedVal>(a, op, sh, k, pos0, i0);
+  if (nl == 0) return;
+#pragma unroll
+  for (int it = 0; it < (int)kItems; it++) {
+    const uint32_t x = it * kThreads + threadIdx.x;
+    const uint64_t q = pos0 + x;
+    if (q < pend) {
+      const uint32_t l = sh.map[x];
+      const uint64_t idx = sh.cb[l] + x;
+      if (idx >= a.edge_bound) {
+        atomicOr(a.err, kErrEdgeIndex);
+        continue;
+      }
+      op.relax(edges[idx], Op::kNeedVal ? sh.val[l] : 0u, q);
+    }
+  }
+}
+
+// ------------------------------------------------------------------ ops
+
+__device__ __forceinline__ uint32_t edge_dst(uint32_t e) { return e; }
+__device__ __forceinline__ uint32_t edge_dst(uint2 e) { return e.x; }
+__device__ __forceinline__ uint32_t edge_w(uint32_t) { return 1u; }
+__device__ __forceinline__ uint32_t edge_w(uint2 e) { return e.y; }
+
+// Level-synchronous BFS with a visited bitmap: every vertex is claimed once.
+struct BfsOp {
+  static constexpr bool kNeedVal = false;
+  uint32_t *visited, *next, *depth, *err;
+  uint32_t V, newdepth;
+  __device__ uint32_t src_val(uint32_t) const { return 0; }
+  template <class Edge>
+  __device__ __forceinline__ void relax(Edge e, uint32_t, uint64_t) const {
+    const uint32_t v = edge_dst(e);
+    if (v >= V) {
+      atomicOr(err, kErrVertex);
+      return;
+    }
+    const uint32_t w = v >> 5, bit = 1u << (v & 31);
+    if (__ldcg(visited + w) & bit) return;
+    const uint32_t old = atomicOr(visited + w, bit);
+    if (old & bit) return;
+    depth[v] = newdepth;
+    atomicOr(next + w, bit);
+  }
+};
+
+// atomicMin relax shared by SSSP (weighted) and CC (label push).
+template <bool kWeighted>
+struct MinOp {
+  static constexpr bool kNeedVal = true;
+  uint32_t *value, *next, *err;
+  uint32_t V;
+  __device__ uint32_t src_val(uint32_t v) const { return __ldcg(value + v); }
+  template <class Edge>
+  __device__ __forceinline__ void relax(Edge e, uint32_t sv, uint64_t) const {
+    const uint32_t v = edge_dst(e);
+    if (v >= V) {
+      atomicOr(err, kErrVertex);
+      return;
+    }
+    const uint32_t cand = kWeighted ? sv + edge_w(e) : sv;
+    if (cand >= __ldcg(value + v)) return;
+    const uint32_t old = atomicMin(value + v, cand);
+    if (cand < old) atomicOr(next + (v >> 5), 1u << (v & 31));
+  }
+};
+
+// Dynamic-region gather: copies the edges of the compacted list from the
+// page-locked host CSR into a device staging buffer (coalesced on both sides).
+template <class Edge>
+struct GatherOp {
+  static constexpr bool kNeedVal = false;
+  Edge *stage;
+  uint64_t stage_base;
+  __device__ uint32_t src_val(uint32_t) const { return 0; }
+  __device__ __forceinline__ void relax(Edge e, uint32_t, uint64_t q) const { stage[q - stage_base] = e; }
+};
+
+// ------------------------------------------------------------------ PageRank
+
+constexpr uint32_t kNoCarry = 0xffffffffu;
+
+struct PrArgs {
+  const float *contrib;   // rank[u] / outdeg[u] (0 for dangling u)
+  float *sum;             // pull sums, written for every listed vertex
+  float *cont;            // per LBS tile: partial of a vertex that began in an earlier tile
+  float *carry;           // per LBS tile: partial of a vertex that began here and continues
+  uint32_t *carry_idx;    // per LBS tile: list index of that vertex, kNoCarry if none
+  uint32_t V;
+};
+
+// Pull sum sum[v] = sum over in-edges (u -> v) of contrib[u]
+// (PR/OneGraph/gpu_kernels.h:107-158).  Contributions are staged in shared
+// memory in edge order and each vertex's segment is added sequentially, so the
+// result depends only on the tiling of the compacted list (deterministic).
+template <class Edge>
+__global__ void __launch_bounds__(kThreads) k_pr_pull(LbsArgs a, const Edge *__restrict__ edges,
+                                                       PrArgs p) {
+  __shared__ LbsShared sh;
+  __shared__ float s_c[kTile];
+  const uint64_t k = a.pos_begin / kTile + blockIdx.x;
+  const uint64_t pos0 = k * kTile;
+  if (pos0 >= a.pos_end) return;
+  const uint64_t pend = min(pos0 + kTile, a.pos_end);
+  const uint32_t tlen = (uint32_t)(pend - pos0);
+  struct NoVal {
+    __device__ uint32_t src_val(uint32_t) const { return 0; }
+  } nv;
+  uint32_t i0;
+  const uint32_t nl = lbs_setup<false>(a, nv, sh, k, pos0, i0);
+  if (nl == 0) return;
+#pragma unroll
+  for (int it = 0; it < (int)kItems; it++) {
+    const uint32_t x = it * kThreads + threadIdx.x;
+    float c = 0.f;
+    if (x < tlen) {
+      const uint32_t l = sh.map[x];
+      const uint64_t idx = sh.cb[l] + x;
+      if (idx < a.edge_bound) {
+        const uint32_t u = edge_dst(edges[idx]);
+        if (u < p.V) c = __ldg(p.contrib + u);
+        else atomicOr(a.err, kErrVertex);
+      } else {
+        atomicOr(a.err, kErrEdgeIndex);
+      }
+    }
+    s_c[x] = c;
+  }
+  __syncthreads();
+  for (uint32_t j = threadIdx.x; j < nl; j += kThreads) {
+    const uint32_t b = sh.rs[j];
+    const uint32_t e = (j + 1 < nl) ? min(sh.rs[j + 1], tlen) : tlen;
+    if (b >= e) continue;
+    float s = 0.f;
+    for (uint32_t x = b; x < e; x++) s += s_c[x];
+    const uint32_t i = i0 + j;
+    const bool before = (j == 0) && (a.pref[i] < pos0);
+    const bool after = a.pref[i + 1] > pos0 + kTile;
+    if (before) {
+      p.cont[k] = s;
+    } else if (after) {
+      p.carry[k] = s;
+      p.carry_idx[k] = i;
+    } else {
+      p.sum[a.list[i]] = s;
+    }
+  }
+}
+
+// Completes the sums of vertices split over several tiles, in tile order.
+__global__ void k_pr_fixup(const uint32_t *list, const uint64_t *pref, uint64_t tile_begin,
+                           uint64_t tile_end, PrArgs p) {
+  const uint64_t k = tile_begin + blockIdx.x * (uint64_t)blockDim.x + threadIdx.x;
+  if (k >= tile_end) return;
+  const uint32_t i = p.carry_idx[k];
+  if (i == kNoCarry) return;
+  float s = p.carry[k];
+  const uint64_t end = pref[i + 1];
+  for (uint64_t t = k + 1; t * kTile < end; t++) s += p.cont[t];
+  p.sum[list[i]] = s;
+}
+
+// prKernel_Opt (PR/OneGraph/gpu_kernels.h:295-319): for every active vertex
+// new = 0.15 + 0.85*sum; it stays active with the new rank iff |new-old| >
+// thresh, otherwise it goes inactive keeping its rank.  One thread per bitmap
+// word; writes the next active bitmap and counts the survivors.
+__global__ void __launch_bounds__(kThreads) k_pr_update_delta(
+    const uint32_t *cur, uint32_t *next, uint64_t nwords, float *rank, float *contrib,
+    const float *sum, const uint32_t *outdeg, float thresh, uint32_t *active) {
+  __shared__ uint32_t s_cnt;
+  if (threadIdx.x == 0) s_cnt = 0;
+  __syncthreads();
+  uint32_t mine = 0;
+  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwords;
+       w += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t word = cur[w];
+    uint32_t keep = 0;
+    for (uint32_t m = word; m; m &= m - 1) {
+      const uint32_t b = __ffs(m) - 1;
+      const uint64_t v = w * 32 + b;
+      const float nvv = 0.15f + 0.85f * sum[v];
+      const float old = rank[v];
+      const float diff = nvv > old ? nvv - old : old - nvv;
+      if (diff > thresh) {
+        rank[v] = nvv;
+        const uint32_t od = outdeg[v];
+        contrib[v] = od ? nvv / (float)od : 0.f;
+        keep |= 1u << b;
+      }
+    }
+    next[w] = keep;
+    mine += __popc(keep);
+  }
+  atomicAdd(&s_cnt, mine);
+  __syncthreads();
+  if (threadIdx.x == 0 && s_cnt) atomicAdd(active, s_cnt);
+}
+
+// Normalised update p' = teleport + damping*sum for every vertex, with the L1
+// delta accumulated in FP64: per-thread, then a fixed-shape block tree, one
+// partial per block (the grid size is fixed, so the order never changes).
+__global__ void __launch_bounds__(kThreads) k_pr_update_l1(uint64_t V, float *rank, float *contrib,
+                                                           const float *sum, const uint32_t *outdeg,
+                                                           float teleport, float damping,
+                                                           double *part) {
+  __shared__ double s_d[kThreads];
+  double acc = 0.0;
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    const float nvv = teleport + damping * sum[v];
+    acc += fabs((double)nvv - (double)rank[v]);
+    rank[v] = nvv;
+    const uint32_t od = outdeg[v];
+    contrib[v] = od ? nvv / (float)od : 0.f;
+  }
+  s_d[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = kThreads / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) s_d[threadIdx.x] += s_d[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) part[blockIdx.x] = s_d[0];
+}
+
+__global__ void k_reduce_f64(const double *part, uint32_t n, double *out) {
+  __shared__ double s_d[kThreads];
+  double acc = 0.0;
+  for (uint32_t i = threadIdx.x; i < n; i += kThreads) acc += part[i];
+  s_d[threadIdx.x] = acc;
+  __syncthreads();
+  for (int s = kThreads / 2; s > 0; s >>= 1) {
+    if ((int)threadIdx.x < s) s_d[threadIdx.x] += s_d[threadIdx.x + s];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *out = s_d[0];
+}
+
+__global__ void k_pr_init(uint64_t V, float *rank, float *contrib, float *sum, const uint32_t *outdeg,
+                          float r0) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    rank[v] = r0;
+    const uint32_t od = outdeg[v];
+    contrib[v] = od ? r0 / (float)od : 0.f;
+    sum[v] = 0.f;
+  }
+}
+
+__global__ void k_degree_from_offsets(uint64_t V, const uint64_t *off, uint32_t *deg) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V;
+       v += (uint64_t)gridDim.x * blockDim.x)
+    deg[v] = (uint32_t)(off[v + 1] - off[v]);
+}
+
+// ------------------------------------------------------------------ fills
+
+__global__ void k_fill_u32(uint32_t *p, uint64_t n, uint32_t v) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    p[i] = v;
+}
+
+__global__ void k_iota_u32(uint32_t *p, uint64_t n) {
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
+       i += (uint64_t)gridDim.x * blockDim.x)
+    p[i] = (uint32_t)i;
+}
+
+// bits [0, V) set, the rest of the words cleared
+__global__ void k_fill_bits(uint32_t *bits, uint64_t nwords, uint64_t V) {
+  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwords;
+       w += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t b = w * 32;
+    bits[w] = b + 32 <= V ? 0xffffffffu : (b >= V ? 0u : ((1u << (V - b)) - 1u));
+  }
+}
+
+__global__ void k_set_source(uint32_t *value, uint32_t src, uint32_t val, uint32_t *bits_a,
+                             uint32_t *bits_b) {
+  value[src] = val;
+  bits_a[src >> 5] |= 1u << (src & 31);
+  if (bits_b) bits_b[src >> 5] |= 1u << (src & 31);
+}
+
+}  // namespace og

@@ -1,0 +1,119 @@
+"""ctypes binding of the CPU oracle (og_oracle.c) — test infrastructure only.
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
+this package, and only as the checker or the timed CPU baseline; libog.so
+never calls it.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build_oracle
+
+_lib = None
+_P = C.c_void_p
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        path = build_oracle.build_oracle()
+        L = C.CDLL(path)
+        u32, u64 = C.c_uint32, C.c_uint64
+        L.ora_bfs.argtypes = [u32, _P, _P, u32, _P]
+        L.ora_cc.argtypes = [u32, _P, _P, _P]
+        L.ora_sssp_dijkstra.argtypes = [u32, _P, _P, u32, _P]
+        L.ora_sssp_dijkstra.restype = None
+        L.ora_sssp_frontier.argtypes = [u32, _P, _P, u32, _P]
+        L.ora_sssp_dijkstra_bounded.argtypes = [u32, _P, _P, u32, u64, _P]
+        L.ora_sssp_dijkstra_bounded.restype = u64
+        L.ora_pr_cpu.argtypes = [u32, _P, _P, _P, _P]
+        L.ora_pr_onegraph.argtypes = [u32, _P, _P, _P, C.c_double, C.c_int, _P]
+        L.ora_pr_l1.argtypes = [u32, _P, _P, _P, C.c_double, C.c_double, C.c_int, _P,
+                                C.POINTER(C.c_double)]
+        for f in ("ora_bfs", "ora_cc", "ora_sssp_frontier", "ora_pr_cpu", "ora_pr_onegraph",
+                  "ora_pr_l1"):
+            getattr(L, f).restype = C.c_int
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(_P)
+
+
+def _csr(off, edges):
+    off = np.ascontiguousarray(off, dtype=np.uint64)
+    edges = np.ascontiguousarray(edges, dtype=np.uint32)
+    return off, edges, off.size - 1
+
+
+def bfs(off, col, src):
+    """runCPUBFS restatement: depth(src) = 1, unreached = 0xFFFFFFFF."""
+    off, col, V = _csr(off, col)
+    out = np.empty(V, np.uint32)
+    rounds = lib().ora_bfs(V, _p(off), _p(col), src, _p(out))
+    return out, rounds
+
+
+def cc(off, col):
+    off, col, V = _csr(off, col)
+    out = np.empty(V, np.uint32)
+    rounds = lib().ora_cc(V, _p(off), _p(col), _p(out))
+    return out, rounds
+
+
+def sssp_dijkstra(off, pairs, src):
+    off, pairs, V = _csr(off, pairs)
+    out = np.empty(V, np.uint32)
+    lib().ora_sssp_dijkstra(V, _p(off), _p(pairs), src, _p(out))
+    return out
+
+
+def sssp_dijkstra_bounded_raw(V, off_ptr, pairs_ptr, src, max_edges, out):
+    """Pointer form (no copies) for timing on large graphs; returns edges scanned."""
+    return int(lib().ora_sssp_dijkstra_bounded(V, off_ptr, pairs_ptr, src, max_edges,
+                                               out.ctypes.data_as(_P)))
+
+
+def sssp_frontier(off, pairs, src):
+    off, pairs, V = _csr(off, pairs)
+    out = np.empty(V, np.uint32)
+    rounds = lib().ora_sssp_frontier(V, _p(off), _p(pairs), src, _p(out))
+    return out, rounds
+
+
+def pr_cpu(off, col, outdeg):
+    off, col, V = _csr(off, col)
+    od = np.ascontiguousarray(outdeg, dtype=np.uint32)
+    out = np.empty(V, np.float64)
+    rounds = lib().ora_pr_cpu(V, _p(off), _p(col), _p(od), _p(out))
+    return out, rounds
+
+
+def pr_onegraph(off, col, outdeg, thresh=0.001, max_rounds=1 << 30):
+    off, col, V = _csr(off, col)
+    od = np.ascontiguousarray(outdeg, dtype=np.uint32)
+    out = np.empty(V, np.float64)
+    rounds = lib().ora_pr_onegraph(V, _p(off), _p(col), _p(od), thresh, max_rounds, _p(out))
+    return out, rounds
+
+
+def pr_l1(off, col, outdeg, damping=0.85, tol=1e-6, max_iter=1000):
+    off, col, V = _csr(off, col)
+    od = np.ascontiguousarray(outdeg, dtype=np.uint32)
+    out = np.empty(V, np.float64)
+    l1 = C.c_double()
+    it = lib().ora_pr_l1(V, _p(off), _p(col), _p(od), damping, tol, max_iter, _p(out), C.byref(l1))
+    return out, it, l1.value
+
+
+def normalise_bfs(depth, V):
+    """Maps OneGraph's unreached value V+1 (GraphMeta.h:378) to cpu_BFS's
+    0xFFFFFFFF (BFS/cpu_BFS/main.cpp:141)."""
+    d = np.array(depth, dtype=np.uint32, copy=True)
+    d[d == np.uint32(V + 1)] = np.uint32(0xFFFFFFFF)
+    return d

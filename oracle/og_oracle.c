@@ -1,0 +1,300 @@
+/*
+ * og_oracle.c — CPU restatement of OneGraph's BFS / SSSP / CC / PageRank
+ * (test infrastructure only: the checker for libog.so, never the product).
+ * Each function cites the reference lines it restates; declarations and the
+ * parity pins are described in og_oracle.h.
+ *
+ * Deliberate widening: the reference walks edges with 32-bit indices
+ * (e.g. BFS/cpu_BFS/main.cpp:168,171 `uint edgeIndex`), which wraps for
+ * E >= 2^32.  These restatements use 64-bit edge indices; for every graph with
+ * E < 2^32 the results are identical.
+ */
+#include "og_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define INF32 0xFFFFFFFFu
+
+/* BFS/cpu_BFS/main.cpp:114-209 */
+int ora_bfs(uint32_t V, const uint64_t *off, const uint32_t *col, uint32_t src,
+            uint32_t *out) {
+  unsigned char *active = (unsigned char *)calloc(V ? V : 1, 1);
+  unsigned char *next = (unsigned char *)calloc(V ? V : 1, 1);
+  int rounds = 0;
+  for (uint32_t i = 0; i < V; i++) out[i] = INF32;
+  if (src >= V) goto done;
+  active[src] = 1;
+  out[src] = 1;
+  for (uint32_t n_active = 1; n_active > 0;) {
+    for (uint32_t u = 0; u < V; u++) {
+      if (!active[u]) continue;
+      const uint32_t cand = out[u] + 1;
+      for (uint64_t e = off[u]; e < off[u + 1]; e++) {
+        const uint32_t v = col[e];
+        if (cand < out[v]) {
+          out[v] = cand;
+          next[v] = 1;
+        }
+      }
+    }
+    n_active = 0;
+    for (uint32_t i = 0; i < V; i++) {
+      active[i] = next[i];
+      n_active += next[i];
+      next[i] = 0;
+    }
+    rounds++;
+  }
+done:
+  free(active);
+  free(next);
+  return rounds;
+}
+
+/* CC/serial/serial.cpp:154-213 */
+int ora_cc(uint32_t V, const uint64_t *off, const uint32_t *col, uint32_t *out) {
+  unsigned char *active = (unsigned char *)malloc(V ? V : 1);
+  unsigned char *next = (unsigned char *)calloc(V ? V : 1, 1);
+  int rounds = 0;
+  for (uint32_t i = 0; i < V; i++) {
+    out[i] = i;
+    active[i] = 1;
+  }
+  for (uint32_t n_active = V; n_active > 0;) {
+    for (uint32_t u = 0; u < V; u++) {
+      if (!active[u]) continue;
+      const uint32_t label = out[u];
+      for (uint64_t e = off[u]; e < off[u + 1]; e++) {
+        const uint32_t v = col[e];
+        if (label < out[v]) {
+          out[v] = label;
+          next[v] = 1;
+        }
+      }
+    }
+    n_active = 0;
+    for (uint32_t i = 0; i < V; i++) {
+      active[i] = next[i];
+      n_active += next[i];
+      next[i] = 0;
+    }
+    rounds++;
+  }
+  free(active);
+  free(next);
+  return rounds;
+}
+
+/* ---- binary min-heap of (distance, vertex) with lazy deletion ---- */
+typedef struct {
+  uint64_t key;
+  uint32_t v;
+} heap_item;
+
+typedef struct {
+  heap_item *a;
+  size_t n, cap;
+} heap;
+
+static void heap_push(heap *h, uint64_t key, uint32_t v) {
+  if (h->n == h->cap) {
+    h->cap = h->cap ? 2 * h->cap : 1024;
+    h->a = (heap_item *)realloc(h->a, h->cap * sizeof(heap_item));
+  }
+  size_t i = h->n++;
+  while (i > 0) {
+    size_t p = (i - 1) / 2;
+    if (h->a[p].key <= key) break;
+    h->a[i] = h->a[p];
+    i = p;
+  }
+  h->a[i].key = key;
+  h->a[i].v = v;
+}
+
+static heap_item heap_pop(heap *h) {
+  heap_item top = h->a[0];
+  heap_item last = h->a[--h->n];
+  size_t i = 0;
+  for (;;) {
+    size_t c = 2 * i + 1;
+    if (c >= h->n) break;
+    if (c + 1 < h->n && h->a[c + 1].key < h->a[c].key) c++;
+    if (last.key <= h->a[c].key) break;
+    h->a[i] = h->a[c];
+    i = c;
+  }
+  if (h->n) h->a[i] = last;
+  return top;
+}
+
+/* Dijkstra with the conventions of SSSP/oneGraph/GraphMeta.h:376-381 */
+uint64_t ora_sssp_dijkstra_bounded(uint32_t V, const uint64_t *off,
+                                   const uint32_t *edges, uint32_t src,
+                                   uint64_t max_edges, uint32_t *out) {
+  uint64_t scanned = 0;
+  for (uint32_t i = 0; i < V; i++) out[i] = INF32;
+  if (src >= V) return 0;
+  heap h = {0, 0, 0};
+  out[src] = 1;
+  heap_push(&h, 1, src);
+  while (h.n && (max_edges == 0 || scanned < max_edges)) {
+    heap_item it = heap_pop(&h);
+    if (it.key != out[it.v]) continue; /* stale entry */
+    for (uint64_t e = off[it.v]; e < off[it.v + 1]; e++) {
+      const uint32_t v = edges[2 * e];
+      const uint64_t cand = it.key + edges[2 * e + 1];
+      if (cand < out[v]) {
+        out[v] = (uint32_t)cand;
+        heap_push(&h, cand, v);
+      }
+    }
+    scanned += off[it.v + 1] - off[it.v];
+  }
+  free(h.a);
+  return scanned;
+}
+
+void ora_sssp_dijkstra(uint32_t V, const uint64_t *off, const uint32_t *edges,
+                       uint32_t src, uint32_t *out) {
+  ora_sssp_dijkstra_bounded(V, off, edges, src, 0, out);
+}
+
+/* SSSP/usm/sssp_usm.cpp:192-236 */
+int ora_sssp_frontier(uint32_t V, const uint64_t *off, const uint32_t *edges,
+                      uint32_t src, uint32_t *out) {
+  unsigned char *active = (unsigned char *)calloc(V ? V : 1, 1);
+  unsigned char *next = (unsigned char *)calloc(V ? V : 1, 1);
+  int rounds = 0;
+  for (uint32_t i = 0; i < V; i++) out[i] = INF32;
+  if (src >= V) goto done;
+  active[src] = 1;
+  out[src] = 1;
+  for (uint32_t n_active = 1; n_active > 0;) {
+    for (uint32_t u = 0; u < V; u++) {
+      if (!active[u]) continue;
+      const uint32_t du = out[u];
+      for (uint64_t e = off[u]; e < off[u + 1]; e++) {
+        const uint32_t v = edges[2 * e];
+        const uint32_t cand = du + edges[2 * e + 1];
+        if (cand < out[v]) {
+          out[v] = cand;
+          next[v] = 1;
+        }
+      }
+    }
+    n_active = 0;
+    for (uint32_t i = 0; i < V; i++) {
+      active[i] = next[i];
+      n_active += next[i];
+      next[i] = 0;
+    }
+    rounds++;
+  }
+done:
+  free(active);
+  free(next);
+  return rounds;
+}
+
+/* Pull sum over the in-neighbours of v (PR/cpu/pr.cpp:134-143,
+ * PR/OneGraph/gpu_kernels.h:143-155): dangling sources are skipped. */
+static double pull_sum(const uint64_t *off, const uint32_t *col,
+                       const uint32_t *outdeg, const double *val, uint32_t v) {
+  double s = 0.0;
+  for (uint64_t e = off[v]; e < off[v + 1]; e++) {
+    const uint32_t u = col[e];
+    if (outdeg[u]) s += val[u] / outdeg[u];
+  }
+  return s;
+}
+
+/* PR/cpu/pr.cpp:112-124 (pr_init) + 126-165 (pr_cal<double>) */
+int ora_pr_cpu(uint32_t V, const uint64_t *off, const uint32_t *col,
+               const uint32_t *outdeg, double *out) {
+  unsigned char *active = (unsigned char *)malloc(V ? V : 1);
+  double *next = (double *)calloc(V ? V : 1, sizeof(double));
+  int rounds = 0;
+  for (uint32_t i = 0; i < V; i++) {
+    out[i] = 1.0 / V;
+    active[i] = 1;
+  }
+  for (uint32_t n_active = V; n_active > 0;) {
+    for (uint32_t v = 0; v < V; v++)
+      if (active[v]) next[v] = 0.15 + 0.15 * pull_sum(off, col, outdeg, out, v);
+    for (uint32_t v = 0; v < V; v++) {
+      if (!active[v]) continue;
+      const double diff = fabs(next[v] - out[v]);
+      out[v] = next[v];
+      next[v] = 0;
+      if (diff < 0.001) {
+        active[v] = 0;
+        n_active--;
+      }
+    }
+    rounds++;
+  }
+  free(active);
+  free(next);
+  return rounds;
+}
+
+/* PR/OneGraph/GraphMeta.h:354-357, gpu_kernels.h:135-158 and 295-319 */
+int ora_pr_onegraph(uint32_t V, const uint64_t *off, const uint32_t *col,
+                    const uint32_t *outdeg, double thresh, int max_rounds,
+                    double *out) {
+  unsigned char *active = (unsigned char *)malloc(V ? V : 1);
+  double *sum = (double *)calloc(V ? V : 1, sizeof(double));
+  int rounds = 0;
+  for (uint32_t i = 0; i < V; i++) {
+    out[i] = 1.0;
+    active[i] = 1;
+  }
+  for (uint32_t n_active = V; n_active > 0 && rounds < max_rounds;) {
+    for (uint32_t v = 0; v < V; v++)
+      if (active[v]) sum[v] = pull_sum(off, col, outdeg, out, v);
+    n_active = 0;
+    for (uint32_t v = 0; v < V; v++) {
+      if (!active[v]) continue;
+      const double nv = 0.15 + 0.85 * sum[v];
+      const double diff = nv > out[v] ? nv - out[v] : out[v] - nv;
+      sum[v] = 0;
+      if (diff > thresh) {
+        out[v] = nv;
+        n_active++;
+      } else {
+        active[v] = 0;
+      }
+    }
+    rounds++;
+  }
+  free(active);
+  free(sum);
+  return rounds;
+}
+
+/* FP64 precision oracle, formula of PR/usm/pr.cpp:149-187 on the normalised scale */
+int ora_pr_l1(uint32_t V, const uint64_t *off, const uint32_t *col,
+              const uint32_t *outdeg, double damping, double tol, int max_iter,
+              double *out, double *final_l1) {
+  double *next = (double *)malloc((V ? V : 1) * sizeof(double));
+  const double teleport = (1.0 - damping) / V;
+  double l1 = 0.0;
+  int it = 0;
+  for (uint32_t i = 0; i < V; i++) out[i] = 1.0 / V;
+  while (it < max_iter) {
+    l1 = 0.0;
+    for (uint32_t v = 0; v < V; v++) {
+      next[v] = teleport + damping * pull_sum(off, col, outdeg, out, v);
+      l1 += fabs(next[v] - out[v]);
+    }
+    memcpy(out, next, (size_t)V * sizeof(double));
+    it++;
+    if (l1 < tol) break;
+  }
+  if (final_l1) *final_l1 = l1;
+  free(next);
+  return it;
+}

@@ -1,0 +1,203 @@
+"""GPU parity: libog.so's CUDA engine against the oracle and the reference's
+own CPU outputs (tests/golden), through the C ABI, at budgets that keep the
+graph resident, split it into a static prefix plus many dynamic chunks, keep
+almost nothing static, or relax the dynamic region straight from host memory.
+
+Tolerances: BFS depths, SSSP distances and CC labels are compared bit for bit.
+PageRank is FP32 against an FP64 oracle: normalised ranks within 1e-6 max-abs
+(ranks are ~1/V), the reference's un-normalised delta form within 5e-3
+relative (its per-vertex 1e-3 stopping rule bounds the deviation).
+"""
+import numpy as np
+import pytest
+
+import onegraph_gb300 as og
+import oracle
+
+from conftest import golden_names
+
+pytestmark = pytest.mark.gpu
+
+EB = {og.PLAIN: 4, og.WEIGHTED: 8, og.PR: 4}
+
+
+def budget_for(g, edge_slots, flags=0):
+    p = og.plan(g.V, g.E, g.offsets, g.kind, budget=1 << 40, flags=flags)
+    return p["vertex_bytes"] + p["fixed_bytes"] + int(edge_slots) * EB[g.kind]
+
+
+def configs(g, flags=0):
+    """(name, engine kwargs) covering the region layouts."""
+    T = max(int(0.3 * g.E), 3 * 2048)
+    return [
+        ("resident", dict(budget=1 << 30, advisek=1.0)),
+        ("oom", dict(budget=budget_for(g, T, flags), advisek=0.5)),
+        ("tiny_static", dict(budget=budget_for(g, max(int(0.1 * g.E), 3 * 2048), flags), advisek=0.02)),
+        ("direct", dict(budget=budget_for(g, T, flags | og.CFG_DIRECT), advisek=0.5, direct=True)),
+    ]
+
+
+def engine(g, **kw):
+    return og.Engine(g, **kw)
+
+
+def test_bfs_and_cc_match_reference_outputs(golden):
+    for n in golden_names(golden, "bfs"):
+        off, col = golden[n + "/off"], golden[n + "/col"]
+        g = og.Graph.from_arrays(off, col)
+        for cname, kw in configs(g):
+            e = engine(g, **kw)
+            for i, s in enumerate(golden[n + "/bfs_src"]):
+                d = e.bfs(int(s))
+                np.testing.assert_array_equal(oracle.normalise_bfs(d, g.V), golden[n + "/bfs"][i],
+                                              err_msg="%s/%s src %d" % (n, cname, s))
+            lab = e.cc()
+            np.testing.assert_array_equal(lab, golden[n + "/cc"], err_msg="%s/%s cc" % (n, cname))
+            e.close()
+
+
+def test_oom_configs_really_split_the_graph():
+    g = og.Graph.rmat(12, 16)
+    cfg = dict(configs(g))
+    e = engine(g, **cfg["oom"])
+    p = e.plan
+    assert 0 < p["static_edges"] < g.E and p["chunk_edges"] < p["dynamic_edges"]
+    src = int(np.argmax(g.degrees()))
+    e.bfs(src)
+    st = e.stats
+    assert st["chunks"] > st["iterations"]  # several chunks in some round
+    assert st["edges_static"] > 0 and st["edges_dynamic"] > 0
+    assert st["link_bytes"] == 4 * st["edges_dynamic"]
+    # BFS expands every reached vertex exactly once
+    d = e.fetch(og.ALGO_BFS)
+    reached = d != g.V + 1
+    assert st["frontier_sum"] == int((reached & (g.degrees() > 0)).sum())
+    assert st["edges_static"] + st["edges_dynamic"] == int(g.degrees()[reached].sum())
+
+
+@pytest.mark.parametrize("scale,seed", [(10, 3), (13, 4)])
+def test_sssp_matches_dijkstra(scale, seed):
+    g = og.Graph.rmat(scale, 16, seed=seed, weighted=True)
+    off, pairs = np.array(g.offsets), np.array(g.edges)
+    rng = np.random.default_rng(3)
+    srcs = [int(np.argmax(g.degrees()))] + rng.integers(0, g.V, 3).tolist()
+    want = {s: oracle.sssp_dijkstra(off, pairs, s) for s in srcs}
+    for cname, kw in configs(g):
+        e = engine(g, **kw)
+        for s in srcs:
+            np.testing.assert_array_equal(e.sssp(s), want[s], err_msg="%s src %d" % (cname, s))
+        e.close()
+
+
+def test_bfs_cc_on_weighted_graph_ignore_weights():
+    g = og.Graph.rmat(11, 16, weighted=True)
+    off, col = np.array(g.offsets), np.array(g.columns)
+    e = engine(g, **dict(configs(g))["oom"])
+    s = int(np.argmax(g.degrees()))
+    np.testing.assert_array_equal(oracle.normalise_bfs(e.bfs(s), g.V), oracle.bfs(off, col, s)[0])
+    np.testing.assert_array_equal(e.cc(), oracle.cc(off, col)[0])
+
+
+def test_repeated_queries_reset_state():
+    g = og.Graph.rmat(12, 16, weighted=True)
+    e = engine(g, **dict(configs(g))["oom"])
+    a = e.sssp(5)
+    e.bfs(7)
+    e.cc()
+    b = e.sssp(5)
+    np.testing.assert_array_equal(a, b)
+    e.sssp(9, out=False)
+    np.testing.assert_array_equal(e.fetch(og.ALGO_SSSP), oracle.sssp_dijkstra(
+        np.array(g.offsets), np.array(g.edges), 9))
+
+
+def test_full_size_config1_bfs_rmat20():
+    """The resident BFS workload (R-MAT scale 20, highest-degree source) bit-exact."""
+    g = og.Graph.rmat(20, 16)
+    off, col = np.array(g.offsets), np.array(g.columns)
+    s = int(np.argmax(g.degrees()))
+    e = engine(g, budget=1 << 32, advisek=1.0)
+    d = e.bfs(s)
+    want, rounds = oracle.bfs(off, col, s)
+    np.testing.assert_array_equal(oracle.normalise_bfs(d, g.V), want)
+    assert e.stats["iterations"] == rounds  # one round per BFS level, as in runCPUBFS
+
+
+def _pr_graph(scale=11, ef=16):
+    g = og.Graph.rmat(scale, ef, pagerank=True, symmetric=False)
+    return g, np.array(g.offsets), np.array(g.columns), np.array(g.outdeg)
+
+
+def test_pagerank_l1_precision_vs_fp64_oracle():
+    g, off, col, od = _pr_graph()
+    want, it_ref, _ = oracle.pr_l1(off, col, od, 0.85, 1e-6, 200)
+    for cname, kw in configs(g):
+        e = engine(g, **kw)
+        r = e.pr_l1(0.85, 1e-6, 200)
+        err = np.abs(r.astype(np.float64) - want)
+        assert err.max() < 1e-6, (cname, err.max())
+        assert err.sum() < 1e-5, (cname, err.sum())
+        assert e.stats["residual"] < 1e-6
+        assert abs(e.stats["iterations"] - it_ref) <= 2
+        e.close()
+
+
+def test_pagerank_delta_form_vs_reference_semantics():
+    g, off, col, od = _pr_graph()
+    want, rounds = oracle.pr_onegraph(off, col, od, 0.001)
+    for cname, kw in configs(g):
+        e = engine(g, **kw)
+        r = e.pr(0.001)
+        rel = np.abs(r.astype(np.float64) - want) / want
+        assert rel.max() < 5e-3, (cname, rel.max())
+        assert abs(e.stats["iterations"] - rounds) <= 2
+        e.close()
+
+
+def test_pagerank_is_deterministic():
+    g, *_ = _pr_graph(12)
+    e = engine(g, **dict(configs(g))["oom"])
+    a = e.pr_l1(0.85, 1e-7, 50)
+    b = e.pr_l1(0.85, 1e-7, 50)
+    np.testing.assert_array_equal(a.view(np.uint32), b.view(np.uint32))
+
+
+def test_pagerank_on_symmetric_graph_with_cfg_pr():
+    g = og.Graph.rmat(11, 16)
+    off, col = np.array(g.offsets), np.array(g.columns)
+    deg = g.degrees()
+    want, _, _ = oracle.pr_l1(off, col, deg, 0.85, 1e-6, 200)
+    e = og.Engine(g, budget=budget_for(g, max(int(0.3 * g.E), 3 * 2048), og.CFG_PR), advisek=0.5,
+                  pagerank=True)
+    r = e.pr_l1()
+    assert np.abs(r - want).max() < 1e-6
+    with pytest.raises(og.OGError) as ex:
+        og.Engine(g, budget=1 << 28).pr_l1()
+    assert ex.value.status == 9
+
+
+def test_error_paths():
+    g = og.Graph.rmat(8, 8)
+    e = engine(g, budget=1 << 28)
+    with pytest.raises(og.OGError) as ex:
+        e.bfs(g.V)
+    assert ex.value.status == 1
+    with pytest.raises(og.OGError) as ex:
+        e.sssp(0)
+    assert ex.value.status == 9
+    with pytest.raises(og.OGError) as ex:
+        e.fetch(og.ALGO_PR)
+    assert ex.value.status == 8
+    with pytest.raises(og.OGError) as ex:  # budget above the device's memory
+        og.Engine(g, budget=1 << 50)
+    assert ex.value.status == 4
+
+
+def test_gpu_generator_matches_host_generator():
+    for kw in [dict(), dict(weighted=True), dict(pagerank=True, symmetric=False)]:
+        a = og.Graph.rmat(12, 16, **kw)
+        b = og.Graph.rmat(12, 16, on_gpu=True, **kw)
+        np.testing.assert_array_equal(a.offsets, b.offsets)
+        np.testing.assert_array_equal(a.edges, b.edges)
+        if a.outdeg is not None:
+            np.testing.assert_array_equal(a.outdeg, b.outdeg)

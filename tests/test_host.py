@@ -1,0 +1,215 @@
+"""Host-side logic of libog.so that needs no GPU: CSR file format, validation,
+the seeded R-MAT generator, the region planner, findbignode, the exported
+ABI and the CLI's argument handling."""
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+import onegraph_gb300 as og
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def _write(path, header, *arrays):
+    with open(path, "wb") as f:
+        np.asarray(header, np.uint64).tofile(f)
+        for a in arrays:
+            a.tofile(f)
+
+
+def test_abi_exports_every_header_symbol():
+    hdr = open(os.path.join(ROOT, "include", "onegraph.h")).read()
+    declared = set(re.findall(r"^\s*(?:[a-z_ ]+\*?\s*)\b(og_[a-z0-9_]+)\s*\(", hdr, re.M))
+    assert "og_bfs" in declared and "og_engine_create" in declared
+    lib = og.lib()
+    for name in sorted(declared):
+        assert hasattr(lib, name), name
+    bound = {n for n, _, _ in og.SIGNATURES}
+    assert declared <= bound, declared - bound
+    assert lib.og_abi_version() == 1
+
+
+def test_csr_roundtrip_all_kinds(tmp_path):
+    for kind, kw in [(og.PLAIN, {}), (og.WEIGHTED, {"weighted": True}),
+                     (og.PR, {"pagerank": True, "symmetric": False})]:
+        g = og.Graph.rmat(8, 8, **kw)
+        p = str(tmp_path / ("g%d.csr" % kind))
+        g.save(p)
+        h = og.Graph.load(p, kind)
+        assert (h.V, h.E, h.kind) == (g.V, g.E, kind)
+        np.testing.assert_array_equal(h.offsets, g.offsets)
+        np.testing.assert_array_equal(h.edges, g.edges)
+        if kind == og.PR:
+            np.testing.assert_array_equal(h.outdeg, g.outdeg)
+        # file layout: V, E, [outdeg], offsets[V] (no sentinel), edges
+        raw = np.fromfile(p, np.uint8)
+        eb = 8 if kind == og.WEIGHTED else 4
+        assert raw.size == 16 + (4 * g.V if kind == og.PR else 0) + 8 * g.V + eb * g.E
+
+
+def test_load_rejects_malformed_files(tmp_path):
+    p = str(tmp_path / "bad.csr")
+    with pytest.raises(og.OGError) as e:
+        og.Graph.load(str(tmp_path / "missing.csr"))
+    assert e.value.status == 2
+    open(p, "wb").write(b"\x01\x02")
+    with pytest.raises(og.OGError) as e:
+        og.Graph.load(p)
+    assert e.value.status == 3  # short header
+    _write(p, [3, 4], np.array([0, 2, 1], np.uint64), np.array([1, 2, 0, 1], np.uint32))
+    with pytest.raises(og.OGError) as e:
+        og.Graph.load(p)
+    assert e.value.status == 3 and "decrease" in str(e.value)
+    _write(p, [3, 4], np.array([0, 2, 3], np.uint64), np.array([1, 2, 0, 7], np.uint32))
+    with pytest.raises(og.OGError) as e:
+        og.Graph.load(p)
+    assert "column" in str(e.value)
+    _write(p, [3, 5], np.array([0, 2, 3], np.uint64), np.array([1, 2, 0, 1], np.uint32))
+    with pytest.raises(og.OGError) as e:  # header says 5 edges, file has 4
+        og.Graph.load(p)
+    assert e.value.status == 3
+    _write(p, [0, 0])
+    with pytest.raises(og.OGError):
+        og.Graph.load(p)
+    _write(p, [1 << 33, 0])
+    with pytest.raises(og.OGError):  # V must fit the reference's 32-bit vertex ids
+        og.Graph.load(p)
+
+
+def test_rmat_properties_and_determinism():
+    g = og.Graph.rmat(10, 16, seed=1)
+    h = og.Graph.rmat(10, 16, seed=1, threads=1)
+    np.testing.assert_array_equal(g.offsets, h.offsets)
+    np.testing.assert_array_equal(g.columns, h.columns)
+    off = g.offsets.astype(np.int64)
+    rows = np.repeat(np.arange(g.V), np.diff(off))
+    col = g.columns.astype(np.int64)
+    assert (rows != col).all()
+    key = (rows << 32) | col
+    assert (np.diff(key) > 0).all()  # sorted rows and columns, no duplicates
+    rev = np.sort((col << 32) | rows)
+    np.testing.assert_array_equal(rev, key)  # symmetric
+    assert og.Graph.rmat(10, 16, seed=2).E != g.E
+    w = og.Graph.rmat(10, 16, seed=1, weighted=True)
+    np.testing.assert_array_equal(w.edges[:, 0], g.columns)
+    ww = w.edges[:, 1]
+    assert ww.min() >= 1 and ww.max() <= 64
+    # weight of {u, v} is the same in both directions
+    wmap = dict(zip(((rows << 32) | col).tolist(), ww.tolist()))
+    assert all(wmap[(c << 32) | r] == x for r, c, x in zip(rows[:500], col[:500], ww[:500]))
+
+
+def test_rmat_pagerank_graph_is_in_edge_csr():
+    g = og.Graph.rmat(9, 8, pagerank=True, symmetric=False)
+    assert g.kind == og.PR
+    off = g.offsets.astype(np.int64)
+    dst = np.repeat(np.arange(g.V), np.diff(off))
+    outdeg = np.bincount(g.columns, minlength=g.V)
+    np.testing.assert_array_equal(outdeg, g.outdeg)
+    assert (dst != g.columns).all()
+
+
+def test_rmat_rejects_bad_parameters():
+    with pytest.raises(og.OGError):
+        og.Graph.rmat(0)
+    with pytest.raises(og.OGError):
+        og.Graph.rmat(8, abc=(0.7, 0.3, 0.3))
+    with pytest.raises(og.OGError):
+        og.Graph.rmat(8, weighted=True, pagerank=True)
+
+
+def test_findbignode_matches_reference_rule():
+    g = og.Graph.rmat(12, 16, permute=False)
+    deg = np.diff(g.offsets.astype(np.int64))
+    last = 0
+    for _ in range(5):
+        nxt = g.findbignode(last)
+        cand = [i for i in range(last + 1, g.V - 1) if deg[i] > 3000]
+        assert nxt == (cand[0] if cand else last)
+        last = nxt
+
+
+def test_planner_reference_semantics():
+    g = og.Graph.rmat(10, 16)
+    off = np.array(g.offsets)
+    base = og.plan(g.V, g.E, off, og.PLAIN, budget=1 << 30)
+    # huge budget: heuristic (10 - E/T)/9 > 1 -> 1.0, everything static
+    assert base["advisek"] == 1.0 and base["dynamic_edges"] == 0 and base["chunk_edges"] == 0
+    vb, fb = base["vertex_bytes"], base["fixed_bytes"]
+    T = g.E // 2
+    p = og.plan(g.V, g.E, off, og.PLAIN, budget=vb + fb + 4 * T, advisek=0.5)
+    assert p["edge_capacity"] == T
+    assert p["max_partition"] == int(0.5 * T)
+    Vs = p["static_vertices"]
+    # the static region is the largest vertex prefix whose edges fit the partition
+    assert off[Vs] <= p["max_partition"] < off[Vs + 1]
+    assert p["static_edges"] == off[Vs] and p["dynamic_edges"] == g.E - off[Vs]
+    assert p["chunk_edges"] % 2048 == 0 and p["chunk_edges"] > 0
+    assert p["static_edges"] + 2 * p["chunk_edges"] <= T
+    # heuristic: E/T = 2 -> (10 - 2)/9
+    q = og.plan(g.V, g.E, off, og.PLAIN, budget=vb + fb + 4 * T)
+    assert abs(q["advisek_auto"] - 8 / 9) < 1e-6 and abs(q["advisek"] - 8 / 9) < 1e-6
+    # E/T > 10 -> negative -> 0.5
+    big = og.Graph.rmat(13, 16)
+    boff = np.array(big.offsets)
+    bb = og.plan(big.V, big.E, boff, og.PLAIN, budget=1 << 30)
+    r = og.plan(big.V, big.E, boff, og.PLAIN,
+                budget=bb["vertex_bytes"] + bb["fixed_bytes"] + 4 * (big.E // 12))
+    assert r["advisek_auto"] == 0.5 and r["static_edges"] <= r["max_partition"]
+    # too small for even two staging tiles
+    with pytest.raises(og.OGError) as e:
+        og.plan(g.V, g.E, off, og.PLAIN, budget=vb + fb + 4 * 3000)
+    assert e.value.status == 4
+    # user value above 1 is clamped
+    s = og.plan(g.V, g.E, off, og.PLAIN, budget=vb + fb + 4 * T, advisek=3.0)
+    assert s["advisek"] == 1.0
+    # direct mode needs no staging
+    d = og.plan(g.V, g.E, off, og.PLAIN, budget=vb + fb + 4 * T, advisek=0.5, flags=og.CFG_DIRECT)
+    assert d["chunk_edges"] == 0 and d["dynamic_edges"] > 0
+
+
+def test_planner_budget_errors_and_weighted_edges():
+    g = og.Graph.rmat(10, 16, weighted=True)
+    off = np.array(g.offsets)
+    with pytest.raises(og.OGError) as e:
+        og.plan(g.V, g.E, off, og.WEIGHTED, budget=1000)
+    assert e.value.status == 4
+    p = og.plan(g.V, g.E, off, og.WEIGHTED, budget=1 << 30)
+    assert p["edge_bytes"] == 8
+    pr = og.plan(g.V, g.E, off, og.WEIGHTED, budget=1 << 30, flags=og.CFG_PR)
+    assert pr["vertex_bytes"] > p["vertex_bytes"]
+    # an advisek of 1.0 that leaves no staging room shrinks the static prefix
+    T = g.E // 3
+    q = og.plan(g.V, g.E, off, og.WEIGHTED, budget=p["vertex_bytes"] + p["fixed_bytes"] + 8 * T,
+                advisek=1.0)
+    assert q["chunk_edges"] >= 2048 and q["static_edges"] + 2 * q["chunk_edges"] <= T
+
+
+def test_default_budget_is_reference_12GiB():
+    g = og.Graph.rmat(8, 4)
+    p = og.plan(g.V, g.E, g.offsets, og.PLAIN)
+    assert p["budget_bytes"] == 12 << 30
+
+
+def _cli(name):
+    return os.path.join(og.BIN_DIR, name)
+
+
+def test_cli_argument_errors(tmp_path):
+    for name in ["BFS_OneGraph", "SSSP_OneGraph", "CC_OneGraph", "PR_OneGraph"]:
+        assert os.access(_cli(name), os.X_OK)
+    r = subprocess.run([_cli("BFS_OneGraph")], capture_output=True, text=True)
+    assert r.returncode == 2 and "usage" in r.stderr
+    g = og.Graph.rmat(6, 4)
+    p = str(tmp_path / "g.csr")
+    g.save(p)
+    r = subprocess.run([_cli("BFS_OneGraph"), "--type", "sssp", "-f", p], capture_output=True, text=True)
+    assert r.returncode == 2 and "not this program" in r.stderr
+    r = subprocess.run([_cli("SSSP_OneGraph"), "-type", "cc", "-f", p], capture_output=True, text=True)
+    assert r.returncode == 2
+    r = subprocess.run([_cli("CC_OneGraph"), "-f", str(tmp_path / "nope.csr")], capture_output=True,
+                       text=True)
+    assert r.returncode == 1 and "og_graph_load" in r.stderr

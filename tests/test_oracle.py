@@ -1,0 +1,110 @@
+"""The CPU oracle pinned against the reference's own CPU programs.
+
+tests/golden/golden.npz holds outputs of BFS/cpu_BFS (runCPUBFS),
+CC/serial and PR/cpu compiled from the reference sources
+(tests/golden/make_golden.py).  The restatement must match them bit for bit.
+"""
+import numpy as np
+import pytest
+
+import oracle
+
+from conftest import golden_names
+
+
+def test_bfs_matches_reference_cpu_bfs(golden):
+    names = golden_names(golden, "bfs")
+    assert len(names) >= 8
+    for n in names:
+        off, col = golden[n + "/off"], golden[n + "/col"]
+        for i, s in enumerate(golden[n + "/bfs_src"]):
+            got, _ = oracle.bfs(off, col, int(s))
+            np.testing.assert_array_equal(got, golden[n + "/bfs"][i], err_msg="%s src %d" % (n, s))
+
+
+def test_cc_matches_reference_serial_cc(golden):
+    for n in golden_names(golden, "cc"):
+        got, _ = oracle.cc(golden[n + "/off"], golden[n + "/col"])
+        np.testing.assert_array_equal(got, golden[n + "/cc"], err_msg=n)
+
+
+def test_pr_cpu_matches_reference_bit_for_bit(golden):
+    names = golden_names(golden, "pr_cpu")
+    assert names
+    for n in names:
+        got, rounds = oracle.pr_cpu(golden[n + "/off"], golden[n + "/col"], golden[n + "/outdeg"])
+        assert rounds == int(golden[n + "/pr_cpu_rounds"][0])
+        np.testing.assert_array_equal(got.view(np.uint64), golden[n + "/pr_cpu"].view(np.uint64))
+
+
+def test_golden_edge_cases_present(golden):
+    # isolated vertices, vertex 0 without edges, a hub above one LBS tile
+    cc = golden["two_comp_isolated/cc"]
+    assert len(np.unique(cc)) == 5
+    off = golden["vertex0_isolated/off"]
+    assert off[1] == off[0]
+    assert np.diff(golden["hub5000/off"].astype(np.int64)).max() > 4096
+
+
+def _weighted(scale=9, seed=5):
+    import onegraph_gb300 as og
+    g = og.Graph.rmat(scale, 16, seed=seed, weighted=True)
+    return np.array(g.offsets), np.array(g.edges)
+
+
+def test_dijkstra_equals_label_correcting_restatement():
+    off, pairs = _weighted()
+    deg = np.diff(off.astype(np.int64))
+    for s in [0, int(np.argmax(deg)), 100]:
+        d = oracle.sssp_dijkstra(off, pairs, s)
+        f, _ = oracle.sssp_frontier(off, pairs, s)
+        np.testing.assert_array_equal(d, f)
+        assert d[s] == 1
+
+
+def test_dijkstra_certificate():
+    """Every edge satisfies d[v] <= d[u] + w and every reached vertex other than
+    the source has a tight in-edge (exact shortest paths)."""
+    off, pairs = _weighted(10, 9)
+    s = 3
+    d = oracle.sssp_dijkstra(off, pairs, s).astype(np.int64)
+    rows = np.repeat(np.arange(off.size - 1), np.diff(off.astype(np.int64)))
+    u, v, w = rows, pairs[:, 0].astype(np.int64), pairs[:, 1].astype(np.int64)
+    INF = 0xFFFFFFFF
+    reach = d[u] != INF
+    assert (d[v][reach] <= d[u][reach] + w[reach]).all()
+    tight = np.zeros(off.size - 1, bool)
+    tight[v[reach & (d[v] == d[u] + w)]] = True
+    reached = np.nonzero(d != INF)[0]
+    assert all(tight[x] or x == s for x in reached)
+
+
+def test_pr_onegraph_semantics_small():
+    """0.15 + 0.85*sum, start 1.0, a vertex freezes its old rank once |delta| <= thresh."""
+    off = np.array([0, 1, 2, 3], np.uint64)  # 3-cycle of in-edges: 1->0, 2->1, 0->2
+    col = np.array([1, 2, 0], np.uint32)
+    od = np.array([1, 1, 1], np.uint32)
+    r, rounds = oracle.pr_onegraph(off, col, od)
+    np.testing.assert_allclose(r, 1.0)  # fixed point of the un-normalised form
+    assert rounds == 1
+
+
+def test_pr_l1_converges_to_stationary_distribution():
+    import onegraph_gb300 as og
+    g = og.Graph.rmat(9, 8, pagerank=True, symmetric=False)
+    off, col, od = np.array(g.offsets), np.array(g.columns), np.array(g.outdeg)
+    p, it, l1 = oracle.pr_l1(off, col, od, 0.85, 1e-12, 1000)
+    assert l1 < 1e-12 and it < 1000
+    # fixed point check with dense matrices
+    V = g.V
+    M = np.zeros((V, V))
+    rows = np.repeat(np.arange(V), np.diff(off.astype(np.int64)))
+    np.add.at(M, (rows, col), 1.0 / np.maximum(od[col], 1))
+    np.testing.assert_allclose(p, 0.15 / V + 0.85 * M @ p, rtol=0, atol=1e-12)
+
+
+@pytest.mark.parametrize("n", ["bfs", "cc"])
+def test_normalise_bfs_unreached(n):
+    d = np.array([1, 2, 6, 6], np.uint32)
+    out = oracle.normalise_bfs(d, 5)
+    assert out.tolist() == [1, 2, 0xFFFFFFFF, 0xFFFFFFFF]
