@@ -206,6 +206,34 @@ int og_pr_l1(og_engine *e, float *out_rank, double damping, double tol,
  * (V entries: u32 for BFS/SSSP/CC, float for PR). */
 int og_result_fetch(og_engine *e, int algo, void *out);
 
+/* ------------------------------------------------------- kernel launchers */
+
+/* Frontier counts written by og_k_compact (device memory, 16 bytes). */
+typedef struct og_counts {
+  uint32_t n;      /* vertices listed (active and with at least one edge) */
+  uint32_t pad;
+  uint64_t total;  /* sum of their degrees                                */
+} og_counts;
+
+/* The frontier compaction kernel on caller-owned device buffers: the active
+ * vertices of [v_begin, v_end) in the bitmap `bits` that have edges, in
+ * increasing id order, their exclusive u64 degree prefix (out_pref[n] =
+ * total) and the 2048-edge tile map of the edge-balanced expansion.  Replaces
+ * setStaticAndOverloadLabelBool + myReduction + myExclusive_scan +
+ * setStaticActiveNodeArray / setOverloadNodePointerSwap
+ * (BFS/oneGraph_BFS/gpu_kernels.h:243-379) and the flag / scan / queue /
+ * pointer steps of SubgraphGenerator::generate (PR/sbw/subgraph_generator.h:189-234).
+ * bits: ceil(v_end/32) u32 words; off: V+1 u64 offsets with V >= v_end;
+ * out_list: list_cap entries; out_pref: list_cap+1; out_tile: tile_cap
+ * (>= total/2048 + 1); out_counts: one og_counts.  The look-back scratch is
+ * allocated and released inside the call; the call synchronises `stream`
+ * (a cudaStream_t, NULL = legacy default stream) and returns OG_E_DEVICE if a
+ * capacity was too small. */
+int og_k_compact(const uint32_t *bits, uint32_t v_begin, uint32_t v_end,
+                 const uint64_t *off, uint32_t *out_list, uint64_t *out_pref,
+                 uint64_t list_cap, uint32_t *out_tile, uint64_t tile_cap,
+                 og_counts *out_counts, void *stream);
+
 const char *og_last_error(void);
 int og_abi_version(void);
 

@@ -724,6 +724,112 @@ extern "C" int og_result_fetch(og_engine *e, int algo, void *out) {
   return guarded([&]() { return fetch(e, out); });
 }
 
+// ------------------------------------------------------- kernel launchers
+
+namespace {
+
+uint32_t compact_tiles(uint32_t v_begin, uint32_t v_end) {
+  const uint32_t wb = v_begin / 32, we = (uint32_t)(((uint64_t)v_end + 31) / 32);
+  return (we - wb + kWordsPerCompactTile - 1) / kWordsPerCompactTile;
+}
+
+// Launches k_compact over [v_begin, v_end) with the given look-back scratch
+// (already cleared) and error word.
+void compact_launch(const uint32_t *bits, uint32_t v_begin, uint32_t v_end, const uint64_t *off,
+                    uint32_t *list, uint64_t *pref, uint64_t list_cap, uint32_t *tile,
+                    uint64_t tile_cap, Counts *counts, const Lookback &lb, uint32_t *err,
+                    cudaStream_t s) {
+  CompactArgs a;
+  a.bits = bits;
+  a.v_begin = v_begin;
+  a.v_end = v_end;
+  a.w_begin = v_begin / 32;
+  a.w_end = (uint32_t)(((uint64_t)v_end + 31) / 32);
+  a.ntiles = compact_tiles(v_begin, v_end);
+  a.off = off;
+  a.list = list;
+  a.pref = pref;
+  a.tile_first = tile;
+  a.counts = counts;
+  a.lb = lb;
+  a.err = err;
+  a.list_cap = list_cap;
+  a.tile_cap = tile_cap;
+  k_compact<<<a.ntiles, kThreads, 0, s>>>(a);
+}
+
+// Look-back scratch of `ntiles` tiles carved out of one allocation:
+// status[ntiles] + ticket, agg_n, inc_n (u32) and agg_e, inc_e (u64).
+uint64_t lookback_bytes(uint32_t ntiles) {
+  const uint64_t n = ntiles;
+  return 4 * (n + 1) + 8 * n + 8 * n + 4 * n + 4 * n + 64;
+}
+
+Lookback lookback_carve(void *base, uint32_t ntiles) {
+  const uint64_t n = ntiles;
+  char *p = (char *)base;
+  Lookback lb;
+  lb.agg_e = (unsigned long long *)p;
+  lb.inc_e = (unsigned long long *)(p + 8 * n);
+  lb.agg_n = (uint32_t *)(p + 16 * n);
+  lb.inc_n = (uint32_t *)(p + 20 * n);
+  lb.status = (uint32_t *)(p + 24 * n);
+  lb.ticket = lb.status + n;
+  return lb;
+}
+
+int compact_args_ok(const uint32_t *bits, uint32_t v_begin, uint32_t v_end, const uint64_t *off,
+                    uint32_t *out_list, uint64_t *out_pref, uint64_t list_cap, uint32_t *out_tile,
+                    uint64_t tile_cap, og_counts *out_counts) {
+  if (!bits || !off || !out_list || !out_pref || !out_tile || !out_counts)
+    return fail(OG_E_ARG, "og_k_compact: null pointer");
+  if (v_end < v_begin) return fail(OG_E_ARG, "og_k_compact: v_end < v_begin");
+  if (list_cap == 0 || tile_cap == 0) return fail(OG_E_ARG, "og_k_compact: zero capacity");
+  static_assert(sizeof(og_counts) == sizeof(Counts), "og_counts layout");
+  return OG_OK;
+}
+
+int compact_status(uint32_t err) {
+  if (!err) return OG_OK;
+  if (err & kErrLookback) return fail(OG_E_TIMEOUT, "compaction look-back wait gave up");
+  return fail(OG_E_DEVICE, "compaction output capacity too small (flags 0x%x)", err);
+}
+
+}  // namespace
+
+extern "C" int og_k_compact(const uint32_t *bits, uint32_t v_begin, uint32_t v_end,
+                            const uint64_t *off, uint32_t *out_list, uint64_t *out_pref,
+                            uint64_t list_cap, uint32_t *out_tile, uint64_t tile_cap,
+                            og_counts *out_counts, void *stream) {
+  clear_error();
+  RC(compact_args_ok(bits, v_begin, v_end, off, out_list, out_pref, list_cap, out_tile, tile_cap,
+                     out_counts));
+  cudaStream_t s = (cudaStream_t)stream;
+  CK(cudaMemsetAsync(out_counts, 0, sizeof(og_counts), s));
+  CK(cudaMemsetAsync(out_pref, 0, sizeof(uint64_t), s));
+  if (v_end == v_begin) {
+    CK(cudaStreamSynchronize(s));
+    return OG_OK;
+  }
+  const uint32_t nt = compact_tiles(v_begin, v_end);
+  void *scratch = nullptr;
+  CK(cudaMalloc(&scratch, lookback_bytes(nt) + 256));
+  char *err_d = (char *)scratch + lookback_bytes(nt);
+  Lookback lb = lookback_carve(scratch, nt);
+  uint32_t err = 0;
+  cudaError_t ce = cudaMemsetAsync(scratch, 0, lookback_bytes(nt) + 256, s);
+  if (ce == cudaSuccess) {
+    compact_launch(bits, v_begin, v_end, off, out_list, out_pref, list_cap, out_tile, tile_cap,
+                   (Counts *)out_counts, lb, (uint32_t *)err_d, s);
+    ce = cudaGetLastError();
+  }
+  if (ce == cudaSuccess) ce = cudaMemcpyAsync(&err, err_d, 4, cudaMemcpyDeviceToHost, s);
+  if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
+  cudaFree(scratch);
+  if (ce != cudaSuccess) return fail(OG_E_CUDA, "og_k_compact: %s", cudaGetErrorString(ce));
+  return compact_status(err);
+}
+
 extern "C" void og_graph_free(og_graph *g) {
   if (!g) return;
   if (g->registered) cudaHostUnregister(g->edges);
