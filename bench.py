@@ -48,7 +48,9 @@ def parse_args():
     ap.add_argument("--advisek", type=float, default=0.8)
     ap.add_argument("--sources", type=int, default=32)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--direct", type=int, default=0)
+    ap.add_argument("--direct", type=int, default=1,
+                    help="1: relax the dynamic region straight from page-locked host memory "
+                         "(fastest); 0: gather into double-buffered device staging first")
     return ap.parse_args()
 
 

@@ -86,6 +86,8 @@ int og_graph_info(const og_graph *g, uint64_t *V, uint64_t *E, int *kind,
                   const uint64_t **offsets, const void **edges,
                   const uint32_t **outdeg);
 
+/* Destroy every engine created on a graph before freeing the graph: engines
+ * page-lock and read its host arrays. */
 void og_graph_free(og_graph *g);
 
 /* GraphMeta::findbignode (GraphMeta.h:150-165): first vertex after `last`
@@ -152,6 +154,7 @@ typedef struct og_config {
 #define OG_CFG_DIRECT 1u  /* dynamic region relaxed straight from pinned host
                              memory instead of through device staging buffers */
 #define OG_CFG_NO_PIN 2u  /* do not page-lock the host CSR (ATS access only)  */
+#define OG_CFG_BATCH 8u   /* also hold the 3 x u64 per-vertex masks of og_bfs_batch */
 #define OG_CFG_PR 4u      /* also hold PageRank state for a PLAIN/WEIGHTED
                              graph, read as symmetric (in-edges = out-edges,
                              outDegree = degree); implied for OG_GRAPH_PR    */
@@ -171,6 +174,7 @@ typedef struct og_stats {
   double ms_compact;         /* device time of frontier compaction          */
   double residual;           /* PR: last L1 delta; otherwise 0              */
   uint64_t launches;         /* kernels launched for the query              */
+  double ms_gather;          /* device time of the dynamic gather kernels   */
 } og_stats;
 
 /* initGraphHost + getMaxPartitionSize + initGraphDevice
@@ -201,6 +205,18 @@ int og_pr(og_engine *e, float *out_rank, double threshold, int max_rounds,
  * No reference counterpart beyond the pr_cal_cpu formula (PR/usm/pr.cpp:149-187). */
 int og_pr_l1(og_engine *e, float *out_rank, double damping, double tol,
              int max_iter, og_stats *st);
+
+/* Multi-source BFS: up to 64 sources in one level-synchronous pass over
+ * per-vertex 64-bit visited / frontier masks, so every edge read (including
+ * those streamed from host memory) serves all sources.  No reference
+ * counterpart: the reference runs its sources one after another
+ * (CalculateOpt.h:55-209).  Needs OG_CFG_BATCH.  out: n x V depths,
+ * source-major, same convention as og_bfs, or NULL (the depth matrix then
+ * needs n*V*4 device bytes outside the budget, only when out != NULL);
+ * checks: 2n values, {vertices reached, sum of their depths} per source, or
+ * NULL.  Depths are identical to n separate og_bfs calls. */
+int og_bfs_batch(og_engine *e, const uint32_t *srcs, int n, uint32_t *out,
+                 uint64_t *checks, og_stats *st);
 
 /* Copies the last result of the given algorithm from device memory into out
  * (V entries: u32 for BFS/SSSP/CC, float for PR). */

@@ -25,7 +25,7 @@ STATUS = {0: "OG_OK", 1: "OG_E_ARG", 2: "OG_E_IO", 3: "OG_E_FORMAT", 4: "OG_E_BU
 PLAIN, WEIGHTED, PR = 0, 1, 2
 ALGO_BFS, ALGO_SSSP, ALGO_CC, ALGO_PR = 0, 1, 2, 3
 RMAT_SYMMETRIC, RMAT_PERMUTE, RMAT_WEIGHTED, RMAT_PR, RMAT_ON_GPU = 1, 2, 4, 8, 16
-CFG_DIRECT, CFG_NO_PIN, CFG_PR = 1, 2, 4
+CFG_DIRECT, CFG_NO_PIN, CFG_PR, CFG_BATCH = 1, 2, 4, 8
 # R-MAT quadrant probabilities of the benchmark graphs
 RMAT_ABC = (0.57, 0.19, 0.19)
 
@@ -65,7 +65,8 @@ class Stats(C.Structure):
                 ("static_vertices", C.c_uint64), ("edges_static", C.c_uint64),
                 ("edges_dynamic", C.c_uint64), ("link_bytes", C.c_uint64),
                 ("ms_total", C.c_double), ("ms_static", C.c_double), ("ms_dynamic", C.c_double),
-                ("ms_compact", C.c_double), ("residual", C.c_double), ("launches", C.c_uint64)]
+                ("ms_compact", C.c_double), ("residual", C.c_double), ("launches", C.c_uint64),
+                ("ms_gather", C.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -95,6 +96,7 @@ SIGNATURES = [
     ("og_cc", C.c_int, [_P, _P, C.POINTER(Stats)]),
     ("og_pr", C.c_int, [_P, _P, C.c_double, C.c_int, C.POINTER(Stats)]),
     ("og_pr_l1", C.c_int, [_P, _P, C.c_double, C.c_double, C.c_int, C.POINTER(Stats)]),
+    ("og_bfs_batch", C.c_int, [_P, _P, C.c_int, _P, _P, C.POINTER(Stats)]),
     ("og_result_fetch", C.c_int, [_P, C.c_int, _P]),
     ("og_k_compact", C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P, C.c_uint64, _P,
                                C.c_uint64, _P, _P]),
@@ -132,6 +134,8 @@ class Graph:
 
     def __init__(self, handle):
         self._h = handle
+        self._engines = 0          # live engines on this graph
+        self._free_pending = False  # close() asked for while engines were alive
         V, E, kind = C.c_uint64(), C.c_uint64(), C.c_int()
         off, edges, outdeg = _P(), _P(), _P()
         _check(lib().og_graph_info(handle, C.byref(V), C.byref(E), C.byref(kind), C.byref(off),
@@ -209,9 +213,22 @@ class Graph:
         return int(lib().og_graph_findbignode(self._h, last))
 
     def close(self):
-        if self._h:
-            lib().og_graph_free(self._h)
-            self._h = None
+        """Frees the host CSR; deferred until the last engine on it is closed
+        (an engine page-locks and reads the graph's arrays).  Finalisers of a
+        garbage cycle run in no fixed order, so this ordering is enforced here."""
+        if not self._h:
+            return
+        if self._engines > 0:
+            self._free_pending = True
+            return
+        lib().og_graph_free(self._h)
+        self._h = None
+
+    def _engine_closed(self):
+        self._engines -= 1
+        if self._engines == 0 and self._free_pending:
+            self._free_pending = False
+            self.close()
 
     def __del__(self):
         try:
@@ -234,13 +251,14 @@ class Engine:
     """og_engine: a graph planned against a device budget, static prefix resident."""
 
     def __init__(self, graph: Graph, budget: int = 0, advisek: float = 0.0, direct: bool = False,
-                 pagerank: bool = False, no_pin: bool = False, device: int = 0):
+                 pagerank: bool = False, no_pin: bool = False, batch: bool = False, device: int = 0):
         self.graph = graph
         cfg = Config(budget, advisek, (CFG_DIRECT if direct else 0) | (CFG_PR if pagerank else 0) |
-                     (CFG_NO_PIN if no_pin else 0), device)
+                     (CFG_NO_PIN if no_pin else 0) | (CFG_BATCH if batch else 0), device)
         h = _P()
         _check(lib().og_engine_create(graph._h, C.byref(cfg), C.byref(h)), "og_engine_create")
         self._h = h
+        graph._engines += 1
         p = Plan()
         _check(lib().og_engine_plan(h, C.byref(p)), "og_engine_plan")
         self.plan = p.as_dict()
@@ -291,6 +309,19 @@ class Engine:
         self.stats = st.as_dict()
         return o
 
+    def bfs_batch(self, srcs, out=None, checks: bool = True):
+        """Up to 64 BFS sources in one pass.  Returns (depths n x V or None,
+        checks n x 2 {reached, depth sum} or None); out=False skips the depths."""
+        s = np.ascontiguousarray(srcs, dtype=np.uint32)
+        n = s.size
+        o = None if out is False else (np.empty((n, self.graph.V), np.uint32) if out is None else out)
+        ck = np.empty((n, 2), np.uint64) if checks else None
+        st = Stats()
+        _check(lib().og_bfs_batch(self._h, _ptr(s), n, _ptr(o), _ptr(ck), C.byref(st)),
+               "og_bfs_batch")
+        self.stats = st.as_dict()
+        return o, ck
+
     def fetch(self, algo: int, dtype=np.uint32) -> np.ndarray:
         o = np.empty(self.graph.V, dtype)
         _check(lib().og_result_fetch(self._h, algo, _ptr(o)), "og_result_fetch")
@@ -300,6 +331,7 @@ class Engine:
         if getattr(self, "_h", None):
             lib().og_engine_destroy(self._h)
             self._h = None
+            self.graph._engine_closed()
 
     def __del__(self):
         try:

@@ -51,6 +51,7 @@ struct og_engine {
   cudaEvent_t ev_round = nullptr, ev_cs = nullptr, ev_cd = nullptr, ev_dyn_done = nullptr;
   cudaEvent_t ev_gat[2] = {nullptr, nullptr}, ev_rel[2] = {nullptr, nullptr};
   cudaEvent_t t_s0 = nullptr, t_s1 = nullptr, t_d0 = nullptr;
+  std::vector<cudaEvent_t> t_gat;  // start/end pairs around each gather launch
 
   uint64_t *off_d = nullptr;
   void *sedges_d = nullptr;
@@ -75,6 +76,12 @@ struct og_engine {
   uint32_t part_n = 0;
   uint64_t pr_tiles = 0;
 
+  // batched BFS state
+  bool batch_enabled = false;
+  unsigned long long *bmask[3] = {nullptr, nullptr, nullptr};  // visited, cur, next
+  unsigned long long *hist_d = nullptr, *hist_h = nullptr;
+  uint32_t *srcs_d = nullptr;
+
   int last_algo = -1;
   uint64_t launches = 0;  // kernels launched since the query began
   std::vector<void *> dallocs;
@@ -82,6 +89,8 @@ struct og_engine {
 };
 
 namespace {
+
+constexpr int kGatherMult = 2;  // gather tiles of 4096 positions
 
 template <class T>
 int dalloc(og_engine *e, T **p, uint64_t count) {
@@ -110,18 +119,21 @@ void destroy(og_engine *e) {
   if (e->s_gat) cudaStreamSynchronize(e->s_gat);
   for (void *p : e->dallocs) cudaFree(p);
   if (e->counts_h) cudaFreeHost(e->counts_h);
+  if (e->hist_h) cudaFreeHost(e->hist_h);
   if (e->err_h) cudaFreeHost(e->err_h);
   if (e->l1_h) cudaFreeHost(e->l1_h);
   cudaEvent_t evs[] = {e->ev_round, e->ev_cs, e->ev_cd, e->ev_dyn_done, e->ev_gat[0], e->ev_gat[1],
                        e->ev_rel[0], e->ev_rel[1], e->t_s0, e->t_s1, e->t_d0};
   for (auto ev : evs)
     if (ev) cudaEventDestroy(ev);
+  for (auto ev : e->t_gat) cudaEventDestroy(ev);
   if (e->s_main) cudaStreamDestroy(e->s_main);
   if (e->s_dyn) cudaStreamDestroy(e->s_dyn);
   if (e->s_gat) cudaStreamDestroy(e->s_gat);
   if (e->registered && e->g) {
     if (--e->g->registered == 0) cudaHostUnregister(e->g->edges);
   }
+  cudaGetLastError();  // a failure while tearing down is not the next call's error
   delete e;
 }
 
@@ -132,6 +144,7 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
   e->V = g->V;
   e->eb = g->edge_bytes();
   e->pr_enabled = g->kind == OG_GRAPH_PR || (cfg->flags & OG_CFG_PR);
+  e->batch_enabled = (cfg->flags & OG_CFG_BATCH) != 0;
   CK(cudaSetDevice(e->dev));
   CK(cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, e->dev));
   uint32_t pflags = cfg->flags;
@@ -151,6 +164,13 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
   cudaEvent_t *evs[] = {&e->ev_round, &e->ev_cs, &e->ev_cd, &e->ev_dyn_done, &e->ev_gat[0],
                         &e->ev_gat[1], &e->ev_rel[0], &e->ev_rel[1], &e->t_s0, &e->t_s1, &e->t_d0};
   for (auto ev : evs) CK(cudaEventCreate(ev));
+
+  // kernels with more than 48 KB of shared memory opt in once per process
+  CK(cudaFuncSetAttribute(k_gather<uint32_t, kGatherMult>,
+                          cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)gather_smem_bytes<kGatherMult>()));
+  CK(cudaFuncSetAttribute(k_gather<uint2, kGatherMult>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                          (int)gather_smem_bytes<kGatherMult>()));
 
   // host CSR: page-lock so kernels can gather from it over the link
   if (P.dynamic_edges > 0) {
@@ -221,6 +241,12 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
     e->part_n = (uint32_t)e->sms * 8;
     RC(dalloc(e, &e->part_d, e->part_n));
     RC(dalloc(e, &e->l1_d, 1));
+  }
+  if (e->batch_enabled) {
+    for (int i = 0; i < 3; i++) RC(dalloc(e, &e->bmask[i], V + 1));
+    RC(dalloc(e, &e->hist_d, 64));
+    RC(dalloc(e, &e->srcs_d, 64));
+    CK(cudaMallocHost(&e->hist_h, 64 * sizeof(unsigned long long)));
   }
   if (e->dbytes > P.budget_bytes)
     return fail(OG_E_BUDGET, "engine allocated %llu B, above the %llu B budget",
@@ -328,24 +354,42 @@ int launch_relax(og_engine *e, const RoundOps &ro, const LbsArgs &a, const Edge 
 
 template <class Edge>
 int launch_gather(og_engine *e, const LbsArgs &a, Edge *stage, cudaStream_t s) {
-  const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
+  constexpr uint64_t T = (uint64_t)kGatherMult * kTile;
+  const unsigned grid = (unsigned)((a.pos_end - a.pos_begin + T - 1) / T);
   if (grid == 0) return OG_OK;
-  GatherOp<Edge> op{stage, a.pos_begin};
-  k_lbs<Edge, GatherOp<Edge>><<<grid, kThreads, 0, s>>>(a, (const Edge *)e->hedges_d, op);
+  k_gather<Edge, kGatherMult><<<grid, kThreads, gather_smem_bytes<kGatherMult>(), s>>>(
+      a, (const Edge *)e->hedges_d, stage);
   e->launches++;
   return OG_OK;
 }
 
 struct Timing {
   bool pend_s = false, pend_d = false;
+  uint32_t pend_g = 0;  // gather launches whose event pair is still to be read
 };
+
+// Event pair g of the gather timing list, created on first use.
+int gather_events(og_engine *e, uint32_t g, cudaEvent_t *b, cudaEvent_t *en) {
+  while (e->t_gat.size() < 2ull * (g + 1)) {
+    cudaEvent_t ev;
+    CK(cudaEventCreate(&ev));
+    e->t_gat.push_back(ev);
+  }
+  *b = e->t_gat[2 * g];
+  *en = e->t_gat[2 * g + 1];
+  return OG_OK;
+}
 
 void collect_timing(og_engine *e, Timing &t, og_stats *st) {
   float ms;
   if (t.pend_s && cudaEventElapsedTime(&ms, e->t_s0, e->t_s1) == cudaSuccess) st->ms_static += ms;
   if (t.pend_d && cudaEventElapsedTime(&ms, e->t_d0, e->ev_dyn_done) == cudaSuccess)
     st->ms_dynamic += ms;
+  for (uint32_t g = 0; g < t.pend_g; g++)
+    if (cudaEventElapsedTime(&ms, e->t_gat[2 * g], e->t_gat[2 * g + 1]) == cudaSuccess)
+      st->ms_gather += ms;
   t.pend_s = t.pend_d = false;
+  t.pend_g = 0;
 }
 
 // One round's region work given the compaction counts (already on the host).
@@ -373,8 +417,13 @@ int run_regions(og_engine *e, og_stats &st, Timing &tm, StaticFn static_fn, DynF
         const uint64_t b = c * C, en = std::min(b + C, cd.total);
         CK(cudaStreamWaitEvent(e->s_gat, e->ev_cd, 0));
         if (c >= 2) CK(cudaStreamWaitEvent(e->s_gat, e->ev_rel[buf], 0));
+        cudaEvent_t g0, g1;
+        RC(gather_events(e, tm.pend_g, &g0, &g1));
+        CK(cudaEventRecord(g0, e->s_gat));
         RC(launch_gather<Edge>(e, lbs_args(e, 1, b, en, true, e->g->E), (Edge *)e->stage_d[buf],
                                e->s_gat));
+        CK(cudaEventRecord(g1, e->s_gat));
+        tm.pend_g++;
         CK(cudaEventRecord(e->ev_gat[buf], e->s_gat));
         CK(cudaStreamWaitEvent(e->s_dyn, e->ev_gat[buf], 0));
         RC(dyn_fn(lbs_args(e, 1, b, en, false, C), (const Edge *)e->stage_d[buf], e->s_dyn));
@@ -460,6 +509,84 @@ int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
   CK(cudaMemcpy(e->err_h, e->err_d, 4, cudaMemcpyDeviceToHost));
   RC(check_device_error(e));
   e->last_algo = algo;
+  return OG_OK;
+}
+
+// ------------------------------------------------------------------ batched BFS
+
+template <class Edge>
+int run_batch(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *out, uint64_t *checks,
+              og_stats &st) {
+  const uint64_t V = e->V;
+  uint32_t *cur_any = e->bm[0], *next_any = e->bm[1];
+  unsigned long long *visited = e->bmask[0], *cur = e->bmask[1], *next = e->bmask[2];
+  cudaStream_t s = e->s_main;
+  uint32_t *depth_d = nullptr;
+  struct Free {
+    uint32_t *&p;
+    ~Free() {
+      if (p) cudaFree(p);
+    }
+  } free_depth{depth_d};
+  if (out) {
+    CK(cudaMalloc(&depth_d, 4ull * n * V));
+    k_fill_u32<<<grid_for(n * V, e->sms), kThreads, 0, s>>>(depth_d, (uint64_t)n * V, (uint32_t)(V + 1));
+    e->launches++;
+  }
+  std::vector<uint64_t> reached(n, 1), dsum(n, 1);  // each source: itself at depth 1
+  CK(cudaMemsetAsync(e->err_d, 0, 16, s));
+  CK(cudaMemsetAsync(cur_any, 0, 4 * e->nwords, s));
+  CK(cudaMemsetAsync(next_any, 0, 4 * e->nwords, s));
+  for (int i = 0; i < 3; i++) CK(cudaMemsetAsync(e->bmask[i], 0, 8 * (V + 1), s));
+  CK(cudaMemcpyAsync(e->srcs_d, srcs, 4 * n, cudaMemcpyHostToDevice, s));
+  k_batch_init<<<1, 64, 0, s>>>(e->srcs_d, n, visited, cur, cur_any, depth_d, V);
+  e->launches++;
+  CK(cudaGetLastError());
+  Timing tm;
+  for (uint32_t level = 1;; level++) {
+    uint64_t nl = 0;
+    RC(compact_round(e, cur_any, st, tm, &nl));
+    if (nl == 0) break;
+    st.iterations++;
+    st.frontier_sum += nl;
+    st.static_vertices += e->counts_h[0].n;
+    BatchOp op{visited, cur, next, next_any, e->err_d, e->V};
+    auto launch = [&](const LbsArgs &a, const Edge *edges, cudaStream_t ls) {
+      const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
+      if (grid) {
+        k_lbs<Edge, BatchOp><<<grid, kThreads, 0, ls>>>(a, edges, op);
+        e->launches++;
+      }
+      return (int)OG_OK;
+    };
+    auto sfn = [&](const LbsArgs &a) { return launch(a, (const Edge *)e->sedges_d, e->s_main); };
+    RC((run_regions<Edge>(e, st, tm, sfn, launch)));
+    CK(cudaMemsetAsync(e->hist_d, 0, 64 * 8, s));
+    k_batch_level<<<grid_for(e->nwords, e->sms), kThreads, 0, s>>>(next_any, next, e->nwords, n,
+                                                                 e->hist_d, depth_d, V, level + 1);
+    e->launches++;
+    CK(cudaMemcpyAsync(e->hist_h, e->hist_d, 64 * 8, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamWaitEvent(s, e->ev_cd, 0));
+    CK(cudaMemsetAsync(cur_any, 0, 4 * e->nwords, s));
+    CK(cudaMemsetAsync(cur, 0, 8 * (V + 1), s));
+    CK(cudaStreamSynchronize(s));
+    for (uint32_t i = 0; i < n; i++) {
+      reached[i] += e->hist_h[i];
+      dsum[i] += (uint64_t)(level + 1) * e->hist_h[i];
+    }
+    std::swap(cur_any, next_any);
+    std::swap(cur, next);
+    CK(cudaGetLastError());
+  }
+  CK(cudaMemcpy(e->err_h, e->err_d, 4, cudaMemcpyDeviceToHost));
+  RC(check_device_error(e));
+  if (out) CK(cudaMemcpy(out, depth_d, 4ull * n * V, cudaMemcpyDeviceToHost));
+  if (checks)
+    for (uint32_t i = 0; i < n; i++) {
+      checks[2 * i] = reached[i];
+      checks[2 * i + 1] = dsum[i];
+    }
+  e->last_algo = -1;  // the engine's value array holds no single result
   return OG_OK;
 }
 
@@ -618,6 +745,7 @@ int query_common(og_engine *e, int algo, og_stats *st_out, void *out,
   return guarded([&]() -> int {
     clear_error();
     CK(cudaSetDevice(e->dev));
+    cudaGetLastError();  // drop a stale error left by an unrelated earlier call
     og_stats st;
     memset(&st, 0, sizeof st);
     e->launches = 0;
@@ -718,6 +846,30 @@ extern "C" int og_pr_l1(og_engine *e, float *out_rank, double damping, double to
   }, &c);
 }
 
+namespace {
+struct BatchCtx {
+  const uint32_t *srcs;
+  uint32_t n;
+  uint32_t *out;
+  uint64_t *checks;
+};
+}  // namespace
+
+extern "C" int og_bfs_batch(og_engine *e, const uint32_t *srcs, int n, uint32_t *out,
+                            uint64_t *checks, og_stats *st) {
+  if (!e || !srcs) return fail(OG_E_ARG, "og_bfs_batch: null argument");
+  if (n < 1 || n > 64) return fail(OG_E_ARG, "og_bfs_batch: %d sources (1..64)", n);
+  if (!e->batch_enabled) return fail(OG_E_UNSUPPORTED, "engine created without OG_CFG_BATCH");
+  for (int i = 0; i < n; i++)
+    if (srcs[i] >= e->V) return fail(OG_E_ARG, "source %u >= V %u", srcs[i], e->V);
+  BatchCtx c{srcs, (uint32_t)n, out, checks};
+  return query_common(e, OG_ALGO_BFS, st, nullptr, [](og_engine *en, og_stats &s, void *cx) {
+    const BatchCtx &b = *(BatchCtx *)cx;
+    return en->g->kind == OG_GRAPH_WEIGHTED ? run_batch<uint2>(en, b.srcs, b.n, b.out, b.checks, s)
+                                            : run_batch<uint32_t>(en, b.srcs, b.n, b.out, b.checks, s);
+  }, &c);
+}
+
 extern "C" int og_result_fetch(og_engine *e, int algo, void *out) {
   if (!e || !out) return fail(OG_E_ARG, "og_result_fetch: null argument");
   if (e->last_algo != algo) return fail(OG_E_STATE, "no result of algorithm %d on the device", algo);
@@ -804,6 +956,7 @@ extern "C" int og_k_compact(const uint32_t *bits, uint32_t v_begin, uint32_t v_e
   clear_error();
   RC(compact_args_ok(bits, v_begin, v_end, off, out_list, out_pref, list_cap, out_tile, tile_cap,
                      out_counts));
+  cudaGetLastError();  // drop a stale error left by an unrelated earlier call
   cudaStream_t s = (cudaStream_t)stream;
   CK(cudaMemsetAsync(out_counts, 0, sizeof(og_counts), s));
   CK(cudaMemsetAsync(out_pref, 0, sizeof(uint64_t), s));

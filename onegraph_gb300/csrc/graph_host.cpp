@@ -111,17 +111,21 @@ uint64_t engine_vertex_bytes(int kind, uint32_t flags) {
   // sum f32 and outdeg u32.
   uint64_t b = 8 + 4 + 4 + 8;
   if (kind == OG_GRAPH_PR || (flags & OG_CFG_PR)) b += 12;
+  if (flags & OG_CFG_BATCH) b += 24;  // visited, frontier, next u64 masks
   return b;
 }
 
-uint64_t engine_fixed_bytes(uint32_t V, uint64_t E) {
+uint64_t engine_fixed_bytes(uint32_t V, uint64_t E, uint32_t flags) {
   const uint64_t words = ((uint64_t)V + 31) / 32 + 2 * kCompactWords;
   const uint64_t bitmaps = 3 * 4 * words;
   const uint64_t ctiles = words / kCompactWords + 2;
   const uint64_t lookback = 2 * ctiles * 32;           // two scans in flight
   const uint64_t lbs_tiles = (E / kLbsTile + 8) * 16;  // tile maps + PR carries
+  // batched BFS: per-level histogram (1024 x 64 u64), per-CTA scan slots and a
+  // tile map for tiles as small as 1024 positions
+  const uint64_t batch = (flags & OG_CFG_BATCH) ? (1024ull * 64 * 8 + 2048 * 16 + 4 * (E / 1024 + 8)) : 0;
   // 64 KiB covers the counters, the FP64 partials and the 256 B allocation floor
-  return bitmaps + lookback + lbs_tiles + (64u << 10);
+  return bitmaps + lookback + lbs_tiles + batch + (64u << 10);
 }
 
 int plan_compute(uint32_t V, uint64_t E, const uint64_t *off, int kind,
@@ -134,7 +138,7 @@ int plan_compute(uint32_t V, uint64_t E, const uint64_t *off, int kind,
   p.budget_bytes = budget;
   p.edge_bytes = kind == OG_GRAPH_WEIGHTED ? 8 : 4;
   p.vertex_bytes = engine_vertex_bytes(kind, flags) * ((uint64_t)V + 1);
-  p.fixed_bytes = engine_fixed_bytes(V, E);
+  p.fixed_bytes = engine_fixed_bytes(V, E, flags);
   if (budget <= p.vertex_bytes + p.fixed_bytes)
     return fail(OG_E_BUDGET,
                 "budget %llu B cannot hold the per-vertex state (%llu B) and scratch (%llu B)",

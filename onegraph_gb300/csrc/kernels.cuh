@@ -256,16 +256,17 @@ struct LbsArgs {
   uint32_t *err;
 };
 
+template <class Val>
 struct LbsShared {
   uint32_t rs[kTile + 2];      // tile-relative start of each local vertex
   unsigned long long cb[kTile + 1];  // edge index of tile position 0 for the vertex
-  uint32_t val[kTile + 1];     // source value of each local vertex
+  Val val[kTile + 1];          // source value of each local vertex
   unsigned short map[kTile];   // tile position -> local vertex
 };
 
 // Builds the local-vertex tables of tile k; returns the local count (0 on error).
-template <bool kNeedVal, class Op>
-__device__ __forceinline__ uint32_t lbs_setup(const LbsArgs &a, const Op &op, LbsShared &sh,
+template <bool kNeedVal, class Op, class Val>
+__device__ __forceinline__ uint32_t lbs_setup(const LbsArgs &a, const Op &op, LbsShared<Val> &sh,
                                               uint64_t k, uint64_t pos0, uint32_t &i0_out) {
   const uint64_t ntiles_total = (a.total + kTile - 1) / kTile;
   const uint32_t i0 = a.tile_first[k];
@@ -319,7 +320,7 @@ __device__ __forceinline__ uint32_t lbs_setup(const LbsArgs &a, const Op &op, Lb
 
 template <class Edge, class Op>
 __global__ void __launch_bounds__(kThreads) k_lbs(LbsArgs a, const Edge *__restrict__ edges, Op op) {
-  __shared__ LbsShared sh;
+  __shared__ LbsShared<typename Op::Val> sh;
   const uint64_t k = a.pos_begin / kTile + blockIdx.x;
   const uint64_t pos0 = k * kTile;
   if (pos0 >= a.pos_end) return;
@@ -327,20 +328,113 @@ __global__ void __launch_bounds__(kThreads) k_lbs(LbsArgs a, const Edge *__restr
   uint32_t i0;
   const uint32_t nl = lbs_setup<Op::kNeedVal>(a, op, sh, k, pos0, i0);
   if (nl == 0) return;
+  // All eight loads are issued before the first relax, so each thread keeps
+  // eight edge reads in flight (the host-link gather is latency bound).
+  Edge ev[kItems];
+  uint32_t lv[kItems];
+  uint32_t okmask = 0;
 #pragma unroll
   for (int it = 0; it < (int)kItems; it++) {
     const uint32_t x = it * kThreads + threadIdx.x;
-    const uint64_t q = pos0 + x;
-    if (q < pend) {
+    lv[it] = 0;
+    if (pos0 + x < pend) {
       const uint32_t l = sh.map[x];
       const uint64_t idx = sh.cb[l] + x;
-      if (idx >= a.edge_bound) {
+      lv[it] = l;
+      if (idx < a.edge_bound) {
+        ev[it] = edges[idx];
+        okmask |= 1u << it;
+      } else {
         atomicOr(a.err, kErrEdgeIndex);
-        continue;
       }
-      op.relax(edges[idx], Op::kNeedVal ? sh.val[l] : 0u, q);
     }
   }
+#pragma unroll
+  for (int it = 0; it < (int)kItems; it++) {
+    if (okmask & (1u << it))
+      op.relax(ev[it], Op::kNeedVal ? sh.val[lv[it]] : typename Op::Val(0),
+               pos0 + it * kThreads + threadIdx.x);
+  }
+}
+
+template <int MULT>
+constexpr size_t gather_smem_bytes() {
+  return 8 * (MULT * kTile + 1) + 4 * (MULT * kTile + 2) + 2 * (MULT * kTile);
+}
+
+// Dynamic-region gather, specialised: MULT x 2048 positions per CTA (the
+// per-tile setup is amortised over more edges) and no per-vertex value table.
+// Positions of a vertex are contiguous both in the host CSR and in the staging
+// buffer, so this is a segmented copy; reads are coalesced 8-byte (or 4-byte)
+// loads over NVLink-C2C, all ITEMS of a thread issued before the first store.
+template <class Edge, int MULT>
+__global__ void __launch_bounds__(kThreads) k_gather(LbsArgs a, const Edge *__restrict__ src,
+                                                     Edge *__restrict__ stage) {
+  constexpr uint32_t TILE = MULT * kTile;
+  constexpr int ITEMS = TILE / kThreads;
+  // dynamic shared memory (gather_smem_bytes<MULT>() bytes, above the static 48 KB)
+  extern __shared__ __align__(16) unsigned char g_smem[];
+  unsigned long long *cb = (unsigned long long *)g_smem;          // TILE + 1
+  uint32_t *rs = (uint32_t *)(cb + TILE + 1);                      // TILE + 2
+  unsigned short *map = (unsigned short *)(rs + TILE + 2);         // TILE
+  const uint64_t pos0 = a.pos_begin + (uint64_t)blockIdx.x * TILE;
+  if (pos0 >= a.pos_end) return;
+  const uint64_t pend = min(pos0 + TILE, a.pos_end);
+  const uint32_t i0 = a.tile_first[pos0 / kTile];
+  const uint32_t i1 = pend < a.total ? a.tile_first[pend / kTile] : a.n - 1;
+  if (i1 < i0 || i1 - i0 > TILE || i1 >= a.n) {
+    if (threadIdx.x == 0) atomicOr(a.err, kErrTileMap);
+    return;
+  }
+  const uint32_t nl = i1 - i0 + 1;
+  for (uint32_t j = threadIdx.x; j < nl; j += kThreads) {
+    const uint32_t v = a.list[i0 + j];
+    const uint64_t p = a.pref[i0 + j];
+    rs[j] = p > pos0 ? (uint32_t)min(p - pos0, (uint64_t)TILE) : 0u;
+    cb[j] = a.off[v] - p + pos0;
+  }
+  for (uint32_t x = threadIdx.x; x < TILE; x += kThreads) map[x] = 0;
+  __syncthreads();
+  for (uint32_t j = 1 + threadIdx.x; j < nl; j += kThreads)
+    if (rs[j] < TILE) map[rs[j]] = 1;
+  __syncthreads();
+  {
+    uint32_t f[ITEMS], sacc = 0;
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++) {
+      f[i] = map[threadIdx.x * ITEMS + i];
+      sacc += f[i];
+    }
+    uint32_t ex, tot;
+    uint64_t ex64, tot64;
+    block_scan_pair(sacc, 0, ex, ex64, tot, tot64);
+#pragma unroll
+    for (int i = 0; i < ITEMS; i++) {
+      ex += f[i];
+      map[threadIdx.x * ITEMS + i] = (unsigned short)ex;
+    }
+  }
+  __syncthreads();
+  const uint32_t tlen = (uint32_t)(pend - pos0);
+  Edge ev[ITEMS];
+  uint32_t okm = 0;
+#pragma unroll
+  for (int it = 0; it < ITEMS; it++) {
+    const uint32_t x = it * kThreads + threadIdx.x;
+    if (x < tlen) {
+      const uint64_t idx = cb[map[x]] + x;
+      if (idx < a.edge_bound) {
+        ev[it] = src[idx];
+        okm |= 1u << it;
+      } else {
+        atomicOr(a.err, kErrEdgeIndex);
+      }
+    }
+  }
+  Edge *dst = stage + (pos0 - a.stage_base);
+#pragma unroll
+  for (int it = 0; it < ITEMS; it++)
+    if (okm & (1u << it)) dst[it * kThreads + threadIdx.x] = ev[it];
 }
 
 // ------------------------------------------------------------------ ops
@@ -352,6 +446,7 @@ __device__ __forceinline__ uint32_t edge_w(uint2 e) { return e.y; }
 
 // Level-synchronous BFS with a visited bitmap: every vertex is claimed once.
 struct BfsOp {
+  using Val = uint32_t;
   static constexpr bool kNeedVal = false;
   uint32_t *visited, *next, *depth, *err;
   uint32_t V, newdepth;
@@ -375,6 +470,7 @@ struct BfsOp {
 // atomicMin relax shared by SSSP (weighted) and CC (label push).
 template <bool kWeighted>
 struct MinOp {
+  using Val = uint32_t;
   static constexpr bool kNeedVal = true;
   uint32_t *value, *next, *err;
   uint32_t V;
@@ -397,12 +493,84 @@ struct MinOp {
 // page-locked host CSR into a device staging buffer (coalesced on both sides).
 template <class Edge>
 struct GatherOp {
+  using Val = uint32_t;
   static constexpr bool kNeedVal = false;
   Edge *stage;
   uint64_t stage_base;
   __device__ uint32_t src_val(uint32_t) const { return 0; }
   __device__ __forceinline__ void relax(Edge e, uint32_t, uint64_t q) const { stage[q - stage_base] = e; }
 };
+
+// ------------------------------------------------------------------ batched BFS
+
+// Up to 64 BFS sources share one pass: bit s of a vertex's masks belongs to
+// source s.  visited = bits already reached, cur = bits first reached at the
+// current level (frontier), next = bits first reached at the next level.
+// Level-synchronous, so a bit's level is its BFS depth, exactly as a
+// single-source run computes it.
+struct BatchOp {
+  using Val = unsigned long long;
+  static constexpr bool kNeedVal = true;
+  unsigned long long *visited, *cur, *next;
+  uint32_t *next_any;  // bitmap of vertices with next != 0
+  uint32_t *err;
+  uint32_t V;
+  __device__ Val src_val(uint32_t v) const { return __ldcg(cur + v); }
+  template <class Edge>
+  __device__ __forceinline__ void relax(Edge e, Val m, uint64_t) const {
+    const uint32_t v = edge_dst(e);
+    if (v >= V) {
+      atomicOr(err, kErrVertex);
+      return;
+    }
+    Val nb = m & ~__ldcg(visited + v);
+    if (!nb) return;
+    nb &= ~atomicOr(visited + v, nb);
+    if (!nb) return;
+    if (atomicOr(next + v, nb) == 0ull) atomicOr(next_any + (v >> 5), 1u << (v & 31));
+  }
+};
+
+__global__ void k_batch_init(const uint32_t *srcs, uint32_t n, unsigned long long *visited,
+                             unsigned long long *cur, uint32_t *cur_any, uint32_t *depth,
+                             uint64_t V) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const uint32_t v = srcs[i];
+  atomicOr(visited + v, 1ull << i);
+  atomicOr(cur + v, 1ull << i);
+  atomicOr(cur_any + (v >> 5), 1u << (v & 31));
+  if (depth) depth[(uint64_t)i * V + v] = 1u;
+}
+
+// Per-source count of the vertices first reached at this level (hist[s]),
+// and, when depth != nullptr, their depth for the n x V output.
+__global__ void __launch_bounds__(kThreads) k_batch_level(const uint32_t *next_any,
+                                                          const unsigned long long *next,
+                                                          uint64_t nwords, uint32_t n,
+                                                          unsigned long long *hist,
+                                                          uint32_t *depth, uint64_t V,
+                                                          uint32_t level) {
+  __shared__ uint32_t s_cnt[64];
+  if (threadIdx.x < 64) s_cnt[threadIdx.x] = 0;
+  __syncthreads();
+  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwords;
+       w += (uint64_t)gridDim.x * blockDim.x) {
+    for (uint32_t bits = next_any[w]; bits; bits &= bits - 1) {
+      const uint64_t v = w * 32 + (__ffs(bits) - 1);
+      if (v >= V) break;
+      for (unsigned long long m = next[v]; m; m &= m - 1) {
+        const uint32_t s = __ffsll((long long)m) - 1;
+        if (s < n) {
+          atomicAdd(&s_cnt[s], 1u);
+          if (depth) depth[(uint64_t)s * V + v] = level;
+        }
+      }
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 64 && s_cnt[threadIdx.x]) atomicAdd(hist + threadIdx.x, (unsigned long long)s_cnt[threadIdx.x]);
+}
 
 // ------------------------------------------------------------------ PageRank
 
@@ -424,7 +592,7 @@ struct PrArgs {
 template <class Edge>
 __global__ void __launch_bounds__(kThreads) k_pr_pull(LbsArgs a, const Edge *__restrict__ edges,
                                                        PrArgs p) {
-  __shared__ LbsShared sh;
+  __shared__ LbsShared<uint32_t> sh;
   __shared__ float s_c[kTile];
   const uint64_t k = a.pos_begin / kTile + blockIdx.x;
   const uint64_t pos0 = k * kTile;

@@ -51,7 +51,7 @@ int plan_compute(uint32_t V, uint64_t E, const uint64_t *off, int kind,
 
 // Per-vertex / fixed device bytes the engine allocates (planner inputs).
 uint64_t engine_vertex_bytes(int kind, uint32_t flags);
-uint64_t engine_fixed_bytes(uint32_t V, uint64_t E);
+uint64_t engine_fixed_bytes(uint32_t V, uint64_t E, uint32_t flags);
 
 constexpr uint32_t kLbsTile = 2048;          // edge positions per LBS tile
 constexpr uint32_t kCompactWords = 256;      // bitmap words per compaction tile

@@ -1,0 +1,72 @@
+"""Batched multi-source BFS: every source's depths must equal a single-source
+og_bfs run bit for bit, in every region layout."""
+import numpy as np
+import pytest
+
+import onegraph_gb300 as og
+import oracle
+
+from test_gpu_engine import budget_for
+
+pytestmark = pytest.mark.gpu
+
+
+def batch_configs(g):
+    flags = og.CFG_BATCH
+    T = max(int(0.3 * g.E), 3 * 2048)
+    return [
+        ("resident", dict(budget=1 << 30, advisek=1.0)),
+        ("oom", dict(budget=budget_for(g, T, flags), advisek=0.5)),
+        ("direct", dict(budget=budget_for(g, T, flags | og.CFG_DIRECT), advisek=0.5, direct=True)),
+    ]
+
+
+@pytest.mark.parametrize("weighted", [False, True])
+def test_batch_equals_single_source(weighted):
+    g = og.Graph.rmat(12, 16, weighted=weighted, seed=7)
+    deg = g.degrees()
+    rng = np.random.default_rng(5)
+    srcs = rng.integers(0, g.V, 64).astype(np.uint32)
+    srcs[0] = np.argmax(deg)
+    srcs[1] = srcs[2]  # duplicate source
+    srcs[3] = np.nonzero(deg == 0)[0][0] if (deg == 0).any() else srcs[3]  # isolated source
+    single = None
+    for cname, kw in batch_configs(g):
+        e = og.Engine(g, batch=True, **kw)
+        if single is None:
+            single = np.stack([e.bfs(int(s)) for s in srcs])
+        depths, checks = e.bfs_batch(srcs)
+        np.testing.assert_array_equal(depths, single, err_msg=cname)
+        reached = single != g.V + 1
+        np.testing.assert_array_equal(checks[:, 0], reached.sum(1))
+        np.testing.assert_array_equal(checks[:, 1], np.where(reached, single, 0).sum(1, dtype=np.uint64))
+        # checks alone (no depth matrix) give the same numbers
+        _, ck2 = e.bfs_batch(srcs, out=False)
+        np.testing.assert_array_equal(ck2, checks)
+        e.close()
+
+
+def test_batch_small_counts_and_oracle():
+    g = og.Graph.rmat(11, 16)
+    off, col = np.array(g.offsets), np.array(g.columns)
+    e = og.Engine(g, batch=True, **dict(batch_configs(g))["oom"])
+    for n in (1, 5, 33):
+        srcs = np.arange(n, dtype=np.uint32) * 7
+        depths, _ = e.bfs_batch(srcs)
+        for i, s in enumerate(srcs):
+            np.testing.assert_array_equal(oracle.normalise_bfs(depths[i], g.V), oracle.bfs(off, col, int(s))[0])
+
+
+def test_batch_errors():
+    g = og.Graph.rmat(8, 8)
+    e = og.Engine(g, budget=1 << 28)
+    with pytest.raises(og.OGError) as ex:
+        e.bfs_batch([1, 2])
+    assert ex.value.status == 9
+    b = og.Engine(g, budget=1 << 28, batch=True)
+    with pytest.raises(og.OGError) as ex:
+        b.bfs_batch(np.zeros(65, np.uint32))
+    assert ex.value.status == 1
+    with pytest.raises(og.OGError) as ex:
+        b.bfs_batch([g.V])
+    assert ex.value.status == 1

@@ -181,6 +181,8 @@ def test_planner_budget_errors_and_weighted_edges():
     assert p["edge_bytes"] == 8
     pr = og.plan(g.V, g.E, off, og.WEIGHTED, budget=1 << 30, flags=og.CFG_PR)
     assert pr["vertex_bytes"] > p["vertex_bytes"]
+    bt = og.plan(g.V, g.E, off, og.WEIGHTED, budget=1 << 30, flags=og.CFG_BATCH)
+    assert bt["vertex_bytes"] == p["vertex_bytes"] + 24 * (g.V + 1)  # three u64 masks
     # an advisek of 1.0 that leaves no staging room shrinks the static prefix
     T = g.E // 3
     q = og.plan(g.V, g.E, off, og.WEIGHTED, budget=p["vertex_bytes"] + p["fixed_bytes"] + 8 * T,
