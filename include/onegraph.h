@@ -250,6 +250,28 @@ int og_k_compact(const uint32_t *bits, uint32_t v_begin, uint32_t v_end,
                  uint64_t list_cap, uint32_t *out_tile, uint64_t tile_cap,
                  og_counts *out_counts, void *stream);
 
+/* og_k_compact without any device allocation.  No counterpart in the
+ * reference: it exists for callers that cannot call cudaMalloc at the point
+ * where they compact a frontier, e.g. a host application that has handed all
+ * device memory to its own pool allocator, a plugin loaded into another
+ * runtime that only allows that runtime's allocator, or a latency-critical
+ * loop that cannot pay for the device synchronisation cudaMalloc/cudaFree
+ * imply.  Same arguments, results and status as og_k_compact; the caller
+ * still passes every input and output buffer.
+ * Scratch: a fixed ~0.9 MB array inside libog.so, present on every device
+ * that loads the library until the process exits.  Limit: one call covers at
+ * most 2^28 vertices (32768 tiles of 8192); larger ranges return OG_E_ARG.
+ * The first call on a device looks up that array's device address, so make it
+ * before any stream capture.  Every call shares the array: calls that overlap
+ * on the GPU (other streams, other host threads) race and must not be issued;
+ * each call clears the part it uses and synchronises `stream` before
+ * returning. */
+int og_k_compact_noalloc(const uint32_t *bits, uint32_t v_begin, uint32_t v_end,
+                         const uint64_t *off, uint32_t *out_list,
+                         uint64_t *out_pref, uint64_t list_cap,
+                         uint32_t *out_tile, uint64_t tile_cap,
+                         og_counts *out_counts, void *stream);
+
 const char *og_last_error(void);
 int og_abi_version(void);
 

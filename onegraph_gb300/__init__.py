@@ -100,6 +100,8 @@ SIGNATURES = [
     ("og_result_fetch", C.c_int, [_P, C.c_int, _P]),
     ("og_k_compact", C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P, C.c_uint64, _P,
                                C.c_uint64, _P, _P]),
+    ("og_k_compact_noalloc", C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P, C.c_uint64, _P,
+                                       C.c_uint64, _P, _P]),
     ("og_last_error", C.c_char_p, []),
     ("og_abi_version", C.c_int, []),
 ]

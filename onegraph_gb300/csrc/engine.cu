@@ -13,6 +13,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -980,6 +981,81 @@ extern "C" int og_k_compact(const uint32_t *bits, uint32_t v_begin, uint32_t v_e
   if (ce == cudaSuccess) ce = cudaStreamSynchronize(s);
   cudaFree(scratch);
   if (ce != cudaSuccess) return fail(OG_E_CUDA, "og_k_compact: %s", cudaGetErrorString(ce));
+  return compact_status(err);
+}
+
+// ------------------------------------------------ allocation-free variant
+//
+// og_k_compact_noalloc runs the same compaction with its look-back scratch in
+// a fixed array that is part of the loaded library instead of memory it asks
+// the driver for.  Limit: kNoAllocTiles compaction tiles of 8192 vertices,
+// i.e. a range of at most 2^28 vertices per call.  The array lives on every
+// device that loads the library, for as long as the process runs.
+
+namespace {
+
+constexpr uint32_t kNoAllocTiles = 32768;
+constexpr uint64_t kNoAllocErrOffset = 4 * (kNoAllocTiles + 1ull) + 24ull * kNoAllocTiles + 64;
+constexpr uint64_t kNoAllocBytes = kNoAllocErrOffset + 256;
+
+static __device__ __align__(256) unsigned char g_compact_scratch[kNoAllocBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_scratch_mu;
+void *g_scratch_addr[kMaxDevices] = {};
+
+// Device address of g_compact_scratch on the current device.  Host code may
+// not use the symbol itself: on the host it names a stand-in, not device
+// memory.  Looked up once per device, the first time that device calls.
+int scratch_address(void **out) {
+  int dev = 0;
+  CK(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= kMaxDevices) return fail(OG_E_UNSUPPORTED, "device ordinal %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_scratch_mu);
+  if (!g_scratch_addr[dev]) {
+    void *p = nullptr;
+    CK(cudaGetSymbolAddress(&p, g_compact_scratch));
+    g_scratch_addr[dev] = p;
+  }
+  *out = g_scratch_addr[dev];
+  return OG_OK;
+}
+
+}  // namespace
+
+extern "C" int og_k_compact_noalloc(const uint32_t *bits, uint32_t v_begin, uint32_t v_end,
+                                    const uint64_t *off, uint32_t *out_list, uint64_t *out_pref,
+                                    uint64_t list_cap, uint32_t *out_tile, uint64_t tile_cap,
+                                    og_counts *out_counts, void *stream) {
+  clear_error();
+  RC(compact_args_ok(bits, v_begin, v_end, off, out_list, out_pref, list_cap, out_tile, tile_cap,
+                     out_counts));
+  const uint32_t nt = v_end > v_begin ? compact_tiles(v_begin, v_end) : 0;
+  if (nt > kNoAllocTiles)
+    return fail(OG_E_ARG,
+                "og_k_compact_noalloc: range of %u vertices needs %u scratch tiles, the fixed "
+                "scratch holds %u (at most 2^28 vertices per call)",
+                v_end - v_begin, nt, kNoAllocTiles);
+  void *base = nullptr;
+  RC(scratch_address(&base));
+  cudaGetLastError();  // drop a stale error left by an unrelated earlier call
+  cudaStream_t s = (cudaStream_t)stream;
+  CK(cudaMemsetAsync(out_counts, 0, sizeof(og_counts), s));
+  CK(cudaMemsetAsync(out_pref, 0, sizeof(uint64_t), s));
+  if (nt == 0) {
+    CK(cudaStreamSynchronize(s));
+    return OG_OK;
+  }
+  // the previous call's look-back state and error word must not leak in
+  uint32_t *err_d = (uint32_t *)((char *)base + kNoAllocErrOffset);
+  CK(cudaMemsetAsync(base, 0, lookback_bytes(nt), s));
+  CK(cudaMemsetAsync(err_d, 0, sizeof(uint32_t), s));
+  compact_launch(bits, v_begin, v_end, off, out_list, out_pref, list_cap, out_tile, tile_cap,
+                 (Counts *)out_counts, lookback_carve(base, nt), err_d, s);
+  CK(cudaGetLastError());
+  uint32_t err = 0;
+  CK(cudaMemcpyAsync(&err, err_d, sizeof err, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
   return compact_status(err);
 }
 
