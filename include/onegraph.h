@@ -155,6 +155,9 @@ typedef struct og_config {
                              memory instead of through device staging buffers */
 #define OG_CFG_NO_PIN 2u  /* do not page-lock the host CSR (ATS access only)  */
 #define OG_CFG_BATCH 8u   /* also hold the 3 x u64 per-vertex masks of og_bfs_batch */
+#define OG_CFG_BATCH_LEVELS 16u /* og_bfs_batch drives levels from the host (one
+                                   kernel sequence per level) instead of the
+                                   persistent cooperative kernel */
 #define OG_CFG_PR 4u      /* also hold PageRank state for a PLAIN/WEIGHTED
                              graph, read as symmetric (in-edges = out-edges,
                              outDegree = degree); implied for OG_GRAPH_PR    */
@@ -217,6 +220,28 @@ int og_pr_l1(og_engine *e, float *out_rank, double damping, double tol,
  * NULL.  Depths are identical to n separate og_bfs calls. */
 int og_bfs_batch(og_engine *e, const uint32_t *srcs, int n, uint32_t *out,
                  uint64_t *checks, og_stats *st);
+/* og_bfs_batch runs all levels in one persistent cooperative kernel (static
+ * edges from HBM, dynamic edges read straight from page-locked host memory);
+ * with out == NULL the whole batch is captured once as a CUDA graph and
+ * replayed (og_stats.chunks == 1 reports a replay).  The persistent kernel
+ * has candidate (CTA size, edges per thread) configurations; the tile they
+ * span is also where high-degree vertices are split. */
+typedef struct og_tune_result {
+  int configs;      /* candidates timed                          */
+  int best;         /* index of the fastest                      */
+  int block[8];     /* CTA size of each candidate                */
+  int items[8];     /* edge positions per thread of each         */
+  float ms[8];      /* best kernel time of each (ms)             */
+} og_tune_result;
+
+/* Autotuner: times every candidate on this engine and these sources (reps
+ * timed runs each after one warm-up run) and keeps the fastest for later
+ * og_bfs_batch calls. */
+int og_bfs_batch_tune(og_engine *e, const uint32_t *srcs, int n, int reps,
+                      og_tune_result *res);
+
+/* Selects a candidate directly (-1 = default), e.g. from a saved tuning. */
+int og_bfs_batch_set_config(og_engine *e, int config);
 
 /* Copies the last result of the given algorithm from device memory into out
  * (V entries: u32 for BFS/SSSP/CC, float for PR). */

@@ -25,7 +25,7 @@ STATUS = {0: "OG_OK", 1: "OG_E_ARG", 2: "OG_E_IO", 3: "OG_E_FORMAT", 4: "OG_E_BU
 PLAIN, WEIGHTED, PR = 0, 1, 2
 ALGO_BFS, ALGO_SSSP, ALGO_CC, ALGO_PR = 0, 1, 2, 3
 RMAT_SYMMETRIC, RMAT_PERMUTE, RMAT_WEIGHTED, RMAT_PR, RMAT_ON_GPU = 1, 2, 4, 8, 16
-CFG_DIRECT, CFG_NO_PIN, CFG_PR, CFG_BATCH = 1, 2, 4, 8
+CFG_DIRECT, CFG_NO_PIN, CFG_PR, CFG_BATCH, CFG_BATCH_LEVELS = 1, 2, 4, 8, 16
 # R-MAT quadrant probabilities of the benchmark graphs
 RMAT_ABC = (0.57, 0.19, 0.19)
 
@@ -53,6 +53,16 @@ class Plan(C.Structure):
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
+
+
+class TuneResult(C.Structure):
+    _fields_ = [("configs", C.c_int), ("best", C.c_int), ("block", C.c_int * 8),
+                ("items", C.c_int * 8), ("ms", C.c_float * 8)]
+
+    def as_dict(self):
+        n = self.configs
+        return {"best": self.best, "candidates": [
+            {"block": self.block[i], "items": self.items[i], "ms": self.ms[i]} for i in range(n)]}
 
 
 class Config(C.Structure):
@@ -97,6 +107,8 @@ SIGNATURES = [
     ("og_pr", C.c_int, [_P, _P, C.c_double, C.c_int, C.POINTER(Stats)]),
     ("og_pr_l1", C.c_int, [_P, _P, C.c_double, C.c_double, C.c_int, C.POINTER(Stats)]),
     ("og_bfs_batch", C.c_int, [_P, _P, C.c_int, _P, _P, C.POINTER(Stats)]),
+    ("og_bfs_batch_tune", C.c_int, [_P, _P, C.c_int, C.c_int, C.POINTER(TuneResult)]),
+    ("og_bfs_batch_set_config", C.c_int, [_P, C.c_int]),
     ("og_result_fetch", C.c_int, [_P, C.c_int, _P]),
     ("og_k_compact", C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P, C.c_uint64, _P,
                                C.c_uint64, _P, _P]),
@@ -253,10 +265,12 @@ class Engine:
     """og_engine: a graph planned against a device budget, static prefix resident."""
 
     def __init__(self, graph: Graph, budget: int = 0, advisek: float = 0.0, direct: bool = False,
-                 pagerank: bool = False, no_pin: bool = False, batch: bool = False, device: int = 0):
+                 pagerank: bool = False, no_pin: bool = False, batch: bool = False,
+                 batch_levels: bool = False, device: int = 0):
         self.graph = graph
         cfg = Config(budget, advisek, (CFG_DIRECT if direct else 0) | (CFG_PR if pagerank else 0) |
-                     (CFG_NO_PIN if no_pin else 0) | (CFG_BATCH if batch else 0), device)
+                     (CFG_NO_PIN if no_pin else 0) | (CFG_BATCH if batch or batch_levels else 0) |
+                     (CFG_BATCH_LEVELS if batch_levels else 0), device)
         h = _P()
         _check(lib().og_engine_create(graph._h, C.byref(cfg), C.byref(h)), "og_engine_create")
         self._h = h
@@ -323,6 +337,16 @@ class Engine:
                "og_bfs_batch")
         self.stats = st.as_dict()
         return o, ck
+
+    def bfs_batch_tune(self, srcs, reps: int = 2) -> dict:
+        s = np.ascontiguousarray(srcs, dtype=np.uint32)
+        r = TuneResult()
+        _check(lib().og_bfs_batch_tune(self._h, _ptr(s), s.size, reps, C.byref(r)),
+               "og_bfs_batch_tune")
+        return r.as_dict()
+
+    def bfs_batch_set_config(self, config: int):
+        _check(lib().og_bfs_batch_set_config(self._h, config), "og_bfs_batch_set_config")
 
     def fetch(self, algo: int, dtype=np.uint32) -> np.ndarray:
         o = np.empty(self.graph.V, dtype)

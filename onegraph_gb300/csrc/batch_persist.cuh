@@ -9,6 +9,9 @@
 // tile (CTA size x items) is also the split granularity of high-degree
 // vertices.  No reference counterpart: the reference runs sources one by one
 // (BFS/oneGraph_BFS/CalculateOpt.h:55-209).
+// Data written by other CTAs during the launch (list, prefix, tile map,
+// frontier words and masks) is read with __ldcg: L1 is not coherent within a
+// kernel, so a plain load could return a line cached in an earlier level.
 #pragma once
 #include "kernels.cuh"
 
@@ -152,7 +155,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
     uint32_t c = 0;
     uint64_t e = 0, dyn = 0;
     for (uint64_t w = wb; w < we; w++)
-      for (uint32_t m = cur_any[w]; m; m &= m - 1) {
+      for (uint32_t m = __ldcg(cur_any + w); m; m &= m - 1) {
         const uint64_t v = w * 32 + (__ffs(m) - 1);
         const uint64_t d = a.off[v + 1] - a.off[v];
         c += d ? 1u : 0u;
@@ -214,7 +217,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
       uint32_t pos = sh.red_n + exc;
       uint64_t ep = sh.red_e + exe;
       for (uint64_t w = wb; w < we; w++)
-        for (uint32_t m = cur_any[w]; m; m &= m - 1) {
+        for (uint32_t m = __ldcg(cur_any + w); m; m &= m - 1) {
           const uint64_t v = w * 32 + (__ffs(m) - 1);
           const uint64_t d = a.off[v + 1] - a.off[v];
           if (!d) continue;
@@ -232,16 +235,16 @@ __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
     for (uint64_t k = blockIdx.x; k < ntiles; k += gridDim.x) {
       const uint64_t pos0 = k * TILE;
       const uint32_t tlen = (uint32_t)min((uint64_t)TILE, total_e - pos0);
-      const uint32_t i0 = a.tile_first[k];
-      const uint32_t i1 = (k + 1 < ntiles) ? a.tile_first[k + 1] : (uint32_t)(total_n - 1);
+      const uint32_t i0 = __ldcg(a.tile_first + k);
+      const uint32_t i1 = (k + 1 < ntiles) ? __ldcg(a.tile_first + k + 1) : (uint32_t)(total_n - 1);
       const uint32_t nl = i1 - i0 + 1;
       if (i1 < i0 || nl > TILE + 1) {  // uniform per tile
         if (threadIdx.x == 0) atomicOr(a.err, kErrTileMap);
         continue;
       }
       for (uint32_t j = threadIdx.x; j < nl; j += BLOCK) {
-        const uint32_t v = a.list[i0 + j];
-        const uint64_t p = a.pref[i0 + j];
+        const uint32_t v = __ldcg(a.list + i0 + j);
+        const uint64_t p = __ldcg(a.pref + i0 + j);
         sh.rs[j] = p > pos0 ? (uint32_t)min(p - pos0, (uint64_t)TILE) : 0u;
         sh.cb[j] = a.off[v] - p + pos0;
         sh.val[j] = __ldcg(cur + v);
@@ -312,9 +315,9 @@ __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
     if (threadIdx.x < 64) sh.cnt[threadIdx.x] = 0;
     __syncthreads();
     for (uint64_t w = wb; w < we; w++) {
-      for (uint32_t m = next_any[w]; m; m &= m - 1) {
+      for (uint32_t m = __ldcg(next_any + w); m; m &= m - 1) {
         const uint64_t v = w * 32 + (__ffs(m) - 1);
-        for (unsigned long long b = next[v]; b; b &= b - 1) {
+        for (unsigned long long b = __ldcg(next + v); b; b &= b - 1) {
           const uint32_t s = __ffsll((long long)b) - 1;
           if (s < a.n_src) {
             atomicAdd(&sh.cnt[s], 1u);
@@ -322,7 +325,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
           }
         }
       }
-      for (uint32_t m = cur_any[w]; m; m &= m - 1) cur[w * 32 + (__ffs(m) - 1)] = 0ull;
+      for (uint32_t m = __ldcg(cur_any + w); m; m &= m - 1) cur[w * 32 + (__ffs(m) - 1)] = 0ull;
       cur_any[w] = 0u;
     }
     __syncthreads();

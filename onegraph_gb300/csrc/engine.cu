@@ -17,6 +17,7 @@
 #include <new>
 #include <vector>
 
+#include "batch_persist.cuh"
 #include "kernels.cuh"
 #include "og_internal.hpp"
 
@@ -81,7 +82,19 @@ struct og_engine {
   bool batch_enabled = false;
   unsigned long long *bmask[3] = {nullptr, nullptr, nullptr};  // visited, cur, next
   unsigned long long *hist_d = nullptr, *hist_h = nullptr;
-  uint32_t *srcs_d = nullptr;
+  uint32_t *srcs_d = nullptr, *srcs_h = nullptr;
+  // persistent kernel state
+  uint32_t *ptile_d = nullptr;
+  uint64_t ptile_cap = 0;
+  uint32_t *cta_n = nullptr;
+  unsigned long long *cta_e = nullptr;
+  uint32_t *bar_d = nullptr;   // [0..1] barrier, [2] error, [3] levels, [4..11] 4 x u64 stats
+  uint32_t *pmisc_h = nullptr;  // host copy of bar_d
+  int tuned = -1;               // index into kPersistConfigs chosen by the autotuner
+  cudaGraphExec_t graph = nullptr;
+  uint32_t graph_n = 0;
+  int graph_cfg = -1;
+  bool graph_broken = false;
 
   int last_algo = -1;
   uint64_t launches = 0;  // kernels launched since the query began
@@ -92,6 +105,7 @@ struct og_engine {
 namespace {
 
 constexpr int kGatherMult = 2;  // gather tiles of 4096 positions
+constexpr uint32_t kMaxPersistCtas = 2048;
 
 template <class T>
 int dalloc(og_engine *e, T **p, uint64_t count) {
@@ -121,6 +135,9 @@ void destroy(og_engine *e) {
   for (void *p : e->dallocs) cudaFree(p);
   if (e->counts_h) cudaFreeHost(e->counts_h);
   if (e->hist_h) cudaFreeHost(e->hist_h);
+  if (e->srcs_h) cudaFreeHost(e->srcs_h);
+  if (e->pmisc_h) cudaFreeHost(e->pmisc_h);
+  if (e->graph) cudaGraphExecDestroy(e->graph);
   if (e->err_h) cudaFreeHost(e->err_h);
   if (e->l1_h) cudaFreeHost(e->l1_h);
   cudaEvent_t evs[] = {e->ev_round, e->ev_cs, e->ev_cd, e->ev_dyn_done, e->ev_gat[0], e->ev_gat[1],
@@ -203,11 +220,14 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
   e->list_cap[1] = std::max<uint64_t>(V - e->Vs, 1);
   e->tile_cap[0] = P.static_edges / kTile + 2;
   e->tile_cap[1] = P.dynamic_edges / kTile + 2;
-  for (int r = 0; r < 2; r++) {
-    RC(dalloc(e, &e->list_d[r], e->list_cap[r]));
-    RC(dalloc(e, &e->pref_d[r], e->list_cap[r] + 1));
-    RC(dalloc(e, &e->tile_d[r], e->tile_cap[r]));
-  }
+  // one allocation per array, the dynamic region's part after the static one,
+  // so the batched kernel can also use them as a single list over [0, V)
+  RC(dalloc(e, &e->list_d[0], e->list_cap[0] + e->list_cap[1]));
+  RC(dalloc(e, &e->pref_d[0], e->list_cap[0] + e->list_cap[1] + 2));
+  RC(dalloc(e, &e->tile_d[0], e->tile_cap[0] + e->tile_cap[1]));
+  e->list_d[1] = e->list_d[0] + e->list_cap[0];
+  e->pref_d[1] = e->pref_d[0] + e->list_cap[0] + 1;
+  e->tile_d[1] = e->tile_d[0] + e->tile_cap[0];
   e->lb_tiles = (uint32_t)((e->nwords + kWordsPerCompactTile - 1) / kWordsPerCompactTile + 1);
   for (int r = 0; r < 2; r++) {
     RC(dalloc(e, &e->lb[r].status, e->lb_tiles + 1));
@@ -245,9 +265,16 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
   }
   if (e->batch_enabled) {
     for (int i = 0; i < 3; i++) RC(dalloc(e, &e->bmask[i], V + 1));
-    RC(dalloc(e, &e->hist_d, 64));
+    RC(dalloc(e, &e->hist_d, (uint64_t)kMaxBatchLevels * 64));
     RC(dalloc(e, &e->srcs_d, 64));
-    CK(cudaMallocHost(&e->hist_h, 64 * sizeof(unsigned long long)));
+    e->ptile_cap = g->E / 1024 + 8;
+    RC(dalloc(e, &e->ptile_d, e->ptile_cap));
+    RC(dalloc(e, &e->cta_n, kMaxPersistCtas));
+    RC(dalloc(e, &e->cta_e, kMaxPersistCtas));
+    RC(dalloc(e, &e->bar_d, 16));  // barrier (2), error, levels, stats (4 u64)
+    CK(cudaMallocHost(&e->hist_h, (size_t)kMaxBatchLevels * 64 * sizeof(unsigned long long)));
+    CK(cudaMallocHost(&e->srcs_h, 64 * sizeof(uint32_t)));
+    CK(cudaMallocHost(&e->pmisc_h, 16 * sizeof(uint32_t)));
   }
   if (e->dbytes > P.budget_bytes)
     return fail(OG_E_BUDGET, "engine allocated %llu B, above the %llu B budget",
@@ -591,6 +618,190 @@ int run_batch(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *out, uin
   return OG_OK;
 }
 
+// ------------------------------------------------------- persistent batched BFS
+
+struct PersistCfg {
+  int block, items;
+};
+// candidate (CTA size, edge positions per thread); the tile is their product
+constexpr PersistCfg kPersistConfigs[] = {{256, 8}, {128, 8}, {256, 4}, {512, 4}, {128, 16}};
+constexpr int kNumPersistConfigs = 5;
+
+template <class Edge, int B, int I>
+int launch_persist_cfg(og_engine *e, const PersistArgs &a, cudaStream_t s) {
+  auto kern = k_batch_persistent<Edge, B, I>;
+  int occ = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, B, 0));
+  if (occ < 1) return fail(OG_E_UNSUPPORTED, "persistent kernel does not fit an SM");
+  const unsigned grid = (unsigned)std::min<uint64_t>((uint64_t)occ * e->sms, kMaxPersistCtas);
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(B);
+  cfg.dynamicSmemBytes = 0;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeCooperative;  // all CTAs co-resident: the grid barriers rely on it
+  attr[0].val.cooperative = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  CK(cudaLaunchKernelEx(&cfg, kern, a));
+  e->launches++;
+  return OG_OK;
+}
+
+template <class Edge>
+int launch_persist(og_engine *e, int ci, const PersistArgs &a, cudaStream_t s) {
+  switch (ci) {
+    case 0: return launch_persist_cfg<Edge, 256, 8>(e, a, s);
+    case 1: return launch_persist_cfg<Edge, 128, 8>(e, a, s);
+    case 2: return launch_persist_cfg<Edge, 256, 4>(e, a, s);
+    case 3: return launch_persist_cfg<Edge, 512, 4>(e, a, s);
+    default: return launch_persist_cfg<Edge, 128, 16>(e, a, s);
+  }
+}
+
+// Enqueues one whole batch on s_main: clear state, upload the sources from the
+// page-locked buffer, seed, run every level in one cooperative kernel, copy
+// the per-level counts and the status words back to page-locked memory.
+template <class Edge>
+int enqueue_persist(og_engine *e, uint32_t n, int ci, uint32_t *depth_d) {
+  const uint64_t V = e->V;
+  cudaStream_t s = e->s_main;
+  for (int i = 0; i < 3; i++) CK(cudaMemsetAsync(e->bmask[i], 0, 8 * (V + 1), s));
+  CK(cudaMemsetAsync(e->bm[0], 0, 4 * e->nwords, s));
+  CK(cudaMemsetAsync(e->bm[1], 0, 4 * e->nwords, s));
+  CK(cudaMemsetAsync(e->hist_d, 0, 8ull * kMaxBatchLevels * 64, s));
+  CK(cudaMemsetAsync(e->bar_d, 0, 64, s));
+  CK(cudaMemcpyAsync(e->srcs_d, e->srcs_h, 4 * n, cudaMemcpyHostToDevice, s));
+  k_batch_init<<<1, 64, 0, s>>>(e->srcs_d, n, e->bmask[0], e->bmask[1], e->bm[0], depth_d, V);
+  e->launches++;
+  PersistArgs a;
+  a.V = e->V;
+  a.nwords = e->nwords;
+  a.off = e->off_d;
+  a.sedges = e->sedges_d;
+  a.hedges = e->hedges_d;
+  a.static_edges = e->plan.static_edges;
+  a.E = e->g->E;
+  a.visited = e->bmask[0];
+  a.cur = e->bmask[1];
+  a.next = e->bmask[2];
+  a.cur_any = e->bm[0];
+  a.next_any = e->bm[1];
+  a.list = e->list_d[0];
+  a.pref = e->pref_d[0];
+  a.tile_first = e->ptile_d;
+  a.list_cap = e->list_cap[0] + e->list_cap[1];
+  a.tile_cap = e->ptile_cap;
+  a.cta_n = e->cta_n;
+  a.cta_e = e->cta_e;
+  a.bar = e->bar_d;
+  a.hist = e->hist_d;
+  a.depth = depth_d;
+  a.n_src = n;
+  a.err = e->bar_d + 2;
+  a.levels = e->bar_d + 3;
+  a.stat = (unsigned long long *)(e->bar_d + 4);
+  a.Vs = e->Vs;
+  RC(launch_persist<Edge>(e, ci, a, s));
+  CK(cudaMemcpyAsync(e->hist_h, e->hist_d, 8ull * kMaxBatchLevels * 64, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(e->pmisc_h, e->bar_d, 64, cudaMemcpyDeviceToHost, s));
+  return OG_OK;
+}
+
+// Captures enqueue_persist for (n, config) as a CUDA graph once and replays it.
+template <class Edge>
+int run_persist_graph(og_engine *e, uint32_t n, int ci, bool *used_graph) {
+  *used_graph = false;
+  if (!e->graph_broken && !(e->graph && e->graph_n == n && e->graph_cfg == ci)) {
+    if (e->graph) {
+      cudaGraphExecDestroy(e->graph);
+      e->graph = nullptr;
+    }
+    cudaGraph_t gr = nullptr;
+    bool ok = cudaStreamBeginCapture(e->s_main, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
+    const uint64_t before = e->launches;
+    const int rc = ok ? enqueue_persist<Edge>(e, n, ci, nullptr) : OG_E_CUDA;
+    e->launches = before;  // captured, not launched
+    if (ok) ok = cudaStreamEndCapture(e->s_main, &gr) == cudaSuccess && rc == OG_OK;
+    if (ok) ok = cudaGraphInstantiate(&e->graph, gr, 0) == cudaSuccess;
+    if (gr) cudaGraphDestroy(gr);
+    if (!ok) {
+      cudaGetLastError();
+      e->graph = nullptr;
+      e->graph_broken = true;  // fall back to direct launches from now on
+    } else {
+      e->graph_n = n;
+      e->graph_cfg = ci;
+    }
+  }
+  if (e->graph) {
+    CK(cudaGraphLaunch(e->graph, e->s_main));
+    e->launches += 2;  // the seed kernel and the persistent kernel
+    *used_graph = true;
+    return OG_OK;
+  }
+  return enqueue_persist<Edge>(e, n, ci, nullptr);
+}
+
+template <class Edge>
+int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *out,
+                      uint64_t *checks, og_stats &st, int ci) {
+  const uint64_t V = e->V;
+  memcpy(e->srcs_h, srcs, 4 * n);
+  uint32_t *depth_d = nullptr;
+  struct Free {
+    uint32_t *&p;
+    ~Free() {
+      if (p) cudaFree(p);
+    }
+  } free_depth{depth_d};
+  bool graph = false;
+  if (out) {
+    CK(cudaMalloc(&depth_d, 4ull * n * V));
+    k_fill_u32<<<grid_for(n * V, e->sms), kThreads, 0, e->s_main>>>(depth_d, (uint64_t)n * V,
+                                                                 (uint32_t)(V + 1));
+    e->launches++;
+  }
+  // events outside any captured graph: they bracket the whole batch on s_main
+  CK(cudaEventRecord(e->t_s0, e->s_main));
+  if (out) {
+    RC(enqueue_persist<Edge>(e, n, ci, depth_d));
+  } else {
+    RC(run_persist_graph<Edge>(e, n, ci, &graph));
+  }
+  CK(cudaEventRecord(e->t_s1, e->s_main));
+  CK(cudaStreamSynchronize(e->s_main));
+  CK(cudaGetLastError());
+  const uint32_t err = e->pmisc_h[2], levels = e->pmisc_h[3];
+  const unsigned long long *stat = (const unsigned long long *)(e->pmisc_h + 4);
+  if (err & kErrBarrier) return fail(OG_E_TIMEOUT, "batched BFS grid barrier wait gave up");
+  if (err & kErrLevels) return fail(OG_E_STATE, "batched BFS needs more than %u levels", kMaxBatchLevels);
+  if (err) return fail(OG_E_DEVICE, "batched BFS kernel reported an out-of-range index (0x%x)", err);
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, e->t_s0, e->t_s1) == cudaSuccess) st.ms_static += ms;
+  st.iterations = levels;
+  st.frontier_sum = stat[0];
+  st.edges_static = stat[1] - stat[2];
+  st.edges_dynamic = stat[2];
+  st.link_bytes = stat[2] * e->eb;
+  st.chunks = graph ? 1u : 0u;  // 1: replayed from the captured CUDA graph
+  if (checks)
+    for (uint32_t i = 0; i < n; i++) {
+      uint64_t r = 1, d = 1;
+      for (uint32_t L = 1; L <= levels && L < kMaxBatchLevels; L++) {
+        const uint64_t c = e->hist_h[(uint64_t)L * 64 + i];
+        r += c;
+        d += (uint64_t)(L + 1) * c;
+      }
+      checks[2 * i] = r;
+      checks[2 * i + 1] = d;
+    }
+  if (out) CK(cudaMemcpy(out, depth_d, 4ull * n * V, cudaMemcpyDeviceToHost));
+  e->last_algo = -1;
+  return OG_OK;
+}
+
 // ------------------------------------------------------------------ PageRank
 
 template <class Edge>
@@ -853,22 +1064,71 @@ struct BatchCtx {
   uint32_t n;
   uint32_t *out;
   uint64_t *checks;
+  int mode;  // 0 persistent (tuned configuration), 1 host-driven levels, 2+k persistent config k
 };
-}  // namespace
 
-extern "C" int og_bfs_batch(og_engine *e, const uint32_t *srcs, int n, uint32_t *out,
-                            uint64_t *checks, og_stats *st) {
+int batch_body(og_engine *en, og_stats &s, void *cx) {
+  const BatchCtx &b = *(BatchCtx *)cx;
+  const bool w = en->g->kind == OG_GRAPH_WEIGHTED;
+  if (b.mode == 1)
+    return w ? run_batch<uint2>(en, b.srcs, b.n, b.out, b.checks, s)
+             : run_batch<uint32_t>(en, b.srcs, b.n, b.out, b.checks, s);
+  const int ci = b.mode >= 2 ? b.mode - 2 : (en->tuned >= 0 ? en->tuned : 0);
+  return w ? run_batch_persist<uint2>(en, b.srcs, b.n, b.out, b.checks, s, ci)
+           : run_batch_persist<uint32_t>(en, b.srcs, b.n, b.out, b.checks, s, ci);
+}
+
+int batch_checks(og_engine *e, const uint32_t *srcs, int n) {
   if (!e || !srcs) return fail(OG_E_ARG, "og_bfs_batch: null argument");
   if (n < 1 || n > 64) return fail(OG_E_ARG, "og_bfs_batch: %d sources (1..64)", n);
   if (!e->batch_enabled) return fail(OG_E_UNSUPPORTED, "engine created without OG_CFG_BATCH");
   for (int i = 0; i < n; i++)
     if (srcs[i] >= e->V) return fail(OG_E_ARG, "source %u >= V %u", srcs[i], e->V);
-  BatchCtx c{srcs, (uint32_t)n, out, checks};
-  return query_common(e, OG_ALGO_BFS, st, nullptr, [](og_engine *en, og_stats &s, void *cx) {
-    const BatchCtx &b = *(BatchCtx *)cx;
-    return en->g->kind == OG_GRAPH_WEIGHTED ? run_batch<uint2>(en, b.srcs, b.n, b.out, b.checks, s)
-                                            : run_batch<uint32_t>(en, b.srcs, b.n, b.out, b.checks, s);
-  }, &c);
+  return OG_OK;
+}
+}  // namespace
+
+extern "C" int og_bfs_batch(og_engine *e, const uint32_t *srcs, int n, uint32_t *out,
+                            uint64_t *checks, og_stats *st) {
+  RC(batch_checks(e, srcs, n));
+  BatchCtx c{srcs, (uint32_t)n, out, checks, (e->cfg.flags & OG_CFG_BATCH_LEVELS) ? 1 : 0};
+  return query_common(e, OG_ALGO_BFS, st, nullptr, batch_body, &c);
+}
+
+extern "C" int og_bfs_batch_tune(og_engine *e, const uint32_t *srcs, int n, int reps,
+                                 og_tune_result *res) {
+  RC(batch_checks(e, srcs, n));
+  if (reps < 1) reps = 1;
+  og_tune_result r;
+  memset(&r, 0, sizeof r);
+  r.configs = kNumPersistConfigs;
+  float best = 1e30f;
+  for (int i = 0; i < kNumPersistConfigs; i++) {
+    r.block[i] = kPersistConfigs[i].block;
+    r.items[i] = kPersistConfigs[i].items;
+    float tmin = 1e30f;
+    for (int k = 0; k <= reps; k++) {  // the first run warms up
+      og_stats st;
+      BatchCtx c{srcs, (uint32_t)n, nullptr, nullptr, 2 + i};
+      RC(query_common(e, OG_ALGO_BFS, &st, nullptr, batch_body, &c));
+      if (k > 0) tmin = std::min(tmin, (float)st.ms_static);
+    }
+    r.ms[i] = tmin;
+    if (tmin < best) {
+      best = tmin;
+      r.best = i;
+    }
+  }
+  e->tuned = r.best;
+  if (res) *res = r;
+  return OG_OK;
+}
+
+extern "C" int og_bfs_batch_set_config(og_engine *e, int config) {
+  if (!e) return fail(OG_E_ARG, "null engine");
+  if (config < -1 || config >= kNumPersistConfigs) return fail(OG_E_ARG, "config %d out of range", config);
+  e->tuned = config;
+  return OG_OK;
 }
 
 extern "C" int og_result_fetch(og_engine *e, int algo, void *out) {

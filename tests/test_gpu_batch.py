@@ -46,6 +46,33 @@ def test_batch_equals_single_source(weighted):
         e.close()
 
 
+def test_persistent_graph_levels_and_all_configs_agree():
+    """The persistent kernel (direct launch or CUDA-graph replay), the
+    host-driven level loop and every autotuner candidate give the same depths."""
+    g = og.Graph.rmat(13, 16, seed=3)
+    rng = np.random.default_rng(9)
+    srcs = rng.integers(0, g.V, 40).astype(np.uint32)
+    for cname, kw in batch_configs(g):
+        e = og.Engine(g, batch=True, **kw)
+        lv = og.Engine(g, batch_levels=True, **kw)
+        want, wck = lv.bfs_batch(srcs)
+        got, ck = e.bfs_batch(srcs)  # persistent, depth matrix (direct launch)
+        np.testing.assert_array_equal(got, want, err_msg=cname)
+        np.testing.assert_array_equal(ck, wck)
+        for rep in range(2):  # captured once, then replayed
+            _, ck2 = e.bfs_batch(srcs, out=False)
+            np.testing.assert_array_equal(ck2, wck)
+        assert e.stats["chunks"] == 1, "second call should replay the CUDA graph"
+        res = e.bfs_batch_tune(srcs, reps=1)
+        assert len(res["candidates"]) == 5 and 0 <= res["best"] < 5
+        for ci in range(5):
+            e.bfs_batch_set_config(ci)
+            d, ck3 = e.bfs_batch(srcs)
+            np.testing.assert_array_equal(d, want, err_msg="%s config %d" % (cname, ci))
+        e.close()
+        lv.close()
+
+
 def test_batch_small_counts_and_oracle():
     g = og.Graph.rmat(11, 16)
     off, col = np.array(g.offsets), np.array(g.columns)
