@@ -43,8 +43,10 @@ def parse_args():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--scale", type=int, default=27)
-    ap.add_argument("--budget-gib", type=float, default=8.0)
+    ap.add_argument("--scale", type=int, default=None,
+                    help="default per workload: 27 (sssp-oom, bfs-batch), 26 (pr-precision), 20 (bfs-resident)")
+    ap.add_argument("--budget-gib", type=float, default=None,
+                    help="default per workload: 8 GiB, 6 GiB for pr-precision")
     ap.add_argument("--advisek", type=float, default=0.8)
     ap.add_argument("--sources", type=int, default=32)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
@@ -52,10 +54,20 @@ def parse_args():
                     choices=["sssp-oom", "bfs-batch", "bfs-resident", "pr-precision", "serving"],
                     help="sssp-oom (default headline), or another measured configuration")
     ap.add_argument("--tune", type=int, default=1, help="bfs-batch: run the autotuner first")
+    ap.add_argument("--serving-scales", default="22,24,26,27")
+    ap.add_argument("--serving-budget-gib", type=float, default=24.0)
+    ap.add_argument("--requests", type=int, default=400)
+    ap.add_argument("--rate", type=float, default=2000.0)
+    ap.add_argument("--workers", type=int, default=4)
     ap.add_argument("--direct", type=int, default=1,
                     help="1: relax the dynamic region straight from page-locked host memory "
                          "(fastest); 0: gather into double-buffered device staging first")
-    return ap.parse_args()
+    a = ap.parse_args()
+    if a.scale is None:
+        a.scale = {"pr-precision": 26, "bfs-resident": 20}.get(a.workload, 27)
+    if a.budget_gib is None:
+        a.budget_gib = 6.0 if a.workload == "pr-precision" else 8.0
+    return a
 
 
 def dist_env():
@@ -445,6 +457,233 @@ def run_bfs_batch(args, rank, world, local):
     eng.close()
 
 
+def run_pr_precision(args, rank, world, local):
+    """PageRank precision study: R-MAT scale 26, directed, in-edge CSR +
+    out-degrees, 6 GiB budget; FP32 ranks with FP32 pull sums and the FP64 L1
+    delta reduced on the GPU, stopped at L1 < 1e-6 (normalised ranks),
+    against the multi-threaded FP64 host oracle; the reference's delta form
+    (og_pr, per-vertex 1e-3) is timed beside it."""
+    import torch
+    import onegraph_gb300 as og
+    import oracle
+    torch.cuda.set_device(local)
+    t0 = time.time()
+    try:
+        g = og.Graph.rmat(args.scale, 16, seed=1, pagerank=True, symmetric=False, on_gpu=True)
+    except og.OGError:
+        g = og.Graph.rmat(args.scale, 16, seed=1, pagerank=True, symmetric=False)
+    gen_s = time.time() - t0
+    eng = og.Engine(g, budget=int(args.budget_gib * GIB), advisek=args.advisek,
+                    direct=bool(args.direct), device=local)
+    eng.pr_l1(0.85, 1e-6, 3, out=False)  # warm-up
+    sampler = ClockSampler(local)
+    sampler.start()
+    t, outs = timed(lambda k: eng.pr_l1(0.85, 1e-6, 500), 1)
+    clocks = sampler.stop()
+    st = dict(eng.stats)
+    rank32 = outs[0].astype(np.float64)
+    t1, _ = timed(lambda k: eng.pr(0.001, 0, out=False), 1)
+    st_delta = dict(eng.stats)
+    threads = os.cpu_count() or 1
+    ref = np.empty(g.V)
+    c0 = time.perf_counter()
+    it_ref, l1_ref = oracle.pr_l1_mt_raw(g.V, g._off_p, g._edges_p, g._outdeg_p, 0.85, 1e-6, 500,
+                                         threads, ref)
+    cpu_s = time.perf_counter() - c0
+    err = np.abs(rank32 - ref)
+    iters = max(st["iterations"], 1)
+    line = {
+        "metric": "pagerank iterations/s", "value": iters / t, "unit": "iterations/s",
+        "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": t * 1e3 / iters,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 (f64 L1 reduction)", "data": "synthetic",
+        "config": {"workload": "pr-precision-rmat%d-directed-%gGiB" % (args.scale, args.budget_gib),
+                   "V": g.V, "E": g.E, "damping": 0.85, "tol_l1": 1e-6, "budget_bytes": int(args.budget_gib * GIB),
+                   "advisek": args.advisek, "dynamic_mode": "direct" if args.direct else "staged"},
+        "iterations": st["iterations"], "residual_l1": st["residual"], "ms_total": t * 1e3,
+        "max_abs_err": float(err.max()), "l1_err": float(err.sum()),
+        "max_rel_err": float((err / ref).max()),
+        "oracle": {"iterations": it_ref, "residual_l1": l1_ref, "seconds": cpu_s, "threads": threads},
+        "link_gb_per_iter": st["link_bytes"] / iters / 1e9,
+        "delta_form": {"rounds": st_delta["iterations"], "ms": t1 * 1e3},
+        "cpu_baseline": {"value": it_ref / cpu_s, "unit": "iterations/s", "cores": threads, "kind": "port",
+                         "sample": "FP64 pull PageRank oracle, full run to L1 < 1e-6"},
+        "clocks": clocks, "setup_s": {"generate": gen_s},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+
+
+def run_bfs_resident(args, rank, world, local):
+    """Single-source BFS on a fully resident graph (advisek 1.0): R-MAT scale
+    20, symmetric, u32 CSR, source = highest-degree vertex; bit-exact against
+    the runCPUBFS restatement.  Plain path (og_bfs) and the persistent
+    one-launch path (og_bfs_batch with one source, CUDA-graph replay)."""
+    import torch
+    import onegraph_gb300 as og
+    import oracle
+    torch.cuda.set_device(local)
+    t0 = time.time()
+    try:
+        g = og.Graph.rmat(args.scale, 16, seed=1, on_gpu=True)
+    except og.OGError:
+        g = og.Graph.rmat(args.scale, 16, seed=1)
+    gen_s = time.time() - t0
+    deg = g.degrees()
+    src = int(np.argmax(deg))
+    eng = og.Engine(g, budget=int(args.budget_gib * GIB), advisek=1.0, batch=True, device=local)
+    for _ in range(args.warmup):
+        eng.bfs(src, out=False)
+        eng.bfs_batch([src], out=False)
+    sampler = ClockSampler(local)
+    sampler.start()
+    stats = []
+
+    def plain(k):
+        eng.bfs(src, out=False)
+        stats.append(dict(eng.stats))
+    t, _ = timed(plain, args.steps)
+    tb, _ = timed(lambda k: eng.bfs_batch([src], out=False), args.steps)
+    clocks = sampler.stop()
+    d = eng.bfs(src)
+    want, _ = oracle.bfs(np.array(g.offsets), np.array(g.columns), src)
+    exact = bool((oracle.normalise_bfs(d, g.V) == want).all())
+    reached = d != g.V + 1
+    comp_edges = int(deg[reached].sum(dtype=np.int64))
+    st_ms = sum(x["ms_static"] for x in stats)
+    st_edges = sum(x["edges_static"] for x in stats)
+    st_verts = sum(x["static_vertices"] for x in stats)
+    peaks = measured_peaks()
+    gbs = (8 * st_edges + 20 * st_verts) / (st_ms / 1e3) / 1e9 if st_ms else 0.0
+    c0 = time.perf_counter()
+    oracle.bfs(np.array(g.offsets), np.array(g.columns), src)
+    cpu_s = time.perf_counter() - c0
+    line = {
+        "metric": "GTEPS", "value": comp_edges * args.steps / t / 1e9, "unit": "GTEPS",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": {"workload": "bfs-resident-rmat%d" % args.scale, "V": g.V, "E": g.E, "source": src,
+                   "advisek": 1.0, "l2": "graph %.0f MB" % (g.E * 4 / 1e6)},
+        "persistent_ms_per_query": tb / args.steps * 1e3,
+        "persistent_gteps": comp_edges * args.steps / tb / 1e9,
+        "bit_exact_vs_runCPUBFS": exact, "levels": stats[0]["iterations"],
+        "roofline": {"bound": "hbm", "kernel": "k_lbs<uint32_t,BfsOp> (static relax)", "achieved": gbs,
+                     "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
+                     "traffic": None, "peak_source": peaks["source"]},
+        "cpu_baseline": {"value": comp_edges / cpu_s / 1e9, "unit": "GTEPS", "cores": 1, "kind": "port",
+                         "sample": "runCPUBFS restatement, one full query"},
+        "gpu_launches": sum(x["launches"] for x in stats), "clocks": clocks, "setup_s": {"generate": gen_s},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+
+
+SERVING_BUDGETS_GIB = {22: 1.5, 24: 3.0, 26: 6.5, 27: 10.0}  # resident graph + first context
+
+
+def run_serving(args, rank, world, local):
+    """Serving mix: four resident weighted R-MAT graphs (scales 22/24/26/27)
+    under a 24 GiB budget, Poisson arrivals at 2000 requests/s (seed 4),
+    60 % BFS / 30 % SSSP / 10 % PageRank (5 iterations), graph by Zipf(1.1)
+    with the smallest graph most popular; the same requests are then run one
+    at a time through the plain per-query path."""
+    import threading
+    import torch
+    import onegraph_gb300 as og
+    torch.cuda.set_device(local)
+    scales = [int(x) for x in args.serving_scales.split(",")]
+    graphs, gen_s = [], 0.0
+    for sc in scales:
+        g, t = make_graph(sc)
+        graphs.append(g)
+        gen_s += t
+    rng = np.random.default_rng(4)
+    z = np.array([1.0 / (k + 1) ** 1.1 for k in range(len(graphs))])
+    z /= z.sum()
+    n = args.requests
+    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n))
+    gsel = rng.choice(len(graphs), n, p=z)
+    u = rng.random(n)
+    algos = np.where(u < 0.6, og.ALGO_BFS, np.where(u < 0.9, og.ALGO_SSSP, og.ALGO_PR))
+    nz = [np.nonzero(g.degrees())[0] for g in graphs]
+    srcs = [int(nz[gi][rng.integers(0, nz[gi].size)]) for gi in gsel]
+    budgets = [int(SERVING_BUDGETS_GIB.get(sc, 2.0) * GIB) for sc in scales]
+    srv = og.Server(budget=int(args.serving_budget_gib * GIB), workers=args.workers, max_batch=64,
+                    device=local)
+    for g, b in zip(graphs, budgets):
+        srv.add_graph(g, budget=b, advisek=args.advisek, direct=True, pagerank=True)
+    sampler = ClockSampler(local)
+    sampler.start()
+    t0 = time.perf_counter()
+
+    def client():
+        for i in range(n):
+            dt = arrivals[i] - (time.perf_counter() - t0)
+            if dt > 0:
+                time.sleep(dt)
+            srv.submit(int(gsel[i]), int(algos[i]), srcs[i], iterations=5, user=i)
+    th = threading.Thread(target=client)
+    th.start()
+    resp = {}
+    while len(resp) < n:
+        for r in srv.poll(1024, wait_ms=200):
+            resp[r["user"]] = r
+    th.join()
+    wall = time.perf_counter() - t0
+    clocks = sampler.stop()
+    st = srv.stats()
+    srv.close()
+    lat = np.array([resp[i]["t_done_ms"] - resp[i]["t_submit_ms"] for i in range(n)])
+    span_ms = max(r["t_done_ms"] for r in resp.values()) - min(r["t_submit_ms"] for r in resp.values())
+    served_qps = n / (span_ms / 1e3)
+    bad = [r for r in resp.values() if r["status"] != 0]
+    # plain per-query path: one engine per graph, requests one after another
+    engines = [og.Engine(g, budget=b, advisek=args.advisek, direct=True, pagerank=True, batch=True)
+               for g, b in zip(graphs, budgets)]
+    mism = 0
+    p0 = time.perf_counter()
+    plain_lat = []
+    for i in range(n):
+        e = engines[gsel[i]]
+        a = int(algos[i])
+        if a == og.ALGO_BFS:
+            e.bfs(srcs[i], out=False)
+        elif a == og.ALGO_SSSP:
+            e.sssp(srcs[i], out=False)
+        else:
+            e.pr_l1(0.85, 0.0, 5, out=False)
+        done = time.perf_counter() - p0
+        plain_lat.append(max(0.0, done - arrivals[i]) * 1e3)
+        mism += e.checksum(a) != resp[i]["checksum"]
+    plain_wall = time.perf_counter() - p0
+    for e in engines:
+        e.close()
+    plain_lat = np.array(plain_lat)
+    line = {
+        "metric": "served queries/s", "value": served_qps, "unit": "queries/s", "n_gpus": world,
+        "steps": n, "warmup": 0, "ms_per_step": span_ms / n, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u32/f32", "data": "synthetic",
+        "config": {"workload": "serving-rmat%s-%gGiB" % ("-".join(map(str, scales)), args.serving_budget_gib),
+                   "graphs": {str(sc): {"V": g.V, "E": g.E, "budget_bytes": b}
+                              for sc, g, b in zip(scales, graphs, budgets)},
+                   "arrivals": "Poisson %g/s, seed 4" % args.rate, "requests": n,
+                   "mix": {"bfs": int((algos == og.ALGO_BFS).sum()), "sssp": int((algos == og.ALGO_SSSP).sum()),
+                           "pr5": int((algos == og.ALGO_PR).sum())},
+                   "zipf": "1.1, smallest graph most popular", "workers": args.workers},
+        "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+        "plain_queries_per_s": n / plain_wall,
+        "plain_p50_ms": float(np.percentile(plain_lat, 50)), "plain_p99_ms": float(np.percentile(plain_lat, 99)),
+        "speedup_vs_plain": served_qps / (n / plain_wall),
+        "results_identical_to_plain": mism == 0, "failed_requests": len(bad),
+        "server": st, "clocks": clocks, "setup_s": {"generate": gen_s}, "wall_s": wall,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse_args()
     rank, world, local = dist_env()
@@ -452,6 +691,12 @@ def main():
         run_reference(args, rank, world)
     elif args.workload == "bfs-batch":
         run_bfs_batch(args, rank, world, local)
+    elif args.workload == "serving":
+        run_serving(args, rank, world, local)
+    elif args.workload == "pr-precision":
+        run_pr_precision(args, rank, world, local)
+    elif args.workload == "bfs-resident":
+        run_bfs_resident(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

@@ -243,6 +243,23 @@ int og_bfs_batch_tune(og_engine *e, const uint32_t *srcs, int n, int reps,
 /* Selects a candidate directly (-1 = default), e.g. from a saved tuning. */
 int og_bfs_batch_set_config(og_engine *e, int config);
 
+/* A query context on a parent engine's resident graph: the offsets, static
+ * edges and page-locked host CSR are shared, the per-query state (values,
+ * frontiers, lists, staging, PageRank/batch arrays, streams) is its own, so
+ * several host threads can run queries on one graph concurrently, one context
+ * each.  Destroy every clone before its parent.  No reference counterpart
+ * (the reference runs one query at a time). */
+int og_engine_clone(og_engine *parent, og_engine **out);
+
+/* Device bytes of the shared resident graph (0 for a clone) and of one
+ * query context. */
+int og_engine_bytes(const og_engine *e, uint64_t *resident, uint64_t *context);
+
+/* Checksum of the last result on the device, reduced in a fixed order:
+ * BFS/SSSP {vertices reached, sum of their values}; CC {components, sum of
+ * labels}; PR {V, bits of the FP64 sum of the ranks}. */
+int og_result_checksum(og_engine *e, int algo, uint64_t *out);
+
 /* Copies the last result of the given algorithm from device memory into out
  * (V entries: u32 for BFS/SSSP/CC, float for PR). */
 int og_result_fetch(og_engine *e, int algo, void *out);
@@ -296,6 +313,69 @@ int og_k_compact_noalloc(const uint32_t *bits, uint32_t v_begin, uint32_t v_end,
                          uint64_t *out_pref, uint64_t list_cap,
                          uint32_t *out_tile, uint64_t tile_cap,
                          og_counts *out_counts, void *stream);
+
+/* ---------------------------------------------------------------- serving */
+
+/* A request loop over several resident graphs (no reference counterpart).
+ * Requests are queued as they arrive and admitted by worker threads when a
+ * query context of their graph is free or a new one fits budget_bytes; the
+ * work of concurrent requests overlaps on the GPU.  BFS requests for the same
+ * graph that queue up while others run are fused into one og_bfs_batch pass
+ * (up to max_batch).  Results are identical to running each request alone. */
+typedef struct og_server og_server;
+
+typedef struct og_server_config {
+  uint64_t budget_bytes; /* device bytes for all resident graphs and query
+                            contexts (0 = limited only by device memory)   */
+  int32_t workers;       /* host threads driving queries (1..64)           */
+  int32_t max_batch;     /* BFS requests per fused pass (1 = no batching)  */
+  int32_t device;
+  uint32_t flags;
+} og_server_config;
+
+typedef struct og_request {
+  int32_t graph;      /* id from og_server_add_graph                       */
+  int32_t algo;       /* og_algo                                           */
+  uint32_t source;    /* BFS / SSSP                                        */
+  int32_t iterations; /* PageRank iterations (og_pr_l1, tol 0), 0 = 5       */
+  void *out;          /* optional caller buffer of V results, valid until the
+                         response arrives; NULL = checksum only             */
+  uint64_t user;      /* echoed in the response                            */
+} og_request;
+
+typedef struct og_response {
+  uint64_t ticket;
+  uint64_t user;
+  int32_t status;     /* og_status of the request                          */
+  int32_t graph;
+  int32_t algo;
+  uint32_t source;
+  uint32_t batch;     /* requests served by the same GPU pass              */
+  uint32_t reserved;
+  double t_submit_ms; /* server clock (ms since og_server_create)          */
+  double t_start_ms;
+  double t_done_ms;
+  uint64_t checksum[2]; /* og_result_checksum, or {reached, depth sum} of a
+                           fused BFS                                       */
+} og_response;
+
+typedef struct og_server_stats {
+  uint64_t submitted, completed, gpu_passes, batched_requests;
+  uint64_t contexts_created, used_bytes;
+} og_server_stats;
+
+int og_server_create(const og_server_config *cfg, og_server **out);
+/* Creates the graph's resident engine with gcfg (its budget and advisek);
+ * must precede the first submit.  The graph must outlive the server. */
+int og_server_add_graph(og_server *s, og_graph *g, const og_config *gcfg, int *graph_id);
+int og_server_submit(og_server *s, const og_request *r, uint64_t *ticket);
+/* Up to max responses; waits up to wait_ms (-1 = until one is ready or
+ * nothing is in flight, 0 = no wait). */
+int og_server_poll(og_server *s, og_response *out, int max, int *n, int wait_ms);
+/* Waits until every submitted request has a response (timeout_ms < 0: no limit). */
+int og_server_drain(og_server *s, int timeout_ms);
+int og_server_get_stats(og_server *s, og_server_stats *out);
+void og_server_destroy(og_server *s);
 
 const char *og_last_error(void);
 int og_abi_version(void);

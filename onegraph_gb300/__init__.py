@@ -82,6 +82,35 @@ class Stats(C.Structure):
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
+class ServerConfig(C.Structure):
+    _fields_ = [("budget_bytes", C.c_uint64), ("workers", C.c_int32), ("max_batch", C.c_int32),
+                ("device", C.c_int32), ("flags", C.c_uint32)]
+
+
+class Request(C.Structure):
+    _fields_ = [("graph", C.c_int32), ("algo", C.c_int32), ("source", C.c_uint32),
+                ("iterations", C.c_int32), ("out", C.c_void_p), ("user", C.c_uint64)]
+
+
+class Response(C.Structure):
+    _fields_ = [("ticket", C.c_uint64), ("user", C.c_uint64), ("status", C.c_int32),
+                ("graph", C.c_int32), ("algo", C.c_int32), ("source", C.c_uint32),
+                ("batch", C.c_uint32), ("reserved", C.c_uint32), ("t_submit_ms", C.c_double),
+                ("t_start_ms", C.c_double), ("t_done_ms", C.c_double),
+                ("checksum", C.c_uint64 * 2)]
+
+    def as_dict(self):
+        d = {f: getattr(self, f) for f, _ in self._fields_ if f not in ("checksum", "reserved")}
+        d["checksum"] = (self.checksum[0], self.checksum[1])
+        return d
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("gpu_passes", C.c_uint64),
+                ("batched_requests", C.c_uint64), ("contexts_created", C.c_uint64),
+                ("used_bytes", C.c_uint64)]
+
+
 _lib = None
 
 # (name, restype, argtypes) for every symbol declared in include/onegraph.h
@@ -110,10 +139,20 @@ SIGNATURES = [
     ("og_bfs_batch_tune", C.c_int, [_P, _P, C.c_int, C.c_int, C.POINTER(TuneResult)]),
     ("og_bfs_batch_set_config", C.c_int, [_P, C.c_int]),
     ("og_result_fetch", C.c_int, [_P, C.c_int, _P]),
+    ("og_result_checksum", C.c_int, [_P, C.c_int, _P]),
+    ("og_engine_clone", C.c_int, [_P, C.POINTER(_P)]),
+    ("og_engine_bytes", C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     ("og_k_compact", C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P, C.c_uint64, _P,
                                C.c_uint64, _P, _P]),
     ("og_k_compact_noalloc", C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P, C.c_uint64, _P,
                                        C.c_uint64, _P, _P]),
+    ("og_server_create", C.c_int, [C.POINTER(ServerConfig), C.POINTER(_P)]),
+    ("og_server_add_graph", C.c_int, [_P, _P, C.POINTER(Config), C.POINTER(C.c_int)]),
+    ("og_server_submit", C.c_int, [_P, C.POINTER(Request), C.POINTER(C.c_uint64)]),
+    ("og_server_poll", C.c_int, [_P, C.POINTER(Response), C.c_int, C.POINTER(C.c_int), C.c_int]),
+    ("og_server_drain", C.c_int, [_P, C.c_int]),
+    ("og_server_get_stats", C.c_int, [_P, C.POINTER(ServerStats)]),
+    ("og_server_destroy", None, [_P]),
     ("og_last_error", C.c_char_p, []),
     ("og_abi_version", C.c_int, []),
 ]
@@ -348,16 +387,113 @@ class Engine:
     def bfs_batch_set_config(self, config: int):
         _check(lib().og_bfs_batch_set_config(self._h, config), "og_bfs_batch_set_config")
 
+    def clone(self) -> "Engine":
+        """A query context sharing this engine's resident graph (og_engine_clone)."""
+        c = Engine.__new__(Engine)
+        h = _P()
+        _check(lib().og_engine_clone(self._h, C.byref(h)), "og_engine_clone")
+        c._h, c.graph, c.plan, c.stats, c._parent = h, self.graph, self.plan, {}, self
+        c._clones, c._close_pending = 0, False
+        self.graph._engines += 1
+        self._clones = getattr(self, "_clones", 0) + 1
+        return c
+
+    def bytes(self) -> tuple:
+        """(device bytes of the resident graph, of one query context)."""
+        r, c = C.c_uint64(), C.c_uint64()
+        _check(lib().og_engine_bytes(self._h, C.byref(r), C.byref(c)), "og_engine_bytes")
+        return r.value, c.value
+
+    def checksum(self, algo: int) -> tuple:
+        out = np.zeros(2, np.uint64)
+        _check(lib().og_result_checksum(self._h, algo, _ptr(out)), "og_result_checksum")
+        return int(out[0]), int(out[1])
+
     def fetch(self, algo: int, dtype=np.uint32) -> np.ndarray:
         o = np.empty(self.graph.V, dtype)
         _check(lib().og_result_fetch(self._h, algo, _ptr(o)), "og_result_fetch")
         return o
 
     def close(self):
+        """Destroys the engine; a parent waits for its clones (they share its
+        resident graph), whatever order finalisers run in."""
+        if not getattr(self, "_h", None):
+            return
+        if getattr(self, "_clones", 0) > 0:
+            self._close_pending = True
+            return
+        lib().og_engine_destroy(self._h)
+        self._h = None
+        self.graph._engine_closed()
+        parent = getattr(self, "_parent", None)
+        if parent is not None:
+            parent._clones -= 1
+            if parent._clones == 0 and getattr(parent, "_close_pending", False):
+                parent._close_pending = False
+                parent.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class Server:
+    """og_server: resident graphs, pooled query contexts, continuous batching."""
+
+    def __init__(self, budget: int = 0, workers: int = 4, max_batch: int = 64, device: int = 0):
+        cfg = ServerConfig(budget, workers, max_batch, device, 0)
+        h = _P()
+        _check(lib().og_server_create(C.byref(cfg), C.byref(h)), "og_server_create")
+        self._h = h
+        self.graphs: list[Graph] = []
+        self._bufs: dict[int, np.ndarray] = {}
+
+    def add_graph(self, graph: Graph, budget: int = 0, advisek: float = 0.0, direct: bool = True,
+                  pagerank: bool = False) -> int:
+        cfg = Config(budget, advisek, (CFG_DIRECT if direct else 0) | (CFG_PR if pagerank else 0), 0)
+        gid = C.c_int()
+        _check(lib().og_server_add_graph(self._h, graph._h, C.byref(cfg), C.byref(gid)),
+               "og_server_add_graph")
+        graph._engines += 1  # the server's engines read the graph until destroy
+        self.graphs.append(graph)
+        return gid.value
+
+    def submit(self, graph: int, algo: int, source: int = 0, iterations: int = 0, out=None,
+               user: int = 0) -> int:
+        if out is not None:
+            assert out.flags.c_contiguous and out.size >= self.graphs[graph].V
+        r = Request(graph, algo, source, iterations, _ptr(out), user)
+        t = C.c_uint64()
+        _check(lib().og_server_submit(self._h, C.byref(r), C.byref(t)), "og_server_submit")
+        if out is not None:
+            self._bufs[t.value] = out  # keep the buffer alive until its response
+        return t.value
+
+    def poll(self, max_n: int = 256, wait_ms: int = -1) -> list[dict]:
+        arr = (Response * max_n)()
+        n = C.c_int()
+        _check(lib().og_server_poll(self._h, arr, max_n, C.byref(n), wait_ms), "og_server_poll")
+        out = [arr[i].as_dict() for i in range(n.value)]
+        for r in out:
+            self._bufs.pop(r["ticket"], None)
+        return out
+
+    def drain(self, timeout_ms: int = -1):
+        _check(lib().og_server_drain(self._h, timeout_ms), "og_server_drain")
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        _check(lib().og_server_get_stats(self._h, C.byref(st)), "og_server_get_stats")
+        return {f: getattr(st, f) for f, _ in st._fields_}
+
+    def close(self):
         if getattr(self, "_h", None):
-            lib().og_engine_destroy(self._h)
+            lib().og_server_destroy(self._h)
             self._h = None
-            self.graph._engine_closed()
+            for g in self.graphs:
+                g._engine_closed()
 
     def __del__(self):
         try:

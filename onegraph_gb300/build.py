@@ -28,7 +28,7 @@ NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-pthread", "-Wall", "-Wno-unused-function",
              "-I", os.path.join(CUDA_HOME, "include")]
 CU_SOURCES = ["engine.cu", "rmat_gpu.cu"]
-CXX_SOURCES = ["graph_host.cpp", "rmat.cpp"]
+CXX_SOURCES = ["graph_host.cpp", "rmat.cpp", "server.cpp"]
 CLI_ALGOS = {"BFS_OneGraph": 0, "SSSP_OneGraph": 1, "CC_OneGraph": 2, "PR_OneGraph": 3}
 
 

@@ -96,6 +96,11 @@ struct og_engine {
   int graph_cfg = -1;
   bool graph_broken = false;
 
+  og_engine *parent = nullptr;  // set on clones: resident state belongs to the parent
+  int clones = 0;               // live clones of this engine
+  uint64_t resident_bytes = 0;  // device bytes of the shared resident state
+  unsigned long long *sum64_d = nullptr;  // result checksum scratch
+
   int last_algo = -1;
   uint64_t launches = 0;  // kernels launched since the query began
   std::vector<void *> dallocs;
@@ -151,8 +156,85 @@ void destroy(og_engine *e) {
   if (e->registered && e->g) {
     if (--e->g->registered == 0) cudaHostUnregister(e->g->edges);
   }
+  if (e->parent) e->parent->clones--;
   cudaGetLastError();  // a failure while tearing down is not the next call's error
   delete e;
+}
+
+// Per-query state: streams, events, frontier/list arrays, staging buffers and
+// the PageRank / batched-BFS working arrays.  A parent engine and each of its
+// clones own one set; the resident graph (offsets, static edges, out-degrees,
+// page-locked host CSR) is shared.
+int create_query_state(og_engine *e) {
+  const og_plan &P = e->plan;
+  const uint64_t V = e->V;
+  CK(cudaStreamCreateWithFlags(&e->s_main, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&e->s_dyn, cudaStreamNonBlocking));
+  CK(cudaStreamCreateWithFlags(&e->s_gat, cudaStreamNonBlocking));
+  cudaEvent_t *evs[] = {&e->ev_round, &e->ev_cs, &e->ev_cd, &e->ev_dyn_done, &e->ev_gat[0],
+                        &e->ev_gat[1], &e->ev_rel[0], &e->ev_rel[1], &e->t_s0, &e->t_s1, &e->t_d0};
+  for (auto ev : evs) CK(cudaEventCreate(ev));
+  RC(dalloc(e, &e->value_d, V + 1));
+  for (int i = 0; i < 3; i++) RC(dalloc(e, &e->bm[i], e->nwords));
+  e->list_cap[0] = std::max<uint64_t>(e->Vs, 1);
+  e->list_cap[1] = std::max<uint64_t>(V - e->Vs, 1);
+  e->tile_cap[0] = P.static_edges / kTile + 2;
+  e->tile_cap[1] = P.dynamic_edges / kTile + 2;
+  // one allocation per array, the dynamic region's part after the static one,
+  // so the batched kernel can also use them as a single list over [0, V)
+  RC(dalloc(e, &e->list_d[0], e->list_cap[0] + e->list_cap[1]));
+  RC(dalloc(e, &e->pref_d[0], e->list_cap[0] + e->list_cap[1] + 2));
+  RC(dalloc(e, &e->tile_d[0], e->tile_cap[0] + e->tile_cap[1]));
+  e->list_d[1] = e->list_d[0] + e->list_cap[0];
+  e->pref_d[1] = e->pref_d[0] + e->list_cap[0] + 1;
+  e->tile_d[1] = e->tile_d[0] + e->tile_cap[0];
+  e->lb_tiles = (uint32_t)((e->nwords + kWordsPerCompactTile - 1) / kWordsPerCompactTile + 1);
+  for (int r = 0; r < 2; r++) {
+    RC(dalloc(e, &e->lb[r].status, e->lb_tiles + 1));
+    e->lb[r].ticket = e->lb[r].status + e->lb_tiles;
+    RC(dalloc(e, &e->lb[r].agg_n, e->lb_tiles));
+    RC(dalloc(e, &e->lb[r].agg_e, e->lb_tiles));
+    RC(dalloc(e, &e->lb[r].inc_n, e->lb_tiles));
+    RC(dalloc(e, &e->lb[r].inc_e, e->lb_tiles));
+  }
+  RC(dalloc(e, &e->counts_d, 2));
+  RC(dalloc(e, &e->err_d, 4));
+  e->active_d = e->err_d + 1;
+  RC(dalloc(e, &e->sum64_d, 3ull * e->sms * 8 + 4));
+  CK(cudaMallocHost(&e->counts_h, 2 * sizeof(Counts)));
+  CK(cudaMallocHost(&e->err_h, 4 * sizeof(uint32_t)));
+  CK(cudaMallocHost(&e->l1_h, sizeof(double)));
+  if (P.chunk_edges && !(e->cfg.flags & OG_CFG_DIRECT)) {
+    RC(dalloc(e, (char **)&e->stage_d[0], P.chunk_edges * e->eb));
+    RC(dalloc(e, (char **)&e->stage_d[1], P.chunk_edges * e->eb));
+  }
+  if (e->pr_enabled) {
+    RC(dalloc(e, &e->contrib_d, V + 1));
+    RC(dalloc(e, &e->sum_d, V + 1));
+    e->pr_tiles = e->tile_cap[0] + e->tile_cap[1];
+    RC(dalloc(e, &e->cont_d, e->pr_tiles));
+    RC(dalloc(e, &e->carry_d, e->pr_tiles));
+    RC(dalloc(e, &e->carry_idx_d, e->pr_tiles));
+    e->part_n = (uint32_t)e->sms * 8;
+    RC(dalloc(e, &e->part_d, e->part_n));
+    RC(dalloc(e, &e->l1_d, 1));
+  }
+  if (e->batch_enabled) {
+    for (int i = 0; i < 3; i++) RC(dalloc(e, &e->bmask[i], V + 1));
+    RC(dalloc(e, &e->hist_d, (uint64_t)kMaxBatchLevels * 64));
+    RC(dalloc(e, &e->srcs_d, 64));
+    e->ptile_cap = e->g->E / 1024 + 8;
+    RC(dalloc(e, &e->ptile_d, e->ptile_cap));
+    RC(dalloc(e, &e->cta_n, kMaxPersistCtas));
+    RC(dalloc(e, &e->cta_e, kMaxPersistCtas));
+    RC(dalloc(e, &e->bar_d, 16));  // barrier (2), error, levels, stats (4 u64)
+    CK(cudaMallocHost(&e->hist_h, (size_t)kMaxBatchLevels * 64 * sizeof(unsigned long long)));
+    CK(cudaMallocHost(&e->srcs_h, 64 * sizeof(uint32_t)));
+    CK(cudaMallocHost(&e->pmisc_h, 16 * sizeof(uint32_t)));
+  }
+  CK(cudaMemsetAsync(e->err_d, 0, 16, e->s_main));
+  CK(cudaStreamSynchronize(e->s_main));
+  return OG_OK;
 }
 
 int create(og_graph *g, const og_config *cfg, og_engine *e) {
@@ -165,8 +247,7 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
   e->batch_enabled = (cfg->flags & OG_CFG_BATCH) != 0;
   CK(cudaSetDevice(e->dev));
   CK(cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, e->dev));
-  uint32_t pflags = cfg->flags;
-  RC(plan_compute(g->V, g->E, g->off, g->kind, cfg->budget_bytes, cfg->advisek, pflags, &e->plan));
+  RC(plan_compute(g->V, g->E, g->off, g->kind, cfg->budget_bytes, cfg->advisek, cfg->flags, &e->plan));
   const og_plan &P = e->plan;
   size_t free_b = 0, total_b = 0;
   CK(cudaMemGetInfo(&free_b, &total_b));
@@ -175,13 +256,6 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
                 (unsigned long long)P.budget_bytes, (unsigned long long)free_b);
   e->Vs = P.static_vertices;
   e->nwords = ((uint64_t)g->V + 31) / 32 + 2 * kWordsPerCompactTile;
-
-  CK(cudaStreamCreateWithFlags(&e->s_main, cudaStreamNonBlocking));
-  CK(cudaStreamCreateWithFlags(&e->s_dyn, cudaStreamNonBlocking));
-  CK(cudaStreamCreateWithFlags(&e->s_gat, cudaStreamNonBlocking));
-  cudaEvent_t *evs[] = {&e->ev_round, &e->ev_cs, &e->ev_cd, &e->ev_dyn_done, &e->ev_gat[0],
-                        &e->ev_gat[1], &e->ev_rel[0], &e->ev_rel[1], &e->t_s0, &e->t_s1, &e->t_d0};
-  for (auto ev : evs) CK(cudaEventCreate(ev));
 
   // kernels with more than 48 KB of shared memory opt in once per process
   CK(cudaFuncSetAttribute(k_gather<uint32_t, kGatherMult>,
@@ -212,70 +286,13 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
     }
   }
 
+  // resident graph state shared with clones
   const uint64_t V = g->V;
   RC(dalloc(e, &e->off_d, V + 1));
-  RC(dalloc(e, &e->value_d, V + 1));
-  for (int i = 0; i < 3; i++) RC(dalloc(e, &e->bm[i], e->nwords));
-  e->list_cap[0] = std::max<uint64_t>(e->Vs, 1);
-  e->list_cap[1] = std::max<uint64_t>(V - e->Vs, 1);
-  e->tile_cap[0] = P.static_edges / kTile + 2;
-  e->tile_cap[1] = P.dynamic_edges / kTile + 2;
-  // one allocation per array, the dynamic region's part after the static one,
-  // so the batched kernel can also use them as a single list over [0, V)
-  RC(dalloc(e, &e->list_d[0], e->list_cap[0] + e->list_cap[1]));
-  RC(dalloc(e, &e->pref_d[0], e->list_cap[0] + e->list_cap[1] + 2));
-  RC(dalloc(e, &e->tile_d[0], e->tile_cap[0] + e->tile_cap[1]));
-  e->list_d[1] = e->list_d[0] + e->list_cap[0];
-  e->pref_d[1] = e->pref_d[0] + e->list_cap[0] + 1;
-  e->tile_d[1] = e->tile_d[0] + e->tile_cap[0];
-  e->lb_tiles = (uint32_t)((e->nwords + kWordsPerCompactTile - 1) / kWordsPerCompactTile + 1);
-  for (int r = 0; r < 2; r++) {
-    RC(dalloc(e, &e->lb[r].status, e->lb_tiles + 1));
-    e->lb[r].ticket = e->lb[r].status + e->lb_tiles;
-    RC(dalloc(e, &e->lb[r].agg_n, e->lb_tiles));
-    RC(dalloc(e, &e->lb[r].agg_e, e->lb_tiles));
-    RC(dalloc(e, &e->lb[r].inc_n, e->lb_tiles));
-    RC(dalloc(e, &e->lb[r].inc_e, e->lb_tiles));
-  }
-  RC(dalloc(e, &e->counts_d, 2));
-  RC(dalloc(e, &e->err_d, 4));
-  e->active_d = e->err_d + 1;
-  CK(cudaMallocHost(&e->counts_h, 2 * sizeof(Counts)));
-  CK(cudaMallocHost(&e->err_h, 4 * sizeof(uint32_t)));
-  CK(cudaMallocHost(&e->l1_h, sizeof(double)));
-
-  if (P.static_edges) {
-    RC(dalloc(e, (char **)&e->sedges_d, P.static_edges * e->eb));
-  }
-  if (P.chunk_edges) {
-    RC(dalloc(e, (char **)&e->stage_d[0], P.chunk_edges * e->eb));
-    RC(dalloc(e, (char **)&e->stage_d[1], P.chunk_edges * e->eb));
-  }
-  if (e->pr_enabled) {
-    RC(dalloc(e, &e->contrib_d, V + 1));
-    RC(dalloc(e, &e->sum_d, V + 1));
-    RC(dalloc(e, &e->outdeg_d, V + 1));
-    e->pr_tiles = e->tile_cap[0] + e->tile_cap[1];
-    RC(dalloc(e, &e->cont_d, e->pr_tiles));
-    RC(dalloc(e, &e->carry_d, e->pr_tiles));
-    RC(dalloc(e, &e->carry_idx_d, e->pr_tiles));
-    e->part_n = (uint32_t)e->sms * 8;
-    RC(dalloc(e, &e->part_d, e->part_n));
-    RC(dalloc(e, &e->l1_d, 1));
-  }
-  if (e->batch_enabled) {
-    for (int i = 0; i < 3; i++) RC(dalloc(e, &e->bmask[i], V + 1));
-    RC(dalloc(e, &e->hist_d, (uint64_t)kMaxBatchLevels * 64));
-    RC(dalloc(e, &e->srcs_d, 64));
-    e->ptile_cap = g->E / 1024 + 8;
-    RC(dalloc(e, &e->ptile_d, e->ptile_cap));
-    RC(dalloc(e, &e->cta_n, kMaxPersistCtas));
-    RC(dalloc(e, &e->cta_e, kMaxPersistCtas));
-    RC(dalloc(e, &e->bar_d, 16));  // barrier (2), error, levels, stats (4 u64)
-    CK(cudaMallocHost(&e->hist_h, (size_t)kMaxBatchLevels * 64 * sizeof(unsigned long long)));
-    CK(cudaMallocHost(&e->srcs_h, 64 * sizeof(uint32_t)));
-    CK(cudaMallocHost(&e->pmisc_h, 16 * sizeof(uint32_t)));
-  }
+  if (P.static_edges) RC(dalloc(e, (char **)&e->sedges_d, P.static_edges * e->eb));
+  if (e->pr_enabled) RC(dalloc(e, &e->outdeg_d, V + 1));
+  e->resident_bytes = e->dbytes;
+  RC(create_query_state(e));
   if (e->dbytes > P.budget_bytes)
     return fail(OG_E_BUDGET, "engine allocated %llu B, above the %llu B budget",
                 (unsigned long long)e->dbytes, (unsigned long long)P.budget_bytes);
@@ -286,15 +303,40 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
     CK(cudaMemcpyAsync(e->sedges_d, g->edges, P.static_edges * e->eb, cudaMemcpyHostToDevice,
                        e->s_main));
   if (e->pr_enabled) {
-    if (g->kind == OG_GRAPH_PR)
+    if (g->kind == OG_GRAPH_PR) {
       CK(cudaMemcpyAsync(e->outdeg_d, g->outdeg, 4 * V, cudaMemcpyHostToDevice, e->s_main));
-    else
+    } else {
       k_degree_from_offsets<<<grid_for(V, e->sms), kThreads, 0, e->s_main>>>(V, e->off_d, e->outdeg_d);
       e->launches++;
+    }
   }
-  CK(cudaMemsetAsync(e->err_d, 0, 16, e->s_main));
   CK(cudaStreamSynchronize(e->s_main));
   CK(cudaGetLastError());
+  return OG_OK;
+}
+
+// A query context on the parent's resident graph (nothing resident is copied).
+int clone(og_engine *parent, og_engine *e) {
+  e->parent = parent;
+  e->g = parent->g;
+  e->cfg = parent->cfg;
+  e->plan = parent->plan;
+  e->dev = parent->dev;
+  e->sms = parent->sms;
+  e->pr_enabled = parent->pr_enabled;
+  e->batch_enabled = parent->batch_enabled;
+  e->V = parent->V;
+  e->Vs = parent->Vs;
+  e->nwords = parent->nwords;
+  e->eb = parent->eb;
+  e->off_d = parent->off_d;
+  e->sedges_d = parent->sedges_d;
+  e->hedges_d = parent->hedges_d;
+  e->outdeg_d = parent->outdeg_d;
+  e->tuned = parent->tuned;
+  CK(cudaSetDevice(e->dev));
+  RC(create_query_state(e));
+  parent->clones++;
   return OG_OK;
 }
 
@@ -996,6 +1038,31 @@ extern "C" int og_engine_create(og_graph *g, const og_config *cfg, og_engine **o
   });
 }
 
+extern "C" int og_engine_clone(og_engine *parent, og_engine **out) {
+  clear_error();
+  if (!parent || !out) return fail(OG_E_ARG, "og_engine_clone: null argument");
+  if (parent->parent) return fail(OG_E_ARG, "og_engine_clone: clone a parent engine, not a clone");
+  *out = nullptr;
+  return guarded([&]() -> int {
+    og_engine *e = new og_engine;
+    int rc = clone(parent, e);
+    if (rc != OG_OK) {
+      std::string keep = og_last_error();
+      destroy(e);
+      return fail(rc, "%s", keep.c_str());
+    }
+    *out = e;
+    return OG_OK;
+  });
+}
+
+extern "C" int og_engine_bytes(const og_engine *e, uint64_t *resident, uint64_t *context) {
+  if (!e) return fail(OG_E_ARG, "og_engine_bytes: null engine");
+  if (resident) *resident = e->parent ? 0 : e->resident_bytes;
+  if (context) *context = e->parent ? e->dbytes : e->dbytes - e->resident_bytes;
+  return OG_OK;
+}
+
 extern "C" int og_engine_plan(const og_engine *e, og_plan *out) {
   if (!e || !out) return fail(OG_E_ARG, "og_engine_plan: null argument");
   *out = e->plan;
@@ -1129,6 +1196,25 @@ extern "C" int og_bfs_batch_set_config(og_engine *e, int config) {
   if (config < -1 || config >= kNumPersistConfigs) return fail(OG_E_ARG, "config %d out of range", config);
   e->tuned = config;
   return OG_OK;
+}
+
+extern "C" int og_result_checksum(og_engine *e, int algo, uint64_t *out) {
+  if (!e || !out) return fail(OG_E_ARG, "og_result_checksum: null argument");
+  if (e->last_algo != algo) return fail(OG_E_STATE, "no result of algorithm %d on the device", algo);
+  return guarded([&]() -> int {
+    CK(cudaSetDevice(e->dev));
+    const int mode = algo == OG_ALGO_CC ? 1 : (algo == OG_ALGO_PR ? 2 : 0);
+    const uint32_t unreached = algo == OG_ALGO_BFS ? e->V + 1 : 0xFFFFFFFFu;
+    const uint32_t nb = (uint32_t)e->sms * 8;
+    unsigned long long *fin = e->sum64_d + 3ull * nb;
+    k_checksum<<<nb, kThreads, 0, e->s_main>>>(e->value_d, e->V, mode, unreached, e->sum64_d);
+    k_checksum_final<<<1, 32, 0, e->s_main>>>(e->sum64_d, nb, mode, fin);
+    CK(cudaGetLastError());
+    CK(cudaMemcpyAsync(e->counts_h, fin, 16, cudaMemcpyDeviceToHost, e->s_main));
+    CK(cudaStreamSynchronize(e->s_main));
+    memcpy(out, e->counts_h, 16);
+    return OG_OK;
+  });
 }
 
 extern "C" int og_result_fetch(og_engine *e, int algo, void *out) {

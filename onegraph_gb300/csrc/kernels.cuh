@@ -748,6 +748,68 @@ __global__ void k_degree_from_offsets(uint64_t V, const uint64_t *off, uint32_t 
     deg[v] = (uint32_t)(off[v + 1] - off[v]);
 }
 
+// ------------------------------------------------------------------ checksums
+
+// Result checksum in a fixed reduction order (fixed grid, fixed trees):
+// mode 0: {#v with value != unreached, sum of those values} (BFS, SSSP)
+// mode 1: {#v with label == v (components), sum of labels}     (CC)
+// mode 2: {#v, bits of the FP64 sum of the FP32 ranks}          (PR)
+__global__ void __launch_bounds__(kThreads) k_checksum(const uint32_t *val, uint64_t V, int mode,
+                                                       uint32_t unreached,
+                                                       unsigned long long *part) {
+  __shared__ unsigned long long s_c[kThreads], s_s[kThreads];
+  __shared__ double s_d[kThreads];
+  unsigned long long c = 0, sum = 0;
+  double d = 0.0;
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V;
+       v += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t x = val[v];
+    if (mode == 0) {
+      if (x != unreached) {
+        c++;
+        sum += x;
+      }
+    } else if (mode == 1) {
+      c += (x == v) ? 1 : 0;
+      sum += x;
+    } else {
+      c++;
+      d += (double)__uint_as_float(x);
+    }
+  }
+  s_c[threadIdx.x] = c;
+  s_s[threadIdx.x] = sum;
+  s_d[threadIdx.x] = d;
+  __syncthreads();
+  for (int k = kThreads / 2; k > 0; k >>= 1) {
+    if ((int)threadIdx.x < k) {
+      s_c[threadIdx.x] += s_c[threadIdx.x + k];
+      s_s[threadIdx.x] += s_s[threadIdx.x + k];
+      s_d[threadIdx.x] += s_d[threadIdx.x + k];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    part[3 * blockIdx.x] = s_c[0];
+    part[3 * blockIdx.x + 1] = s_s[0];
+    part[3 * blockIdx.x + 2] = __double_as_longlong(s_d[0]);
+  }
+}
+
+__global__ void k_checksum_final(const unsigned long long *part, uint32_t n, int mode,
+                                 unsigned long long *out) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  unsigned long long c = 0, sum = 0;
+  double d = 0.0;
+  for (uint32_t i = 0; i < n; i++) {
+    c += part[3 * i];
+    sum += part[3 * i + 1];
+    d += __longlong_as_double(part[3 * i + 2]);
+  }
+  out[0] = c;
+  out[1] = mode == 2 ? (unsigned long long)__double_as_longlong(d) : sum;
+}
+
 // ------------------------------------------------------------------ fills
 
 __global__ void k_fill_u32(uint32_t *p, uint64_t n, uint32_t v) {

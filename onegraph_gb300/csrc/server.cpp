@@ -1,0 +1,312 @@
+// server.cpp — the serving loop behind og_server_* (onegraph.h).
+//
+// Several graphs stay resident (one parent engine each: offsets + static edge
+// prefix in HBM, the host CSR page-locked).  Requests (BFS / SSSP / CC /
+// PageRank) are queued as they arrive; worker threads admit them when a query
+// context of the request's graph is free or a new one fits the server's
+// device-memory budget, run them (each context has its own streams, so the
+// work of different requests overlaps on the GPU), and post responses.
+// Continuous batching: when a worker admits a BFS request it also takes the
+// BFS requests for the same graph that queued up meanwhile (up to max_batch)
+// and serves them in one og_bfs_batch pass.  Built on the public C ABI only.
+// No reference counterpart: the reference runs one query per process run.
+#include <algorithm>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <mutex>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "og_internal.hpp"
+
+namespace {
+
+struct Pending {
+  og_request r;
+  uint64_t ticket;
+  double t_submit;
+};
+
+struct GraphSlot {
+  og_graph *g = nullptr;
+  og_engine *parent = nullptr;
+  uint64_t ctx_bytes = 0;            // device bytes of one extra query context
+  std::vector<og_engine *> idle;     // contexts ready for a request
+  std::vector<og_engine *> clones;   // every clone created (destroyed with the server)
+  bool batch = false, pagerank = false;
+};
+
+double now_ms(std::chrono::steady_clock::time_point t0) {
+  return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+}
+
+}  // namespace
+
+struct og_server {
+  og_server_config cfg{};
+  std::chrono::steady_clock::time_point t0;
+  std::mutex m;
+  std::condition_variable cv_work, cv_done;
+  std::deque<Pending> queue;
+  std::deque<og_response> done;
+  std::vector<GraphSlot> graphs;
+  std::vector<std::thread> workers;
+  bool stop = false;
+  bool started = false;
+  uint64_t used_bytes = 0;
+  uint64_t next_ticket = 1;
+  uint64_t in_flight = 0;  // submitted and not yet responded
+  og_server_stats st{};
+};
+
+namespace {
+
+using og::fail;
+
+struct Job {
+  std::vector<Pending> reqs;
+  og_engine *ctx = nullptr;
+  int graph = -1;
+};
+
+// Takes the first admissible request (FIFO with skipping) and, for BFS, the
+// queued BFS requests of the same graph.  Called with the lock held.
+bool pick(og_server *s, Job &job) {
+  for (auto it = s->queue.begin(); it != s->queue.end(); ++it) {
+    GraphSlot &gs = s->graphs[it->r.graph];
+    og_engine *ctx = nullptr;
+    if (!gs.idle.empty()) {
+      ctx = gs.idle.back();
+      gs.idle.pop_back();
+    } else if (s->cfg.budget_bytes == 0 || s->used_bytes + gs.ctx_bytes <= s->cfg.budget_bytes) {
+      // admission by free memory: a new context only if it fits the budget
+      if (og_engine_clone(gs.parent, &ctx) != OG_OK) {
+        ctx = nullptr;
+      } else {
+        gs.clones.push_back(ctx);
+        s->used_bytes += gs.ctx_bytes;
+        s->st.contexts_created++;
+      }
+    }
+    if (!ctx) continue;
+    job.ctx = ctx;
+    job.graph = it->r.graph;
+    job.reqs.push_back(*it);
+    const bool bfs_batch = it->r.algo == OG_ALGO_BFS && gs.batch && s->cfg.max_batch > 1 && !it->r.out;
+    it = s->queue.erase(it);
+    if (bfs_batch) {
+      for (auto jt = s->queue.begin(); jt != s->queue.end() && (int)job.reqs.size() < s->cfg.max_batch;) {
+        if (jt->r.graph == job.graph && jt->r.algo == OG_ALGO_BFS && !jt->r.out) {
+          job.reqs.push_back(*jt);
+          jt = s->queue.erase(jt);
+        } else {
+          ++jt;
+        }
+      }
+    }
+    return true;
+  }
+  return false;
+}
+
+void run_job(og_server *s, Job &job, std::vector<og_response> &out) {
+  const double t_start = now_ms(s->t0);
+  og_engine *e = job.ctx;
+  og_stats st;
+  auto respond = [&](const Pending &p, int status, const uint64_t *ck) {
+    og_response r;
+    memset(&r, 0, sizeof r);
+    r.ticket = p.ticket;
+    r.user = p.r.user;
+    r.status = status;
+    r.graph = p.r.graph;
+    r.algo = p.r.algo;
+    r.source = p.r.source;
+    r.batch = (uint32_t)job.reqs.size();
+    r.t_submit_ms = p.t_submit;
+    r.t_start_ms = t_start;
+    if (ck) {
+      r.checksum[0] = ck[0];
+      r.checksum[1] = ck[1];
+    }
+    out.push_back(r);
+  };
+  if (job.reqs.size() > 1) {
+    std::vector<uint32_t> srcs;
+    for (auto &p : job.reqs) srcs.push_back(p.r.source);
+    std::vector<uint64_t> checks(2 * srcs.size());
+    const int rc = og_bfs_batch(e, srcs.data(), (int)srcs.size(), nullptr, checks.data(), &st);
+    for (size_t i = 0; i < job.reqs.size(); i++) respond(job.reqs[i], rc, rc == OG_OK ? &checks[2 * i] : nullptr);
+  } else {
+    const Pending &p = job.reqs[0];
+    int rc;
+    switch (p.r.algo) {
+      case OG_ALGO_BFS: rc = og_bfs(e, p.r.source, (uint32_t *)p.r.out, &st); break;
+      case OG_ALGO_SSSP: rc = og_sssp(e, p.r.source, (uint32_t *)p.r.out, &st); break;
+      case OG_ALGO_CC: rc = og_cc(e, (uint32_t *)p.r.out, &st); break;
+      case OG_ALGO_PR:
+        rc = og_pr_l1(e, (float *)p.r.out, 0.85, 0.0, p.r.iterations > 0 ? p.r.iterations : 5, &st);
+        break;
+      default: rc = OG_E_ARG;
+    }
+    uint64_t ck[2] = {0, 0};
+    if (rc == OG_OK) rc = og_result_checksum(e, p.r.algo, ck);
+    respond(p, rc, rc == OG_OK ? ck : nullptr);
+  }
+  const double t_done = now_ms(s->t0);
+  for (auto &r : out) r.t_done_ms = t_done;
+}
+
+void worker_loop(og_server *s) {
+  cudaSetDevice(s->cfg.device);
+  std::unique_lock<std::mutex> lk(s->m);
+  for (;;) {
+    Job job;
+    while (!s->stop && !pick(s, job)) s->cv_work.wait(lk);
+    if (job.reqs.empty()) break;  // stop requested, nothing admitted
+    s->st.gpu_passes++;
+    if (job.reqs.size() > 1) s->st.batched_requests += job.reqs.size();
+    lk.unlock();
+    std::vector<og_response> out;
+    run_job(s, job, out);
+    lk.lock();
+    s->graphs[job.graph].idle.push_back(job.ctx);
+    for (auto &r : out) s->done.push_back(r);
+    s->in_flight -= out.size();
+    s->st.completed += out.size();
+    s->cv_done.notify_all();
+    s->cv_work.notify_all();  // a context came back: something may be admissible
+  }
+}
+
+void start_workers(og_server *s) {
+  if (s->started) return;
+  s->started = true;
+  for (int i = 0; i < s->cfg.workers; i++) s->workers.emplace_back(worker_loop, s);
+}
+
+}  // namespace
+
+// ====================================================================== C ABI
+
+extern "C" int og_server_create(const og_server_config *cfg, og_server **out) {
+  og::clear_error();
+  if (!cfg || !out) return fail(OG_E_ARG, "og_server_create: null argument");
+  if (cfg->workers < 1 || cfg->workers > 64) return fail(OG_E_ARG, "workers must be 1..64");
+  if (cfg->max_batch < 1 || cfg->max_batch > 64) return fail(OG_E_ARG, "max_batch must be 1..64");
+  og_server *s = new (std::nothrow) og_server;
+  if (!s) return fail(OG_E_NOMEM, "cannot allocate the server");
+  s->cfg = *cfg;
+  s->t0 = std::chrono::steady_clock::now();
+  *out = s;
+  return OG_OK;
+}
+
+extern "C" int og_server_add_graph(og_server *s, og_graph *g, const og_config *gcfg, int *graph_id) {
+  og::clear_error();
+  if (!s || !g || !gcfg) return fail(OG_E_ARG, "og_server_add_graph: null argument");
+  std::lock_guard<std::mutex> lk(s->m);
+  if (s->started) return fail(OG_E_STATE, "graphs must be added before the first request");
+  og_config c = *gcfg;
+  c.device = s->cfg.device;
+  if (s->cfg.max_batch > 1) c.flags |= OG_CFG_BATCH;
+  og_engine *e = nullptr;
+  int rc = og_engine_create(g, &c, &e);
+  if (rc != OG_OK) return rc;
+  uint64_t resident = 0, ctx = 0;
+  og_engine_bytes(e, &resident, &ctx);
+  if (s->cfg.budget_bytes && s->used_bytes + resident + ctx > s->cfg.budget_bytes) {
+    og_engine_destroy(e);
+    return fail(OG_E_BUDGET, "graph does not fit the server budget (%llu B used of %llu B)",
+                (unsigned long long)s->used_bytes, (unsigned long long)s->cfg.budget_bytes);
+  }
+  GraphSlot gs;
+  gs.g = g;
+  gs.parent = e;
+  gs.ctx_bytes = ctx;
+  gs.idle.push_back(e);  // the parent is the first context
+  gs.batch = (c.flags & OG_CFG_BATCH) != 0;
+  gs.pagerank = g->kind == OG_GRAPH_PR || (c.flags & OG_CFG_PR);
+  s->used_bytes += resident + ctx;
+  s->graphs.push_back(std::move(gs));
+  if (graph_id) *graph_id = (int)s->graphs.size() - 1;
+  return OG_OK;
+}
+
+extern "C" int og_server_submit(og_server *s, const og_request *r, uint64_t *ticket) {
+  if (!s || !r) return fail(OG_E_ARG, "og_server_submit: null argument");
+  std::lock_guard<std::mutex> lk(s->m);
+  if (r->graph < 0 || r->graph >= (int)s->graphs.size()) return fail(OG_E_ARG, "unknown graph %d", r->graph);
+  const GraphSlot &gs = s->graphs[r->graph];
+  if (r->algo < OG_ALGO_BFS || r->algo > OG_ALGO_PR) return fail(OG_E_ARG, "unknown algorithm %d", r->algo);
+  if ((r->algo == OG_ALGO_BFS || r->algo == OG_ALGO_SSSP) && r->source >= gs.g->V)
+    return fail(OG_E_ARG, "source %u >= V", r->source);
+  if (r->algo == OG_ALGO_SSSP && gs.g->kind != OG_GRAPH_WEIGHTED)
+    return fail(OG_E_UNSUPPORTED, "SSSP needs a weighted graph");
+  if (r->algo == OG_ALGO_PR && !gs.pagerank) return fail(OG_E_UNSUPPORTED, "graph has no PageRank state");
+  Pending p;
+  p.r = *r;
+  p.ticket = s->next_ticket++;
+  p.t_submit = now_ms(s->t0);
+  s->queue.push_back(p);
+  s->in_flight++;
+  s->st.submitted++;
+  if (ticket) *ticket = p.ticket;
+  start_workers(s);
+  s->cv_work.notify_one();
+  return OG_OK;
+}
+
+extern "C" int og_server_poll(og_server *s, og_response *out, int max, int *n, int wait_ms) {
+  if (!s || !out || !n || max < 1) return fail(OG_E_ARG, "og_server_poll: bad argument");
+  std::unique_lock<std::mutex> lk(s->m);
+  if (s->done.empty() && wait_ms != 0) {
+    auto pred = [&] { return !s->done.empty() || s->in_flight == 0; };
+    if (wait_ms < 0) s->cv_done.wait(lk, pred);
+    else s->cv_done.wait_for(lk, std::chrono::milliseconds(wait_ms), pred);
+  }
+  int k = 0;
+  while (k < max && !s->done.empty()) {
+    out[k++] = s->done.front();
+    s->done.pop_front();
+  }
+  *n = k;
+  return OG_OK;
+}
+
+extern "C" int og_server_drain(og_server *s, int timeout_ms) {
+  if (!s) return fail(OG_E_ARG, "og_server_drain: null server");
+  std::unique_lock<std::mutex> lk(s->m);
+  auto pred = [&] { return s->in_flight == 0; };
+  if (timeout_ms < 0) s->cv_done.wait(lk, pred);
+  else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred))
+    return fail(OG_E_TIMEOUT, "%llu requests still in flight", (unsigned long long)s->in_flight);
+  return OG_OK;
+}
+
+extern "C" int og_server_get_stats(og_server *s, og_server_stats *out) {
+  if (!s || !out) return fail(OG_E_ARG, "og_server_get_stats: null argument");
+  std::lock_guard<std::mutex> lk(s->m);
+  *out = s->st;
+  out->used_bytes = s->used_bytes;
+  return OG_OK;
+}
+
+extern "C" void og_server_destroy(og_server *s) {
+  if (!s) return;
+  {
+    std::lock_guard<std::mutex> lk(s->m);
+    s->stop = true;
+  }
+  s->cv_work.notify_all();
+  for (auto &t : s->workers) t.join();
+  for (auto &gs : s->graphs) {
+    for (og_engine *c : gs.clones) og_engine_destroy(c);
+    og_engine_destroy(gs.parent);
+  }
+  delete s;
+}

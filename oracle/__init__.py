@@ -34,8 +34,10 @@ def lib():
         L.ora_pr_onegraph.argtypes = [u32, _P, _P, _P, C.c_double, C.c_int, _P]
         L.ora_pr_l1.argtypes = [u32, _P, _P, _P, C.c_double, C.c_double, C.c_int, _P,
                                 C.POINTER(C.c_double)]
+        L.ora_pr_l1_mt.argtypes = [u32, _P, _P, _P, C.c_double, C.c_double, C.c_int, C.c_int, _P,
+                                   C.POINTER(C.c_double)]
         for f in ("ora_bfs", "ora_cc", "ora_sssp_frontier", "ora_pr_cpu", "ora_pr_onegraph",
-                  "ora_pr_l1"):
+                  "ora_pr_l1", "ora_pr_l1_mt"):
             getattr(L, f).restype = C.c_int
         _lib = L
     return _lib
@@ -109,6 +111,14 @@ def pr_l1(off, col, outdeg, damping=0.85, tol=1e-6, max_iter=1000):
     l1 = C.c_double()
     it = lib().ora_pr_l1(V, _p(off), _p(col), _p(od), damping, tol, max_iter, _p(out), C.byref(l1))
     return out, it, l1.value
+
+
+def pr_l1_mt_raw(V, off_ptr, col_ptr, outdeg_ptr, damping, tol, max_iter, threads, out):
+    """Pointer form of the multi-threaded FP64 oracle (no copies of large graphs)."""
+    l1 = C.c_double()
+    it = lib().ora_pr_l1_mt(V, off_ptr, col_ptr, outdeg_ptr, damping, tol, max_iter, threads,
+                            out.ctypes.data_as(_P), C.byref(l1))
+    return it, l1.value
 
 
 def normalise_bfs(depth, V):

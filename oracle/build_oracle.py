@@ -44,7 +44,7 @@ def build_oracle(force: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + ".tmp%d" % os.getpid()
     _run(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", "-o", tmp,
-          src, "-lm"])
+          src, "-lm", "-lpthread"])
     os.replace(tmp, LIB)
     return LIB
 

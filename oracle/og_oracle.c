@@ -12,6 +12,7 @@
 #include "og_oracle.h"
 
 #include <math.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -296,5 +297,73 @@ int ora_pr_l1(uint32_t V, const uint64_t *off, const uint32_t *col,
   }
   if (final_l1) *final_l1 = l1;
   free(next);
+  return it;
+}
+
+/* ---- multi-threaded FP64 precision oracle ---- */
+typedef struct {
+  uint32_t V, b, e;
+  const uint64_t *off;
+  const uint32_t *col, *outdeg;
+  const double *cur;
+  double *next, teleport, damping, l1;
+} pr_job;
+
+static void *pr_worker(void *arg) {
+  pr_job *j = (pr_job *)arg;
+  double l1 = 0.0;
+  for (uint32_t v = j->b; v < j->e; v++) {
+    j->next[v] = j->teleport + j->damping * pull_sum(j->off, j->col, j->outdeg, j->cur, v);
+    l1 += fabs(j->next[v] - j->cur[v]);
+  }
+  j->l1 = l1;
+  return NULL;
+}
+
+int ora_pr_l1_mt(uint32_t V, const uint64_t *off, const uint32_t *col,
+                 const uint32_t *outdeg, double damping, double tol, int max_iter,
+                 int threads, double *out, double *final_l1) {
+  if (threads < 1) threads = 1;
+  double *next = (double *)malloc((V ? V : 1) * sizeof(double));
+  pr_job *jobs = (pr_job *)calloc((size_t)threads, sizeof(pr_job));
+  pthread_t *tid = (pthread_t *)calloc((size_t)threads, sizeof(pthread_t));
+  double l1 = 0.0;
+  int it = 0;
+  for (uint32_t i = 0; i < V; i++) out[i] = 1.0 / V;
+  double *cur = out;
+  while (it < max_iter) {
+    for (int t = 0; t < threads; t++) {
+      pr_job *j = &jobs[t];
+      j->V = V;
+      j->b = (uint32_t)((uint64_t)V * t / threads);
+      j->e = (uint32_t)((uint64_t)V * (t + 1) / threads);
+      j->off = off;
+      j->col = col;
+      j->outdeg = outdeg;
+      j->cur = cur;
+      j->next = next;
+      j->teleport = (1.0 - damping) / V;
+      j->damping = damping;
+      pthread_create(&tid[t], NULL, pr_worker, j);
+    }
+    l1 = 0.0;
+    for (int t = 0; t < threads; t++) {
+      pthread_join(tid[t], NULL);
+      l1 += jobs[t].l1;
+    }
+    double *tmp = cur;
+    cur = next;
+    next = tmp;
+    it++;
+    if (l1 < tol) break;
+  }
+  if (cur != out) {
+    memcpy(out, cur, (size_t)V * sizeof(double));
+    next = cur;
+  }
+  if (final_l1) *final_l1 = l1;
+  free(next);
+  free(jobs);
+  free(tid);
   return it;
 }

@@ -76,6 +76,12 @@ int ora_pr_l1(uint32_t V, const uint64_t *off, const uint32_t *col,
               const uint32_t *outdeg, double damping, double tol, int max_iter,
               double *out, double *final_l1);
 
+/* ora_pr_l1 on `threads` host threads (vertex ranges; the L1 partials are
+ * added in thread order, so the result does not depend on scheduling). */
+int ora_pr_l1_mt(uint32_t V, const uint64_t *off, const uint32_t *col,
+                 const uint32_t *outdeg, double damping, double tol, int max_iter,
+                 int threads, double *out, double *final_l1);
+
 #ifdef __cplusplus
 }
 #endif

@@ -108,3 +108,14 @@ def test_normalise_bfs_unreached(n):
     d = np.array([1, 2, 6, 6], np.uint32)
     out = oracle.normalise_bfs(d, 5)
     assert out.tolist() == [1, 2, 0xFFFFFFFF, 0xFFFFFFFF]
+
+
+def test_pr_l1_multithreaded_equals_serial():
+    import onegraph_gb300 as og
+    g = og.Graph.rmat(11, 16, pagerank=True, symmetric=False)
+    off, col, od = np.array(g.offsets), np.array(g.columns), np.array(g.outdeg)
+    a, ia, la = oracle.pr_l1(off, col, od, 0.85, 1e-9, 500)
+    b = np.empty(g.V)
+    ib, lb = oracle.pr_l1_mt_raw(g.V, g._off_p, g._edges_p, g._outdeg_p, 0.85, 1e-9, 500, 5, b)
+    assert ia == ib and la == lb
+    np.testing.assert_array_equal(a, b)
