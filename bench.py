@@ -34,6 +34,8 @@ import numpy as np
 ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
+from onegraph_gb300 import replicas  # noqa: E402
+
 GIB = 1 << 30
 
 
@@ -59,6 +61,8 @@ def parse_args():
     ap.add_argument("--requests", type=int, default=400)
     ap.add_argument("--rate", type=float, default=2000.0)
     ap.add_argument("--workers", type=int, default=4)
+    ap.add_argument("--delta", type=float, default=0.0,
+                    help="SSSP near/far split width (0: plain frontier relaxation)")
     ap.add_argument("--direct", type=int, default=1,
                     help="1: relax the dynamic region straight from page-locked host memory "
                          "(fastest); 0: gather into double-buffered device staging first")
@@ -71,10 +75,7 @@ def parse_args():
 
 
 def dist_env():
-    rank = int(os.environ.get("RANK", "0"))
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return rank, world, local
+    return replicas.rank_info()
 
 
 def pick_sources(deg: np.ndarray, n: int, seed: int = 3) -> list[int]:
@@ -254,7 +255,7 @@ def config_dict(args, g):
             "V": g.V, "E": g.E, "budget_bytes": int(args.budget_gib * GIB), "advisek": args.advisek,
             "sources": args.sources, "seeds": {"graph": 1, "weights": 2, "sources": 3},
             "l2": "inputs larger than L2 (graph %.1f GB)" % (g.E * 8 / 1e9),
-            "dynamic_mode": "direct" if args.direct else "staged"}
+            "dynamic_mode": "direct" if args.direct else "staged", "sssp_delta": args.delta}
 
 
 def run_ours(args, rank, world, local):
@@ -269,17 +270,16 @@ def run_ours(args, rank, world, local):
     deg = g.degrees()
     srcs = pick_sources(deg, args.sources)
     # replicas: each rank serves its own slice of the source list
-    srcs = srcs[rank::world] if world > 1 else srcs
+    srcs = replicas.slice_queries(srcs, rank, world)
     t0 = time.time()
     eng = og.Engine(g, budget=int(args.budget_gib * GIB), advisek=args.advisek,
                     direct=bool(args.direct), device=local)
     engine_s = time.time() - t0
+    eng.set_param(og.PARAM_SSSP_DELTA, args.delta)
     plan = eng.plan
 
     def barrier():
-        if world > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        replicas.barrier(world)
 
     for i in range(args.warmup):
         eng.sssp(srcs[i % len(srcs)], out=False)
@@ -299,13 +299,8 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize()
     barrier()
     clocks = sampler.stop()
-    t_dev = ev0.elapsed_time(ev1) / 1e3
-    if world > 1:
-        import torch.distributed as dist
-        t = torch.tensor([t_dev], device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_dev = float(t.item())
-    value = args.steps * world / t_dev
+    t_dev = replicas.max_over_ranks(ev0.elapsed_time(ev1) / 1e3, world)
+    value = replicas.whole_job_rate(args.steps, world, t_dev)
     # end-to-end through the C ABI into a page-locked host buffer
     host = torch.empty(g.V, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
     torch.cuda.synchronize()

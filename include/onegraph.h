@@ -90,6 +90,11 @@ int og_graph_info(const og_graph *g, uint64_t *V, uint64_t *E, int *kind,
  * page-lock and read its host arrays. */
 void og_graph_free(og_graph *g);
 
+/* Graph::convert2BEL (BFS/cpu_BFS/Graph.h:134-163): writes <prefix>.bel.col
+ * (u64 V, u64 0, u64 offsets[V]), <prefix>.bel.dst (u64 E, u64 0, u64
+ * dst[E]) and, for weighted graphs, <prefix>.bel.val (u64 E, u64 0, u32 w[E]). */
+int og_graph_save_bel(const og_graph *g, const char *prefix);
+
 /* GraphMeta::findbignode (GraphMeta.h:150-165): first vertex after `last`
  * whose degree exceeds 3000, or `last` when there is none. */
 uint32_t og_graph_findbignode(const og_graph *g, uint32_t last);
@@ -158,6 +163,11 @@ typedef struct og_config {
 #define OG_CFG_BATCH_LEVELS 16u /* og_bfs_batch drives levels from the host (one
                                    kernel sequence per level) instead of the
                                    persistent cooperative kernel */
+#define OG_CFG_NO_STATIC 32u /* keep no static region: every active edge comes
+                                 from host memory each round.  With staging this
+                                 is the Subway scheme (BFS/sbw_BFS/main.cpp:323-506),
+                                 with OG_CFG_DIRECT|OG_CFG_NO_PIN the unified-
+                                 memory scheme (BFS/usm_BFS/main.cpp:120-222) */
 #define OG_CFG_PR 4u      /* also hold PageRank state for a PLAIN/WEIGHTED
                              graph, read as symmetric (in-edges = out-edges,
                              outDegree = degree); implied for OG_GRAPH_PR    */
@@ -251,6 +261,16 @@ int og_bfs_batch_set_config(og_engine *e, int config);
  * (the reference runs one query at a time). */
 int og_engine_clone(og_engine *parent, og_engine **out);
 
+/* Engine parameters.
+ * OG_PARAM_SSSP_DELTA: width of og_sssp's near/far split.  0 (default)
+ *   relaxes every frontier vertex each round, as the reference does
+ *   (SSSP/oneGraph/CalculateOpt.h:73-185); d > 0 expands only frontier
+ *   vertices whose distance is below a threshold that moves in steps of d,
+ *   which re-expands fewer vertices (fewer edges over the host link) at the
+ *   cost of more rounds.  Distances are exact either way.  Clones inherit it. */
+#define OG_PARAM_SSSP_DELTA 1
+int og_engine_set_param(og_engine *e, int param, double value);
+
 /* Device bytes of the shared resident graph (0 for a clone) and of one
  * query context. */
 int og_engine_bytes(const og_engine *e, uint64_t *resident, uint64_t *context);
@@ -321,7 +341,9 @@ int og_k_compact_noalloc(const uint32_t *bits, uint32_t v_begin, uint32_t v_end,
  * query context of their graph is free or a new one fits budget_bytes; the
  * work of concurrent requests overlaps on the GPU.  BFS requests for the same
  * graph that queue up while others run are fused into one og_bfs_batch pass
- * (up to max_batch).  Results are identical to running each request alone. */
+ * (up to max_batch), and queued PageRank requests for the same graph and
+ * iteration count share one computation.  Results are identical to running
+ * each request alone. */
 typedef struct og_server og_server;
 
 typedef struct og_server_config {

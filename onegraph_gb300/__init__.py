@@ -25,7 +25,8 @@ STATUS = {0: "OG_OK", 1: "OG_E_ARG", 2: "OG_E_IO", 3: "OG_E_FORMAT", 4: "OG_E_BU
 PLAIN, WEIGHTED, PR = 0, 1, 2
 ALGO_BFS, ALGO_SSSP, ALGO_CC, ALGO_PR = 0, 1, 2, 3
 RMAT_SYMMETRIC, RMAT_PERMUTE, RMAT_WEIGHTED, RMAT_PR, RMAT_ON_GPU = 1, 2, 4, 8, 16
-CFG_DIRECT, CFG_NO_PIN, CFG_PR, CFG_BATCH, CFG_BATCH_LEVELS = 1, 2, 4, 8, 16
+CFG_DIRECT, CFG_NO_PIN, CFG_PR, CFG_BATCH, CFG_BATCH_LEVELS, CFG_NO_STATIC = 1, 2, 4, 8, 16, 32
+PARAM_SSSP_DELTA = 1
 # R-MAT quadrant probabilities of the benchmark graphs
 RMAT_ABC = (0.57, 0.19, 0.19)
 
@@ -124,6 +125,7 @@ SIGNATURES = [
                                 C.POINTER(C.c_int), C.POINTER(_P), C.POINTER(_P), C.POINTER(_P)]),
     ("og_graph_free", None, [_P]),
     ("og_graph_findbignode", C.c_uint32, [_P, C.c_uint32]),
+    ("og_graph_save_bel", C.c_int, [_P, C.c_char_p]),
     ("og_rmat_generate", C.c_int, [C.POINTER(RmatParams), C.POINTER(_P)]),
     ("og_plan_compute", C.c_int, [C.c_uint64, C.c_uint64, _P, C.c_int, C.c_uint64, C.c_double,
                                   C.c_uint32, C.POINTER(Plan)]),
@@ -142,6 +144,7 @@ SIGNATURES = [
     ("og_result_checksum", C.c_int, [_P, C.c_int, _P]),
     ("og_engine_clone", C.c_int, [_P, C.POINTER(_P)]),
     ("og_engine_bytes", C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
+    ("og_engine_set_param", C.c_int, [_P, C.c_int, C.c_double]),
     ("og_k_compact", C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P, C.c_uint64, _P,
                                C.c_uint64, _P, _P]),
     ("og_k_compact_noalloc", C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P, C.c_uint64, _P,
@@ -234,6 +237,9 @@ class Graph:
     def save(self, path: str):
         _check(lib().og_graph_save(self._h, path.encode()), "og_graph_save")
 
+    def save_bel(self, prefix: str):
+        _check(lib().og_graph_save_bel(self._h, prefix.encode()), "og_graph_save_bel")
+
     @property
     def offsets(self) -> np.ndarray:
         """V+1 offsets (borrowed view, valid while the graph lives)."""
@@ -305,11 +311,12 @@ class Engine:
 
     def __init__(self, graph: Graph, budget: int = 0, advisek: float = 0.0, direct: bool = False,
                  pagerank: bool = False, no_pin: bool = False, batch: bool = False,
-                 batch_levels: bool = False, device: int = 0):
+                 batch_levels: bool = False, no_static: bool = False, device: int = 0):
         self.graph = graph
         cfg = Config(budget, advisek, (CFG_DIRECT if direct else 0) | (CFG_PR if pagerank else 0) |
                      (CFG_NO_PIN if no_pin else 0) | (CFG_BATCH if batch or batch_levels else 0) |
-                     (CFG_BATCH_LEVELS if batch_levels else 0), device)
+                     (CFG_BATCH_LEVELS if batch_levels else 0) |
+                     (CFG_NO_STATIC if no_static else 0), device)
         h = _P()
         _check(lib().og_engine_create(graph._h, C.byref(cfg), C.byref(h)), "og_engine_create")
         self._h = h
@@ -397,6 +404,9 @@ class Engine:
         self.graph._engines += 1
         self._clones = getattr(self, "_clones", 0) + 1
         return c
+
+    def set_param(self, param: int, value: float):
+        _check(lib().og_engine_set_param(self._h, param, value), "og_engine_set_param")
 
     def bytes(self) -> tuple:
         """(device bytes of the resident graph, of one query context)."""

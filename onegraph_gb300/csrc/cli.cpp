@@ -4,7 +4,8 @@
 // Argument handling follows ArgumentParser::Parse (BFS/oneGraph_BFS/
 // ArgumentParser.h:40-73): argv is read in (flag, value) pairs from index 1.
 // Accepted flags: -f <csr>, --type/-type <bfs|sssp|cc|pr>, -r <source>,
-// --method/-method <unused>, --adviseK/-adviseK/--advisek/-advisek <ratio>,
+// --method/-method <0 OneGraph | 1 Subway | 2 USM> (parsed but unused by the
+// reference), --adviseK/-adviseK/--advisek/-advisek <ratio>,
 // plus --budget <bytes|NNG|NNM>, --dump <file>, --sources <n>,
 // --direct <0|1>, --json <0|1>, --threshold <pr delta>, --device <ordinal>.
 // Differences from the reference, on purpose: a --type naming another
@@ -42,6 +43,7 @@ struct Args {
   uint64_t budget = 0;
   int sources = 5;  // CalculateOpt.h:7 testTimes
   int direct = 0, json = 0, device = 0;
+  int method = 0;  // 0 OneGraph/Ascetic, 1 Subway (no static region, staged), 2 USM (no static region, pageable host reads)
   double threshold = 0.001;
 };
 
@@ -54,6 +56,7 @@ static bool parse(int argc, char **argv, Args &a) {
       a.source = atoi(v);
       a.has_source = true;
     } else if (!strcmp(k, "--method") || !strcmp(k, "-method")) {
+      a.method = atoi(v);
     } else if (!strcmp(k, "--adviseK") || !strcmp(k, "-adviseK") || !strcmp(k, "--advisek") ||
                !strcmp(k, "-advisek"))
       a.advisek = atof(v);
@@ -125,6 +128,8 @@ int main(int argc, char **argv) {
   cfg.budget_bytes = a.budget;
   cfg.advisek = a.advisek;
   cfg.flags = a.direct ? OG_CFG_DIRECT : 0;
+  if (a.method == 1) cfg.flags = OG_CFG_NO_STATIC;
+  if (a.method == 2) cfg.flags = OG_CFG_NO_STATIC | OG_CFG_DIRECT | OG_CFG_NO_PIN;
   cfg.device = a.device;
   og_engine *e = nullptr;
   rc = og_engine_create(g, &cfg, &e);

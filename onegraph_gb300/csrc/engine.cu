@@ -101,6 +101,8 @@ struct og_engine {
   uint64_t resident_bytes = 0;  // device bytes of the shared resident state
   unsigned long long *sum64_d = nullptr;  // result checksum scratch
 
+  uint32_t sssp_delta = 0;  // near/far split width (0: plain frontier relaxation)
+
   int last_algo = -1;
   uint64_t launches = 0;  // kernels launched since the query began
   std::vector<void *> dallocs;
@@ -334,6 +336,7 @@ int clone(og_engine *parent, og_engine *e) {
   e->hedges_d = parent->hedges_d;
   e->outdeg_d = parent->outdeg_d;
   e->tuned = parent->tuned;
+  e->sssp_delta = parent->sssp_delta;
   CK(cudaSetDevice(e->dev));
   RC(create_query_state(e));
   parent->clones++;
@@ -343,8 +346,9 @@ int clone(og_engine *parent, og_engine *e) {
 // ------------------------------------------------------------------ rounds
 
 int launch_compact(og_engine *e, int r, const uint32_t *bits, uint32_t vb, uint32_t ve,
-                   cudaStream_t s) {
+                   cudaStream_t s, uint32_t *far_bits = nullptr, uint32_t thr = 0) {
   CK(cudaMemsetAsync(e->counts_d + r, 0, sizeof(Counts), s));
+  CK(cudaMemsetAsync(&e->counts_d[r].far_min, 0xff, sizeof(uint32_t), s));  // far minimum
   if (ve <= vb) return OG_OK;
   CompactArgs a;
   a.bits = bits;
@@ -362,6 +366,10 @@ int launch_compact(og_engine *e, int r, const uint32_t *bits, uint32_t vb, uint3
   a.err = e->err_d;
   a.list_cap = e->list_cap[r];
   a.tile_cap = e->tile_cap[r];
+  a.value = e->value_d;
+  a.thr = thr;
+  a.far_bits = far_bits;
+  a.far_min = &e->counts_d[r].far_min;
   if (a.ntiles + 1 > e->lb_tiles) return fail(OG_E_STATE, "compaction scratch too small");
   CK(cudaMemsetAsync(e->lb[r].status, 0, sizeof(uint32_t) * (e->lb_tiles + 1), s));
   k_compact<<<a.ntiles, kThreads, 0, s>>>(a);
@@ -512,12 +520,13 @@ int run_regions(og_engine *e, og_stats &st, Timing &tm, StaticFn static_fn, DynF
 
 // Compacts both regions of `cur` and brings the counts (and the error word) to
 // the host.  Returns the number of listed vertices through *n.
-int compact_round(og_engine *e, const uint32_t *cur, og_stats &st, Timing &tm, uint64_t *n) {
+int compact_round(og_engine *e, const uint32_t *cur, og_stats &st, Timing &tm, uint64_t *n,
+                  uint32_t *far_bits = nullptr, uint32_t thr = 0) {
   CK(cudaEventRecord(e->ev_round, e->s_main));
-  RC(launch_compact(e, 0, cur, 0, e->Vs, e->s_main));
+  RC(launch_compact(e, 0, cur, 0, e->Vs, e->s_main, far_bits, thr));
   CK(cudaEventRecord(e->ev_cs, e->s_main));
   CK(cudaStreamWaitEvent(e->s_dyn, e->ev_round, 0));
-  RC(launch_compact(e, 1, cur, e->Vs, e->V, e->s_dyn));
+  RC(launch_compact(e, 1, cur, e->Vs, e->V, e->s_dyn, far_bits, thr));
   CK(cudaEventRecord(e->ev_cd, e->s_dyn));
   CK(cudaStreamWaitEvent(e->s_dyn, e->ev_cs, 0));
   CK(cudaMemcpyAsync(e->counts_h, e->counts_d, 2 * sizeof(Counts), cudaMemcpyDeviceToHost, e->s_dyn));
@@ -557,10 +566,24 @@ int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
   CK(cudaGetLastError());
   Timing tm;
   RoundOps ro{algo, 1};
+  // SSSP near/far split: a round expands only frontier vertices closer than
+  // thr; the others stay in the frontier until no near vertex is left, then
+  // thr moves to the smallest waiting distance + delta
+  const bool split = algo == OG_ALGO_SSSP && e->sssp_delta > 0;
+  uint64_t thr = 1ull + e->sssp_delta;
   for (;;) {
     uint64_t n = 0;
-    RC(compact_round(e, cur, st, tm, &n));
-    if (n == 0) break;
+    RC(compact_round(e, cur, st, tm, &n, split ? next : nullptr,
+                     (uint32_t)std::min<uint64_t>(thr, 0xffffffffull)));
+    if (n == 0) {
+      const uint32_t fm = std::min(e->counts_h[0].far_min, e->counts_h[1].far_min);
+      if (!split || fm == 0xffffffffu) break;
+      thr = (uint64_t)fm + e->sssp_delta;  // the waiting vertices are now in next
+      CK(cudaStreamWaitEvent(e->s_main, e->ev_cd, 0));
+      CK(cudaMemsetAsync(cur, 0, 4 * e->nwords, e->s_main));
+      std::swap(cur, next);
+      continue;
+    }
     st.iterations++;
     st.frontier_sum += n;
     st.static_vertices += e->counts_h[0].n;
@@ -1056,6 +1079,16 @@ extern "C" int og_engine_clone(og_engine *parent, og_engine **out) {
   });
 }
 
+extern "C" int og_engine_set_param(og_engine *e, int param, double value) {
+  if (!e) return fail(OG_E_ARG, "og_engine_set_param: null engine");
+  if (param == OG_PARAM_SSSP_DELTA) {
+    if (value < 0 || value > 4294967295.0) return fail(OG_E_ARG, "delta out of range");
+    e->sssp_delta = (uint32_t)value;
+    return OG_OK;
+  }
+  return fail(OG_E_ARG, "unknown parameter %d", param);
+}
+
 extern "C" int og_engine_bytes(const og_engine *e, uint64_t *resident, uint64_t *context) {
   if (!e) return fail(OG_E_ARG, "og_engine_bytes: null engine");
   if (resident) *resident = e->parent ? 0 : e->resident_bytes;
@@ -1254,6 +1287,10 @@ void compact_launch(const uint32_t *bits, uint32_t v_begin, uint32_t v_end, cons
   a.err = err;
   a.list_cap = list_cap;
   a.tile_cap = tile_cap;
+  a.value = nullptr;
+  a.thr = 0;
+  a.far_bits = nullptr;
+  a.far_min = nullptr;
   k_compact<<<a.ntiles, kThreads, 0, s>>>(a);
 }
 

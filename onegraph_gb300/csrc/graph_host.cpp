@@ -157,6 +157,7 @@ int plan_compute(uint32_t V, uint64_t E, const uint64_t *off, int kind,
   p.advisek = use;
   uint64_t mps = (uint64_t)(use * (double)T);
   if (mps > E) mps = E;
+  if (flags & OG_CFG_NO_STATIC) mps = 0;
   const bool direct = (flags & OG_CFG_DIRECT) != 0;
   auto prefix_for = [&](uint64_t limit) -> uint32_t {
     // largest Vs with off[Vs] <= limit (off is monotone, off[0] == 0)
@@ -325,6 +326,42 @@ extern "C" int og_graph_info(const og_graph *g, uint64_t *V, uint64_t *E, int *k
   if (edges) *edges = g->edges;
   if (outdeg) *outdeg = g->outdeg;
   return OG_OK;
+}
+
+extern "C" int og_graph_save_bel(const og_graph *g, const char *prefix) {
+  clear_error();
+  if (!g || !prefix) return fail(OG_E_ARG, "og_graph_save_bel: null argument");
+  const std::string base(prefix);
+  const uint64_t zero = 0, V = g->V, E = g->E;
+  const bool weighted = g->kind == OG_GRAPH_WEIGHTED;
+  const uint32_t *c = (const uint32_t *)g->edges;
+  const uint64_t stride = weighted ? 2 : 1;
+  auto open_w = [&](const char *ext) { return fopen((base + ext).c_str(), "wb"); };
+  FILE *f = open_w(".bel.col");
+  if (!f) return fail(OG_E_IO, "cannot create %s.bel.col", prefix);
+  bool ok = fwrite(&V, 8, 1, f) == 1 && fwrite(&zero, 8, 1, f) == 1 && fwrite(g->off, 8, V, f) == V;
+  ok = (fclose(f) == 0) && ok;
+  f = ok ? open_w(".bel.dst") : nullptr;
+  ok = ok && f && fwrite(&E, 8, 1, f) == 1 && fwrite(&zero, 8, 1, f) == 1;
+  std::vector<uint64_t> buf(1 << 20);
+  for (uint64_t e0 = 0; ok && e0 < E; e0 += buf.size()) {
+    const uint64_t n = std::min<uint64_t>(buf.size(), E - e0);
+    for (uint64_t i = 0; i < n; i++) buf[i] = c[(e0 + i) * stride];
+    ok = fwrite(buf.data(), 8, n, f) == n;
+  }
+  if (f) ok = (fclose(f) == 0) && ok;
+  if (ok && weighted) {
+    f = open_w(".bel.val");
+    ok = f && fwrite(&E, 8, 1, f) == 1 && fwrite(&zero, 8, 1, f) == 1;
+    std::vector<uint32_t> w(1 << 20);
+    for (uint64_t e0 = 0; ok && e0 < E; e0 += w.size()) {
+      const uint64_t n = std::min<uint64_t>(w.size(), E - e0);
+      for (uint64_t i = 0; i < n; i++) w[i] = c[2 * (e0 + i) + 1];
+      ok = fwrite(w.data(), 4, n, f) == n;
+    }
+    if (f) ok = (fclose(f) == 0) && ok;
+  }
+  return ok ? OG_OK : fail(OG_E_IO, "writing %s.bel.* failed", prefix);
 }
 
 extern "C" uint32_t og_graph_findbignode(const og_graph *g, uint32_t last) {

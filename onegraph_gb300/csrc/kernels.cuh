@@ -37,9 +37,9 @@ constexpr uint32_t kErrTileMap = 8u;     // LBS tile map inconsistent
 constexpr uint32_t kSpinLimit = 1u << 24;
 
 struct Counts {
-  uint32_t n;      // compacted vertices
-  uint32_t pad;
-  uint64_t total;  // sum of their degrees (edge positions)
+  uint32_t n;        // compacted vertices
+  uint32_t far_min;  // near/far split: smallest value left for later rounds
+  uint64_t total;    // sum of their degrees (edge positions)
 };
 
 struct Lookback {
@@ -64,6 +64,13 @@ struct CompactArgs {
   uint32_t *err;
   uint64_t list_cap;     // entries of list (pref has list_cap + 1)
   uint64_t tile_cap;     // entries of tile_first
+  // near/far split (SSSP): when far_bits != nullptr only vertices with
+  // value < thr are listed; the others with edges are OR-ed into far_bits and
+  // the smallest of their values goes to *far_min
+  const uint32_t *value;
+  uint32_t thr;
+  uint32_t *far_bits;
+  uint32_t *far_min;
 };
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
@@ -150,17 +157,28 @@ __global__ void __launch_bounds__(kThreads) k_compact(CompactArgs a) {
     }
   }
   // drop vertices without edges: nothing to expand
-  uint32_t keep = 0, cnt = 0;
+  uint32_t keep = 0, cnt = 0, far = 0, fmin = 0xffffffffu;
   uint64_t sum = 0;
   for (uint32_t m = word; m; m &= m - 1) {
     const uint32_t b = __ffs(m) - 1;
     const uint64_t v = vbase + b;
     const uint64_t d = a.off[v + 1] - a.off[v];
-    if (d) {
-      keep |= 1u << b;
-      cnt++;
-      sum += d;
+    if (!d) continue;
+    if (a.far_bits) {
+      const uint32_t x = __ldcg(a.value + v);
+      if (x >= a.thr) {
+        far |= 1u << b;
+        fmin = min(fmin, x);
+        continue;
+      }
     }
+    keep |= 1u << b;
+    cnt++;
+    sum += d;
+  }
+  if (far) {
+    atomicOr(a.far_bits + w, far);
+    atomicMin(a.far_min, fmin);
   }
   uint32_t ex_n, tot_n;
   uint64_t ex_e, tot_e;

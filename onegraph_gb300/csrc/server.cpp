@@ -8,7 +8,8 @@
 // work of different requests overlaps on the GPU), and post responses.
 // Continuous batching: when a worker admits a BFS request it also takes the
 // BFS requests for the same graph that queued up meanwhile (up to max_batch)
-// and serves them in one og_bfs_batch pass.  Built on the public C ABI only.
+// and serves them in one og_bfs_batch pass; queued PageRank requests for the
+// same graph share one computation.  Built on the public C ABI only.
 // No reference counterpart: the reference runs one query per process run.
 #include <algorithm>
 #include <chrono>
@@ -97,10 +98,16 @@ bool pick(og_server *s, Job &job) {
     job.graph = it->r.graph;
     job.reqs.push_back(*it);
     const bool bfs_batch = it->r.algo == OG_ALGO_BFS && gs.batch && s->cfg.max_batch > 1 && !it->r.out;
+    // PageRank does not depend on a source: queued PR requests for the same
+    // graph and iteration count are answered by one computation
+    const bool pr_share = it->r.algo == OG_ALGO_PR && s->cfg.max_batch > 1;
+    const int iters = it->r.iterations;
     it = s->queue.erase(it);
-    if (bfs_batch) {
+    if (bfs_batch || pr_share) {
       for (auto jt = s->queue.begin(); jt != s->queue.end() && (int)job.reqs.size() < s->cfg.max_batch;) {
-        if (jt->r.graph == job.graph && jt->r.algo == OG_ALGO_BFS && !jt->r.out) {
+        const bool same_bfs = bfs_batch && jt->r.algo == OG_ALGO_BFS && !jt->r.out;
+        const bool same_pr = pr_share && jt->r.algo == OG_ALGO_PR && jt->r.iterations == iters;
+        if (jt->r.graph == job.graph && (same_bfs || same_pr)) {
           job.reqs.push_back(*jt);
           jt = s->queue.erase(jt);
         } else {
@@ -135,7 +142,17 @@ void run_job(og_server *s, Job &job, std::vector<og_response> &out) {
     }
     out.push_back(r);
   };
-  if (job.reqs.size() > 1) {
+  if (job.reqs.size() > 1 && job.reqs[0].r.algo == OG_ALGO_PR) {
+    const Pending &p = job.reqs[0];
+    int rc = og_pr_l1(e, nullptr, 0.85, 0.0, p.r.iterations > 0 ? p.r.iterations : 5, &st);
+    uint64_t ck[2] = {0, 0};
+    if (rc == OG_OK) rc = og_result_checksum(e, OG_ALGO_PR, ck);
+    for (auto &q : job.reqs) {
+      int rq = rc;
+      if (rq == OG_OK && q.r.out) rq = og_result_fetch(e, OG_ALGO_PR, q.r.out);
+      respond(q, rq, rq == OG_OK ? ck : nullptr);
+    }
+  } else if (job.reqs.size() > 1) {
     std::vector<uint32_t> srcs;
     for (auto &p : job.reqs) srcs.push_back(p.r.source);
     std::vector<uint64_t> checks(2 * srcs.size());

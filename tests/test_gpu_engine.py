@@ -84,8 +84,11 @@ def test_sssp_matches_dijkstra(scale, seed):
     want = {s: oracle.sssp_dijkstra(off, pairs, s) for s in srcs}
     for cname, kw in configs(g):
         e = engine(g, **kw)
-        for s in srcs:
-            np.testing.assert_array_equal(e.sssp(s), want[s], err_msg="%s src %d" % (cname, s))
+        for delta in (0, 8, 64, 300):  # plain frontier relaxation and near/far splits
+            e.set_param(og.PARAM_SSSP_DELTA, delta)
+            for s in srcs:
+                np.testing.assert_array_equal(e.sssp(s), want[s],
+                                              err_msg="%s delta %d src %d" % (cname, delta, s))
         e.close()
 
 
@@ -201,3 +204,20 @@ def test_gpu_generator_matches_host_generator():
         np.testing.assert_array_equal(a.edges, b.edges)
         if a.outdeg is not None:
             np.testing.assert_array_equal(a.outdeg, b.outdeg)
+
+
+@pytest.mark.parametrize("mode", ["subway", "usm"])
+def test_subway_and_unified_memory_modes(mode):
+    """No static region: every active edge comes from host memory each round,
+    gathered into staging (Subway scheme) or read from pageable memory through
+    address translation (unified-memory scheme)."""
+    g = og.Graph.rmat(12, 16, weighted=True, seed=11)
+    off, pairs = np.array(g.offsets), np.array(g.edges)
+    kw = dict(no_static=True) if mode == "subway" else dict(no_static=True, direct=True, no_pin=True)
+    e = og.Engine(g, budget=budget_for(g, max(int(0.3 * g.E), 3 * 2048)), **kw)
+    assert e.plan["static_edges"] == 0
+    s = int(np.argmax(g.degrees()))
+    np.testing.assert_array_equal(e.sssp(s), oracle.sssp_dijkstra(off, pairs, s))
+    np.testing.assert_array_equal(oracle.normalise_bfs(e.bfs(s), g.V), oracle.bfs(off, pairs[:, 0].copy(), s)[0])
+    np.testing.assert_array_equal(e.cc(), oracle.cc(off, pairs[:, 0].copy())[0])
+    assert e.stats["edges_static"] == 0 and e.stats["edges_dynamic"] > 0

@@ -60,7 +60,8 @@ def test_results_identical_alone_and_in_the_mix():
     assert len(resp) == len(reqs)
     st = srv.stats()
     assert st["completed"] == len(reqs)
-    assert any(r["batch"] > 1 for r in resp.values()), "queued BFS requests should be fused"
+    assert any(r["batch"] > 1 and r["algo"] == og.ALGO_BFS for r in resp.values()), \
+        "queued BFS requests should be fused"
     # alone: each request on its own engine planned exactly like the server's
     alone = [og.Engine(g, budget=_budget(g), advisek=0.5, direct=True, pagerank=True, batch=True)
              for g in graphs]

@@ -215,3 +215,25 @@ def test_cli_argument_errors(tmp_path):
     r = subprocess.run([_cli("CC_OneGraph"), "-f", str(tmp_path / "nope.csr")], capture_output=True,
                        text=True)
     assert r.returncode == 1 and "og_graph_load" in r.stderr
+
+
+def test_bel_export_layout(tmp_path):
+    g = og.Graph.rmat(8, 8, weighted=True)
+    prefix = str(tmp_path / "g")
+    g.save_bel(prefix)
+    col = np.fromfile(prefix + ".bel.col", np.uint64)
+    dst = np.fromfile(prefix + ".bel.dst", np.uint64)
+    val = np.fromfile(prefix + ".bel.val", np.uint8)
+    assert col[0] == g.V and col[1] == 0
+    np.testing.assert_array_equal(col[2:], g.offsets[:-1])
+    assert dst[0] == g.E and dst[1] == 0
+    np.testing.assert_array_equal(dst[2:], g.edges[:, 0])
+    assert val[:16].view(np.uint64).tolist() == [g.E, 0]
+    np.testing.assert_array_equal(val[16:].view(np.uint32), g.edges[:, 1])
+
+
+def test_no_static_plan_keeps_every_edge_dynamic():
+    g = og.Graph.rmat(10, 16)
+    p = og.plan(g.V, g.E, g.offsets, og.PLAIN, budget=1 << 30, flags=og.CFG_NO_STATIC)
+    assert p["static_edges"] == 0 and p["static_vertices"] == 0 and p["dynamic_edges"] == g.E
+    assert p["chunk_edges"] > 0
