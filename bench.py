@@ -254,7 +254,7 @@ def config_dict(args, g):
             "graph": "R-MAT scale %d ef16 a,b,c=.57,.19,.19 symmetric dedup weights U[1,64]" % args.scale,
             "V": g.V, "E": g.E, "budget_bytes": int(args.budget_gib * GIB), "advisek": args.advisek,
             "sources": args.sources, "seeds": {"graph": 1, "weights": 2, "sources": 3},
-            "l2": "inputs larger than L2 (graph %.1f GB)" % (g.E * 8 / 1e9),
+            "l2": "inputs larger than L2 (graph %.1f GB)" % (g.E * 5 / 1e9),
             "dynamic_mode": "direct" if args.direct else "staged", "sssp_delta": args.delta}
 
 
@@ -323,14 +323,17 @@ def run_ours(args, rank, world, local):
     launches = sum(s["launches"] for s in stats)
     peaks = measured_peaks()
     h2d = h2d_peak_gbs()
-    # algorithmic bytes: 12 B per edge ({dst,w} 8 B + dist 4 B), 20 B per vertex
-    static_gbs = (12 * st_edges + 20 * st_verts) / (st_ms / 1e3) / 1e9 if st_ms else 0.0
+    # algorithmic bytes: per edge the column (4 B), the weight (plan edge_bytes - 4,
+    # 1 B for weights in [1, 64]) and the target distance (4 B); 20 B per vertex
+    eb = plan["edge_bytes"]
+    static_gbs = ((eb + 4) * st_edges + 20 * st_verts) / (st_ms / 1e3) / 1e9 if st_ms else 0.0
     link_gbs = dyn_bytes / (dyn_ms / 1e3) / 1e9 if dyn_ms else 0.0
-    roof_static = {"bound": "hbm", "kernel": "k_lbs<uint2,MinOp<true>> (static region relax)",
+    roof_static = {"bound": "hbm", "kernel": "k_lbs<SrcW<u8>,MinOp<true>> (static region relax)",
                    "achieved": static_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                    "frac": static_gbs / peaks["hbm_gbs"], "traffic": None,
                    "peak_source": peaks["source"]}
-    roof_link = {"bound": "host-link", "kernel": "k_lbs<uint2,GatherOp> + dynamic relax",
+    roof_link = {"bound": "host-link", "kernel": "k_lbs<SrcW<u8>,MinOp<true>> over host-mapped edges"
+                 if args.direct else "k_gather<SrcW<u8>,DstW<u8>> + staged relax",
                  "achieved": link_gbs, "peak": h2d, "unit": "GB/s", "frac": link_gbs / h2d if h2d else None,
                  "traffic": None, "peak_source": "measured pinned H2D copy in this run"}
     dominant = roof_link if dyn_ms > st_ms else roof_static
@@ -358,7 +361,7 @@ def run_ours(args, rank, world, local):
         "roofline": dominant, "roofline_static": roof_static, "roofline_link": roof_link,
         "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
         "plan": {k: plan[k] for k in ("static_vertices", "static_edges", "dynamic_edges",
-                                      "chunk_edges", "advisek")},
+                                      "chunk_edges", "advisek", "edge_bytes")},
         "per_query": {"iterations": statistics.mean(s["iterations"] for s in stats),
                       "chunks": statistics.mean(s["chunks"] for s in stats),
                       "ms_static": st_ms / len(stats), "ms_dynamic": dyn_ms / len(stats),
@@ -564,7 +567,7 @@ def run_bfs_resident(args, rank, world, local):
         "persistent_ms_per_query": tb / args.steps * 1e3,
         "persistent_gteps": comp_edges * args.steps / tb / 1e9,
         "bit_exact_vs_runCPUBFS": exact, "levels": stats[0]["iterations"],
-        "roofline": {"bound": "hbm", "kernel": "k_lbs<uint32_t,BfsOp> (static relax)", "achieved": gbs,
+        "roofline": {"bound": "hbm", "kernel": "k_lbs<SrcU,BfsOp> (static relax)", "achieved": gbs,
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
                      "traffic": None, "peak_source": peaks["source"]},
         "cpu_baseline": {"value": comp_edges / cpu_s / 1e9, "unit": "GTEPS", "cores": 1, "kind": "port",
@@ -641,9 +644,11 @@ def run_serving(args, rank, world, local):
     mism = 0
     p0 = time.perf_counter()
     plain_lat = []
+    plain_svc = []
     for i in range(n):
         e = engines[gsel[i]]
         a = int(algos[i])
+        q0 = time.perf_counter()
         if a == og.ALGO_BFS:
             e.bfs(srcs[i], out=False)
         elif a == og.ALGO_SSSP:
@@ -651,12 +656,32 @@ def run_serving(args, rank, world, local):
         else:
             e.pr_l1(0.85, 0.0, 5, out=False)
         done = time.perf_counter() - p0
+        plain_svc.append((time.perf_counter() - q0) * 1e3)
         plain_lat.append(max(0.0, done - arrivals[i]) * 1e3)
         mism += e.checksum(a) != resp[i]["checksum"]
     plain_wall = time.perf_counter() - p0
     for e in engines:
         e.close()
     plain_lat = np.array(plain_lat)
+    plain_svc = np.array(plain_svc)
+    # per (graph, algorithm): request count, plain service time, served latency
+    # and the mean fused batch the server ran the request in
+    names = {og.ALGO_BFS: "bfs", og.ALGO_SSSP: "sssp", og.ALGO_PR: "pr5"}
+    breakdown = {}
+    for gi, sc in enumerate(scales):
+        for a, nm in names.items():
+            idx = [i for i in range(n) if gsel[i] == gi and algos[i] == a]
+            if not idx:
+                continue
+            breakdown["rmat%d/%s" % (sc, nm)] = {
+                "requests": len(idx),
+                "plain_service_ms_mean": float(plain_svc[idx].mean()),
+                "plain_service_ms_total": float(plain_svc[idx].sum()),
+                "served_p50_ms": float(np.percentile(lat[idx], 50)),
+                "served_batch_mean": float(np.mean([resp[i]["batch"] for i in idx])),
+                "served_run_ms_mean": float(np.mean([resp[i]["t_done_ms"] - resp[i]["t_start_ms"]
+                                                     for i in idx])),
+            }
     line = {
         "metric": "served queries/s", "value": served_qps, "unit": "queries/s", "n_gpus": world,
         "steps": n, "warmup": 0, "ms_per_step": span_ms / n, "higher_is_better": True,
@@ -673,7 +698,7 @@ def run_serving(args, rank, world, local):
         "plain_p50_ms": float(np.percentile(plain_lat, 50)), "plain_p99_ms": float(np.percentile(plain_lat, 99)),
         "speedup_vs_plain": served_qps / (n / plain_wall),
         "results_identical_to_plain": mism == 0, "failed_requests": len(bad),
-        "server": st, "clocks": clocks, "setup_s": {"generate": gen_s}, "wall_s": wall,
+        "breakdown": breakdown, "server": st, "clocks": clocks, "setup_s": {"generate": gen_s}, "wall_s": wall,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -95,6 +95,13 @@ void og_graph_free(og_graph *g);
  * dst[E]) and, for weighted graphs, <prefix>.bel.val (u64 E, u64 0, u32 w[E]). */
 int og_graph_save_bel(const og_graph *g, const char *prefix);
 
+/* GraphMeta::transFileUintToUlong (BFS/oneGraph_BFS/GraphMeta.h:169-193):
+ * reads the 32-bit-header CSR (u32 V, u32 E, u32 offsets[V], u32 dst[E]) and
+ * writes the same graph with 64-bit edge entries (u32 V, u32 E, u32
+ * offsets[V], u64 dst[E]).  out_path NULL follows the reference's naming: the
+ * input path without its last four characters, plus "lcsr". */
+int og_convert_uint_to_ulong(const char *in_path, const char *out_path);
+
 /* GraphMeta::findbignode (GraphMeta.h:150-165): first vertex after `last`
  * whose degree exceeds 3000, or `last` when there is none. */
 uint32_t og_graph_findbignode(const og_graph *g, uint32_t last);
@@ -146,6 +153,14 @@ typedef struct og_plan {
 int og_plan_compute(uint64_t V, uint64_t E, const uint64_t *offsets, int kind,
                     uint64_t budget_bytes, double advisek, uint32_t flags,
                     og_plan *out);
+
+/* The planner for a given graph with the engine's real edge width: the
+ * engine keeps edges as u32 columns plus weights in the narrowest of 1, 2 or
+ * 4 bytes that holds the graph's largest weight (so 5 bytes per edge for the
+ * R-MAT weights in [1, 64]); og_plan_compute, which has no graph, assumes
+ * 4-byte weights. */
+int og_graph_plan(og_graph *g, uint64_t budget_bytes, double advisek, uint32_t flags,
+                  og_plan *out);
 
 /* ---------------------------------------------------------------- engine */
 

@@ -126,9 +126,11 @@ SIGNATURES = [
     ("og_graph_free", None, [_P]),
     ("og_graph_findbignode", C.c_uint32, [_P, C.c_uint32]),
     ("og_graph_save_bel", C.c_int, [_P, C.c_char_p]),
+    ("og_convert_uint_to_ulong", C.c_int, [C.c_char_p, C.c_char_p]),
     ("og_rmat_generate", C.c_int, [C.POINTER(RmatParams), C.POINTER(_P)]),
     ("og_plan_compute", C.c_int, [C.c_uint64, C.c_uint64, _P, C.c_int, C.c_uint64, C.c_double,
                                   C.c_uint32, C.POINTER(Plan)]),
+    ("og_graph_plan", C.c_int, [_P, C.c_uint64, C.c_double, C.c_uint32, C.POINTER(Plan)]),
     ("og_engine_create", C.c_int, [_P, C.POINTER(Config), C.POINTER(_P)]),
     ("og_engine_plan", C.c_int, [_P, C.POINTER(Plan)]),
     ("og_engine_destroy", None, [_P]),
@@ -268,6 +270,12 @@ class Graph:
     def degrees(self) -> np.ndarray:
         return np.diff(self.offsets).astype(np.uint32)
 
+    def plan(self, budget: int = 0, advisek: float = 0.0, flags: int = 0) -> dict:
+        """The engine's plan for this graph (with its real per-edge bytes)."""
+        p = Plan()
+        _check(lib().og_graph_plan(self._h, budget, advisek, flags, C.byref(p)), "og_graph_plan")
+        return p.as_dict()
+
     def findbignode(self, last: int) -> int:
         return int(lib().og_graph_findbignode(self._h, last))
 
@@ -294,6 +302,12 @@ class Graph:
             self.close()
         except Exception:
             pass
+
+
+def convert_uint_to_ulong(in_path: str, out_path: str | None = None):
+    """GraphMeta::transFileUintToUlong: 32-bit-header CSR -> 64-bit edge entries."""
+    _check(lib().og_convert_uint_to_ulong(in_path.encode(), out_path.encode() if out_path else None),
+           "og_convert_uint_to_ulong")
 
 
 def plan(V: int, E: int, offsets: np.ndarray, kind: int = PLAIN, budget: int = 0,

@@ -25,8 +25,8 @@ struct PersistArgs {
   uint32_t V;
   uint64_t nwords;
   const uint64_t *off;
-  const void *sedges;      // device copy of edges [0, static_edges)
-  const void *hedges;      // page-locked host CSR (all edges), may be null if E == static_edges
+  const uint32_t *scols;   // device copy of the columns [0, static_edges)
+  const uint32_t *hcols;   // page-locked host columns (all edges), null if E == static_edges
   uint64_t static_edges;
   uint64_t E;
   unsigned long long *visited, *cur, *next;
@@ -135,13 +135,13 @@ __device__ __forceinline__ void pscan(SH &sh, uint32_t c, uint64_t e, uint32_t &
   __syncthreads();
 }
 
-template <class Edge, int BLOCK, int ITEMS>
+template <int BLOCK, int ITEMS>
 __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
   using SH = PersistShared<BLOCK, ITEMS>;
   constexpr uint32_t TILE = SH::TILE;
   __shared__ SH sh;
-  const Edge *sedges = (const Edge *)a.sedges;
-  const Edge *hedges = (const Edge *)a.hedges;
+  const uint32_t *sedges = a.scols;
+  const uint32_t *hedges = a.hcols;
   unsigned long long *cur = a.cur, *next = a.next;
   uint32_t *cur_any = a.cur_any, *next_any = a.next_any;
   // contiguous word range of this CTA, split into contiguous per-thread runs
@@ -271,7 +271,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
         }
       }
       __syncthreads();
-      Edge ev[ITEMS];
+      uint32_t ev[ITEMS];
       uint32_t lv[ITEMS];
       uint32_t okm = 0;
 #pragma unroll

@@ -56,9 +56,14 @@ struct og_engine {
   std::vector<cudaEvent_t> t_gat;  // start/end pairs around each gather launch
 
   uint64_t *off_d = nullptr;
-  void *sedges_d = nullptr;
-  void *stage_d[2] = {nullptr, nullptr};
-  const void *hedges_d = nullptr;
+  // edges as structure-of-arrays: u32 columns + weights of wbytes (0, 1, 2, 4)
+  uint32_t *scols_d = nullptr;               // static region columns (HBM)
+  void *sw_d = nullptr;                      // static region weights (HBM)
+  uint32_t *stage_col[2] = {nullptr, nullptr};  // staging buffers (columns)
+  void *stage_w[2] = {nullptr, nullptr};        // staging buffers (weights)
+  const uint32_t *hcols_d = nullptr;         // page-locked host columns, device view
+  const void *hw_d = nullptr;                // page-locked host weights, device view
+  uint32_t wbytes = 0;
   uint32_t *value_d = nullptr;
   uint32_t *bm[3] = {nullptr, nullptr, nullptr};
   uint32_t *list_d[2] = {nullptr, nullptr};
@@ -156,7 +161,10 @@ void destroy(og_engine *e) {
   if (e->s_dyn) cudaStreamDestroy(e->s_dyn);
   if (e->s_gat) cudaStreamDestroy(e->s_gat);
   if (e->registered && e->g) {
-    if (--e->g->registered == 0) cudaHostUnregister(e->g->edges);
+    if (--e->g->registered == 0) {
+      cudaHostUnregister(e->g->cols);
+      if (e->g->wts) cudaHostUnregister(e->g->wts);
+    }
   }
   if (e->parent) e->parent->clones--;
   cudaGetLastError();  // a failure while tearing down is not the next call's error
@@ -207,8 +215,10 @@ int create_query_state(og_engine *e) {
   CK(cudaMallocHost(&e->err_h, 4 * sizeof(uint32_t)));
   CK(cudaMallocHost(&e->l1_h, sizeof(double)));
   if (P.chunk_edges && !(e->cfg.flags & OG_CFG_DIRECT)) {
-    RC(dalloc(e, (char **)&e->stage_d[0], P.chunk_edges * e->eb));
-    RC(dalloc(e, (char **)&e->stage_d[1], P.chunk_edges * e->eb));
+    for (int b = 0; b < 2; b++) {
+      RC(dalloc(e, &e->stage_col[b], P.chunk_edges));
+      if (e->wbytes) RC(dalloc(e, (char **)&e->stage_w[b], P.chunk_edges * e->wbytes));
+    }
   }
   if (e->pr_enabled) {
     RC(dalloc(e, &e->contrib_d, V + 1));
@@ -244,12 +254,15 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
   e->cfg = *cfg;
   e->dev = cfg->device;
   e->V = g->V;
-  e->eb = g->edge_bytes();
   e->pr_enabled = g->kind == OG_GRAPH_PR || (cfg->flags & OG_CFG_PR);
   e->batch_enabled = (cfg->flags & OG_CFG_BATCH) != 0;
   CK(cudaSetDevice(e->dev));
   CK(cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, e->dev));
-  RC(plan_compute(g->V, g->E, g->off, g->kind, cfg->budget_bytes, cfg->advisek, cfg->flags, &e->plan));
+  RC(graph_prepare_soa(g));
+  e->wbytes = g->wbytes;
+  e->eb = g->soa_edge_bytes();
+  RC(plan_compute(g->V, g->E, g->off, g->kind, cfg->budget_bytes, cfg->advisek, cfg->flags, &e->plan,
+                  e->eb));
   const og_plan &P = e->plan;
   size_t free_b = 0, total_b = 0;
   CK(cudaMemGetInfo(&free_b, &total_b));
@@ -260,11 +273,14 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
   e->nwords = ((uint64_t)g->V + 31) / 32 + 2 * kWordsPerCompactTile;
 
   // kernels with more than 48 KB of shared memory opt in once per process
-  CK(cudaFuncSetAttribute(k_gather<uint32_t, kGatherMult>,
-                          cudaFuncAttributeMaxDynamicSharedMemorySize,
-                          (int)gather_smem_bytes<kGatherMult>()));
-  CK(cudaFuncSetAttribute(k_gather<uint2, kGatherMult>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                          (int)gather_smem_bytes<kGatherMult>()));
+  const int gsm = (int)gather_smem_bytes<kGatherMult>();
+  CK(cudaFuncSetAttribute(k_gather<SrcU, DstU, kGatherMult>, cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
+  CK(cudaFuncSetAttribute(k_gather<SrcW<uint8_t>, DstW<uint8_t>, kGatherMult>,
+                          cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
+  CK(cudaFuncSetAttribute(k_gather<SrcW<uint16_t>, DstW<uint16_t>, kGatherMult>,
+                          cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
+  CK(cudaFuncSetAttribute(k_gather<SrcW<uint32_t>, DstW<uint32_t>, kGatherMult>,
+                          cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
 
   // host CSR: page-lock so kernels can gather from it over the link
   if (P.dynamic_edges > 0) {
@@ -272,26 +288,41 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
       int pageable = 0;
       CK(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, e->dev));
       if (!pageable) return fail(OG_E_UNSUPPORTED, "device cannot read pageable host memory");
-      e->hedges_d = g->edges;
+      e->hcols_d = g->cols;
+      e->hw_d = g->wts;
     } else {
       if (g->registered == 0) {
         int ro = 0;
         cudaDeviceGetAttribute(&ro, cudaDevAttrHostRegisterReadOnlySupported, e->dev);
-        CK(cudaHostRegister(g->edges, g->E * e->eb,
-                            cudaHostRegisterMapped | (ro ? cudaHostRegisterReadOnly : 0)));
+        const unsigned fl = cudaHostRegisterMapped | (ro ? cudaHostRegisterReadOnly : 0);
+        CK(cudaHostRegister(g->cols, g->E * 4, fl));
+        if (g->wts) {
+          cudaError_t rw = cudaHostRegister(g->wts, g->E * g->wbytes, fl);
+          if (rw != cudaSuccess) {
+            cudaHostUnregister(g->cols);
+            return fail(OG_E_CUDA, "cudaHostRegister(weights): %s", cudaGetErrorString(rw));
+          }
+        }
       }
       g->registered++;
       e->registered = true;
       void *dp = nullptr;
-      CK(cudaHostGetDevicePointer(&dp, g->edges, 0));
-      e->hedges_d = dp;
+      CK(cudaHostGetDevicePointer(&dp, g->cols, 0));
+      e->hcols_d = (const uint32_t *)dp;
+      if (g->wts) {
+        CK(cudaHostGetDevicePointer(&dp, g->wts, 0));
+        e->hw_d = dp;
+      }
     }
   }
 
   // resident graph state shared with clones
   const uint64_t V = g->V;
   RC(dalloc(e, &e->off_d, V + 1));
-  if (P.static_edges) RC(dalloc(e, (char **)&e->sedges_d, P.static_edges * e->eb));
+  if (P.static_edges) {
+    RC(dalloc(e, &e->scols_d, P.static_edges));
+    if (e->wbytes) RC(dalloc(e, (char **)&e->sw_d, P.static_edges * e->wbytes));
+  }
   if (e->pr_enabled) RC(dalloc(e, &e->outdeg_d, V + 1));
   e->resident_bytes = e->dbytes;
   RC(create_query_state(e));
@@ -301,9 +332,12 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
 
   // initGraphDevice: offsets, the static edge prefix, PageRank out-degrees
   CK(cudaMemcpyAsync(e->off_d, g->off, 8 * (V + 1), cudaMemcpyHostToDevice, e->s_main));
-  if (P.static_edges)
-    CK(cudaMemcpyAsync(e->sedges_d, g->edges, P.static_edges * e->eb, cudaMemcpyHostToDevice,
-                       e->s_main));
+  if (P.static_edges) {
+    CK(cudaMemcpyAsync(e->scols_d, g->cols, P.static_edges * 4, cudaMemcpyHostToDevice, e->s_main));
+    if (e->wbytes)
+      CK(cudaMemcpyAsync(e->sw_d, g->wts, P.static_edges * e->wbytes, cudaMemcpyHostToDevice,
+                         e->s_main));
+  }
   if (e->pr_enabled) {
     if (g->kind == OG_GRAPH_PR) {
       CK(cudaMemcpyAsync(e->outdeg_d, g->outdeg, 4 * V, cudaMemcpyHostToDevice, e->s_main));
@@ -332,8 +366,11 @@ int clone(og_engine *parent, og_engine *e) {
   e->nwords = parent->nwords;
   e->eb = parent->eb;
   e->off_d = parent->off_d;
-  e->sedges_d = parent->sedges_d;
-  e->hedges_d = parent->hedges_d;
+  e->scols_d = parent->scols_d;
+  e->sw_d = parent->sw_d;
+  e->hcols_d = parent->hcols_d;
+  e->hw_d = parent->hw_d;
+  e->wbytes = parent->wbytes;
   e->outdeg_d = parent->outdeg_d;
   e->tuned = parent->tuned;
   e->sssp_delta = parent->sssp_delta;
@@ -403,40 +440,62 @@ int check_device_error(og_engine *e) {
   return fail(OG_E_DEVICE, "kernel reported an out-of-range index (flags 0x%x)", err);
 }
 
+// Edge views of an engine: EK<void> reads columns only (BFS, CC, PageRank,
+// batched BFS), EK<W> columns and W-wide weights (SSSP).
+template <class W>
+struct EK {
+  using Src = SrcW<W>;
+  using Dst = DstW<W>;
+  static constexpr uint32_t kBytes = 4 + sizeof(W);
+  static Src stat(const og_engine *e) { return Src{e->scols_d, (const W *)e->sw_d}; }
+  static Src host(const og_engine *e) { return Src{e->hcols_d, (const W *)e->hw_d}; }
+  static Src stage(const og_engine *e, int b) { return Src{e->stage_col[b], (const W *)e->stage_w[b]}; }
+  static Dst stage_dst(const og_engine *e, int b) { return Dst{e->stage_col[b], (W *)e->stage_w[b]}; }
+};
+template <>
+struct EK<void> {
+  using Src = SrcU;
+  using Dst = DstU;
+  static constexpr uint32_t kBytes = 4;
+  static Src stat(const og_engine *e) { return Src{e->scols_d}; }
+  static Src host(const og_engine *e) { return Src{e->hcols_d}; }
+  static Src stage(const og_engine *e, int b) { return Src{e->stage_col[b]}; }
+  static Dst stage_dst(const og_engine *e, int b) { return Dst{e->stage_col[b]}; }
+};
+using EKU = EK<void>;
+
 // Relax op factory per algorithm; `level` is the BFS depth of the frontier.
 struct RoundOps {
   int algo;
   uint32_t level;
 };
 
-template <class Edge>
-int launch_relax(og_engine *e, const RoundOps &ro, const LbsArgs &a, const Edge *edges,
-                 uint32_t *next, cudaStream_t s) {
+template <class Src>
+int launch_relax(og_engine *e, const RoundOps &ro, const LbsArgs &a, Src src, uint32_t *next,
+                 cudaStream_t s) {
   const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
   if (grid == 0) return OG_OK;
   if (ro.algo == OG_ALGO_BFS) {
     BfsOp op{e->bm[2], next, e->value_d, e->err_d, e->V, ro.level + 1};
-    k_lbs<Edge, BfsOp><<<grid, kThreads, 0, s>>>(a, edges, op);
-    e->launches++;
+    k_lbs<Src, BfsOp><<<grid, kThreads, 0, s>>>(a, src, op);
   } else if (ro.algo == OG_ALGO_SSSP) {
     MinOp<true> op{e->value_d, next, e->err_d, e->V};
-    k_lbs<Edge, MinOp<true>><<<grid, kThreads, 0, s>>>(a, edges, op);
-    e->launches++;
+    k_lbs<Src, MinOp<true>><<<grid, kThreads, 0, s>>>(a, src, op);
   } else {
     MinOp<false> op{e->value_d, next, e->err_d, e->V};
-    k_lbs<Edge, MinOp<false>><<<grid, kThreads, 0, s>>>(a, edges, op);
-    e->launches++;
+    k_lbs<Src, MinOp<false>><<<grid, kThreads, 0, s>>>(a, src, op);
   }
+  e->launches++;
   return OG_OK;
 }
 
-template <class Edge>
-int launch_gather(og_engine *e, const LbsArgs &a, Edge *stage, cudaStream_t s) {
+template <class K>
+int launch_gather(og_engine *e, const LbsArgs &a, int buf, cudaStream_t s) {
   constexpr uint64_t T = (uint64_t)kGatherMult * kTile;
   const unsigned grid = (unsigned)((a.pos_end - a.pos_begin + T - 1) / T);
   if (grid == 0) return OG_OK;
-  k_gather<Edge, kGatherMult><<<grid, kThreads, gather_smem_bytes<kGatherMult>(), s>>>(
-      a, (const Edge *)e->hedges_d, stage);
+  k_gather<typename K::Src, typename K::Dst, kGatherMult>
+      <<<grid, kThreads, gather_smem_bytes<kGatherMult>(), s>>>(a, K::host(e), K::stage_dst(e, buf));
   e->launches++;
   return OG_OK;
 }
@@ -472,7 +531,7 @@ void collect_timing(og_engine *e, Timing &t, og_stats *st) {
 
 // One round's region work given the compaction counts (already on the host).
 // `body_static(a)` / `body_dyn(a, edges, ...)` launch the per-region kernel.
-template <class Edge, class StaticFn, class DynFn>
+template <class K, class StaticFn, class DynFn>
 int run_regions(og_engine *e, og_stats &st, Timing &tm, StaticFn static_fn, DynFn dyn_fn) {
   const Counts cs = e->counts_h[0], cd = e->counts_h[1];
   if (cs.n) {
@@ -485,7 +544,7 @@ int run_regions(og_engine *e, og_stats &st, Timing &tm, StaticFn static_fn, DynF
   if (cd.n) {
     CK(cudaEventRecord(e->t_d0, e->s_dyn));
     if (e->cfg.flags & OG_CFG_DIRECT) {
-      RC(dyn_fn(lbs_args(e, 1, 0, cd.total, true, e->g->E), (const Edge *)e->hedges_d, e->s_dyn));
+      RC(dyn_fn(lbs_args(e, 1, 0, cd.total, true, e->g->E), K::host(e), e->s_dyn));
       st.chunks += 1;
     } else {
       const uint64_t C = e->plan.chunk_edges;
@@ -498,13 +557,12 @@ int run_regions(og_engine *e, og_stats &st, Timing &tm, StaticFn static_fn, DynF
         cudaEvent_t g0, g1;
         RC(gather_events(e, tm.pend_g, &g0, &g1));
         CK(cudaEventRecord(g0, e->s_gat));
-        RC(launch_gather<Edge>(e, lbs_args(e, 1, b, en, true, e->g->E), (Edge *)e->stage_d[buf],
-                               e->s_gat));
+        RC(launch_gather<K>(e, lbs_args(e, 1, b, en, true, e->g->E), buf, e->s_gat));
         CK(cudaEventRecord(g1, e->s_gat));
         tm.pend_g++;
         CK(cudaEventRecord(e->ev_gat[buf], e->s_gat));
         CK(cudaStreamWaitEvent(e->s_dyn, e->ev_gat[buf], 0));
-        RC(dyn_fn(lbs_args(e, 1, b, en, false, C), (const Edge *)e->stage_d[buf], e->s_dyn));
+        RC(dyn_fn(lbs_args(e, 1, b, en, false, C), K::stage(e, buf), e->s_dyn));
         CK(cudaEventRecord(e->ev_rel[buf], e->s_dyn));
       }
       st.chunks += (uint32_t)nch;
@@ -513,7 +571,7 @@ int run_regions(og_engine *e, og_stats &st, Timing &tm, StaticFn static_fn, DynF
     CK(cudaStreamWaitEvent(e->s_main, e->ev_dyn_done, 0));
     tm.pend_d = true;
     st.edges_dynamic += cd.total;
-    st.link_bytes += cd.total * e->eb;
+    st.link_bytes += cd.total * K::kBytes;
   }
   return OG_OK;
 }
@@ -540,7 +598,7 @@ int compact_round(og_engine *e, const uint32_t *cur, og_stats &st, Timing &tm, u
   return OG_OK;
 }
 
-template <class Edge>
+template <class K>
 int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
   const uint64_t V = e->V;
   uint32_t *cur = e->bm[0], *next = e->bm[1];
@@ -587,11 +645,11 @@ int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
     st.iterations++;
     st.frontier_sum += n;
     st.static_vertices += e->counts_h[0].n;
-    auto sfn = [&](const LbsArgs &a) { return launch_relax<Edge>(e, ro, a, (const Edge *)e->sedges_d, next, e->s_main); };
-    auto dfn = [&](const LbsArgs &a, const Edge *edges, cudaStream_t ds) {
-      return launch_relax<Edge>(e, ro, a, edges, next, ds);
+    auto sfn = [&](const LbsArgs &a) { return launch_relax(e, ro, a, K::stat(e), next, e->s_main); };
+    auto dfn = [&](const LbsArgs &a, typename K::Src src, cudaStream_t ds) {
+      return launch_relax(e, ro, a, src, next, ds);
     };
-    RC((run_regions<Edge>(e, st, tm, sfn, dfn)));
+    RC((run_regions<K>(e, st, tm, sfn, dfn)));
     CK(cudaStreamWaitEvent(e->s_main, e->ev_cd, 0));
     CK(cudaMemsetAsync(cur, 0, 4 * e->nwords, e->s_main));
     std::swap(cur, next);
@@ -607,7 +665,6 @@ int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
 
 // ------------------------------------------------------------------ batched BFS
 
-template <class Edge>
 int run_batch(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *out, uint64_t *checks,
               og_stats &st) {
   const uint64_t V = e->V;
@@ -644,16 +701,16 @@ int run_batch(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *out, uin
     st.frontier_sum += nl;
     st.static_vertices += e->counts_h[0].n;
     BatchOp op{visited, cur, next, next_any, e->err_d, e->V};
-    auto launch = [&](const LbsArgs &a, const Edge *edges, cudaStream_t ls) {
+    auto launch = [&](const LbsArgs &a, SrcU src, cudaStream_t ls) {
       const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
       if (grid) {
-        k_lbs<Edge, BatchOp><<<grid, kThreads, 0, ls>>>(a, edges, op);
+        k_lbs<SrcU, BatchOp><<<grid, kThreads, 0, ls>>>(a, src, op);
         e->launches++;
       }
       return (int)OG_OK;
     };
-    auto sfn = [&](const LbsArgs &a) { return launch(a, (const Edge *)e->sedges_d, e->s_main); };
-    RC((run_regions<Edge>(e, st, tm, sfn, launch)));
+    auto sfn = [&](const LbsArgs &a) { return launch(a, EKU::stat(e), e->s_main); };
+    RC((run_regions<EKU>(e, st, tm, sfn, launch)));
     CK(cudaMemsetAsync(e->hist_d, 0, 64 * 8, s));
     k_batch_level<<<grid_for(e->nwords, e->sms), kThreads, 0, s>>>(next_any, next, e->nwords, n,
                                                                  e->hist_d, depth_d, V, level + 1);
@@ -692,9 +749,9 @@ struct PersistCfg {
 constexpr PersistCfg kPersistConfigs[] = {{256, 8}, {128, 8}, {256, 4}, {512, 4}, {128, 16}};
 constexpr int kNumPersistConfigs = 5;
 
-template <class Edge, int B, int I>
+template <int B, int I>
 int launch_persist_cfg(og_engine *e, const PersistArgs &a, cudaStream_t s) {
-  auto kern = k_batch_persistent<Edge, B, I>;
+  auto kern = k_batch_persistent<B, I>;
   int occ = 0;
   CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kern, B, 0));
   if (occ < 1) return fail(OG_E_UNSUPPORTED, "persistent kernel does not fit an SM");
@@ -714,21 +771,19 @@ int launch_persist_cfg(og_engine *e, const PersistArgs &a, cudaStream_t s) {
   return OG_OK;
 }
 
-template <class Edge>
 int launch_persist(og_engine *e, int ci, const PersistArgs &a, cudaStream_t s) {
   switch (ci) {
-    case 0: return launch_persist_cfg<Edge, 256, 8>(e, a, s);
-    case 1: return launch_persist_cfg<Edge, 128, 8>(e, a, s);
-    case 2: return launch_persist_cfg<Edge, 256, 4>(e, a, s);
-    case 3: return launch_persist_cfg<Edge, 512, 4>(e, a, s);
-    default: return launch_persist_cfg<Edge, 128, 16>(e, a, s);
+    case 0: return launch_persist_cfg<256, 8>(e, a, s);
+    case 1: return launch_persist_cfg<128, 8>(e, a, s);
+    case 2: return launch_persist_cfg<256, 4>(e, a, s);
+    case 3: return launch_persist_cfg<512, 4>(e, a, s);
+    default: return launch_persist_cfg<128, 16>(e, a, s);
   }
 }
 
 // Enqueues one whole batch on s_main: clear state, upload the sources from the
 // page-locked buffer, seed, run every level in one cooperative kernel, copy
 // the per-level counts and the status words back to page-locked memory.
-template <class Edge>
 int enqueue_persist(og_engine *e, uint32_t n, int ci, uint32_t *depth_d) {
   const uint64_t V = e->V;
   cudaStream_t s = e->s_main;
@@ -744,8 +799,8 @@ int enqueue_persist(og_engine *e, uint32_t n, int ci, uint32_t *depth_d) {
   a.V = e->V;
   a.nwords = e->nwords;
   a.off = e->off_d;
-  a.sedges = e->sedges_d;
-  a.hedges = e->hedges_d;
+  a.scols = e->scols_d;
+  a.hcols = e->hcols_d;
   a.static_edges = e->plan.static_edges;
   a.E = e->g->E;
   a.visited = e->bmask[0];
@@ -768,14 +823,13 @@ int enqueue_persist(og_engine *e, uint32_t n, int ci, uint32_t *depth_d) {
   a.levels = e->bar_d + 3;
   a.stat = (unsigned long long *)(e->bar_d + 4);
   a.Vs = e->Vs;
-  RC(launch_persist<Edge>(e, ci, a, s));
+  RC(launch_persist(e, ci, a, s));
   CK(cudaMemcpyAsync(e->hist_h, e->hist_d, 8ull * kMaxBatchLevels * 64, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(e->pmisc_h, e->bar_d, 64, cudaMemcpyDeviceToHost, s));
   return OG_OK;
 }
 
 // Captures enqueue_persist for (n, config) as a CUDA graph once and replays it.
-template <class Edge>
 int run_persist_graph(og_engine *e, uint32_t n, int ci, bool *used_graph) {
   *used_graph = false;
   if (!e->graph_broken && !(e->graph && e->graph_n == n && e->graph_cfg == ci)) {
@@ -786,7 +840,7 @@ int run_persist_graph(og_engine *e, uint32_t n, int ci, bool *used_graph) {
     cudaGraph_t gr = nullptr;
     bool ok = cudaStreamBeginCapture(e->s_main, cudaStreamCaptureModeThreadLocal) == cudaSuccess;
     const uint64_t before = e->launches;
-    const int rc = ok ? enqueue_persist<Edge>(e, n, ci, nullptr) : OG_E_CUDA;
+    const int rc = ok ? enqueue_persist(e, n, ci, nullptr) : OG_E_CUDA;
     e->launches = before;  // captured, not launched
     if (ok) ok = cudaStreamEndCapture(e->s_main, &gr) == cudaSuccess && rc == OG_OK;
     if (ok) ok = cudaGraphInstantiate(&e->graph, gr, 0) == cudaSuccess;
@@ -806,10 +860,9 @@ int run_persist_graph(og_engine *e, uint32_t n, int ci, bool *used_graph) {
     *used_graph = true;
     return OG_OK;
   }
-  return enqueue_persist<Edge>(e, n, ci, nullptr);
+  return enqueue_persist(e, n, ci, nullptr);
 }
 
-template <class Edge>
 int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *out,
                       uint64_t *checks, og_stats &st, int ci) {
   const uint64_t V = e->V;
@@ -831,9 +884,9 @@ int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *
   // events outside any captured graph: they bracket the whole batch on s_main
   CK(cudaEventRecord(e->t_s0, e->s_main));
   if (out) {
-    RC(enqueue_persist<Edge>(e, n, ci, depth_d));
+    RC(enqueue_persist(e, n, ci, depth_d));
   } else {
-    RC(run_persist_graph<Edge>(e, n, ci, &graph));
+    RC(run_persist_graph(e, n, ci, &graph));
   }
   CK(cudaEventRecord(e->t_s1, e->s_main));
   CK(cudaStreamSynchronize(e->s_main));
@@ -849,7 +902,7 @@ int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *
   st.frontier_sum = stat[0];
   st.edges_static = stat[1] - stat[2];
   st.edges_dynamic = stat[2];
-  st.link_bytes = stat[2] * e->eb;
+  st.link_bytes = stat[2] * 4;  // columns only
   st.chunks = graph ? 1u : 0u;  // 1: replayed from the captured CUDA graph
   if (checks)
     for (uint32_t i = 0; i < n; i++) {
@@ -869,7 +922,6 @@ int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *
 
 // ------------------------------------------------------------------ PageRank
 
-template <class Edge>
 int pr_sums(og_engine *e, og_stats &st, Timing &tm) {
   PrArgs p;
   p.contrib = e->contrib_d;
@@ -891,20 +943,20 @@ int pr_sums(og_engine *e, og_stats &st, Timing &tm) {
   auto sfn = [&](const LbsArgs &a) {
     const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
     if (grid) {
-      k_pr_pull<Edge><<<grid, kThreads, 0, e->s_main>>>(a, (const Edge *)e->sedges_d, args_for(0));
+      k_pr_pull<SrcU><<<grid, kThreads, 0, e->s_main>>>(a, EKU::stat(e), args_for(0));
       e->launches++;
     }
     return (int)OG_OK;
   };
-  auto dfn = [&](const LbsArgs &a, const Edge *edges, cudaStream_t ds) {
+  auto dfn = [&](const LbsArgs &a, SrcU src, cudaStream_t ds) {
     const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
     if (grid) {
-      k_pr_pull<Edge><<<grid, kThreads, 0, ds>>>(a, edges, args_for(1));
+      k_pr_pull<SrcU><<<grid, kThreads, 0, ds>>>(a, src, args_for(1));
       e->launches++;
     }
     return (int)OG_OK;
   };
-  RC((run_regions<Edge>(e, st, tm, sfn, dfn)));
+  RC((run_regions<EKU>(e, st, tm, sfn, dfn)));
   for (int r = 0; r < 2; r++) {
     const Counts c = e->counts_h[r];
     if (!c.n) continue;
@@ -917,7 +969,6 @@ int pr_sums(og_engine *e, og_stats &st, Timing &tm) {
   return OG_OK;
 }
 
-template <class Edge>
 int run_pr_delta(og_engine *e, float thresh, int max_rounds, og_stats &st) {
   const uint64_t V = e->V;
   uint32_t *cur = e->bm[0], *next = e->bm[1];
@@ -936,7 +987,7 @@ int run_pr_delta(og_engine *e, float thresh, int max_rounds, og_stats &st) {
     st.iterations++;
     st.frontier_sum += n;
     st.static_vertices += e->counts_h[0].n;
-    RC(pr_sums<Edge>(e, st, tm));
+    RC(pr_sums(e, st, tm));
     CK(cudaMemsetAsync(e->active_d, 0, 4, s));
     k_pr_update_delta<<<grid_for(e->nwords, e->sms), kThreads, 0, s>>>(
         cur, next, e->nwords, (float *)e->value_d, e->contrib_d, e->sum_d, e->outdeg_d, thresh,
@@ -954,7 +1005,6 @@ int run_pr_delta(og_engine *e, float thresh, int max_rounds, og_stats &st) {
   return OG_OK;
 }
 
-template <class Edge>
 int run_pr_l1(og_engine *e, float damping, double tol, int max_iter, og_stats &st) {
   const uint64_t V = e->V;
   uint32_t *cur = e->bm[0];
@@ -975,7 +1025,7 @@ int run_pr_l1(og_engine *e, float damping, double tol, int max_iter, og_stats &s
     st.iterations++;
     st.frontier_sum += n;
     st.static_vertices += e->counts_h[0].n;
-    RC(pr_sums<Edge>(e, st, tm));
+    RC(pr_sums(e, st, tm));
     k_pr_update_l1<<<e->part_n, kThreads, 0, s>>>(V, (float *)e->value_d, e->contrib_d, e->sum_d,
                                                   e->outdeg_d, teleport, damping, e->part_d);
     e->launches++;
@@ -1108,8 +1158,7 @@ extern "C" int og_bfs(og_engine *e, uint32_t src, uint32_t *out_depth, og_stats 
   if (e && src >= e->V) return fail(OG_E_ARG, "source %u >= V %u", src, e->V);
   return query_common(e, OG_ALGO_BFS, st, out_depth, [](og_engine *en, og_stats &s, void *c) {
     const uint32_t src_ = *(uint32_t *)c;
-    return en->g->kind == OG_GRAPH_WEIGHTED ? run_frontier<uint2>(en, OG_ALGO_BFS, src_, s)
-                                            : run_frontier<uint32_t>(en, OG_ALGO_BFS, src_, s);
+    return run_frontier<EKU>(en, OG_ALGO_BFS, src_, s);
   }, &src);
 }
 
@@ -1117,15 +1166,17 @@ extern "C" int og_sssp(og_engine *e, uint32_t src, uint32_t *out_dist, og_stats 
   if (e && src >= e->V) return fail(OG_E_ARG, "source %u >= V %u", src, e->V);
   if (e && e->g->kind != OG_GRAPH_WEIGHTED) return fail(OG_E_UNSUPPORTED, "SSSP needs a weighted graph");
   return query_common(e, OG_ALGO_SSSP, st, out_dist, [](og_engine *en, og_stats &s, void *c) {
-    return run_frontier<uint2>(en, OG_ALGO_SSSP, *(uint32_t *)c, s);
+    const uint32_t src_ = *(uint32_t *)c;
+    if (en->wbytes == 1) return run_frontier<EK<uint8_t>>(en, OG_ALGO_SSSP, src_, s);
+    if (en->wbytes == 2) return run_frontier<EK<uint16_t>>(en, OG_ALGO_SSSP, src_, s);
+    return run_frontier<EK<uint32_t>>(en, OG_ALGO_SSSP, src_, s);
   }, &src);
 }
 
 extern "C" int og_cc(og_engine *e, uint32_t *out_label, og_stats *st) {
   uint32_t dummy = 0;
   return query_common(e, OG_ALGO_CC, st, out_label, [](og_engine *en, og_stats &s, void *) {
-    return en->g->kind == OG_GRAPH_WEIGHTED ? run_frontier<uint2>(en, OG_ALGO_CC, 0, s)
-                                            : run_frontier<uint32_t>(en, OG_ALGO_CC, 0, s);
+    return run_frontier<EKU>(en, OG_ALGO_CC, 0, s);
   }, &dummy);
 }
 
@@ -1141,8 +1192,7 @@ extern "C" int og_pr(og_engine *e, float *out_rank, double threshold, int max_ro
   PrCtx c{threshold, 0, max_rounds};
   return query_common(e, OG_ALGO_PR, st, out_rank, [](og_engine *en, og_stats &s, void *cx) {
     const PrCtx &p = *(PrCtx *)cx;
-    return en->g->kind == OG_GRAPH_WEIGHTED ? run_pr_delta<uint2>(en, (float)p.a, p.n, s)
-                                            : run_pr_delta<uint32_t>(en, (float)p.a, p.n, s);
+    return run_pr_delta(en, (float)p.a, p.n, s);
   }, &c);
 }
 
@@ -1153,8 +1203,7 @@ extern "C" int og_pr_l1(og_engine *e, float *out_rank, double damping, double to
   PrCtx c{damping, tol, max_iter};
   return query_common(e, OG_ALGO_PR, st, out_rank, [](og_engine *en, og_stats &s, void *cx) {
     const PrCtx &p = *(PrCtx *)cx;
-    return en->g->kind == OG_GRAPH_WEIGHTED ? run_pr_l1<uint2>(en, (float)p.a, p.b, p.n, s)
-                                            : run_pr_l1<uint32_t>(en, (float)p.a, p.b, p.n, s);
+    return run_pr_l1(en, (float)p.a, p.b, p.n, s);
   }, &c);
 }
 
@@ -1170,12 +1219,9 @@ struct BatchCtx {
 int batch_body(og_engine *en, og_stats &s, void *cx) {
   const BatchCtx &b = *(BatchCtx *)cx;
   const bool w = en->g->kind == OG_GRAPH_WEIGHTED;
-  if (b.mode == 1)
-    return w ? run_batch<uint2>(en, b.srcs, b.n, b.out, b.checks, s)
-             : run_batch<uint32_t>(en, b.srcs, b.n, b.out, b.checks, s);
+  if (b.mode == 1) return run_batch(en, b.srcs, b.n, b.out, b.checks, s);
   const int ci = b.mode >= 2 ? b.mode - 2 : (en->tuned >= 0 ? en->tuned : 0);
-  return w ? run_batch_persist<uint2>(en, b.srcs, b.n, b.out, b.checks, s, ci)
-           : run_batch_persist<uint32_t>(en, b.srcs, b.n, b.out, b.checks, s, ci);
+  return run_batch_persist(en, b.srcs, b.n, b.out, b.checks, s, ci);
 }
 
 int batch_checks(og_engine *e, const uint32_t *srcs, int n) {
@@ -1444,6 +1490,9 @@ extern "C" int og_k_compact_noalloc(const uint32_t *bits, uint32_t v_begin, uint
 
 extern "C" void og_graph_free(og_graph *g) {
   if (!g) return;
-  if (g->registered) cudaHostUnregister(g->edges);
+  if (g->registered) {
+    cudaHostUnregister(g->cols);
+    if (g->wts) cudaHostUnregister(g->wts);
+  }
   og::graph_delete(g);
 }

@@ -6,6 +6,7 @@
 #include <cstdarg>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 #include <thread>
 
 #include "og_internal.hpp"
@@ -64,10 +65,60 @@ og_graph *graph_new(uint32_t V, uint64_t E, int kind) {
 
 void graph_delete(og_graph *g) {
   if (!g) return;
+  if (g->cols && (void *)g->cols != g->edges) host_free(g->cols);
+  host_free(g->wts);
   host_free(g->off);
   host_free(g->edges);
   host_free(g->outdeg);
   delete g;
+}
+
+// Splits the (column, weight) pairs into a u32 column array and a weight
+// array of the narrowest width (1, 2 or 4 bytes) that holds the largest
+// weight.  Runs once per graph; engines created concurrently on one graph
+// serialise here.
+int graph_prepare_soa(og_graph *g) {
+  static std::mutex mu;
+  std::lock_guard<std::mutex> lock(mu);
+  if (g->soa) return OG_OK;
+  if (g->kind != OG_GRAPH_WEIGHTED) {
+    g->cols = (uint32_t *)g->edges;
+    g->wbytes = 0;
+    g->soa = true;
+    return OG_OK;
+  }
+  const uint64_t E = g->E;
+  const uint32_t *pairs = (const uint32_t *)g->edges;
+  const unsigned nt = hw_threads(0);
+  std::vector<uint32_t> tmax(nt, 0);
+  parallel_for_threads(nt, [&](unsigned t, unsigned n) {
+    uint32_t m = 0;
+    for (uint64_t e = E * t / n, ee = E * (t + 1) / n; e < ee; e++) m = std::max(m, pairs[2 * e + 1]);
+    tmax[t] = m;
+  });
+  const uint32_t wmax = *std::max_element(tmax.begin(), tmax.end());
+  const uint32_t wb = wmax < 256 ? 1 : (wmax < 65536 ? 2 : 4);
+  uint32_t *cols = (uint32_t *)host_alloc(4 * (size_t)E);
+  void *wts = host_alloc((size_t)wb * E);
+  if (!cols || !wts) {
+    host_free(cols);
+    host_free(wts);
+    return fail(OG_E_NOMEM, "cannot allocate the column/weight arrays (%llu edges)", (unsigned long long)E);
+  }
+  parallel_for_threads(nt, [&](unsigned t, unsigned n) {
+    for (uint64_t e = E * t / n, ee = E * (t + 1) / n; e < ee; e++) {
+      cols[e] = pairs[2 * e];
+      const uint32_t w = pairs[2 * e + 1];
+      if (wb == 1) ((uint8_t *)wts)[e] = (uint8_t)w;
+      else if (wb == 2) ((uint16_t *)wts)[e] = (uint16_t)w;
+      else ((uint32_t *)wts)[e] = w;
+    }
+  });
+  g->cols = cols;
+  g->wts = wts;
+  g->wbytes = wb;
+  g->soa = true;
+  return OG_OK;
 }
 
 int graph_validate(const og_graph *g) {
@@ -129,14 +180,15 @@ uint64_t engine_fixed_bytes(uint32_t V, uint64_t E, uint32_t flags) {
 }
 
 int plan_compute(uint32_t V, uint64_t E, const uint64_t *off, int kind,
-                 uint64_t budget, double advisek, uint32_t flags, og_plan *out) {
+                 uint64_t budget, double advisek, uint32_t flags, og_plan *out,
+                 uint32_t edge_bytes) {
   if (!out || !off) return fail(OG_E_ARG, "plan_compute: null argument");
   if (kind < OG_GRAPH_PLAIN || kind > OG_GRAPH_PR) return fail(OG_E_ARG, "bad graph kind %d", kind);
   if (budget == 0) budget = kDefaultBudget;
   og_plan p;
   memset(&p, 0, sizeof p);
   p.budget_bytes = budget;
-  p.edge_bytes = kind == OG_GRAPH_WEIGHTED ? 8 : 4;
+  p.edge_bytes = edge_bytes;
   p.vertex_bytes = engine_vertex_bytes(kind, flags) * ((uint64_t)V + 1);
   p.fixed_bytes = engine_fixed_bytes(V, E, flags);
   if (budget <= p.vertex_bytes + p.fixed_bytes)
@@ -202,6 +254,12 @@ int plan_compute(uint32_t V, uint64_t E, const uint64_t *off, int kind,
 // ====================================================================== C ABI
 
 using namespace og;
+
+#define RC_HOST(x)              \
+  do {                          \
+    int r_ = (x);               \
+    if (r_ != OG_OK) return r_; \
+  } while (0)
 
 extern "C" const char *og_last_error(void) { return t_err.c_str(); }
 extern "C" int og_abi_version(void) { return OG_ABI_VERSION; }
@@ -364,6 +422,42 @@ extern "C" int og_graph_save_bel(const og_graph *g, const char *prefix) {
   return ok ? OG_OK : fail(OG_E_IO, "writing %s.bel.* failed", prefix);
 }
 
+extern "C" int og_convert_uint_to_ulong(const char *in_path, const char *out_path) {
+  clear_error();
+  if (!in_path) return fail(OG_E_ARG, "og_convert_uint_to_ulong: null input path");
+  std::string out = out_path ? std::string(out_path) : std::string(in_path);
+  if (!out_path) {
+    if (out.size() < 4) return fail(OG_E_ARG, "input path '%s' is shorter than its extension", in_path);
+    out = out.substr(0, out.size() - 4) + "lcsr";
+  }
+  FILE *f = fopen(in_path, "rb");
+  if (!f) return fail(OG_E_IO, "cannot open %s", in_path);
+  uint32_t hdr[2];
+  if (fread(hdr, 4, 2, f) != 2) {
+    fclose(f);
+    return fail(OG_E_FORMAT, "%s: truncated header", in_path);
+  }
+  const uint32_t V = hdr[0], E = hdr[1];
+  std::vector<uint32_t> off(V), col(E);
+  const bool ok_in = fread(off.data(), 4, V, f) == V && fread(col.data(), 4, E, f) == E;
+  fclose(f);
+  if (!ok_in) return fail(OG_E_FORMAT, "%s: file shorter than V=%u, E=%u", in_path, V, E);
+  for (uint32_t v = 0; v < V; v++)
+    if (off[v] > E || (v && off[v] < off[v - 1]))
+      return fail(OG_E_FORMAT, "%s: offsets[%u] = %u out of order or above E", in_path, v, off[v]);
+  FILE *o = fopen(out.c_str(), "wb");
+  if (!o) return fail(OG_E_IO, "cannot create %s", out.c_str());
+  bool ok = fwrite(hdr, 4, 2, o) == 2 && fwrite(off.data(), 4, V, o) == V;
+  std::vector<uint64_t> buf(1 << 20);
+  for (uint64_t e0 = 0; ok && e0 < E; e0 += buf.size()) {
+    const uint64_t n = std::min<uint64_t>(buf.size(), E - e0);
+    for (uint64_t i = 0; i < n; i++) buf[i] = col[e0 + i];
+    ok = fwrite(buf.data(), 8, n, o) == n;
+  }
+  ok = (fclose(o) == 0) && ok;
+  return ok ? OG_OK : fail(OG_E_IO, "writing %s failed", out.c_str());
+}
+
 extern "C" uint32_t og_graph_findbignode(const og_graph *g, uint32_t last) {
   // GraphMeta.h:150-165
   if (!g || g->V < 2) return last;
@@ -377,5 +471,16 @@ extern "C" int og_plan_compute(uint64_t V, uint64_t E, const uint64_t *offsets, 
                                og_plan *out) {
   clear_error();
   if (V == 0 || V > 0xFFFFFFFFull) return fail(OG_E_ARG, "vertex count out of range");
-  return plan_compute((uint32_t)V, E, offsets, kind, budget_bytes, advisek, flags, out);
+  // without the graph the weight width is unknown: 4-byte weights assumed
+  return plan_compute((uint32_t)V, E, offsets, kind, budget_bytes, advisek, flags, out,
+                      kind == OG_GRAPH_WEIGHTED ? 8 : 4);
+}
+
+extern "C" int og_graph_plan(og_graph *g, uint64_t budget_bytes, double advisek, uint32_t flags,
+                             og_plan *out) {
+  clear_error();
+  if (!g) return fail(OG_E_ARG, "og_graph_plan: null graph");
+  RC_HOST(graph_prepare_soa(g));
+  return plan_compute(g->V, g->E, g->off, g->kind, budget_bytes, advisek, flags, out,
+                      g->soa_edge_bytes());
 }

@@ -274,6 +274,36 @@ struct LbsArgs {
   uint32_t *err;
 };
 
+// Edge storage is structure-of-arrays: u32 columns plus, for weighted graphs,
+// weights in the narrowest width that holds them (W = uint8_t / uint16_t /
+// uint32_t).  A source yields one edge as a u32 column or a {column, weight}
+// pair; BFS, CC and PageRank read columns only.
+struct SrcU {
+  using Item = uint32_t;
+  const uint32_t *col;
+  __device__ __forceinline__ Item load(uint64_t i) const { return col[i]; }
+};
+template <class W>
+struct SrcW {
+  using Item = uint2;
+  const uint32_t *col;
+  const W *w;
+  __device__ __forceinline__ Item load(uint64_t i) const { return make_uint2(col[i], (uint32_t)w[i]); }
+};
+struct DstU {
+  uint32_t *col;
+  __device__ __forceinline__ void store(uint64_t i, uint32_t x) const { col[i] = x; }
+};
+template <class W>
+struct DstW {
+  uint32_t *col;
+  W *w;
+  __device__ __forceinline__ void store(uint64_t i, uint2 x) const {
+    col[i] = x.x;
+    w[i] = (W)x.y;
+  }
+};
+
 template <class Val>
 struct LbsShared {
   uint32_t rs[kTile + 2];      // tile-relative start of each local vertex
@@ -336,8 +366,8 @@ __device__ __forceinline__ uint32_t lbs_setup(const LbsArgs &a, const Op &op, Lb
   return nl;
 }
 
-template <class Edge, class Op>
-__global__ void __launch_bounds__(kThreads) k_lbs(LbsArgs a, const Edge *__restrict__ edges, Op op) {
+template <class Src, class Op>
+__global__ void __launch_bounds__(kThreads) k_lbs(LbsArgs a, Src src, Op op) {
   __shared__ LbsShared<typename Op::Val> sh;
   const uint64_t k = a.pos_begin / kTile + blockIdx.x;
   const uint64_t pos0 = k * kTile;
@@ -348,7 +378,7 @@ __global__ void __launch_bounds__(kThreads) k_lbs(LbsArgs a, const Edge *__restr
   if (nl == 0) return;
   // All eight loads are issued before the first relax, so each thread keeps
   // eight edge reads in flight (the host-link gather is latency bound).
-  Edge ev[kItems];
+  typename Src::Item ev[kItems];
   uint32_t lv[kItems];
   uint32_t okmask = 0;
 #pragma unroll
@@ -360,7 +390,7 @@ __global__ void __launch_bounds__(kThreads) k_lbs(LbsArgs a, const Edge *__restr
       const uint64_t idx = sh.cb[l] + x;
       lv[it] = l;
       if (idx < a.edge_bound) {
-        ev[it] = edges[idx];
+        ev[it] = src.load(idx);
         okmask |= 1u << it;
       } else {
         atomicOr(a.err, kErrEdgeIndex);
@@ -385,9 +415,8 @@ constexpr size_t gather_smem_bytes() {
 // Positions of a vertex are contiguous both in the host CSR and in the staging
 // buffer, so this is a segmented copy; reads are coalesced 8-byte (or 4-byte)
 // loads over NVLink-C2C, all ITEMS of a thread issued before the first store.
-template <class Edge, int MULT>
-__global__ void __launch_bounds__(kThreads) k_gather(LbsArgs a, const Edge *__restrict__ src,
-                                                     Edge *__restrict__ stage) {
+template <class Src, class Dst, int MULT>
+__global__ void __launch_bounds__(kThreads) k_gather(LbsArgs a, Src src, Dst stage) {
   constexpr uint32_t TILE = MULT * kTile;
   constexpr int ITEMS = TILE / kThreads;
   // dynamic shared memory (gather_smem_bytes<MULT>() bytes, above the static 48 KB)
@@ -434,7 +463,7 @@ __global__ void __launch_bounds__(kThreads) k_gather(LbsArgs a, const Edge *__re
   }
   __syncthreads();
   const uint32_t tlen = (uint32_t)(pend - pos0);
-  Edge ev[ITEMS];
+  typename Src::Item ev[ITEMS];
   uint32_t okm = 0;
 #pragma unroll
   for (int it = 0; it < ITEMS; it++) {
@@ -442,17 +471,17 @@ __global__ void __launch_bounds__(kThreads) k_gather(LbsArgs a, const Edge *__re
     if (x < tlen) {
       const uint64_t idx = cb[map[x]] + x;
       if (idx < a.edge_bound) {
-        ev[it] = src[idx];
+        ev[it] = src.load(idx);
         okm |= 1u << it;
       } else {
         atomicOr(a.err, kErrEdgeIndex);
       }
     }
   }
-  Edge *dst = stage + (pos0 - a.stage_base);
+  const uint64_t base = pos0 - a.stage_base;
 #pragma unroll
   for (int it = 0; it < ITEMS; it++)
-    if (okm & (1u << it)) dst[it * kThreads + threadIdx.x] = ev[it];
+    if (okm & (1u << it)) stage.store(base + it * kThreads + threadIdx.x, ev[it]);
 }
 
 // ------------------------------------------------------------------ ops
@@ -505,18 +534,6 @@ struct MinOp {
     const uint32_t old = atomicMin(value + v, cand);
     if (cand < old) atomicOr(next + (v >> 5), 1u << (v & 31));
   }
-};
-
-// Dynamic-region gather: copies the edges of the compacted list from the
-// page-locked host CSR into a device staging buffer (coalesced on both sides).
-template <class Edge>
-struct GatherOp {
-  using Val = uint32_t;
-  static constexpr bool kNeedVal = false;
-  Edge *stage;
-  uint64_t stage_base;
-  __device__ uint32_t src_val(uint32_t) const { return 0; }
-  __device__ __forceinline__ void relax(Edge e, uint32_t, uint64_t q) const { stage[q - stage_base] = e; }
 };
 
 // ------------------------------------------------------------------ batched BFS
@@ -607,9 +624,8 @@ struct PrArgs {
 // (PR/OneGraph/gpu_kernels.h:107-158).  Contributions are staged in shared
 // memory in edge order and each vertex's segment is added sequentially, so the
 // result depends only on the tiling of the compacted list (deterministic).
-template <class Edge>
-__global__ void __launch_bounds__(kThreads) k_pr_pull(LbsArgs a, const Edge *__restrict__ edges,
-                                                       PrArgs p) {
+template <class Src>
+__global__ void __launch_bounds__(kThreads) k_pr_pull(LbsArgs a, Src src, PrArgs p) {
   __shared__ LbsShared<uint32_t> sh;
   __shared__ float s_c[kTile];
   const uint64_t k = a.pos_begin / kTile + blockIdx.x;
@@ -631,7 +647,7 @@ __global__ void __launch_bounds__(kThreads) k_pr_pull(LbsArgs a, const Edge *__r
       const uint32_t l = sh.map[x];
       const uint64_t idx = sh.cb[l] + x;
       if (idx < a.edge_bound) {
-        const uint32_t u = edge_dst(edges[idx]);
+        const uint32_t u = edge_dst(src.load(idx));
         if (u < p.V) c = __ldg(p.contrib + u);
         else atomicOr(a.err, kErrVertex);
       } else {

@@ -20,7 +20,15 @@ struct og_graph {
   uint32_t *outdeg = nullptr;  // V (OG_GRAPH_PR only)
   int registered = 0;          // number of engines holding a registration
   bool host_pinned = false;    // allocated page-locked (cudaMallocHost)
+  // Structure-of-arrays copy used by the engines (built once, on first use):
+  // u32 columns (the edge array itself for unweighted kinds) and, for
+  // weighted graphs, the weights in the narrowest of 1, 2 or 4 bytes.
+  uint32_t *cols = nullptr;
+  void *wts = nullptr;
+  uint32_t wbytes = 0;
+  bool soa = false;
   uint32_t edge_bytes() const { return kind == OG_GRAPH_WEIGHTED ? 8u : 4u; }
+  uint32_t soa_edge_bytes() const { return 4u + wbytes; }
 };
 
 namespace og {
@@ -45,9 +53,14 @@ unsigned hw_threads(unsigned requested);
 template <class F>
 void parallel_for_threads(unsigned nthreads, F fn);
 
-// Region planner shared by og_plan_compute and the engine.
+// Builds g->cols / g->wts / g->wbytes if not built yet.
+int graph_prepare_soa(og_graph *g);
+
+// Region planner shared by og_plan_compute and the engine; edge_bytes is the
+// device bytes per edge (4 + weight bytes).
 int plan_compute(uint32_t V, uint64_t E, const uint64_t *off, int kind,
-                 uint64_t budget, double advisek, uint32_t flags, og_plan *out);
+                 uint64_t budget, double advisek, uint32_t flags, og_plan *out,
+                 uint32_t edge_bytes);
 
 // Per-vertex / fixed device bytes the engine allocates (planner inputs).
 uint64_t engine_vertex_bytes(int kind, uint32_t flags);

@@ -18,12 +18,11 @@ from conftest import golden_names
 
 pytestmark = pytest.mark.gpu
 
-EB = {og.PLAIN: 4, og.WEIGHTED: 8, og.PR: 4}
 
 
 def budget_for(g, edge_slots, flags=0):
-    p = og.plan(g.V, g.E, g.offsets, g.kind, budget=1 << 40, flags=flags)
-    return p["vertex_bytes"] + p["fixed_bytes"] + int(edge_slots) * EB[g.kind]
+    p = g.plan(budget=1 << 40, flags=flags)
+    return p["vertex_bytes"] + p["fixed_bytes"] + int(edge_slots) * p["edge_bytes"]
 
 
 def configs(g, flags=0):

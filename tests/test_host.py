@@ -237,3 +237,51 @@ def test_no_static_plan_keeps_every_edge_dynamic():
     p = og.plan(g.V, g.E, g.offsets, og.PLAIN, budget=1 << 30, flags=og.CFG_NO_STATIC)
     assert p["static_edges"] == 0 and p["static_vertices"] == 0 and p["dynamic_edges"] == g.E
     assert p["chunk_edges"] > 0
+
+
+def test_graph_plan_uses_split_edge_width():
+    """Weighted graphs are kept as u32 columns + narrow weights: R-MAT weights
+    in [1, 64] fit one byte, so the planner budgets 5 bytes per edge; the
+    graph-free planner assumes 4-byte weights (8 bytes per edge)."""
+    g = og.Graph.rmat(10, 16, weighted=True, seed=3)
+    pg = g.plan(budget=1 << 40)
+    pc = og.plan(g.V, g.E, g.offsets, og.WEIGHTED, budget=1 << 40)
+    assert pg["edge_bytes"] == 5 and pc["edge_bytes"] == 8
+    # same budget: the split layout holds more static edges
+    b = pg["vertex_bytes"] + pg["fixed_bytes"] + int(0.5 * g.E) * 8
+    assert g.plan(budget=b, advisek=1.0)["static_edges"] > og.plan(
+        g.V, g.E, g.offsets, og.WEIGHTED, budget=b, advisek=1.0)["static_edges"]
+    u = og.Graph.rmat(10, 16, seed=3)
+    assert u.plan(budget=1 << 40)["edge_bytes"] == 4
+
+
+def test_graph_plan_wide_weights():
+    """A weight above 65535 needs 4-byte weights; above 255 two bytes."""
+    off = np.array([0, 2, 3, 3], np.uint64)
+    for wmax, eb in [(200, 5), (300, 6), (70000, 8)]:
+        pairs = np.array([[1, 1], [2, wmax], [2, 3]], np.uint32)
+        g = og.Graph.from_arrays(off, pairs, kind=og.WEIGHTED)
+        assert g.plan(budget=1 << 30)["edge_bytes"] == eb
+
+
+def test_convert_uint_to_ulong(tmp_path):
+    """transFileUintToUlong: header and offsets kept as u32, edges widened to u64,
+    output named <input minus 4 chars>lcsr."""
+    rng = np.random.default_rng(0)
+    V, E = 50, 300
+    off = np.sort(rng.integers(0, E + 1, V)).astype(np.uint32)
+    off[0] = 0
+    col = rng.integers(0, V, E).astype(np.uint32)
+    src = tmp_path / "g.bcsr"
+    with open(src, "wb") as f:
+        f.write(np.array([V, E], np.uint32).tobytes() + off.tobytes() + col.tobytes())
+    og.convert_uint_to_ulong(str(src))
+    raw = (tmp_path / "g.lcsr").read_bytes()
+    assert len(raw) == 8 + 4 * V + 8 * E
+    assert np.frombuffer(raw[:8], np.uint32).tolist() == [V, E]
+    np.testing.assert_array_equal(np.frombuffer(raw[8:8 + 4 * V], np.uint32), off)
+    np.testing.assert_array_equal(np.frombuffer(raw[8 + 4 * V:], np.uint64), col.astype(np.uint64))
+    bad = tmp_path / "bad.bcsr"
+    bad.write_bytes(np.array([V, E], np.uint32).tobytes() + off.tobytes())  # no edges
+    with pytest.raises(og.OGError):
+        og.convert_uint_to_ulong(str(bad), str(tmp_path / "x.lcsr"))
