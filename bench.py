@@ -254,7 +254,7 @@ def config_dict(args, g):
             "graph": "R-MAT scale %d ef16 a,b,c=.57,.19,.19 symmetric dedup weights U[1,64]" % args.scale,
             "V": g.V, "E": g.E, "budget_bytes": int(args.budget_gib * GIB), "advisek": args.advisek,
             "sources": args.sources, "seeds": {"graph": 1, "weights": 2, "sources": 3},
-            "l2": "inputs larger than L2 (graph %.1f GB)" % (g.E * 5 / 1e9),
+            "l2": "inputs larger than L2 (packed graph %.1f GB)" % (g.E * g.plan(1 << 40)["edge_bits"] / 8e9),
             "dynamic_mode": "direct" if args.direct else "staged", "sssp_delta": args.delta}
 
 
@@ -323,17 +323,17 @@ def run_ours(args, rank, world, local):
     launches = sum(s["launches"] for s in stats)
     peaks = measured_peaks()
     h2d = h2d_peak_gbs()
-    # algorithmic bytes: per edge the column (4 B), the weight (plan edge_bytes - 4,
-    # 1 B for weights in [1, 64]) and the target distance (4 B); 20 B per vertex
-    eb = plan["edge_bytes"]
+    # algorithmic bytes: per edge one packed record (plan edge_bits: 27 column +
+    # 6 weight bits at scale 27) and the target distance (4 B); 20 B per vertex
+    eb = plan["edge_bits"] / 8
     static_gbs = ((eb + 4) * st_edges + 20 * st_verts) / (st_ms / 1e3) / 1e9 if st_ms else 0.0
     link_gbs = dyn_bytes / (dyn_ms / 1e3) / 1e9 if dyn_ms else 0.0
-    roof_static = {"bound": "hbm", "kernel": "k_lbs<SrcW<u8>,MinOp<true>> (static region relax)",
+    roof_static = {"bound": "hbm", "kernel": "k_lbs<SrcP<true>,MinOp<true>> (static region relax)",
                    "achieved": static_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
                    "frac": static_gbs / peaks["hbm_gbs"], "traffic": None,
                    "peak_source": peaks["source"]}
-    roof_link = {"bound": "host-link", "kernel": "k_lbs<SrcW<u8>,MinOp<true>> over host-mapped edges"
-                 if args.direct else "k_gather<SrcW<u8>,DstW<u8>> + staged relax",
+    roof_link = {"bound": "host-link", "kernel": "k_lbs<SrcP<true>,MinOp<true>> over host-mapped records"
+                 if args.direct else "k_gather<SrcP<true>,DstW<u8>> + staged relax",
                  "achieved": link_gbs, "peak": h2d, "unit": "GB/s", "frac": link_gbs / h2d if h2d else None,
                  "traffic": None, "peak_source": "measured pinned H2D copy in this run"}
     dominant = roof_link if dyn_ms > st_ms else roof_static
@@ -361,7 +361,7 @@ def run_ours(args, rank, world, local):
         "roofline": dominant, "roofline_static": roof_static, "roofline_link": roof_link,
         "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": launches,
         "plan": {k: plan[k] for k in ("static_vertices", "static_edges", "dynamic_edges",
-                                      "chunk_edges", "advisek", "edge_bytes")},
+                                      "chunk_edges", "advisek", "edge_bits")},
         "per_query": {"iterations": statistics.mean(s["iterations"] for s in stats),
                       "chunks": statistics.mean(s["chunks"] for s in stats),
                       "ms_static": st_ms / len(stats), "ms_dynamic": dyn_ms / len(stats),
@@ -553,7 +553,9 @@ def run_bfs_resident(args, rank, world, local):
     st_edges = sum(x["edges_static"] for x in stats)
     st_verts = sum(x["static_vertices"] for x in stats)
     peaks = measured_peaks()
-    gbs = (8 * st_edges + 20 * st_verts) / (st_ms / 1e3) / 1e9 if st_ms else 0.0
+    # per edge: one packed column record (edge_bits) + the 4 B visited probe
+    eb = eng.plan["edge_bits"] / 8
+    gbs = ((eb + 4) * st_edges + 20 * st_verts) / (st_ms / 1e3) / 1e9 if st_ms else 0.0
     c0 = time.perf_counter()
     oracle.bfs(np.array(g.offsets), np.array(g.columns), src)
     cpu_s = time.perf_counter() - c0
@@ -567,7 +569,7 @@ def run_bfs_resident(args, rank, world, local):
         "persistent_ms_per_query": tb / args.steps * 1e3,
         "persistent_gteps": comp_edges * args.steps / tb / 1e9,
         "bit_exact_vs_runCPUBFS": exact, "levels": stats[0]["iterations"],
-        "roofline": {"bound": "hbm", "kernel": "k_lbs<SrcU,BfsOp> (static relax)", "achieved": gbs,
+        "roofline": {"bound": "hbm", "kernel": "k_lbs<SrcP<false>,BfsOp> (static relax)", "achieved": gbs,
                      "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": gbs / peaks["hbm_gbs"],
                      "traffic": None, "peak_source": peaks["source"]},
         "cpu_baseline": {"value": comp_edges / cpu_s / 1e9, "unit": "GTEPS", "cores": 1, "kind": "port",

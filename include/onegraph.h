@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define OG_ABI_VERSION 1
+#define OG_ABI_VERSION 2
 
 typedef enum og_status {
   OG_OK = 0,
@@ -143,7 +143,9 @@ typedef struct og_plan {
   uint64_t static_edges;     /* off[Vs]: edges preloaded once                */
   uint64_t dynamic_edges;    /* E - static_edges                             */
   uint64_t chunk_edges;      /* staging capacity per buffer (two buffers)    */
-  uint32_t edge_bytes;       /* 4 or 8                                       */
+  uint32_t edge_bytes;       /* packed record size rounded up to bytes       */
+  uint32_t edge_bits;        /* packed record size: column + weight bits     */
+  uint32_t stage_edge_bytes; /* unpacked edge in a staging buffer            */
   uint32_t reserved;
 } og_plan;
 
@@ -155,12 +157,21 @@ int og_plan_compute(uint64_t V, uint64_t E, const uint64_t *offsets, int kind,
                     og_plan *out);
 
 /* The planner for a given graph with the engine's real edge width: the
- * engine keeps edges as u32 columns plus weights in the narrowest of 1, 2 or
- * 4 bytes that holds the graph's largest weight (so 5 bytes per edge for the
- * R-MAT weights in [1, 64]); og_plan_compute, which has no graph, assumes
- * 4-byte weights. */
+ * engine keeps edges as bit-packed records of bits(V-1) column bits plus
+ * bits(wmax - wmin) weight bits (33 bits for R-MAT 27 with weights in
+ * [1, 64]) in the page-locked host copy and the static region; staging
+ * buffers hold unpacked edges (u32 column + 1, 2 or 4 weight bytes).
+ * og_plan_compute, which has no graph, charges the reference's sizeof(Edge)
+ * (4 or 8 bytes) per edge. */
 int og_graph_plan(og_graph *g, uint64_t budget_bytes, double advisek, uint32_t flags,
                   og_plan *out);
+
+/* The bit-packed edge records engines read (built on first use): record e
+ * is bits [e*bpe, (e+1)*bpe) of `words` (bit i of the stream is bit i%32 of
+ * word i/32), column in the low bc bits, weight - wmin in the bits above.
+ * nwords includes two zero padding words.  The arrays belong to the graph. */
+int og_graph_records(og_graph *g, const uint32_t **words, uint64_t *nwords, uint32_t *bpe,
+                     uint32_t *bc, uint32_t *wmin);
 
 /* ---------------------------------------------------------------- engine */
 

@@ -50,7 +50,8 @@ class Plan(C.Structure):
                 ("advisek", C.c_double), ("advisek_auto", C.c_double),
                 ("max_partition", C.c_uint64), ("static_vertices", C.c_uint32),
                 ("static_edges", C.c_uint64), ("dynamic_edges", C.c_uint64),
-                ("chunk_edges", C.c_uint64), ("edge_bytes", C.c_uint32), ("reserved", C.c_uint32)]
+                ("chunk_edges", C.c_uint64), ("edge_bytes", C.c_uint32), ("edge_bits", C.c_uint32),
+                ("stage_edge_bytes", C.c_uint32), ("reserved", C.c_uint32)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_ if f != "reserved"}
@@ -127,6 +128,8 @@ SIGNATURES = [
     ("og_graph_findbignode", C.c_uint32, [_P, C.c_uint32]),
     ("og_graph_save_bel", C.c_int, [_P, C.c_char_p]),
     ("og_convert_uint_to_ulong", C.c_int, [C.c_char_p, C.c_char_p]),
+    ("og_graph_records", C.c_int, [_P, C.POINTER(_P), C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
+                                   C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     ("og_rmat_generate", C.c_int, [C.POINTER(RmatParams), C.POINTER(_P)]),
     ("og_plan_compute", C.c_int, [C.c_uint64, C.c_uint64, _P, C.c_int, C.c_uint64, C.c_double,
                                   C.c_uint32, C.POINTER(Plan)]),
@@ -163,6 +166,9 @@ SIGNATURES = [
 ]
 
 
+ABI_VERSION = 2  # OG_ABI_VERSION of include/onegraph.h these bindings follow
+
+
 def lib():
     """Loads libog.so (built by onegraph_gb300.build / __graft_entry__.build)."""
     global _lib
@@ -174,6 +180,8 @@ def lib():
             f = getattr(L, name)
             f.restype = res
             f.argtypes = args
+        if L.og_abi_version() != ABI_VERSION:
+            raise OSError("libog.so ABI %d, bindings expect %d: rebuild" % (L.og_abi_version(), ABI_VERSION))
         _lib = L
     return _lib
 
@@ -275,6 +283,15 @@ class Graph:
         p = Plan()
         _check(lib().og_graph_plan(self._h, budget, advisek, flags, C.byref(p)), "og_graph_plan")
         return p.as_dict()
+
+    def records(self) -> dict:
+        """The packed edge records the engines read: words (borrowed view),
+        bits per record, column bits and the weight offset."""
+        w, n, bpe, bc, wmin = _P(), C.c_uint64(), C.c_uint32(), C.c_uint32(), C.c_uint32()
+        _check(lib().og_graph_records(self._h, C.byref(w), C.byref(n), C.byref(bpe), C.byref(bc),
+                                      C.byref(wmin)), "og_graph_records")
+        words = np.ctypeslib.as_array(C.cast(w, C.POINTER(C.c_uint32)), (n.value,))
+        return {"words": words, "bpe": bpe.value, "bc": bc.value, "wmin": wmin.value}
 
     def findbignode(self, last: int) -> int:
         return int(lib().og_graph_findbignode(self._h, last))

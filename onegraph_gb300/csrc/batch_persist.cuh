@@ -25,8 +25,8 @@ struct PersistArgs {
   uint32_t V;
   uint64_t nwords;
   const uint64_t *off;
-  const uint32_t *scols;   // device copy of the columns [0, static_edges)
-  const uint32_t *hcols;   // page-locked host columns (all edges), null if E == static_edges
+  SrcP<false> ssrc;        // packed static records [0, static_edges) in HBM
+  SrcP<false> hsrc;        // packed page-locked host records (all edges); words null if E == static_edges
   uint64_t static_edges;
   uint64_t E;
   unsigned long long *visited, *cur, *next;
@@ -140,8 +140,6 @@ __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
   using SH = PersistShared<BLOCK, ITEMS>;
   constexpr uint32_t TILE = SH::TILE;
   __shared__ SH sh;
-  const uint32_t *sedges = a.scols;
-  const uint32_t *hedges = a.hcols;
   unsigned long long *cur = a.cur, *next = a.next;
   uint32_t *cur_any = a.cur_any, *next_any = a.next_any;
   // contiguous word range of this CTA, split into contiguous per-thread runs
@@ -283,10 +281,10 @@ __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
           const uint64_t idx = sh.cb[l] + x;
           lv[it] = l;
           if (idx < a.static_edges) {
-            ev[it] = sedges[idx];
+            ev[it] = a.ssrc.load(idx);
             okm |= 1u << it;
-          } else if (idx < a.E && hedges) {
-            ev[it] = hedges[idx];
+          } else if (idx < a.E && a.hsrc.words) {
+            ev[it] = a.hsrc.load(idx);
             okm |= 1u << it;
           } else {
             atomicOr(a.err, kErrEdgeIndex);

@@ -47,7 +47,6 @@ struct og_engine {
   bool registered = false;
   uint32_t V = 0, Vs = 0;
   uint64_t nwords = 0;
-  uint32_t eb = 4;
 
   cudaStream_t s_main = nullptr, s_dyn = nullptr, s_gat = nullptr;
   cudaEvent_t ev_round = nullptr, ev_cs = nullptr, ev_cd = nullptr, ev_dyn_done = nullptr;
@@ -56,13 +55,13 @@ struct og_engine {
   std::vector<cudaEvent_t> t_gat;  // start/end pairs around each gather launch
 
   uint64_t *off_d = nullptr;
-  // edges as structure-of-arrays: u32 columns + weights of wbytes (0, 1, 2, 4)
-  uint32_t *scols_d = nullptr;               // static region columns (HBM)
-  void *sw_d = nullptr;                      // static region weights (HBM)
+  // edges as bit-packed records (host copy and static region) and as
+  // unpacked u32 columns + weights of wbytes (1, 2, 4) in the staging buffers
+  uint32_t *spk_d = nullptr;                 // static region records (HBM)
+  uint32_t bpe = 0, bc = 0, wmin = 0;        // record layout
   uint32_t *stage_col[2] = {nullptr, nullptr};  // staging buffers (columns)
   void *stage_w[2] = {nullptr, nullptr};        // staging buffers (weights)
-  const uint32_t *hcols_d = nullptr;         // page-locked host columns, device view
-  const void *hw_d = nullptr;                // page-locked host weights, device view
+  const uint32_t *hpk_d = nullptr;           // page-locked host records, device view
   uint32_t wbytes = 0;
   uint32_t *value_d = nullptr;
   uint32_t *bm[3] = {nullptr, nullptr, nullptr};
@@ -162,8 +161,7 @@ void destroy(og_engine *e) {
   if (e->s_gat) cudaStreamDestroy(e->s_gat);
   if (e->registered && e->g) {
     if (--e->g->registered == 0) {
-      cudaHostUnregister(e->g->cols);
-      if (e->g->wts) cudaHostUnregister(e->g->wts);
+      cudaHostUnregister(e->g->packed);
     }
   }
   if (e->parent) e->parent->clones--;
@@ -258,11 +256,13 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
   e->batch_enabled = (cfg->flags & OG_CFG_BATCH) != 0;
   CK(cudaSetDevice(e->dev));
   CK(cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, e->dev));
-  RC(graph_prepare_soa(g));
+  RC(graph_prepare(g));
   e->wbytes = g->wbytes;
-  e->eb = g->soa_edge_bytes();
+  e->bpe = g->bpe;
+  e->bc = g->bc;
+  e->wmin = g->wmin;
   RC(plan_compute(g->V, g->E, g->off, g->kind, cfg->budget_bytes, cfg->advisek, cfg->flags, &e->plan,
-                  e->eb));
+                  g->bpe, 4 + g->wbytes));
   const og_plan &P = e->plan;
   size_t free_b = 0, total_b = 0;
   CK(cudaMemGetInfo(&free_b, &total_b));
@@ -274,12 +274,13 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
 
   // kernels with more than 48 KB of shared memory opt in once per process
   const int gsm = (int)gather_smem_bytes<kGatherMult>();
-  CK(cudaFuncSetAttribute(k_gather<SrcU, DstU, kGatherMult>, cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
-  CK(cudaFuncSetAttribute(k_gather<SrcW<uint8_t>, DstW<uint8_t>, kGatherMult>,
+  CK(cudaFuncSetAttribute(k_gather<SrcP<false>, DstU, kGatherMult>,
                           cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
-  CK(cudaFuncSetAttribute(k_gather<SrcW<uint16_t>, DstW<uint16_t>, kGatherMult>,
+  CK(cudaFuncSetAttribute(k_gather<SrcP<true>, DstW<uint8_t>, kGatherMult>,
                           cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
-  CK(cudaFuncSetAttribute(k_gather<SrcW<uint32_t>, DstW<uint32_t>, kGatherMult>,
+  CK(cudaFuncSetAttribute(k_gather<SrcP<true>, DstW<uint16_t>, kGatherMult>,
+                          cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
+  CK(cudaFuncSetAttribute(k_gather<SrcP<true>, DstW<uint32_t>, kGatherMult>,
                           cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
 
   // host CSR: page-lock so kernels can gather from it over the link
@@ -288,41 +289,26 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
       int pageable = 0;
       CK(cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, e->dev));
       if (!pageable) return fail(OG_E_UNSUPPORTED, "device cannot read pageable host memory");
-      e->hcols_d = g->cols;
-      e->hw_d = g->wts;
+      e->hpk_d = g->packed;
     } else {
       if (g->registered == 0) {
         int ro = 0;
         cudaDeviceGetAttribute(&ro, cudaDevAttrHostRegisterReadOnlySupported, e->dev);
-        const unsigned fl = cudaHostRegisterMapped | (ro ? cudaHostRegisterReadOnly : 0);
-        CK(cudaHostRegister(g->cols, g->E * 4, fl));
-        if (g->wts) {
-          cudaError_t rw = cudaHostRegister(g->wts, g->E * g->wbytes, fl);
-          if (rw != cudaSuccess) {
-            cudaHostUnregister(g->cols);
-            return fail(OG_E_CUDA, "cudaHostRegister(weights): %s", cudaGetErrorString(rw));
-          }
-        }
+        CK(cudaHostRegister(g->packed, g->packed_words * 4,
+                            cudaHostRegisterMapped | (ro ? cudaHostRegisterReadOnly : 0)));
       }
       g->registered++;
       e->registered = true;
       void *dp = nullptr;
-      CK(cudaHostGetDevicePointer(&dp, g->cols, 0));
-      e->hcols_d = (const uint32_t *)dp;
-      if (g->wts) {
-        CK(cudaHostGetDevicePointer(&dp, g->wts, 0));
-        e->hw_d = dp;
-      }
+      CK(cudaHostGetDevicePointer(&dp, g->packed, 0));
+      e->hpk_d = (const uint32_t *)dp;
     }
   }
 
   // resident graph state shared with clones
   const uint64_t V = g->V;
   RC(dalloc(e, &e->off_d, V + 1));
-  if (P.static_edges) {
-    RC(dalloc(e, &e->scols_d, P.static_edges));
-    if (e->wbytes) RC(dalloc(e, (char **)&e->sw_d, P.static_edges * e->wbytes));
-  }
+  if (P.static_edges) RC(dalloc(e, &e->spk_d, g->packed_words_for(P.static_edges)));
   if (e->pr_enabled) RC(dalloc(e, &e->outdeg_d, V + 1));
   e->resident_bytes = e->dbytes;
   RC(create_query_state(e));
@@ -332,12 +318,9 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
 
   // initGraphDevice: offsets, the static edge prefix, PageRank out-degrees
   CK(cudaMemcpyAsync(e->off_d, g->off, 8 * (V + 1), cudaMemcpyHostToDevice, e->s_main));
-  if (P.static_edges) {
-    CK(cudaMemcpyAsync(e->scols_d, g->cols, P.static_edges * 4, cudaMemcpyHostToDevice, e->s_main));
-    if (e->wbytes)
-      CK(cudaMemcpyAsync(e->sw_d, g->wts, P.static_edges * e->wbytes, cudaMemcpyHostToDevice,
-                         e->s_main));
-  }
+  if (P.static_edges)
+    CK(cudaMemcpyAsync(e->spk_d, g->packed, 4 * g->packed_words_for(P.static_edges),
+                       cudaMemcpyHostToDevice, e->s_main));
   if (e->pr_enabled) {
     if (g->kind == OG_GRAPH_PR) {
       CK(cudaMemcpyAsync(e->outdeg_d, g->outdeg, 4 * V, cudaMemcpyHostToDevice, e->s_main));
@@ -364,12 +347,12 @@ int clone(og_engine *parent, og_engine *e) {
   e->V = parent->V;
   e->Vs = parent->Vs;
   e->nwords = parent->nwords;
-  e->eb = parent->eb;
   e->off_d = parent->off_d;
-  e->scols_d = parent->scols_d;
-  e->sw_d = parent->sw_d;
-  e->hcols_d = parent->hcols_d;
-  e->hw_d = parent->hw_d;
+  e->spk_d = parent->spk_d;
+  e->hpk_d = parent->hpk_d;
+  e->bpe = parent->bpe;
+  e->bc = parent->bc;
+  e->wmin = parent->wmin;
   e->wbytes = parent->wbytes;
   e->outdeg_d = parent->outdeg_d;
   e->tuned = parent->tuned;
@@ -441,24 +424,26 @@ int check_device_error(og_engine *e) {
 }
 
 // Edge views of an engine: EK<void> reads columns only (BFS, CC, PageRank,
-// batched BFS), EK<W> columns and W-wide weights (SSSP).
+// batched BFS), EK<W> columns and weights (SSSP, W = staging weight type).
+// The static region and the host copy are packed records (PSrc); staging
+// buffers hold unpacked edges (Src / Dst).
 template <class W>
 struct EK {
+  using PSrc = SrcP<true>;
   using Src = SrcW<W>;
   using Dst = DstW<W>;
-  static constexpr uint32_t kBytes = 4 + sizeof(W);
-  static Src stat(const og_engine *e) { return Src{e->scols_d, (const W *)e->sw_d}; }
-  static Src host(const og_engine *e) { return Src{e->hcols_d, (const W *)e->hw_d}; }
+  static PSrc stat(const og_engine *e) { return PSrc{e->spk_d, e->bpe, e->bc, e->wmin}; }
+  static PSrc host(const og_engine *e) { return PSrc{e->hpk_d, e->bpe, e->bc, e->wmin}; }
   static Src stage(const og_engine *e, int b) { return Src{e->stage_col[b], (const W *)e->stage_w[b]}; }
   static Dst stage_dst(const og_engine *e, int b) { return Dst{e->stage_col[b], (W *)e->stage_w[b]}; }
 };
 template <>
 struct EK<void> {
+  using PSrc = SrcP<false>;
   using Src = SrcU;
   using Dst = DstU;
-  static constexpr uint32_t kBytes = 4;
-  static Src stat(const og_engine *e) { return Src{e->scols_d}; }
-  static Src host(const og_engine *e) { return Src{e->hcols_d}; }
+  static PSrc stat(const og_engine *e) { return PSrc{e->spk_d, e->bpe, e->bc, e->wmin}; }
+  static PSrc host(const og_engine *e) { return PSrc{e->hpk_d, e->bpe, e->bc, e->wmin}; }
   static Src stage(const og_engine *e, int b) { return Src{e->stage_col[b]}; }
   static Dst stage_dst(const og_engine *e, int b) { return Dst{e->stage_col[b]}; }
 };
@@ -494,7 +479,7 @@ int launch_gather(og_engine *e, const LbsArgs &a, int buf, cudaStream_t s) {
   constexpr uint64_t T = (uint64_t)kGatherMult * kTile;
   const unsigned grid = (unsigned)((a.pos_end - a.pos_begin + T - 1) / T);
   if (grid == 0) return OG_OK;
-  k_gather<typename K::Src, typename K::Dst, kGatherMult>
+  k_gather<typename K::PSrc, typename K::Dst, kGatherMult>
       <<<grid, kThreads, gather_smem_bytes<kGatherMult>(), s>>>(a, K::host(e), K::stage_dst(e, buf));
   e->launches++;
   return OG_OK;
@@ -571,7 +556,7 @@ int run_regions(og_engine *e, og_stats &st, Timing &tm, StaticFn static_fn, DynF
     CK(cudaStreamWaitEvent(e->s_main, e->ev_dyn_done, 0));
     tm.pend_d = true;
     st.edges_dynamic += cd.total;
-    st.link_bytes += cd.total * K::kBytes;
+    st.link_bytes += (cd.total * e->bpe + 7) / 8;
   }
   return OG_OK;
 }
@@ -646,7 +631,7 @@ int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
     st.frontier_sum += n;
     st.static_vertices += e->counts_h[0].n;
     auto sfn = [&](const LbsArgs &a) { return launch_relax(e, ro, a, K::stat(e), next, e->s_main); };
-    auto dfn = [&](const LbsArgs &a, typename K::Src src, cudaStream_t ds) {
+    auto dfn = [&](const LbsArgs &a, auto src, cudaStream_t ds) {
       return launch_relax(e, ro, a, src, next, ds);
     };
     RC((run_regions<K>(e, st, tm, sfn, dfn)));
@@ -701,10 +686,10 @@ int run_batch(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *out, uin
     st.frontier_sum += nl;
     st.static_vertices += e->counts_h[0].n;
     BatchOp op{visited, cur, next, next_any, e->err_d, e->V};
-    auto launch = [&](const LbsArgs &a, SrcU src, cudaStream_t ls) {
+    auto launch = [&](const LbsArgs &a, auto src, cudaStream_t ls) {
       const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
       if (grid) {
-        k_lbs<SrcU, BatchOp><<<grid, kThreads, 0, ls>>>(a, src, op);
+        k_lbs<decltype(src), BatchOp><<<grid, kThreads, 0, ls>>>(a, src, op);
         e->launches++;
       }
       return (int)OG_OK;
@@ -799,8 +784,8 @@ int enqueue_persist(og_engine *e, uint32_t n, int ci, uint32_t *depth_d) {
   a.V = e->V;
   a.nwords = e->nwords;
   a.off = e->off_d;
-  a.scols = e->scols_d;
-  a.hcols = e->hcols_d;
+  a.ssrc = EKU::stat(e);
+  a.hsrc = EKU::host(e);
   a.static_edges = e->plan.static_edges;
   a.E = e->g->E;
   a.visited = e->bmask[0];
@@ -902,7 +887,7 @@ int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *
   st.frontier_sum = stat[0];
   st.edges_static = stat[1] - stat[2];
   st.edges_dynamic = stat[2];
-  st.link_bytes = stat[2] * 4;  // columns only
+  st.link_bytes = (stat[2] * e->bpe + 7) / 8;  // packed records read over the link
   st.chunks = graph ? 1u : 0u;  // 1: replayed from the captured CUDA graph
   if (checks)
     for (uint32_t i = 0; i < n; i++) {
@@ -943,15 +928,15 @@ int pr_sums(og_engine *e, og_stats &st, Timing &tm) {
   auto sfn = [&](const LbsArgs &a) {
     const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
     if (grid) {
-      k_pr_pull<SrcU><<<grid, kThreads, 0, e->s_main>>>(a, EKU::stat(e), args_for(0));
+      k_pr_pull<EKU::PSrc><<<grid, kThreads, 0, e->s_main>>>(a, EKU::stat(e), args_for(0));
       e->launches++;
     }
     return (int)OG_OK;
   };
-  auto dfn = [&](const LbsArgs &a, SrcU src, cudaStream_t ds) {
+  auto dfn = [&](const LbsArgs &a, auto src, cudaStream_t ds) {
     const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
     if (grid) {
-      k_pr_pull<SrcU><<<grid, kThreads, 0, ds>>>(a, src, args_for(1));
+      k_pr_pull<decltype(src)><<<grid, kThreads, 0, ds>>>(a, src, args_for(1));
       e->launches++;
     }
     return (int)OG_OK;
@@ -1218,7 +1203,6 @@ struct BatchCtx {
 
 int batch_body(og_engine *en, og_stats &s, void *cx) {
   const BatchCtx &b = *(BatchCtx *)cx;
-  const bool w = en->g->kind == OG_GRAPH_WEIGHTED;
   if (b.mode == 1) return run_batch(en, b.srcs, b.n, b.out, b.checks, s);
   const int ci = b.mode >= 2 ? b.mode - 2 : (en->tuned >= 0 ? en->tuned : 0);
   return run_batch_persist(en, b.srcs, b.n, b.out, b.checks, s, ci);
@@ -1491,8 +1475,7 @@ extern "C" int og_k_compact_noalloc(const uint32_t *bits, uint32_t v_begin, uint
 extern "C" void og_graph_free(og_graph *g) {
   if (!g) return;
   if (g->registered) {
-    cudaHostUnregister(g->cols);
-    if (g->wts) cudaHostUnregister(g->wts);
+    cudaHostUnregister(g->packed);
   }
   og::graph_delete(g);
 }

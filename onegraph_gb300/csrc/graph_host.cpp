@@ -65,59 +65,78 @@ og_graph *graph_new(uint32_t V, uint64_t E, int kind) {
 
 void graph_delete(og_graph *g) {
   if (!g) return;
-  if (g->cols && (void *)g->cols != g->edges) host_free(g->cols);
-  host_free(g->wts);
+  host_free(g->packed);
   host_free(g->off);
   host_free(g->edges);
   host_free(g->outdeg);
   delete g;
 }
 
-// Splits the (column, weight) pairs into a u32 column array and a weight
-// array of the narrowest width (1, 2 or 4 bytes) that holds the largest
-// weight.  Runs once per graph; engines created concurrently on one graph
-// serialise here.
-int graph_prepare_soa(og_graph *g) {
+// Packs the edges into bpe-bit records (column in the low bc bits, weight
+// minus the smallest weight above them), so that the host link and the static
+// region carry bc + bw bits per edge: 33 bits for an R-MAT 27 graph with
+// weights in [1, 64], 20 bits for an unweighted R-MAT 20 graph.  Threads pack
+// ranges that start on multiples of 32 records, i.e. on whole words.  Runs
+// once per graph; engines created concurrently on one graph serialise here.
+int graph_prepare(og_graph *g) {
   static std::mutex mu;
   std::lock_guard<std::mutex> lock(mu);
-  if (g->soa) return OG_OK;
-  if (g->kind != OG_GRAPH_WEIGHTED) {
-    g->cols = (uint32_t *)g->edges;
-    g->wbytes = 0;
-    g->soa = true;
-    return OG_OK;
-  }
+  if (g->prepared) return OG_OK;
   const uint64_t E = g->E;
-  const uint32_t *pairs = (const uint32_t *)g->edges;
+  const bool weighted = g->kind == OG_GRAPH_WEIGHTED;
+  const uint32_t *ed = (const uint32_t *)g->edges;
   const unsigned nt = hw_threads(0);
-  std::vector<uint32_t> tmax(nt, 0);
-  parallel_for_threads(nt, [&](unsigned t, unsigned n) {
-    uint32_t m = 0;
-    for (uint64_t e = E * t / n, ee = E * (t + 1) / n; e < ee; e++) m = std::max(m, pairs[2 * e + 1]);
-    tmax[t] = m;
-  });
-  const uint32_t wmax = *std::max_element(tmax.begin(), tmax.end());
-  const uint32_t wb = wmax < 256 ? 1 : (wmax < 65536 ? 2 : 4);
-  uint32_t *cols = (uint32_t *)host_alloc(4 * (size_t)E);
-  void *wts = host_alloc((size_t)wb * E);
-  if (!cols || !wts) {
-    host_free(cols);
-    host_free(wts);
-    return fail(OG_E_NOMEM, "cannot allocate the column/weight arrays (%llu edges)", (unsigned long long)E);
+  uint32_t wmin = 0, wmax = 0;
+  if (weighted && E) {
+    std::vector<uint32_t> tmin(nt, UINT32_MAX), tmax(nt, 0);
+    parallel_for_threads(nt, [&](unsigned t, unsigned n) {
+      uint32_t lo = UINT32_MAX, hi = 0;
+      for (uint64_t e = E * t / n, ee = E * (t + 1) / n; e < ee; e++) {
+        lo = std::min(lo, ed[2 * e + 1]);
+        hi = std::max(hi, ed[2 * e + 1]);
+      }
+      tmin[t] = lo;
+      tmax[t] = hi;
+    });
+    wmin = *std::min_element(tmin.begin(), tmin.end());
+    wmax = *std::max_element(tmax.begin(), tmax.end());
   }
+  const uint32_t bc = std::max<uint32_t>(1, bits_for(g->V - 1));
+  const uint32_t bw = weighted ? bits_for(wmax - wmin) : 0;
+  g->bc = bc;
+  g->bw = bw;
+  g->bpe = bc + bw;
+  g->wmin = wmin;
+  g->wbytes = weighted ? (wmax < 256 ? 1 : (wmax < 65536 ? 2 : 4)) : 0;
+  const uint64_t words = g->packed_words_for(E);
+  uint32_t *pk = (uint32_t *)host_alloc(4 * (size_t)words);
+  if (!pk) return fail(OG_E_NOMEM, "cannot allocate the packed edge records (%llu words)", (unsigned long long)words);
+  const uint64_t groups = (E + 31) / 32;
+  const uint32_t bpe = g->bpe;
   parallel_for_threads(nt, [&](unsigned t, unsigned n) {
-    for (uint64_t e = E * t / n, ee = E * (t + 1) / n; e < ee; e++) {
-      cols[e] = pairs[2 * e];
-      const uint32_t w = pairs[2 * e + 1];
-      if (wb == 1) ((uint8_t *)wts)[e] = (uint8_t)w;
-      else if (wb == 2) ((uint16_t *)wts)[e] = (uint16_t)w;
-      else ((uint32_t *)wts)[e] = w;
+    const uint64_t e0 = std::min(E, groups * t / n * 32), e1 = std::min(E, groups * (t + 1) / n * 32);
+    if (e0 >= e1) return;
+    uint64_t q = e0 * bpe / 32;  // e0 is a multiple of 32: a word boundary
+    unsigned __int128 acc = 0;
+    uint32_t nb = 0;
+    for (uint64_t e = e0; e < e1; e++) {
+      const uint64_t rec = weighted ? ((uint64_t)ed[2 * e] | ((uint64_t)(ed[2 * e + 1] - wmin) << bc))
+                                    : (uint64_t)ed[e];
+      acc |= (unsigned __int128)rec << nb;
+      nb += bpe;
+      while (nb >= 32) {
+        pk[q++] = (uint32_t)acc;
+        acc >>= 32;
+        nb -= 32;
+      }
     }
+    if (nb) pk[q++] = (uint32_t)acc;  // only the last range ends inside a word
   });
-  g->cols = cols;
-  g->wts = wts;
-  g->wbytes = wb;
-  g->soa = true;
+  const uint64_t full = (E * bpe + 31) / 32;
+  for (uint64_t q = full; q < words; q++) pk[q] = 0;
+  g->packed = pk;
+  g->packed_words = words;
+  g->prepared = true;
   return OG_OK;
 }
 
@@ -181,14 +200,17 @@ uint64_t engine_fixed_bytes(uint32_t V, uint64_t E, uint32_t flags) {
 
 int plan_compute(uint32_t V, uint64_t E, const uint64_t *off, int kind,
                  uint64_t budget, double advisek, uint32_t flags, og_plan *out,
-                 uint32_t edge_bytes) {
+                 uint32_t edge_bits, uint32_t stage_bytes) {
   if (!out || !off) return fail(OG_E_ARG, "plan_compute: null argument");
   if (kind < OG_GRAPH_PLAIN || kind > OG_GRAPH_PR) return fail(OG_E_ARG, "bad graph kind %d", kind);
+  if (edge_bits == 0 || edge_bits > 64 || stage_bytes == 0) return fail(OG_E_ARG, "bad edge width");
   if (budget == 0) budget = kDefaultBudget;
   og_plan p;
   memset(&p, 0, sizeof p);
   p.budget_bytes = budget;
-  p.edge_bytes = edge_bytes;
+  p.edge_bits = edge_bits;
+  p.edge_bytes = (edge_bits + 7) / 8;
+  p.stage_edge_bytes = stage_bytes;
   p.vertex_bytes = engine_vertex_bytes(kind, flags) * ((uint64_t)V + 1);
   p.fixed_bytes = engine_fixed_bytes(V, E, flags);
   if (budget <= p.vertex_bytes + p.fixed_bytes)
@@ -196,7 +218,10 @@ int plan_compute(uint32_t V, uint64_t E, const uint64_t *off, int kind,
                 "budget %llu B cannot hold the per-vertex state (%llu B) and scratch (%llu B)",
                 (unsigned long long)budget, (unsigned long long)p.vertex_bytes,
                 (unsigned long long)p.fixed_bytes);
-  const uint64_t T = (budget - p.vertex_bytes - p.fixed_bytes) / p.edge_bytes;
+  // T counts packed records (the static region's unit); staging buffers hold
+  // unpacked edges of stage_bytes each and are charged in bytes below
+  const uint64_t avail = budget - p.vertex_bytes - p.fixed_bytes;
+  const uint64_t T = (uint64_t)((unsigned __int128)avail * 8 / edge_bits);
   p.edge_capacity = T;
   // GraphMeta.h:311-324: adviseK = (10 - E/T)/9, <0 -> 0.5, >1 -> 1, a positive
   // user value overrides it.  A user value above 1 is clamped to 1 here (the
@@ -227,16 +252,21 @@ int plan_compute(uint32_t V, uint64_t E, const uint64_t *off, int kind,
     const uint64_t eighth = std::max<uint64_t>(kLbsTile, T / 8 / kLbsTile * kLbsTile);
     const uint64_t need = std::min<uint64_t>(
         std::min<uint64_t>(kMinChunkEdges, eighth), (dyn + kLbsTile - 1) / kLbsTile * kLbsTile);
-    uint64_t room = (T - st) / 2 / kLbsTile * kLbsTile;
+    // bytes left after the static records, as staged edges per buffer
+    auto room_for = [&](uint64_t st_edges) -> uint64_t {
+      const uint64_t used = (st_edges * edge_bits + 7) / 8;
+      return used >= avail ? 0 : (avail - used) / stage_bytes / 2 / kLbsTile * kLbsTile;
+    };
+    uint64_t room = room_for(st);
     if (room < need) {
       // leave room for two staging buffers by shrinking the static prefix
-      if (T < 2 * need)
-        return fail(OG_E_BUDGET, "budget leaves no room for the dynamic staging buffers");
-      mps = std::min(mps, T - 2 * need);
+      const uint64_t stage = 2 * need * stage_bytes;
+      if (avail < stage) return fail(OG_E_BUDGET, "budget leaves no room for the dynamic staging buffers");
+      mps = std::min<uint64_t>(mps, (uint64_t)((unsigned __int128)(avail - stage) * 8 / edge_bits));
       Vs = prefix_for(mps);
       st = off[Vs];
       dyn = E - st;
-      room = (T - st) / 2 / kLbsTile * kLbsTile;
+      room = room_for(st);
     }
     chunk = std::min(room, (dyn + kLbsTile - 1) / kLbsTile * kLbsTile);
   }
@@ -422,6 +452,19 @@ extern "C" int og_graph_save_bel(const og_graph *g, const char *prefix) {
   return ok ? OG_OK : fail(OG_E_IO, "writing %s.bel.* failed", prefix);
 }
 
+extern "C" int og_graph_records(og_graph *g, const uint32_t **words, uint64_t *nwords, uint32_t *bpe,
+                                uint32_t *bc, uint32_t *wmin) {
+  clear_error();
+  if (!g) return fail(OG_E_ARG, "og_graph_records: null graph");
+  RC_HOST(graph_prepare(g));
+  if (words) *words = g->packed;
+  if (nwords) *nwords = g->packed_words;
+  if (bpe) *bpe = g->bpe;
+  if (bc) *bc = g->bc;
+  if (wmin) *wmin = g->wmin;
+  return OG_OK;
+}
+
 extern "C" int og_convert_uint_to_ulong(const char *in_path, const char *out_path) {
   clear_error();
   if (!in_path) return fail(OG_E_ARG, "og_convert_uint_to_ulong: null input path");
@@ -471,16 +514,18 @@ extern "C" int og_plan_compute(uint64_t V, uint64_t E, const uint64_t *offsets, 
                                og_plan *out) {
   clear_error();
   if (V == 0 || V > 0xFFFFFFFFull) return fail(OG_E_ARG, "vertex count out of range");
-  // without the graph the weight width is unknown: 4-byte weights assumed
-  return plan_compute((uint32_t)V, E, offsets, kind, budget_bytes, advisek, flags, out,
-                      kind == OG_GRAPH_WEIGHTED ? 8 : 4);
+  // the reference's accounting, sizeof(Edge) per edge (GraphMeta.h:307-309):
+  // without the graph the packed record width is unknown
+  const bool w = kind == OG_GRAPH_WEIGHTED;
+  return plan_compute((uint32_t)V, E, offsets, kind, budget_bytes, advisek, flags, out, w ? 64 : 32,
+                      w ? 8 : 4);
 }
 
 extern "C" int og_graph_plan(og_graph *g, uint64_t budget_bytes, double advisek, uint32_t flags,
                              og_plan *out) {
   clear_error();
   if (!g) return fail(OG_E_ARG, "og_graph_plan: null graph");
-  RC_HOST(graph_prepare_soa(g));
-  return plan_compute(g->V, g->E, g->off, g->kind, budget_bytes, advisek, flags, out,
-                      g->soa_edge_bytes());
+  RC_HOST(graph_prepare(g));
+  return plan_compute(g->V, g->E, g->off, g->kind, budget_bytes, advisek, flags, out, g->bpe,
+                      4 + g->wbytes);
 }

@@ -21,6 +21,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <type_traits>
+
 namespace og {
 
 constexpr int kThreads = 256;
@@ -290,6 +292,39 @@ struct SrcW {
   const W *w;
   __device__ __forceinline__ Item load(uint64_t i) const { return make_uint2(col[i], (uint32_t)w[i]); }
 };
+// Bit-packed records (the page-locked host copy and the static region):
+// record i holds bits [i*bpe, (i+1)*bpe) of `words`, column in the low bc
+// bits, weight - wmin above it.  A record spans at most two words when
+// bpe <= 33, else three; arrays carry two padding words at the end, so the
+// reads below stay inside the array for every i below the record count.
+// Consecutive lanes read consecutive records: the two loads of a warp touch
+// the same bpe*4 contiguous bytes.
+template <bool kW>
+struct SrcP {
+  using Item = typename std::conditional<kW, uint2, uint32_t>::type;
+  const uint32_t *words;
+  uint32_t bpe, bc, wmin;
+  __device__ __forceinline__ uint64_t bits(uint64_t i) const {
+    const uint64_t b = i * bpe;
+    const uint64_t q = b >> 5;
+    const uint32_t r = (uint32_t)b & 31u;
+    uint64_t x = (((uint64_t)words[q + 1] << 32) | words[q]) >> r;
+    if (r + bpe > 64) x |= (uint64_t)words[q + 2] << (64 - r);
+    return x;
+  }
+  __device__ __forceinline__ Item load(uint64_t i) const {
+    const uint64_t x = bits(i);
+    const uint32_t col = bc >= 32 ? (uint32_t)x : (uint32_t)x & ((1u << bc) - 1u);
+    if constexpr (kW) {
+      const uint32_t bw = bpe - bc;
+      const uint64_t w = bw == 0 ? 0 : (x >> bc) & ((bw >= 32) ? 0xffffffffull : ((1ull << bw) - 1));
+      return make_uint2(col, (uint32_t)w + wmin);
+    } else {
+      return col;
+    }
+  }
+};
+
 struct DstU {
   uint32_t *col;
   __device__ __forceinline__ void store(uint64_t i, uint32_t x) const { col[i] = x; }

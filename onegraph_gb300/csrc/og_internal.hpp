@@ -20,15 +20,22 @@ struct og_graph {
   uint32_t *outdeg = nullptr;  // V (OG_GRAPH_PR only)
   int registered = 0;          // number of engines holding a registration
   bool host_pinned = false;    // allocated page-locked (cudaMallocHost)
-  // Structure-of-arrays copy used by the engines (built once, on first use):
-  // u32 columns (the edge array itself for unweighted kinds) and, for
-  // weighted graphs, the weights in the narrowest of 1, 2 or 4 bytes.
-  uint32_t *cols = nullptr;
-  void *wts = nullptr;
+  // Bit-packed edge records used by the engines (built once, on first use):
+  // record e occupies bits [e*bpe, (e+1)*bpe) of the u32 word array `packed`
+  // (little-endian bit order), low bc bits the column, the next bw bits the
+  // weight minus wmin.  bc = bits of V-1, bw = bits of (wmax - wmin), 0 for
+  // unweighted kinds.  Two zero words pad the end so that a record is always
+  // read as two (three when bpe > 33) whole words.
+  uint32_t *packed = nullptr;
+  uint64_t packed_words = 0;
+  uint32_t bpe = 0, bc = 0, bw = 0, wmin = 0;
+  // width of an unpacked weight in the device staging buffers (1, 2, 4; 0 unweighted)
   uint32_t wbytes = 0;
-  bool soa = false;
+  bool prepared = false;
+  // bytes of one edge in the reference layout (the `edges` array)
   uint32_t edge_bytes() const { return kind == OG_GRAPH_WEIGHTED ? 8u : 4u; }
-  uint32_t soa_edge_bytes() const { return 4u + wbytes; }
+  // words holding records [0, n) plus the padding
+  uint64_t packed_words_for(uint64_t n) const { return (n * bpe + 31) / 32 + 2; }
 };
 
 namespace og {
@@ -53,14 +60,25 @@ unsigned hw_threads(unsigned requested);
 template <class F>
 void parallel_for_threads(unsigned nthreads, F fn);
 
-// Builds g->cols / g->wts / g->wbytes if not built yet.
-int graph_prepare_soa(og_graph *g);
+// Builds the packed records (g->packed, bpe, bc, bw, wmin, wbytes) if not built yet.
+int graph_prepare(og_graph *g);
 
-// Region planner shared by og_plan_compute and the engine; edge_bytes is the
-// device bytes per edge (4 + weight bytes).
+// Region planner shared by og_plan_compute and the engine: edge_bits is the
+// size of one packed record (static region), stage_bytes the bytes of one
+// unpacked edge in a staging buffer (4 + weight bytes).
 int plan_compute(uint32_t V, uint64_t E, const uint64_t *off, int kind,
                  uint64_t budget, double advisek, uint32_t flags, og_plan *out,
-                 uint32_t edge_bytes);
+                 uint32_t edge_bits, uint32_t stage_bytes);
+
+// Bits needed to hold values 0..x (0 for x == 0).
+inline uint32_t bits_for(uint64_t x) {
+  uint32_t b = 0;
+  while (x) {
+    b++;
+    x >>= 1;
+  }
+  return b;
+}
 
 // Per-vertex / fixed device bytes the engine allocates (planner inputs).
 uint64_t engine_vertex_bytes(int kind, uint32_t flags);

@@ -43,7 +43,7 @@ def test_sssp_cc_pr_cli(tmp_path):
     p = str(tmp_path / "w.csr")
     gw.save(p)
     out = str(tmp_path / "sssp.bin")
-    run("SSSP_OneGraph", "-type", "sssp", "-f", p, "-r", 17, "-adviseK", "0.4", "--budget", "1M",
+    run("SSSP_OneGraph", "-type", "sssp", "-f", p, "-r", 17, "-adviseK", "0.4", "--budget", "300K",
         "--dump", out)
     off, pairs = np.array(gw.offsets), np.array(gw.edges)
     np.testing.assert_array_equal(np.fromfile(out, np.uint32), oracle.sssp_dijkstra(off, pairs, 17))
@@ -51,14 +51,14 @@ def test_sssp_cc_pr_cli(tmp_path):
     p = str(tmp_path / "p.csr")
     g.save(p)
     out = str(tmp_path / "cc.bin")
-    run("CC_OneGraph", "-f", p, "--advisek", "0.5", "--budget", "1M", "--dump", out, "--direct", "1")
+    run("CC_OneGraph", "-f", p, "--advisek", "0.5", "--budget", "300K", "--dump", out, "--direct", "1")
     np.testing.assert_array_equal(np.fromfile(out, np.uint32),
                                   oracle.cc(np.array(g.offsets), np.array(g.columns))[0])
     gp = og.Graph.rmat(11, 16, pagerank=True, symmetric=False)
     p = str(tmp_path / "pr.csr")
     gp.save(p)
     out = str(tmp_path / "pr.bin")
-    run("PR_OneGraph", "-f", p, "-adviseK", "0.5", "--budget", "1M", "--dump", out)
+    run("PR_OneGraph", "-f", p, "-adviseK", "0.5", "--budget", "180K", "--dump", out)
     want, _ = oracle.pr_onegraph(np.array(gp.offsets), np.array(gp.columns), np.array(gp.outdeg))
     got = np.fromfile(out, np.float32).astype(np.float64)
     assert (np.abs(got - want) / want).max() < 5e-3

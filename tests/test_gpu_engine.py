@@ -21,8 +21,10 @@ pytestmark = pytest.mark.gpu
 
 
 def budget_for(g, edge_slots, flags=0):
+    """Budget whose edge share is edge_slots unpacked (staging-width) edges:
+    about 2.5 x edge_slots packed static records for R-MAT 10-12 weights."""
     p = g.plan(budget=1 << 40, flags=flags)
-    return p["vertex_bytes"] + p["fixed_bytes"] + int(edge_slots) * p["edge_bytes"]
+    return p["vertex_bytes"] + p["fixed_bytes"] + int(edge_slots) * p["stage_edge_bytes"]
 
 
 def configs(g, flags=0):
@@ -66,7 +68,11 @@ def test_oom_configs_really_split_the_graph():
     st = e.stats
     assert st["chunks"] > st["iterations"]  # several chunks in some round
     assert st["edges_static"] > 0 and st["edges_dynamic"] > 0
-    assert st["link_bytes"] == 4 * st["edges_dynamic"]
+    # packed records of bits(V-1) = 12 bits cross the link, rounded up to a byte per round
+    bits = p["edge_bits"]
+    assert bits == 12
+    assert st["edges_dynamic"] * bits // 8 <= st["link_bytes"] <= \
+        st["edges_dynamic"] * bits // 8 + st["iterations"]
     # BFS expands every reached vertex exactly once
     d = e.fetch(og.ALGO_BFS)
     reached = d != g.V + 1

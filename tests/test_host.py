@@ -29,7 +29,7 @@ def test_abi_exports_every_header_symbol():
         assert hasattr(lib, name), name
     bound = {n for n, _, _ in og.SIGNATURES}
     assert declared <= bound, declared - bound
-    assert lib.og_abi_version() == 1
+    assert lib.og_abi_version() == og.ABI_VERSION == 2
 
 
 def test_csr_roundtrip_all_kinds(tmp_path):
@@ -239,29 +239,85 @@ def test_no_static_plan_keeps_every_edge_dynamic():
     assert p["chunk_edges"] > 0
 
 
-def test_graph_plan_uses_split_edge_width():
-    """Weighted graphs are kept as u32 columns + narrow weights: R-MAT weights
-    in [1, 64] fit one byte, so the planner budgets 5 bytes per edge; the
-    graph-free planner assumes 4-byte weights (8 bytes per edge)."""
+def decode_records(rec, E):
+    """Independent decoder of the packed edge records: record e is bits
+    [e*bpe, (e+1)*bpe) of the little-endian bit stream of the u32 words."""
+    words, bpe, bc = rec["words"], rec["bpe"], rec["bc"]
+    bits = np.unpackbits(words.view(np.uint8), bitorder="little")
+    idx = np.arange(E, dtype=np.int64)[:, None] * bpe + np.arange(bpe, dtype=np.int64)[None, :]
+    vals = (bits[idx].astype(np.uint64) << np.arange(bpe, dtype=np.uint64)[None, :]).sum(axis=1)
+    cols = (vals & np.uint64((1 << bc) - 1)).astype(np.uint32)
+    w = (vals >> np.uint64(bc)).astype(np.uint64) + np.uint64(rec["wmin"])
+    return cols, w
+
+
+def test_packed_records_rmat():
+    """R-MAT weights in [1, 64]: bits(V-1) column bits + 6 weight bits; the
+    records decode to exactly the graph's (column, weight) pairs."""
+    g = og.Graph.rmat(10, 16, weighted=True, seed=3)
+    rec = g.records()
+    assert rec["bc"] == 10 and rec["wmin"] == 1 and rec["bpe"] == 16
+    assert rec["words"].size == (g.E * rec["bpe"] + 31) // 32 + 2
+    assert (rec["words"][-2:] == 0).all()
+    pairs = np.array(g.edges)
+    cols, w = decode_records(rec, g.E)
+    np.testing.assert_array_equal(cols, pairs[:, 0])
+    np.testing.assert_array_equal(w, pairs[:, 1].astype(np.uint64))
+    u = og.Graph.rmat(9, 8, seed=4)
+    ru = u.records()
+    assert ru["bpe"] == ru["bc"] == 9
+    np.testing.assert_array_equal(decode_records(ru, u.E)[0], np.array(u.columns))
+
+
+@pytest.mark.parametrize("V,wlo,whi", [(1, 7, 7), (2, 0, 1), (3, 5, 300), (200, 5, 5 + (1 << 26)),
+                                       (70, 0, 0xFFFFFFFF)])
+def test_packed_records_widths(V, wlo, whi):
+    """Edge widths from 1 bit up to 64 bits per record (bc + bw > 33 takes
+    three words), constant weights (no weight bits) and E not a multiple of 32."""
+    rng = np.random.default_rng(V)
+    E = 1000 + V
+    off = np.sort(rng.integers(0, E + 1, V + 1)).astype(np.uint64)
+    off[0], off[-1] = 0, E
+    pairs = np.empty((E, 2), np.uint32)
+    pairs[:, 0] = rng.integers(0, V, E)
+    pairs[:, 1] = rng.integers(wlo, whi, E, endpoint=True, dtype=np.uint64)
+    pairs[0, 1], pairs[1, 1] = wlo, whi
+    g = og.Graph.from_arrays(off, pairs, kind=og.WEIGHTED)
+    rec = g.records()
+    bc = max(1, int(V - 1).bit_length())
+    assert rec["bc"] == bc and rec["wmin"] == wlo
+    assert rec["bpe"] == bc + int(whi - wlo).bit_length()
+    cols, w = decode_records(rec, E)
+    np.testing.assert_array_equal(cols, pairs[:, 0])
+    np.testing.assert_array_equal(w, pairs[:, 1].astype(np.uint64))
+
+
+def test_graph_plan_uses_packed_width():
+    """The planner budgets bpe bits per static edge: a fixed budget holds more
+    static edges than the graph-free planner's 32-bit-weight assumption."""
     g = og.Graph.rmat(10, 16, weighted=True, seed=3)
     pg = g.plan(budget=1 << 40)
     pc = og.plan(g.V, g.E, g.offsets, og.WEIGHTED, budget=1 << 40)
-    assert pg["edge_bytes"] == 5 and pc["edge_bytes"] == 8
-    # same budget: the split layout holds more static edges
-    b = pg["vertex_bytes"] + pg["fixed_bytes"] + int(0.5 * g.E) * 8
-    assert g.plan(budget=b, advisek=1.0)["static_edges"] > og.plan(
-        g.V, g.E, g.offsets, og.WEIGHTED, budget=b, advisek=1.0)["static_edges"]
+    assert pg["edge_bits"] == 16 and pg["stage_edge_bytes"] == 5
+    assert pc["edge_bits"] == 64 and pc["stage_edge_bytes"] == 8  # the reference's sizeof(Edge)
+    b = pg["vertex_bytes"] + pg["fixed_bytes"] + g.E * 4
+    assert g.plan(budget=b, advisek=1.0, flags=og.CFG_DIRECT)["static_edges"] == g.E
+    assert og.plan(g.V, g.E, g.offsets, og.WEIGHTED, budget=b, advisek=1.0,
+                   flags=og.CFG_DIRECT)["static_edges"] <= g.E // 2
     u = og.Graph.rmat(10, 16, seed=3)
-    assert u.plan(budget=1 << 40)["edge_bytes"] == 4
+    assert u.plan(budget=1 << 40)["edge_bits"] == 10
 
 
-def test_graph_plan_wide_weights():
-    """A weight above 65535 needs 4-byte weights; above 255 two bytes."""
-    off = np.array([0, 2, 3, 3], np.uint64)
-    for wmax, eb in [(200, 5), (300, 6), (70000, 8)]:
-        pairs = np.array([[1, 1], [2, wmax], [2, 3]], np.uint32)
-        g = og.Graph.from_arrays(off, pairs, kind=og.WEIGHTED)
-        assert g.plan(budget=1 << 30)["edge_bytes"] == eb
+def test_graph_plan_staged_budget():
+    """Staged mode: static records + two staging buffers of unpacked edges fit
+    the budget's edge share."""
+    g = og.Graph.rmat(11, 16, weighted=True, seed=5)
+    pg = g.plan(budget=1 << 40)
+    avail = int(0.5 * g.E * pg["edge_bits"] / 8)
+    p = g.plan(budget=pg["vertex_bytes"] + pg["fixed_bytes"] + avail, advisek=0.8)
+    assert p["dynamic_edges"] > 0 and p["chunk_edges"] > 0
+    used = (p["static_edges"] * p["edge_bits"] + 7) // 8 + 2 * p["chunk_edges"] * p["stage_edge_bytes"]
+    assert used <= avail
 
 
 def test_convert_uint_to_ulong(tmp_path):
