@@ -61,8 +61,9 @@ def parse_args():
     ap.add_argument("--requests", type=int, default=400)
     ap.add_argument("--rate", type=float, default=2000.0)
     ap.add_argument("--workers", type=int, default=4)
-    ap.add_argument("--delta", type=float, default=0.0,
-                    help="SSSP near/far split width (0: plain frontier relaxation)")
+    ap.add_argument("--delta", type=float, default=None,
+                    help="SSSP near/far split width (default: the engine's, (wmin + wmax) / 16; "
+                         "0: plain frontier relaxation as in the reference)")
     ap.add_argument("--direct", type=int, default=1,
                     help="1: relax the dynamic region straight from page-locked host memory "
                          "(fastest); 0: gather into double-buffered device staging first")
@@ -275,7 +276,9 @@ def run_ours(args, rank, world, local):
     eng = og.Engine(g, budget=int(args.budget_gib * GIB), advisek=args.advisek,
                     direct=bool(args.direct), device=local)
     engine_s = time.time() - t0
-    eng.set_param(og.PARAM_SSSP_DELTA, args.delta)
+    if args.delta is not None:
+        eng.set_param(og.PARAM_SSSP_DELTA, args.delta)
+    args.delta = eng.get_param(og.PARAM_SSSP_DELTA)
     plan = eng.plan
 
     def barrier():

@@ -288,14 +288,17 @@ int og_bfs_batch_set_config(og_engine *e, int config);
 int og_engine_clone(og_engine *parent, og_engine **out);
 
 /* Engine parameters.
- * OG_PARAM_SSSP_DELTA: width of og_sssp's near/far split.  0 (default)
- *   relaxes every frontier vertex each round, as the reference does
+ * OG_PARAM_SSSP_DELTA: width of og_sssp's near/far split.  0 relaxes every
+ *   frontier vertex each round, as the reference does
  *   (SSSP/oneGraph/CalculateOpt.h:73-185); d > 0 expands only frontier
  *   vertices whose distance is below a threshold that moves in steps of d,
  *   which re-expands fewer vertices (fewer edges over the host link) at the
- *   cost of more rounds.  Distances are exact either way.  Clones inherit it. */
+ *   cost of more rounds.  Default: (smallest + largest weight) / 16, at least
+ *   1 (4 for weights in [1, 64]).  Distances are exact for every value.
+ *   Clones inherit it. */
 #define OG_PARAM_SSSP_DELTA 1
 int og_engine_set_param(og_engine *e, int param, double value);
+int og_engine_get_param(const og_engine *e, int param, double *value);
 
 /* Device bytes of the shared resident graph (0 for a clone) and of one
  * query context. */
@@ -348,7 +351,7 @@ int og_k_compact(const uint32_t *bits, uint32_t v_begin, uint32_t v_end,
  * still passes every input and output buffer.
  * Scratch: a fixed ~0.9 MB array inside libog.so, present on every device
  * that loads the library until the process exits.  Limit: one call covers at
- * most 2^28 vertices (32768 tiles of 8192); larger ranges return OG_E_ARG.
+ * most 2^28 vertices (8192 tiles of 32768); larger ranges return OG_E_ARG.
  * The first call on a device looks up that array's device address, so make it
  * before any stream capture.  Every call shares the array: calls that overlap
  * on the GPU (other streams, other host threads) race and must not be issued;

@@ -150,6 +150,7 @@ SIGNATURES = [
     ("og_engine_clone", C.c_int, [_P, C.POINTER(_P)]),
     ("og_engine_bytes", C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     ("og_engine_set_param", C.c_int, [_P, C.c_int, C.c_double]),
+    ("og_engine_get_param", C.c_int, [_P, C.c_int, C.POINTER(C.c_double)]),
     ("og_k_compact", C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P, C.c_uint64, _P,
                                C.c_uint64, _P, _P]),
     ("og_k_compact_noalloc", C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P, C.c_uint64, _P,
@@ -438,6 +439,11 @@ class Engine:
 
     def set_param(self, param: int, value: float):
         _check(lib().og_engine_set_param(self._h, param, value), "og_engine_set_param")
+
+    def get_param(self, param: int) -> float:
+        v = C.c_double()
+        _check(lib().og_engine_get_param(self._h, param, C.byref(v)), "og_engine_get_param")
+        return v.value
 
     def bytes(self) -> tuple:
         """(device bytes of the resident graph, of one query context)."""

@@ -291,6 +291,17 @@ __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
           }
         }
       }
+      // probe every target's visited mask before the first atomic (the reads
+      // overlap; a stale probe only costs an extra atomic)
+      unsigned long long pv[ITEMS];
+#pragma unroll
+      for (int it = 0; it < ITEMS; it++) {
+        pv[it] = ~0ull;
+        if ((okm >> it) & 1u) {
+          const uint32_t v = edge_dst(ev[it]);
+          if (v < a.V) pv[it] = __ldcg(a.visited + v);
+        }
+      }
 #pragma unroll
       for (int it = 0; it < ITEMS; it++) {
         if (!(okm & (1u << it))) continue;
@@ -299,7 +310,7 @@ __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
           atomicOr(a.err, kErrVertex);
           continue;
         }
-        unsigned long long nb = sh.val[lv[it]] & ~__ldcg(a.visited + v);
+        unsigned long long nb = sh.val[lv[it]] & ~pv[it];
         if (!nb) continue;
         nb &= ~atomicOr(a.visited + v, nb);
         if (!nb) continue;

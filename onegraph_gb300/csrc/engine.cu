@@ -257,6 +257,9 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
   CK(cudaSetDevice(e->dev));
   CK(cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, e->dev));
   RC(graph_prepare(g));
+  // default near/far width: a sixteenth of the weight range's midpoint sum
+  // (4 for weights in [1, 64]), at least 1
+  e->sssp_delta = g->kind == OG_GRAPH_WEIGHTED ? std::max<uint32_t>(1, (uint32_t)(((uint64_t)g->wmin + g->wmax) / 16)) : 0;
   e->wbytes = g->wbytes;
   e->bpe = g->bpe;
   e->bc = g->bc;
@@ -365,8 +368,18 @@ int clone(og_engine *parent, og_engine *e) {
 
 // ------------------------------------------------------------------ rounds
 
+// Near/far split (SplitArgs::on): list only vertices with value < thr; the
+// waiting ones go to far_bits (when not null) and their minimum to the
+// region's Counts::far_min; listed ones are cleared from clear_bits.
+struct SplitArgs {
+  bool on = false;
+  uint32_t thr = 0;
+  uint32_t *far_bits = nullptr;
+  uint32_t *clear_bits = nullptr;
+};
+
 int launch_compact(og_engine *e, int r, const uint32_t *bits, uint32_t vb, uint32_t ve,
-                   cudaStream_t s, uint32_t *far_bits = nullptr, uint32_t thr = 0) {
+                   cudaStream_t s, const SplitArgs &sp = SplitArgs()) {
   CK(cudaMemsetAsync(e->counts_d + r, 0, sizeof(Counts), s));
   CK(cudaMemsetAsync(&e->counts_d[r].far_min, 0xff, sizeof(uint32_t), s));  // far minimum
   if (ve <= vb) return OG_OK;
@@ -387,9 +400,11 @@ int launch_compact(og_engine *e, int r, const uint32_t *bits, uint32_t vb, uint3
   a.list_cap = e->list_cap[r];
   a.tile_cap = e->tile_cap[r];
   a.value = e->value_d;
-  a.thr = thr;
-  a.far_bits = far_bits;
+  a.thr = sp.thr;
+  a.split = sp.on ? 1u : 0u;
+  a.far_bits = sp.far_bits;
   a.far_min = &e->counts_d[r].far_min;
+  a.clear_bits = sp.clear_bits;
   if (a.ntiles + 1 > e->lb_tiles) return fail(OG_E_STATE, "compaction scratch too small");
   CK(cudaMemsetAsync(e->lb[r].status, 0, sizeof(uint32_t) * (e->lb_tiles + 1), s));
   k_compact<<<a.ntiles, kThreads, 0, s>>>(a);
@@ -564,12 +579,12 @@ int run_regions(og_engine *e, og_stats &st, Timing &tm, StaticFn static_fn, DynF
 // Compacts both regions of `cur` and brings the counts (and the error word) to
 // the host.  Returns the number of listed vertices through *n.
 int compact_round(og_engine *e, const uint32_t *cur, og_stats &st, Timing &tm, uint64_t *n,
-                  uint32_t *far_bits = nullptr, uint32_t thr = 0) {
+                  const SplitArgs &sp = SplitArgs()) {
   CK(cudaEventRecord(e->ev_round, e->s_main));
-  RC(launch_compact(e, 0, cur, 0, e->Vs, e->s_main, far_bits, thr));
+  RC(launch_compact(e, 0, cur, 0, e->Vs, e->s_main, sp));
   CK(cudaEventRecord(e->ev_cs, e->s_main));
   CK(cudaStreamWaitEvent(e->s_dyn, e->ev_round, 0));
-  RC(launch_compact(e, 1, cur, e->Vs, e->V, e->s_dyn, far_bits, thr));
+  RC(launch_compact(e, 1, cur, e->Vs, e->V, e->s_dyn, sp));
   CK(cudaEventRecord(e->ev_cd, e->s_dyn));
   CK(cudaStreamWaitEvent(e->s_dyn, e->ev_cs, 0));
   CK(cudaMemcpyAsync(e->counts_h, e->counts_d, 2 * sizeof(Counts), cudaMemcpyDeviceToHost, e->s_dyn));
@@ -598,6 +613,7 @@ int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
     k_set_source<<<1, 1, 0, s>>>(e->value_d, src, 1u, cur, e->bm[2]);
     e->launches += 2;
   } else if (algo == OG_ALGO_SSSP) {
+    if (e->sssp_delta > 0) CK(cudaMemsetAsync(e->bm[2], 0, 4 * e->nwords, s));  // waiting set
     k_fill_u32<<<g, kThreads, 0, s>>>(e->value_d, V, 0xFFFFFFFFu);  // SSSP GraphMeta.h:377
     k_set_source<<<1, 1, 0, s>>>(e->value_d, src, 1u, cur, nullptr);
     e->launches += 2;
@@ -609,24 +625,39 @@ int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
   CK(cudaGetLastError());
   Timing tm;
   RoundOps ro{algo, 1};
-  // SSSP near/far split: a round expands only frontier vertices closer than
-  // thr; the others stay in the frontier until no near vertex is left, then
-  // thr moves to the smallest waiting distance + delta
+  // SSSP near/far split (two-bucket delta stepping): a round expands only
+  // frontier vertices closer than thr; the others move to the waiting set
+  // (bm[2]) and are not looked at again until no near vertex is left.  Then
+  // thr moves to the smallest waiting distance + delta and one scan of the
+  // waiting set lists the vertices below it.  far_min is the minimum over
+  // the waiting set as of the last scan, lowered by every insertion since; a
+  // vertex listed from the frontier leaves the waiting set, so the minimum
+  // may be stale-low, in which case the scan lists nothing and returns the
+  // true minimum for the next try.
   const bool split = algo == OG_ALGO_SSSP && e->sssp_delta > 0;
+  uint32_t *waiting = e->bm[2];
   uint64_t thr = 1ull + e->sssp_delta;
+  uint32_t far_min = 0xffffffffu;
+  bool advance = false;
   for (;;) {
     uint64_t n = 0;
-    RC(compact_round(e, cur, st, tm, &n, split ? next : nullptr,
-                     (uint32_t)std::min<uint64_t>(thr, 0xffffffffull)));
-    if (n == 0) {
+    SplitArgs sp;
+    sp.on = split;
+    sp.thr = (uint32_t)std::min<uint64_t>(thr, 0xffffffffull);
+    sp.clear_bits = split ? waiting : nullptr;
+    sp.far_bits = split && !advance ? waiting : nullptr;
+    RC(compact_round(e, advance ? waiting : cur, st, tm, &n, sp));
+    if (split) {
       const uint32_t fm = std::min(e->counts_h[0].far_min, e->counts_h[1].far_min);
-      if (!split || fm == 0xffffffffu) break;
-      thr = (uint64_t)fm + e->sssp_delta;  // the waiting vertices are now in next
-      CK(cudaStreamWaitEvent(e->s_main, e->ev_cd, 0));
-      CK(cudaMemsetAsync(cur, 0, 4 * e->nwords, e->s_main));
-      std::swap(cur, next);
+      far_min = advance ? fm : std::min(far_min, fm);
+    }
+    if (n == 0) {
+      if (!split || far_min == 0xffffffffu) break;
+      thr = (uint64_t)far_min + e->sssp_delta;
+      advance = true;
       continue;
     }
+    advance = false;
     st.iterations++;
     st.frontier_sum += n;
     st.static_vertices += e->counts_h[0].n;
@@ -1124,6 +1155,15 @@ extern "C" int og_engine_set_param(og_engine *e, int param, double value) {
   return fail(OG_E_ARG, "unknown parameter %d", param);
 }
 
+extern "C" int og_engine_get_param(const og_engine *e, int param, double *value) {
+  if (!e || !value) return fail(OG_E_ARG, "og_engine_get_param: null argument");
+  if (param == OG_PARAM_SSSP_DELTA) {
+    *value = e->sssp_delta;
+    return OG_OK;
+  }
+  return fail(OG_E_ARG, "unknown parameter %d", param);
+}
+
 extern "C" int og_engine_bytes(const og_engine *e, uint64_t *resident, uint64_t *context) {
   if (!e) return fail(OG_E_ARG, "og_engine_bytes: null engine");
   if (resident) *resident = e->parent ? 0 : e->resident_bytes;
@@ -1319,8 +1359,10 @@ void compact_launch(const uint32_t *bits, uint32_t v_begin, uint32_t v_end, cons
   a.tile_cap = tile_cap;
   a.value = nullptr;
   a.thr = 0;
+  a.split = 0;
   a.far_bits = nullptr;
   a.far_min = nullptr;
+  a.clear_bits = nullptr;
   k_compact<<<a.ntiles, kThreads, 0, s>>>(a);
 }
 
@@ -1401,13 +1443,13 @@ extern "C" int og_k_compact(const uint32_t *bits, uint32_t v_begin, uint32_t v_e
 //
 // og_k_compact_noalloc runs the same compaction with its look-back scratch in
 // a fixed array that is part of the loaded library instead of memory it asks
-// the driver for.  Limit: kNoAllocTiles compaction tiles of 8192 vertices,
+// the driver for.  Limit: kNoAllocTiles compaction tiles of 32768 vertices,
 // i.e. a range of at most 2^28 vertices per call.  The array lives on every
 // device that loads the library, for as long as the process runs.
 
 namespace {
 
-constexpr uint32_t kNoAllocTiles = 32768;
+constexpr uint32_t kNoAllocTiles = 8192;
 constexpr uint64_t kNoAllocErrOffset = 4 * (kNoAllocTiles + 1ull) + 24ull * kNoAllocTiles + 64;
 constexpr uint64_t kNoAllocBytes = kNoAllocErrOffset + 256;
 

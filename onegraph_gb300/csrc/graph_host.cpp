@@ -107,6 +107,7 @@ int graph_prepare(og_graph *g) {
   g->bw = bw;
   g->bpe = bc + bw;
   g->wmin = wmin;
+  g->wmax = wmax;
   g->wbytes = weighted ? (wmax < 256 ? 1 : (wmax < 65536 ? 2 : 4)) : 0;
   const uint64_t words = g->packed_words_for(E);
   uint32_t *pk = (uint32_t *)host_alloc(4 * (size_t)words);

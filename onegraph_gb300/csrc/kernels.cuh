@@ -28,7 +28,8 @@ namespace og {
 constexpr int kThreads = 256;
 constexpr uint32_t kTile = 2048;             // LBS edge positions per CTA
 constexpr uint32_t kItems = kTile / kThreads;  // 8
-constexpr uint32_t kWordsPerCompactTile = 256;
+constexpr uint32_t kCompactWordsPerThread = 4;
+constexpr uint32_t kWordsPerCompactTile = kThreads * kCompactWordsPerThread;  // 32768 vertices
 
 // device error bits (OR-ed into the engine's error word)
 constexpr uint32_t kErrLookback = 1u;    // look-back wait gave up
@@ -66,13 +67,18 @@ struct CompactArgs {
   uint32_t *err;
   uint64_t list_cap;     // entries of list (pref has list_cap + 1)
   uint64_t tile_cap;     // entries of tile_first
-  // near/far split (SSSP): when far_bits != nullptr only vertices with
-  // value < thr are listed; the others with edges are OR-ed into far_bits and
-  // the smallest of their values goes to *far_min
+  // near/far split (SSSP): when split != 0 only vertices with value < thr
+  // are listed; the others stay waiting: they are OR-ed into far_bits (when
+  // not null) and the smallest of their values goes to *far_min.  Vertices
+  // that leave the waiting state (value < thr) have their bit cleared in
+  // clear_bits (when not null).  The value is read before the offsets, so a
+  // waiting vertex costs 4 bytes.
   const uint32_t *value;
   uint32_t thr;
+  uint32_t split;
   uint32_t *far_bits;
   uint32_t *far_min;
+  uint32_t *clear_bits;
 };
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
@@ -133,9 +139,10 @@ __device__ __forceinline__ void block_scan_pair(uint32_t cnt, uint64_t sum, uint
   __syncthreads();  // shared arrays are reused by the next call
 }
 
-// Frontier compaction for the vertex range [v_begin, v_end).  One thread per
-// bitmap word (32 vertices), 256 words per CTA tile, tiles ordered by a ticket
-// so that every predecessor a tile waits for is already running.
+// Frontier compaction for the vertex range [v_begin, v_end).  Four
+// consecutive bitmap words (128 vertices) per thread, 1024 words per CTA
+// tile, tiles ordered by a ticket so that every predecessor a tile waits for
+// is already running.
 __global__ void __launch_bounds__(kThreads) k_compact(CompactArgs a) {
   __shared__ uint32_t s_tile;
   __shared__ uint32_t s_excl_n;
@@ -144,119 +151,161 @@ __global__ void __launch_bounds__(kThreads) k_compact(CompactArgs a) {
   if (threadIdx.x == 0) s_tile = atomicAdd(a.lb.ticket, 1u);
   __syncthreads();
   const uint32_t tile = s_tile;
-  const uint32_t w = a.w_begin + tile * kWordsPerCompactTile + threadIdx.x;
-  const uint64_t vbase = (uint64_t)w * 32;
-  uint32_t word = 0;
-  if (w < a.w_end) {
-    word = a.bits[w];
-    if (vbase < a.v_begin) {
-      const uint32_t sh = a.v_begin - (uint32_t)vbase;
-      word = sh >= 32 ? 0 : word & (0xffffffffu << sh);
-    }
-    if (vbase + 32 > a.v_end) {
-      const uint64_t keep = a.v_end > vbase ? a.v_end - vbase : 0;
-      word = keep >= 32 ? word : word & ((1u << keep) - 1u);
-    }
-  }
+  const uint32_t w0 = a.w_begin + tile * kWordsPerCompactTile + threadIdx.x * kCompactWordsPerThread;
   // drop vertices without edges: nothing to expand
-  uint32_t keep = 0, cnt = 0, far = 0, fmin = 0xffffffffu;
+  uint32_t keep[kCompactWordsPerThread];
+  uint32_t cnt = 0;
   uint64_t sum = 0;
-  for (uint32_t m = word; m; m &= m - 1) {
-    const uint32_t b = __ffs(m) - 1;
-    const uint64_t v = vbase + b;
-    const uint64_t d = a.off[v + 1] - a.off[v];
-    if (!d) continue;
-    if (a.far_bits) {
-      const uint32_t x = __ldcg(a.value + v);
-      if (x >= a.thr) {
-        far |= 1u << b;
-        fmin = min(fmin, x);
-        continue;
+#pragma unroll
+  for (uint32_t j = 0; j < kCompactWordsPerThread; j++) {
+    const uint32_t w = w0 + j;
+    const uint64_t vbase = (uint64_t)w * 32;
+    uint32_t word = 0;
+    if (w < a.w_end) {
+      word = a.bits[w];
+      if (vbase < a.v_begin) {
+        const uint32_t sh = a.v_begin - (uint32_t)vbase;
+        word = sh >= 32 ? 0 : word & (0xffffffffu << sh);
+      }
+      if (vbase + 32 > a.v_end) {
+        const uint64_t k = a.v_end > vbase ? a.v_end - vbase : 0;
+        word = k >= 32 ? word : word & ((1u << k) - 1u);
       }
     }
-    keep |= 1u << b;
-    cnt++;
-    sum += d;
-  }
-  if (far) {
-    atomicOr(a.far_bits + w, far);
-    atomicMin(a.far_min, fmin);
+    uint32_t kp = 0, far = 0, fmin = 0xffffffffu, leave = 0;
+    for (uint32_t m = word; m; m &= m - 1) {
+      const uint32_t b = __ffs(m) - 1;
+      const uint64_t v = vbase + b;
+      if (a.split) {
+        const uint32_t x = __ldcg(a.value + v);
+        if (x >= a.thr) {
+          far |= 1u << b;
+          fmin = min(fmin, x);
+          continue;
+        }
+        leave |= 1u << b;
+      }
+      const uint64_t d = a.off[v + 1] - a.off[v];
+      if (!d) continue;
+      kp |= 1u << b;
+      cnt++;
+      sum += d;
+    }
+    keep[j] = kp;
+    if (far) {
+      if (a.far_bits) atomicOr(a.far_bits + w, far);
+      atomicMin(a.far_min, fmin);
+    }
+    if (leave && a.clear_bits) atomicAnd(a.clear_bits + w, ~leave);
   }
   uint32_t ex_n, tot_n;
   uint64_t ex_e, tot_e;
   block_scan_pair(cnt, sum, ex_n, ex_e, tot_n, tot_e);
-  if (threadIdx.x == 0) {
+  // Warp-wide decoupled look-back (warp 0): each pass reads the status of the
+  // 32 nearest unaccounted predecessors at once, sums their aggregates up to
+  // the nearest one holding an inclusive prefix, and stops there; tiles
+  // before the first count as an inclusive prefix of 0.  Waits are bounded:
+  // a status that never appears sets kErrLookback and the tile writes nothing.
+  if (threadIdx.x < 32) {
+    const int lane = threadIdx.x;
     uint32_t pn = 0;
     uint64_t pe = 0;
     int bad = 0;
     if (tile == 0) {
-      a.lb.inc_n[0] = tot_n;
-      a.lb.inc_e[0] = tot_e;
-      __threadfence();
-      st_release(&a.lb.status[0], 2u);
+      if (lane == 0) {
+        a.lb.inc_n[0] = tot_n;
+        a.lb.inc_e[0] = tot_e;
+        __threadfence();
+        st_release(&a.lb.status[0], 2u);
+      }
     } else {
-      a.lb.agg_n[tile] = tot_n;
-      a.lb.agg_e[tile] = tot_e;
-      __threadfence();
-      st_release(&a.lb.status[tile], 1u);
-      for (int p = (int)tile - 1; p >= 0;) {
-        uint32_t st;
-        uint32_t spins = 0;
-        while ((st = ld_acquire(&a.lb.status[p])) == 0u) {
-          if (++spins > kSpinLimit) break;
-          __nanosleep(64);
+      if (lane == 0) {
+        a.lb.agg_n[tile] = tot_n;
+        a.lb.agg_e[tile] = tot_e;
+        __threadfence();
+        st_release(&a.lb.status[tile], 1u);
+      }
+      for (int p = (int)tile - 1;; p -= 32) {
+        const int q = p - lane;  // lane 0: nearest predecessor of the window
+        uint32_t st = 2u;
+        if (q >= 0) {
+          uint32_t spins = 0;
+          while ((st = ld_acquire(&a.lb.status[q])) == 0u) {
+            if (++spins > kSpinLimit) break;
+            __nanosleep(64);
+          }
         }
-        if (st == 0u) {  // bounded wait expired: report, never hang
-          atomicOr(a.err, kErrLookback);
+        __syncwarp();
+        if (__any_sync(0xffffffffu, st == 0u)) {  // bounded wait expired: report, never hang
+          if (lane == 0) atomicOr(a.err, kErrLookback);
           bad = 1;
           break;
         }
-        if (st == 2u) {
-          pn += __ldcg(&a.lb.inc_n[p]);
-          pe += __ldcg(&a.lb.inc_e[p]);
-          break;
+        const unsigned incl = __ballot_sync(0xffffffffu, st == 2u);
+        const int k = incl ? __ffs(incl) - 1 : 32;
+        uint32_t vn = 0;
+        uint64_t ve = 0;
+        if (q >= 0 && lane < k) {
+          vn = __ldcg(&a.lb.agg_n[q]);
+          ve = __ldcg(&a.lb.agg_e[q]);
+        } else if (q >= 0 && lane == k) {
+          vn = __ldcg(&a.lb.inc_n[q]);
+          ve = __ldcg(&a.lb.inc_e[q]);
         }
-        pn += __ldcg(&a.lb.agg_n[p]);
-        pe += __ldcg(&a.lb.agg_e[p]);
-        p--;
+#pragma unroll
+        for (int o = 16; o; o >>= 1) {
+          vn += __shfl_xor_sync(0xffffffffu, vn, o);
+          ve += __shfl_xor_sync(0xffffffffu, ve, o);
+        }
+        pn += vn;
+        pe += ve;
+        if (k < 32) break;
       }
-      a.lb.inc_n[tile] = pn + tot_n;
-      a.lb.inc_e[tile] = pe + tot_e;
-      __threadfence();
-      st_release(&a.lb.status[tile], 2u);
+      if (lane == 0) {
+        a.lb.inc_n[tile] = pn + tot_n;
+        a.lb.inc_e[tile] = pe + tot_e;
+        __threadfence();
+        st_release(&a.lb.status[tile], 2u);  // published even when bad: successors never wait forever
+      }
     }
-    if (!bad && (uint64_t)pn + tot_n > a.list_cap) {
-      atomicOr(a.err, kErrTileMap);
-      bad = 1;
-    }
-    s_excl_n = pn;
-    s_excl_e = pe;
-    s_bad = bad;
-    if (!bad && tile == a.ntiles - 1) {
-      a.counts->n = pn + tot_n;
-      a.counts->total = pe + tot_e;
-      a.pref[pn + tot_n] = pe + tot_e;
+    if (lane == 0) {
+      if (!bad && (uint64_t)pn + tot_n > a.list_cap) {
+        atomicOr(a.err, kErrTileMap);
+        bad = 1;
+      }
+      s_excl_n = pn;
+      s_excl_e = pe;
+      s_bad = bad;
+      if (!bad && tile == a.ntiles - 1) {
+        a.counts->n = pn + tot_n;
+        a.counts->total = pe + tot_e;
+        a.pref[pn + tot_n] = pe + tot_e;
+      }
     }
   }
   __syncthreads();
   if (s_bad) return;  // positions unknown: write nothing
   uint32_t pos = s_excl_n + ex_n;
   uint64_t ep = s_excl_e + ex_e;
-  for (uint32_t m = keep; m; m &= m - 1) {
-    const uint32_t b = __ffs(m) - 1;
-    const uint64_t v = vbase + b;
-    const uint64_t d = a.off[v + 1] - a.off[v];
-    a.list[pos] = (uint32_t)v;
-    a.pref[pos] = ep;
-    for (uint64_t t = (ep + kTile - 1) / kTile; t * kTile < ep + d; t++) {
-      if (t >= a.tile_cap) {
-        atomicOr(a.err, kErrTileMap);
-        break;
+#pragma unroll
+  for (uint32_t j = 0; j < kCompactWordsPerThread; j++) {
+    const uint64_t vbase = (uint64_t)(w0 + j) * 32;
+    for (uint32_t m = keep[j]; m; m &= m - 1) {
+      const uint32_t b = __ffs(m) - 1;
+      const uint64_t v = vbase + b;
+      const uint64_t d = a.off[v + 1] - a.off[v];
+      a.list[pos] = (uint32_t)v;
+      a.pref[pos] = ep;
+      for (uint64_t t = (ep + kTile - 1) / kTile; t * kTile < ep + d; t++) {
+        if (t >= a.tile_cap) {
+          atomicOr(a.err, kErrTileMap);
+          break;
+        }
+        a.tile_first[t] = pos;
       }
-      a.tile_first[t] = pos;
+      pos++;
+      ep += d;
     }
-    pos++;
-    ep += d;
   }
 }
 
@@ -276,10 +325,11 @@ struct LbsArgs {
   uint32_t *err;
 };
 
-// Edge storage is structure-of-arrays: u32 columns plus, for weighted graphs,
-// weights in the narrowest width that holds them (W = uint8_t / uint16_t /
-// uint32_t).  A source yields one edge as a u32 column or a {column, weight}
-// pair; BFS, CC and PageRank read columns only.
+// Edge sources.  Staging buffers hold unpacked edges: u32 columns plus, for
+// weighted graphs, weights in the narrowest width that holds them (W =
+// uint8_t / uint16_t / uint32_t).  The static region and the page-locked host
+// copy hold bit-packed records (SrcP).  A source yields one edge as a u32
+// column or a {column, weight} pair; BFS, CC and PageRank read columns only.
 struct SrcU {
   using Item = uint32_t;
   const uint32_t *col;
@@ -432,11 +482,20 @@ __global__ void __launch_bounds__(kThreads) k_lbs(LbsArgs a, Src src, Op op) {
       }
     }
   }
+  // Probe phase: every target's current state is read before the first
+  // atomic, so the eight random reads of a thread overlap (in program order
+  // the compiler may not lift a load above an earlier atomic).  A probe is
+  // only a filter: relax() acts through atomics, so a stale probe costs an
+  // extra atomic, never a wrong result.
+  typename Op::Probe pr[kItems];
+#pragma unroll
+  for (int it = 0; it < (int)kItems; it++)
+    if (okmask & (1u << it)) pr[it] = op.probe(ev[it]);
 #pragma unroll
   for (int it = 0; it < (int)kItems; it++) {
     if (okmask & (1u << it))
       op.relax(ev[it], Op::kNeedVal ? sh.val[lv[it]] : typename Op::Val(0),
-               pos0 + it * kThreads + threadIdx.x);
+               pos0 + it * kThreads + threadIdx.x, pr[it]);
   }
 }
 
@@ -533,15 +592,21 @@ struct BfsOp {
   uint32_t *visited, *next, *depth, *err;
   uint32_t V, newdepth;
   __device__ uint32_t src_val(uint32_t) const { return 0; }
+  using Probe = uint32_t;  // the target's visited word
   template <class Edge>
-  __device__ __forceinline__ void relax(Edge e, uint32_t, uint64_t) const {
+  __device__ __forceinline__ Probe probe(Edge e) const {
+    const uint32_t v = edge_dst(e);
+    return v < V ? __ldcg(visited + (v >> 5)) : 0u;
+  }
+  template <class Edge>
+  __device__ __forceinline__ void relax(Edge e, uint32_t, uint64_t, Probe p) const {
     const uint32_t v = edge_dst(e);
     if (v >= V) {
       atomicOr(err, kErrVertex);
       return;
     }
     const uint32_t w = v >> 5, bit = 1u << (v & 31);
-    if (__ldcg(visited + w) & bit) return;
+    if (p & bit) return;
     const uint32_t old = atomicOr(visited + w, bit);
     if (old & bit) return;
     depth[v] = newdepth;
@@ -557,15 +622,21 @@ struct MinOp {
   uint32_t *value, *next, *err;
   uint32_t V;
   __device__ uint32_t src_val(uint32_t v) const { return __ldcg(value + v); }
+  using Probe = uint32_t;  // the target's current value
   template <class Edge>
-  __device__ __forceinline__ void relax(Edge e, uint32_t sv, uint64_t) const {
+  __device__ __forceinline__ Probe probe(Edge e) const {
+    const uint32_t v = edge_dst(e);
+    return v < V ? __ldcg(value + v) : 0u;
+  }
+  template <class Edge>
+  __device__ __forceinline__ void relax(Edge e, uint32_t sv, uint64_t, Probe p) const {
     const uint32_t v = edge_dst(e);
     if (v >= V) {
       atomicOr(err, kErrVertex);
       return;
     }
     const uint32_t cand = kWeighted ? sv + edge_w(e) : sv;
-    if (cand >= __ldcg(value + v)) return;
+    if (cand >= p) return;
     const uint32_t old = atomicMin(value + v, cand);
     if (cand < old) atomicOr(next + (v >> 5), 1u << (v & 31));
   }
@@ -586,14 +657,20 @@ struct BatchOp {
   uint32_t *err;
   uint32_t V;
   __device__ Val src_val(uint32_t v) const { return __ldcg(cur + v); }
+  using Probe = unsigned long long;  // the target's visited mask
   template <class Edge>
-  __device__ __forceinline__ void relax(Edge e, Val m, uint64_t) const {
+  __device__ __forceinline__ Probe probe(Edge e) const {
+    const uint32_t v = edge_dst(e);
+    return v < V ? __ldcg(visited + v) : ~0ull;
+  }
+  template <class Edge>
+  __device__ __forceinline__ void relax(Edge e, Val m, uint64_t, Probe p) const {
     const uint32_t v = edge_dst(e);
     if (v >= V) {
       atomicOr(err, kErrVertex);
       return;
     }
-    Val nb = m & ~__ldcg(visited + v);
+    Val nb = m & ~p;
     if (!nb) return;
     nb &= ~atomicOr(visited + v, nb);
     if (!nb) return;

@@ -28,7 +28,7 @@ struct og_graph {
   // read as two (three when bpe > 33) whole words.
   uint32_t *packed = nullptr;
   uint64_t packed_words = 0;
-  uint32_t bpe = 0, bc = 0, bw = 0, wmin = 0;
+  uint32_t bpe = 0, bc = 0, bw = 0, wmin = 0, wmax = 0;
   // width of an unpacked weight in the device staging buffers (1, 2, 4; 0 unweighted)
   uint32_t wbytes = 0;
   bool prepared = false;

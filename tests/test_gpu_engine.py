@@ -89,7 +89,7 @@ def test_sssp_matches_dijkstra(scale, seed):
     want = {s: oracle.sssp_dijkstra(off, pairs, s) for s in srcs}
     for cname, kw in configs(g):
         e = engine(g, **kw)
-        for delta in (0, 8, 64, 300):  # plain frontier relaxation and near/far splits
+        for delta in (0, 1, 8, 64, 300):  # plain frontier relaxation and near/far splits
             e.set_param(og.PARAM_SSSP_DELTA, delta)
             for s in srcs:
                 np.testing.assert_array_equal(e.sssp(s), want[s],
@@ -226,3 +226,19 @@ def test_subway_and_unified_memory_modes(mode):
     np.testing.assert_array_equal(oracle.normalise_bfs(e.bfs(s), g.V), oracle.bfs(off, pairs[:, 0].copy(), s)[0])
     np.testing.assert_array_equal(e.cc(), oracle.cc(off, pairs[:, 0].copy())[0])
     assert e.stats["edges_static"] == 0 and e.stats["edges_dynamic"] > 0
+
+
+def test_sssp_delta_default_and_roundtrip():
+    """Default near/far width (wmin + wmax) / 16: 4 for R-MAT weights in [1, 64];
+    set/get round trip; the plain frontier form (0) gives the same distances."""
+    g = og.Graph.rmat(11, 16, weighted=True)
+    e = og.Engine(g, budget=1 << 28, advisek=1.0)
+    assert e.get_param(og.PARAM_SSSP_DELTA) == 4
+    d4 = e.sssp(5)
+    e.set_param(og.PARAM_SSSP_DELTA, 0)
+    assert e.get_param(og.PARAM_SSSP_DELTA) == 0
+    np.testing.assert_array_equal(e.sssp(5), d4)
+    c = e.clone()
+    assert c.get_param(og.PARAM_SSSP_DELTA) == 0
+    c.close()
+    e.close()

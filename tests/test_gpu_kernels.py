@@ -62,6 +62,31 @@ def test_compact_matches_model():
         np.testing.assert_array_equal(gtile[:tiles.size], tiles)
 
 
+@pytest.mark.parametrize("density", [0.0005, 0.1, 1.0])
+def test_compact_many_tiles(density):
+    """About 367 look-back tiles (3M vertices, 8192 per tile): the warp-wide
+    look-back crosses many 32-tile windows, with sparse tiles of zero
+    aggregate and dense ones."""
+    rng = np.random.default_rng(7)
+    V = 3_000_017
+    deg = rng.integers(0, 40, V).astype(np.uint64)
+    deg[rng.random(V) < 0.2] = 0
+    off = np.concatenate([[0], np.cumsum(deg)]).astype(np.uint64)
+    bits = rng.random(((V + 31) // 32) * 32) < density
+    words = np.packbits(bits, bitorder="little").view(np.uint32).copy()
+    bits_d = torch.from_numpy(words.view(np.int32)).cuda()
+    off_d = torch.from_numpy(off.view(np.int64)).cuda()
+    E = int(off[-1])
+    for vb, ve in [(0, V), (12345, V - 77)]:
+        lst, pref, tiles = compact_model(words, vb, ve, off)
+        rc, n, total, (glist, gpref, gtile) = run_compact(bits_d, vb, ve, off_d, V, E // 2048 + 2)
+        assert rc == 0, og.lib().og_last_error()
+        assert n == lst.size and total == int(pref[-1])
+        np.testing.assert_array_equal(glist[:n], lst)
+        np.testing.assert_array_equal(gpref[:n + 1], pref)
+        np.testing.assert_array_equal(gtile[:tiles.size], tiles)
+
+
 def test_compact_reports_small_capacity():
     g = og.Graph.rmat(12, 8)
     off_d = torch.from_numpy(np.array(g.offsets).view(np.int64)).cuda()
