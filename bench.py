@@ -53,7 +53,7 @@ def parse_args():
     ap.add_argument("--sources", type=int, default=32)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--workload", default="sssp-oom",
-                    choices=["sssp-oom", "bfs-batch", "bfs-resident", "pr-precision", "serving"],
+                    choices=["sssp-oom", "cc-oom", "bfs-batch", "bfs-resident", "pr-precision", "serving"],
                     help="sssp-oom (default headline), or another measured configuration")
     ap.add_argument("--tune", type=int, default=1, help="bfs-batch: run the autotuner first")
     ap.add_argument("--serving-scales", default="22,24,26,27")
@@ -584,6 +584,85 @@ def run_bfs_resident(args, rank, world, local):
     eng.close()
 
 
+def run_cc_oom(args, rank, world, local):
+    """Connected components out of memory: the R-MAT 27 graph of the SSSP
+    workload (columns only), 8 GiB budget, advisek 0.8, direct dynamic region.
+    One step = one full CC (labels reset to the vertex ids, label propagation
+    to the fixed point)."""
+    import torch
+    import onegraph_gb300 as og
+    import oracle
+    torch.cuda.set_device(local)
+    g, gen_s = make_graph(args.scale)
+    eng = og.Engine(g, budget=int(args.budget_gib * GIB), advisek=args.advisek,
+                    direct=bool(args.direct), device=local)
+    for _ in range(args.warmup):
+        eng.cc(out=False)
+    sampler = ClockSampler(local)
+    sampler.start()
+    stats = []
+
+    def one(k):
+        eng.cc(out=False)
+        stats.append(dict(eng.stats))
+    t, _ = timed(one, args.steps)
+    clocks = sampler.stop()
+    check = eng.checksum(og.ALGO_CC)
+    host = torch.empty(g.V, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    e0 = time.perf_counter()
+    for _ in range(args.steps):
+        eng.cc(out=host)
+    e2e_s = time.perf_counter() - e0
+    visits = statistics.mean(x["edges_static"] + x["edges_dynamic"] for x in stats)
+    dyn_ms = sum(x["ms_dynamic"] for x in stats)
+    dyn_bytes = sum(x["link_bytes"] for x in stats)
+    h2d = h2d_peak_gbs()
+    link_gbs = dyn_bytes / (dyn_ms / 1e3) / 1e9 if dyn_ms else 0.0
+    # CPU: the serial label propagation's first round over the same graph,
+    # bounded, as an edge-visit rate; the full run is extrapolated by the edge
+    # visits of the GPU run (the same frontier-synchronous propagation)
+    lab = np.empty(g.V, np.uint32)
+    c0 = time.perf_counter()
+    n0 = oracle.cc_round_bounded_raw(g.V, g._off_p, g._edges_p, 2, 20_000_000, lab)
+    rate = n0 / (time.perf_counter() - c0)
+    budget_edges = int(rate * args.cpu_seconds)
+    c0 = time.perf_counter()
+    n1 = oracle.cc_round_bounded_raw(g.V, g._off_p, g._edges_p, 2, budget_edges, lab)
+    rate = n1 / (time.perf_counter() - c0)
+    plan = eng.plan
+    line = {
+        "metric": "CC runs/s", "value": args.steps * world / t, "unit": "runs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
+        "data": "synthetic",
+        "config": {"workload": "oom-cc-rmat%d-%gGiB" % (args.scale, args.budget_gib), "V": g.V, "E": g.E,
+                   "budget_bytes": int(args.budget_gib * GIB), "advisek": args.advisek,
+                   "dynamic_mode": "direct" if args.direct else "staged",
+                   "l2": "inputs larger than L2 (packed graph %.1f GB)" % (g.E * plan["edge_bits"] / 8e9)},
+        "gteps": visits / (t / args.steps) / 1e9, "rounds": stats[0]["iterations"],
+        "components_checksum": check,
+        "e2e": {"value": args.steps / e2e_s, "unit": "runs/s", "h2d_bytes_per_step":
+                int(statistics.mean(x["link_bytes"] for x in stats)), "d2h_bytes_per_step": 4 * g.V},
+        "roofline": {"bound": "host-link", "kernel": "k_lbs<SrcP<false>,MinOp<false>> over host-mapped records",
+                     "achieved": link_gbs, "peak": h2d, "unit": "GB/s", "frac": link_gbs / h2d if h2d else None,
+                     "traffic": None, "peak_source": "measured pinned H2D copy in this run"},
+        "cpu_baseline": {"value": rate / visits, "unit": "runs/s", "cores": 1, "kind": "port",
+                         "sample": "first round of the serial label propagation (CC/serial restatement) "
+                                   "bounded at %d edges (~%.0f s, %.2f G edge visits/s), extrapolated to "
+                                   "the %.2f G edge visits of one GPU run" % (n1, args.cpu_seconds, rate / 1e9,
+                                                                            visits / 1e9)},
+        "per_run": {"edge_visits": visits, "link_gb": statistics.mean(x["link_bytes"] for x in stats) / 1e9,
+                    "ms_static": statistics.mean(x["ms_static"] for x in stats),
+                    "ms_dynamic": statistics.mean(x["ms_dynamic"] for x in stats),
+                    "ms_compact": statistics.mean(x["ms_compact"] for x in stats)},
+        "plan": {k: plan[k] for k in ("static_vertices", "static_edges", "dynamic_edges", "edge_bits")},
+        "gpu_launches": sum(x["launches"] for x in stats), "clocks": clocks, "setup_s": {"generate": gen_s},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    eng.close()
+
+
 SERVING_BUDGETS_GIB = {22: 1.5, 24: 3.0, 26: 6.5, 27: 10.0}  # resident graph + first context
 
 
@@ -722,6 +801,8 @@ def main():
         run_pr_precision(args, rank, world, local)
     elif args.workload == "bfs-resident":
         run_bfs_resident(args, rank, world, local)
+    elif args.workload == "cc-oom":
+        run_cc_oom(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

@@ -30,6 +30,8 @@ def lib():
         L.ora_sssp_frontier.argtypes = [u32, _P, _P, u32, _P]
         L.ora_sssp_dijkstra_bounded.argtypes = [u32, _P, _P, u32, u64, _P]
         L.ora_sssp_dijkstra_bounded.restype = u64
+        L.ora_cc_round_bounded.argtypes = [u32, _P, _P, u32, u64, _P]
+        L.ora_cc_round_bounded.restype = u64
         L.ora_pr_cpu.argtypes = [u32, _P, _P, _P, _P]
         L.ora_pr_onegraph.argtypes = [u32, _P, _P, _P, C.c_double, C.c_int, _P]
         L.ora_pr_l1.argtypes = [u32, _P, _P, _P, C.c_double, C.c_double, C.c_int, _P,
@@ -66,6 +68,12 @@ def cc(off, col):
     out = np.empty(V, np.uint32)
     rounds = lib().ora_cc(V, _p(off), _p(col), _p(out))
     return out, rounds
+
+
+def cc_round_bounded_raw(V, off_ptr, edges_ptr, stride, max_edges, out):
+    """Pointer form of the first label-propagation round of cc(), stopped after
+    max_edges edges (stride 2 reads {column, weight} pairs); returns edges scanned."""
+    return lib().ora_cc_round_bounded(V, off_ptr, edges_ptr, stride, max_edges, _p(out))
 
 
 def sssp_dijkstra(off, pairs, src):

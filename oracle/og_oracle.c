@@ -88,6 +88,25 @@ int ora_cc(uint32_t V, const uint64_t *off, const uint32_t *col, uint32_t *out) 
   return rounds;
 }
 
+/* The first round of ora_cc (every vertex active, labels = ids), stopped
+ * after max_edges edges; edges are read with a stride of `stride` u32 words
+ * (1: columns, 2: {column, weight} pairs).  Returns the edges scanned: a
+ * bounded timing sample of the serial label propagation on a large graph. */
+uint64_t ora_cc_round_bounded(uint32_t V, const uint64_t *off, const uint32_t *edges, uint32_t stride,
+                              uint64_t max_edges, uint32_t *out) {
+  uint64_t scanned = 0;
+  for (uint32_t i = 0; i < V; i++) out[i] = i;
+  for (uint32_t u = 0; u < V && scanned < max_edges; u++) {
+    const uint32_t label = out[u];
+    for (uint64_t e = off[u]; e < off[u + 1]; e++) {
+      const uint32_t v = edges[e * stride];
+      if (label < out[v]) out[v] = label;
+    }
+    scanned += off[u + 1] - off[u];
+  }
+  return scanned;
+}
+
 /* ---- binary min-heap of (distance, vertex) with lazy deletion ---- */
 typedef struct {
   uint64_t key;

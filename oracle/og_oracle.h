@@ -34,6 +34,8 @@ int ora_bfs(uint32_t V, const uint64_t *off, const uint32_t *col, uint32_t src,
 /* CC/serial/serial.cpp:154-213: min-label propagation, labels start at the
  * vertex id, every vertex active in round 0.  Returns the number of rounds. */
 int ora_cc(uint32_t V, const uint64_t *off, const uint32_t *col, uint32_t *out);
+uint64_t ora_cc_round_bounded(uint32_t V, const uint64_t *off, const uint32_t *edges, uint32_t stride,
+                              uint64_t max_edges, uint32_t *out);
 
 /* Serial binary-heap Dijkstra with the reference's SSSP conventions
  * (SSSP/oneGraph/GraphMeta.h:376-381): dist(src) = 1, unreached = 0xFFFFFFFF.

@@ -119,3 +119,22 @@ def test_pr_l1_multithreaded_equals_serial():
     ib, lb = oracle.pr_l1_mt_raw(g.V, g._off_p, g._edges_p, g._outdeg_p, 0.85, 1e-9, 500, 5, b)
     assert ia == ib and la == lb
     np.testing.assert_array_equal(a, b)
+
+
+def test_cc_round_bounded_is_the_first_round():
+    """The bounded timing sample performs exactly cc()'s first round over the
+    edges it scans (pairs read with stride 2)."""
+    import onegraph_gb300 as og
+    g = og.Graph.rmat(10, 16, weighted=True)
+    off, pairs = np.array(g.offsets), np.array(g.edges)
+    out = np.empty(g.V, np.uint32)
+    n = oracle.cc_round_bounded_raw(g.V, g._off_p, g._edges_p, 2, 1 << 62, out)
+    assert n == g.E
+    want = np.arange(g.V, dtype=np.uint32)
+    for u in range(g.V):  # serial order, labels updated in place as in ora_cc
+        lab = want[u]
+        for v in pairs[off[u]:off[u + 1], 0]:
+            if lab < want[v]:
+                want[v] = lab
+    np.testing.assert_array_equal(out, want)
+    assert oracle.cc_round_bounded_raw(g.V, g._off_p, g._edges_p, 2, 100, out) < g.E
