@@ -11,6 +11,7 @@
 //    previous buffer is relaxed and the static region is relaxed on the main
 //    stream (CalculateOpt.h:75-188, GraphMeta.h:471-557).
 #include <algorithm>
+#include <type_traits>
 #include <chrono>
 #include <cstring>
 #include <mutex>
@@ -71,7 +72,9 @@ struct og_engine {
   uint64_t list_cap[2] = {0, 0}, tile_cap[2] = {0, 0};
   Lookback lb[2]{};
   uint32_t lb_tiles = 0;
+  // counts of the two regions followed by their two far keys (u64), one D2H
   Counts *counts_d = nullptr, *counts_h = nullptr;
+  uint32_t epoch = 0;  // look-back epoch of the last compaction launch
   uint32_t *err_d = nullptr, *err_h = nullptr;
   uint32_t *active_d = nullptr;
 
@@ -205,11 +208,14 @@ int create_query_state(og_engine *e) {
     RC(dalloc(e, &e->lb[r].inc_n, e->lb_tiles));
     RC(dalloc(e, &e->lb[r].inc_e, e->lb_tiles));
   }
-  RC(dalloc(e, &e->counts_d, 2));
+  for (int r = 0; r < 2; r++)  // epochs start at 1: zeroed status words are "empty"
+    CK(cudaMemsetAsync(e->lb[r].status, 0, sizeof(uint32_t) * (e->lb_tiles + 1), e->s_main));
+  RC(dalloc(e, &e->counts_d, 3));  // Counts[2] + u64 far key[2]
+  CK(cudaMemsetAsync(e->counts_d, 0, 3 * sizeof(Counts), e->s_main));
   RC(dalloc(e, &e->err_d, 4));
   e->active_d = e->err_d + 1;
   RC(dalloc(e, &e->sum64_d, 3ull * e->sms * 8 + 4));
-  CK(cudaMallocHost(&e->counts_h, 2 * sizeof(Counts)));
+  CK(cudaMallocHost(&e->counts_h, 3 * sizeof(Counts)));
   CK(cudaMallocHost(&e->err_h, 4 * sizeof(uint32_t)));
   CK(cudaMallocHost(&e->l1_h, sizeof(double)));
   if (P.chunk_edges && !(e->cfg.flags & OG_CFG_DIRECT)) {
@@ -380,9 +386,10 @@ struct SplitArgs {
 
 int launch_compact(og_engine *e, int r, const uint32_t *bits, uint32_t vb, uint32_t ve,
                    cudaStream_t s, const SplitArgs &sp = SplitArgs()) {
-  CK(cudaMemsetAsync(e->counts_d + r, 0, sizeof(Counts), s));
-  CK(cudaMemsetAsync(&e->counts_d[r].far_min, 0xff, sizeof(uint32_t), s));  // far minimum
-  if (ve <= vb) return OG_OK;
+  if (ve <= vb) {  // empty region: no kernel writes its counts
+    CK(cudaMemsetAsync(e->counts_d + r, 0, sizeof(Counts), s));
+    return OG_OK;
+  }
   CompactArgs a;
   a.bits = bits;
   a.v_begin = vb;
@@ -403,10 +410,10 @@ int launch_compact(og_engine *e, int r, const uint32_t *bits, uint32_t vb, uint3
   a.thr = sp.thr;
   a.split = sp.on ? 1u : 0u;
   a.far_bits = sp.far_bits;
-  a.far_min = &e->counts_d[r].far_min;
+  a.far_key = (unsigned long long *)(e->counts_d + 2) + r;
   a.clear_bits = sp.clear_bits;
+  a.epoch = e->epoch;
   if (a.ntiles + 1 > e->lb_tiles) return fail(OG_E_STATE, "compaction scratch too small");
-  CK(cudaMemsetAsync(e->lb[r].status, 0, sizeof(uint32_t) * (e->lb_tiles + 1), s));
   k_compact<<<a.ntiles, kThreads, 0, s>>>(a);
   e->launches++;
   return OG_OK;
@@ -470,6 +477,27 @@ struct RoundOps {
   uint32_t level;
 };
 
+template <class Src0, class Src1>
+int launch_relax_pair(og_engine *e, const RoundOps &ro, const LbsArgs &a0, Src0 s0, const LbsArgs &a1,
+                      Src1 s1, uint32_t *next, cudaStream_t s) {
+  const uint64_t n0 = lbs_grid(a0.pos_begin, a0.pos_end), n1 = lbs_grid(a1.pos_begin, a1.pos_end);
+  const uint64_t n = n0 + n1;
+  if (n == 0) return OG_OK;
+  if (n > 0x7fffffffull) return fail(OG_E_STATE, "relax grid of %llu tiles", (unsigned long long)n);
+  if (ro.algo == OG_ALGO_BFS) {
+    BfsOp op{e->bm[2], next, e->value_d, e->err_d, e->V, ro.level + 1};
+    k_lbs_pair<Src0, Src1, BfsOp><<<(unsigned)n, kThreads, 0, s>>>(a0, s0, a1, s1, op, n0, n);
+  } else if (ro.algo == OG_ALGO_SSSP) {
+    MinOp<true> op{e->value_d, next, e->err_d, e->V};
+    k_lbs_pair<Src0, Src1, MinOp<true>><<<(unsigned)n, kThreads, 0, s>>>(a0, s0, a1, s1, op, n0, n);
+  } else {
+    MinOp<false> op{e->value_d, next, e->err_d, e->V};
+    k_lbs_pair<Src0, Src1, MinOp<false>><<<(unsigned)n, kThreads, 0, s>>>(a0, s0, a1, s1, op, n0, n);
+  }
+  e->launches++;
+  return OG_OK;
+}
+
 template <class Src>
 int launch_relax(og_engine *e, const RoundOps &ro, const LbsArgs &a, Src src, uint32_t *next,
                  cudaStream_t s) {
@@ -529,11 +557,32 @@ void collect_timing(og_engine *e, Timing &t, og_stats *st) {
   t.pend_g = 0;
 }
 
+struct NoPair {};
+
 // One round's region work given the compaction counts (already on the host).
-// `body_static(a)` / `body_dyn(a, edges, ...)` launch the per-region kernel.
-template <class K, class StaticFn, class DynFn>
-int run_regions(og_engine *e, og_stats &st, Timing &tm, StaticFn static_fn, DynFn dyn_fn) {
+// `static_fn(a)` / `dyn_fn(a, src, stream)` launch the per-region kernel;
+// `pair_fn(a0, src0, a1, src1, stream)`, when given, launches both regions
+// as one interleaved kernel (direct mode with both regions non-empty): the
+// static tiles then overlap the link-bound dynamic ones instead of taking the
+// SMs first.  Its time is counted as dynamic-region time.
+template <class K, class StaticFn, class DynFn, class PairFn = NoPair>
+int run_regions(og_engine *e, og_stats &st, Timing &tm, StaticFn static_fn, DynFn dyn_fn,
+                PairFn pair_fn = PairFn()) {
   const Counts cs = e->counts_h[0], cd = e->counts_h[1];
+  if constexpr (!std::is_same<PairFn, NoPair>::value) {
+    if (cs.n && cd.n && (e->cfg.flags & OG_CFG_DIRECT)) {
+      CK(cudaEventRecord(e->t_d0, e->s_main));
+      RC(pair_fn(lbs_args(e, 0, 0, cs.total, true, e->plan.static_edges), K::stat(e),
+                 lbs_args(e, 1, 0, cd.total, true, e->g->E), K::host(e), e->s_main));
+      CK(cudaEventRecord(e->ev_dyn_done, e->s_main));
+      tm.pend_d = true;
+      st.chunks += 1;
+      st.edges_static += cs.total;
+      st.edges_dynamic += cd.total;
+      st.link_bytes += (cd.total * e->bpe + 7) / 8;
+      return OG_OK;
+    }
+  }
   if (cs.n) {
     CK(cudaEventRecord(e->t_s0, e->s_main));
     RC(static_fn(lbs_args(e, 0, 0, cs.total, true, e->plan.static_edges)));
@@ -578,8 +627,21 @@ int run_regions(og_engine *e, og_stats &st, Timing &tm, StaticFn static_fn, DynF
 
 // Compacts both regions of `cur` and brings the counts (and the error word) to
 // the host.  Returns the number of listed vertices through *n.
+// Smallest waiting value the last compaction of region r saw, or UINT32_MAX
+// (its far key carries the launch epoch; another epoch means "none").
+uint32_t far_of(const og_engine *e, int r) {
+  const uint64_t key = ((const uint64_t *)(e->counts_h + 2))[r];
+  return (uint32_t)(key >> 32) == e->epoch ? ~(uint32_t)key : 0xffffffffu;
+}
+
 int compact_round(og_engine *e, const uint32_t *cur, og_stats &st, Timing &tm, uint64_t *n,
                   const SplitArgs &sp = SplitArgs()) {
+  if (++e->epoch >= (1u << 30)) {  // epoch wrap: clear the status words and far keys once
+    for (int r = 0; r < 2; r++)
+      CK(cudaMemsetAsync(e->lb[r].status, 0, sizeof(uint32_t) * e->lb_tiles, e->s_main));
+    CK(cudaMemsetAsync(e->counts_d + 2, 0, sizeof(Counts), e->s_main));
+    e->epoch = 1;
+  }
   CK(cudaEventRecord(e->ev_round, e->s_main));
   RC(launch_compact(e, 0, cur, 0, e->Vs, e->s_main, sp));
   CK(cudaEventRecord(e->ev_cs, e->s_main));
@@ -587,7 +649,7 @@ int compact_round(og_engine *e, const uint32_t *cur, og_stats &st, Timing &tm, u
   RC(launch_compact(e, 1, cur, e->Vs, e->V, e->s_dyn, sp));
   CK(cudaEventRecord(e->ev_cd, e->s_dyn));
   CK(cudaStreamWaitEvent(e->s_dyn, e->ev_cs, 0));
-  CK(cudaMemcpyAsync(e->counts_h, e->counts_d, 2 * sizeof(Counts), cudaMemcpyDeviceToHost, e->s_dyn));
+  CK(cudaMemcpyAsync(e->counts_h, e->counts_d, 3 * sizeof(Counts), cudaMemcpyDeviceToHost, e->s_dyn));
   CK(cudaMemcpyAsync(e->err_h, e->err_d, 4, cudaMemcpyDeviceToHost, e->s_dyn));
   CK(cudaStreamSynchronize(e->s_dyn));
   collect_timing(e, tm, &st);
@@ -648,7 +710,7 @@ int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
     sp.far_bits = split && !advance ? waiting : nullptr;
     RC(compact_round(e, advance ? waiting : cur, st, tm, &n, sp));
     if (split) {
-      const uint32_t fm = std::min(e->counts_h[0].far_min, e->counts_h[1].far_min);
+      const uint32_t fm = std::min(far_of(e, 0), far_of(e, 1));
       far_min = advance ? fm : std::min(far_min, fm);
     }
     if (n == 0) {
@@ -665,7 +727,10 @@ int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
     auto dfn = [&](const LbsArgs &a, auto src, cudaStream_t ds) {
       return launch_relax(e, ro, a, src, next, ds);
     };
-    RC((run_regions<K>(e, st, tm, sfn, dfn)));
+    auto pfn = [&](const LbsArgs &a0, auto s0, const LbsArgs &a1, auto s1, cudaStream_t ps) {
+      return launch_relax_pair(e, ro, a0, s0, a1, s1, next, ps);
+    };
+    RC((run_regions<K>(e, st, tm, sfn, dfn, pfn)));
     CK(cudaStreamWaitEvent(e->s_main, e->ev_cd, 0));
     CK(cudaMemsetAsync(cur, 0, 4 * e->nwords, e->s_main));
     std::swap(cur, next);
@@ -726,7 +791,15 @@ int run_batch(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *out, uin
       return (int)OG_OK;
     };
     auto sfn = [&](const LbsArgs &a) { return launch(a, EKU::stat(e), e->s_main); };
-    RC((run_regions<EKU>(e, st, tm, sfn, launch)));
+    auto pfn = [&](const LbsArgs &a0, auto s0, const LbsArgs &a1, auto s1, cudaStream_t ps) {
+      const uint64_t n0 = lbs_grid(a0.pos_begin, a0.pos_end), n1 = lbs_grid(a1.pos_begin, a1.pos_end);
+      if (n0 + n1 > 0x7fffffffull) return fail(OG_E_STATE, "relax grid too large");
+      k_lbs_pair<decltype(s0), decltype(s1), BatchOp><<<(unsigned)(n0 + n1), kThreads, 0, ps>>>(
+          a0, s0, a1, s1, op, n0, n0 + n1);
+      e->launches++;
+      return (int)OG_OK;
+    };
+    RC((run_regions<EKU>(e, st, tm, sfn, launch, pfn)));
     CK(cudaMemsetAsync(e->hist_d, 0, 64 * 8, s));
     k_batch_level<<<grid_for(e->nwords, e->sms), kThreads, 0, s>>>(next_any, next, e->nwords, n,
                                                                  e->hist_d, depth_d, V, level + 1);
@@ -1361,8 +1434,9 @@ void compact_launch(const uint32_t *bits, uint32_t v_begin, uint32_t v_end, cons
   a.thr = 0;
   a.split = 0;
   a.far_bits = nullptr;
-  a.far_min = nullptr;
+  a.far_key = nullptr;
   a.clear_bits = nullptr;
+  a.epoch = 1;  // the caller's scratch is zeroed before every launch
   k_compact<<<a.ntiles, kThreads, 0, s>>>(a);
 }
 

@@ -46,7 +46,7 @@ struct Counts {
 };
 
 struct Lookback {
-  uint32_t *status;  // 0 empty, 1 aggregate, 2 inclusive prefix
+  uint32_t *status;  // (epoch << 2) | state; state 1 aggregate, 2 inclusive prefix
   uint32_t *agg_n;
   unsigned long long *agg_e;
   uint32_t *inc_n;
@@ -77,8 +77,15 @@ struct CompactArgs {
   uint32_t thr;
   uint32_t split;
   uint32_t *far_bits;
-  uint32_t *far_min;
+  // atomicMax of (epoch << 32) | ~value over the waiting vertices: a key of
+  // an older epoch (or zeroed memory) is always smaller, and within an epoch
+  // the largest ~value is the smallest value
+  unsigned long long *far_key;
   uint32_t *clear_bits;
+  // Launch epoch in [1, 2^30): status words of other epochs read as empty, so
+  // the status array needs no clearing between launches.  The CTA that takes
+  // the last ticket resets the ticket counter for the next launch.
+  uint32_t epoch;
 };
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
@@ -148,13 +155,16 @@ __global__ void __launch_bounds__(kThreads) k_compact(CompactArgs a) {
   __shared__ uint32_t s_excl_n;
   __shared__ uint64_t s_excl_e;
   __shared__ int s_bad;
-  if (threadIdx.x == 0) s_tile = atomicAdd(a.lb.ticket, 1u);
+  if (threadIdx.x == 0) {
+    s_tile = atomicAdd(a.lb.ticket, 1u);
+    if (s_tile == a.ntiles - 1) *a.lb.ticket = 0u;  // every CTA of this launch has its ticket
+  }
   __syncthreads();
   const uint32_t tile = s_tile;
   const uint32_t w0 = a.w_begin + tile * kWordsPerCompactTile + threadIdx.x * kCompactWordsPerThread;
   // drop vertices without edges: nothing to expand
   uint32_t keep[kCompactWordsPerThread];
-  uint32_t cnt = 0;
+  uint32_t cnt = 0, tmin = 0xffffffffu;  // smallest waiting value of this thread
   uint64_t sum = 0;
 #pragma unroll
   for (uint32_t j = 0; j < kCompactWordsPerThread; j++) {
@@ -172,7 +182,7 @@ __global__ void __launch_bounds__(kThreads) k_compact(CompactArgs a) {
         word = k >= 32 ? word : word & ((1u << k) - 1u);
       }
     }
-    uint32_t kp = 0, far = 0, fmin = 0xffffffffu, leave = 0;
+    uint32_t kp = 0, far = 0, leave = 0;
     for (uint32_t m = word; m; m &= m - 1) {
       const uint32_t b = __ffs(m) - 1;
       const uint64_t v = vbase + b;
@@ -180,7 +190,7 @@ __global__ void __launch_bounds__(kThreads) k_compact(CompactArgs a) {
         const uint32_t x = __ldcg(a.value + v);
         if (x >= a.thr) {
           far |= 1u << b;
-          fmin = min(fmin, x);
+          tmin = min(tmin, x);
           continue;
         }
         leave |= 1u << b;
@@ -192,15 +202,24 @@ __global__ void __launch_bounds__(kThreads) k_compact(CompactArgs a) {
       sum += d;
     }
     keep[j] = kp;
-    if (far) {
-      if (a.far_bits) atomicOr(a.far_bits + w, far);
-      atomicMin(a.far_min, fmin);
-    }
+    if (far && a.far_bits) atomicOr(a.far_bits + w, far);
     if (leave && a.clear_bits) atomicAnd(a.clear_bits + w, ~leave);
   }
   uint32_t ex_n, tot_n;
   uint64_t ex_e, tot_e;
-  block_scan_pair(cnt, sum, ex_n, ex_e, tot_n, tot_e);
+  // smallest waiting value of the CTA: one far-key atomic per CTA
+  __shared__ uint32_t s_wmin[kThreads / 32];
+  if (a.far_key) {
+    const uint32_t wm = __reduce_min_sync(0xffffffffu, tmin);
+    if ((threadIdx.x & 31) == 0) s_wmin[threadIdx.x >> 5] = wm;
+  }
+  block_scan_pair(cnt, sum, ex_n, ex_e, tot_n, tot_e);  // its barriers publish s_wmin
+  if (a.far_key && threadIdx.x == 0) {
+    uint32_t m = 0xffffffffu;
+#pragma unroll
+    for (int i = 0; i < kThreads / 32; i++) m = min(m, s_wmin[i]);
+    if (m != 0xffffffffu) atomicMax(a.far_key, ((unsigned long long)a.epoch << 32) | (~m & 0xffffffffu));
+  }
   // Warp-wide decoupled look-back (warp 0): each pass reads the status of the
   // 32 nearest unaccounted predecessors at once, sums their aggregates up to
   // the nearest one holding an inclusive prefix, and stops there; tiles
@@ -216,22 +235,24 @@ __global__ void __launch_bounds__(kThreads) k_compact(CompactArgs a) {
         a.lb.inc_n[0] = tot_n;
         a.lb.inc_e[0] = tot_e;
         __threadfence();
-        st_release(&a.lb.status[0], 2u);
+        st_release(&a.lb.status[0], (a.epoch << 2) | 2u);
       }
     } else {
       if (lane == 0) {
         a.lb.agg_n[tile] = tot_n;
         a.lb.agg_e[tile] = tot_e;
         __threadfence();
-        st_release(&a.lb.status[tile], 1u);
+        st_release(&a.lb.status[tile], (a.epoch << 2) | 1u);
       }
       for (int p = (int)tile - 1;; p -= 32) {
         const int q = p - lane;  // lane 0: nearest predecessor of the window
         uint32_t st = 2u;
         if (q >= 0) {
           uint32_t spins = 0;
-          while ((st = ld_acquire(&a.lb.status[q])) == 0u) {
-            if (++spins > kSpinLimit) break;
+          for (;;) {
+            const uint32_t raw = ld_acquire(&a.lb.status[q]);
+            st = (raw >> 2) == a.epoch ? (raw & 3u) : 0u;
+            if (st != 0u || ++spins > kSpinLimit) break;
             __nanosleep(64);
           }
         }
@@ -265,7 +286,7 @@ __global__ void __launch_bounds__(kThreads) k_compact(CompactArgs a) {
         a.lb.inc_n[tile] = pn + tot_n;
         a.lb.inc_e[tile] = pe + tot_e;
         __threadfence();
-        st_release(&a.lb.status[tile], 2u);  // published even when bad: successors never wait forever
+        st_release(&a.lb.status[tile], (a.epoch << 2) | 2u);  // published even when bad: successors never wait forever
       }
     }
     if (lane == 0) {
@@ -451,10 +472,10 @@ __device__ __forceinline__ uint32_t lbs_setup(const LbsArgs &a, const Op &op, Lb
   return nl;
 }
 
+// One LBS tile (kTile positions starting at tile k of the list) of a CTA.
 template <class Src, class Op>
-__global__ void __launch_bounds__(kThreads) k_lbs(LbsArgs a, Src src, Op op) {
-  __shared__ LbsShared<typename Op::Val> sh;
-  const uint64_t k = a.pos_begin / kTile + blockIdx.x;
+__device__ __forceinline__ void lbs_tile(const LbsArgs &a, const Src &src, const Op &op,
+                                         LbsShared<typename Op::Val> &sh, uint64_t k) {
   const uint64_t pos0 = k * kTile;
   if (pos0 >= a.pos_end) return;
   const uint64_t pend = min(pos0 + kTile, a.pos_end);
@@ -497,6 +518,29 @@ __global__ void __launch_bounds__(kThreads) k_lbs(LbsArgs a, Src src, Op op) {
       op.relax(ev[it], Op::kNeedVal ? sh.val[lv[it]] : typename Op::Val(0),
                pos0 + it * kThreads + threadIdx.x, pr[it]);
   }
+}
+
+template <class Src, class Op>
+__global__ void __launch_bounds__(kThreads) k_lbs(LbsArgs a, Src src, Op op) {
+  __shared__ LbsShared<typename Op::Val> sh;
+  lbs_tile(a, src, op, sh, a.pos_begin / kTile + blockIdx.x);
+}
+
+// Both regions of a round in one launch: n0 tiles of list 0 (static region,
+// read from HBM) and n1 tiles of list 1 (dynamic region, read over the host
+// link), interleaved in CTA order in proportion to their counts, so that at
+// any time about n0 / (n0 + n1) of the resident CTAs work from HBM while the
+// rest keep the link busy.  CTA b is a static tile iff
+// floor((b + 1) n0 / n) > floor(b n0 / n); its tile index is floor(b n0 / n),
+// else b - floor((b + 1) n0 / n) among the dynamic tiles.
+template <class Src0, class Src1, class Op>
+__global__ void __launch_bounds__(kThreads) k_lbs_pair(LbsArgs a0, Src0 s0, LbsArgs a1, Src1 s1, Op op,
+                                                       uint64_t n0, uint64_t n) {
+  __shared__ LbsShared<typename Op::Val> sh;
+  const uint64_t b = blockIdx.x;
+  const uint64_t lo = b * n0 / n, hi = (b + 1) * n0 / n;
+  if (hi > lo) lbs_tile(a0, s0, op, sh, a0.pos_begin / kTile + lo);
+  else lbs_tile(a1, s1, op, sh, a1.pos_begin / kTile + (b - hi));
 }
 
 template <int MULT>
