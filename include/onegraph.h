@@ -102,6 +102,17 @@ int og_graph_save_bel(const og_graph *g, const char *prefix);
  * input path without its last four characters, plus "lcsr". */
 int og_convert_uint_to_ulong(const char *in_path, const char *out_path);
 
+/* Symmetry of the edge set (every (u, v) has its reverse (v, u)), which lets
+ * og_cc use its union-find path.  og_graph_set_symmetric records the caller's
+ * assertion (1 or 0) without checking it; a wrong 1 gives wrong components.
+ * og_graph_symmetric stores 1 or 0 in *symmetric, checking exactly on first use when not
+ * known: every adjacency list sorted and every reverse edge found by binary
+ * search, on all host threads (one pass over the edges plus E binary
+ * searches).  Graphs from og_rmat_generate with OG_RMAT_SYMMETRIC are known
+ * symmetric; unsorted adjacency lists count as not symmetric. */
+int og_graph_set_symmetric(og_graph *g, int symmetric);
+int og_graph_symmetric(og_graph *g, int *symmetric);
+
 /* GraphMeta::findbignode (GraphMeta.h:150-165): first vertex after `last`
  * whose degree exceeds 3000, or `last` when there is none. */
 uint32_t og_graph_findbignode(const og_graph *g, uint32_t last);
@@ -297,6 +308,19 @@ int og_engine_clone(og_engine *parent, og_engine **out);
  *   1 (4 for weights in [1, 64]).  Distances are exact for every value.
  *   Clones inherit it. */
 #define OG_PARAM_SSSP_DELTA 1
+/* OG_PARAM_CC_METHOD: how og_cc computes the labels (minimum vertex id that
+ *   reaches each vertex; the component minimum on a symmetric graph).
+ *   OG_CC_AUTO (default): union-find when the graph is known symmetric
+ *   (og_graph_symmetric / og_graph_set_symmetric / symmetric R-MAT), label
+ *   propagation otherwise.  OG_CC_LABEL_PROPAGATION: the reference's frontier
+ *   propagation (CC/onegraph/gpu_kernels.h:105-157).  OG_CC_UNION_FIND:
+ *   sampling union-find (hook each vertex with its first two neighbours,
+ *   expand only the edges of vertices outside the giant component), an error
+ *   on a graph not known symmetric.  Labels are identical either way. */
+#define OG_PARAM_CC_METHOD 2
+#define OG_CC_AUTO 0
+#define OG_CC_LABEL_PROPAGATION 1
+#define OG_CC_UNION_FIND 2
 int og_engine_set_param(og_engine *e, int param, double value);
 int og_engine_get_param(const og_engine *e, int param, double *value);
 

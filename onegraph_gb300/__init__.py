@@ -27,6 +27,8 @@ ALGO_BFS, ALGO_SSSP, ALGO_CC, ALGO_PR = 0, 1, 2, 3
 RMAT_SYMMETRIC, RMAT_PERMUTE, RMAT_WEIGHTED, RMAT_PR, RMAT_ON_GPU = 1, 2, 4, 8, 16
 CFG_DIRECT, CFG_NO_PIN, CFG_PR, CFG_BATCH, CFG_BATCH_LEVELS, CFG_NO_STATIC = 1, 2, 4, 8, 16, 32
 PARAM_SSSP_DELTA = 1
+PARAM_CC_METHOD = 2
+CC_AUTO, CC_LABEL_PROPAGATION, CC_UNION_FIND = 0, 1, 2
 # R-MAT quadrant probabilities of the benchmark graphs
 RMAT_ABC = (0.57, 0.19, 0.19)
 
@@ -128,6 +130,8 @@ SIGNATURES = [
     ("og_graph_findbignode", C.c_uint32, [_P, C.c_uint32]),
     ("og_graph_save_bel", C.c_int, [_P, C.c_char_p]),
     ("og_convert_uint_to_ulong", C.c_int, [C.c_char_p, C.c_char_p]),
+    ("og_graph_set_symmetric", C.c_int, [_P, C.c_int]),
+    ("og_graph_symmetric", C.c_int, [_P, C.POINTER(C.c_int)]),
     ("og_graph_records", C.c_int, [_P, C.POINTER(_P), C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
                                    C.POINTER(C.c_uint32), C.POINTER(C.c_uint32)]),
     ("og_rmat_generate", C.c_int, [C.POINTER(RmatParams), C.POINTER(_P)]),
@@ -284,6 +288,16 @@ class Graph:
         p = Plan()
         _check(lib().og_graph_plan(self._h, budget, advisek, flags, C.byref(p)), "og_graph_plan")
         return p.as_dict()
+
+    def set_symmetric(self, symmetric: bool):
+        """Asserts (without checking) whether every edge has its reverse."""
+        _check(lib().og_graph_set_symmetric(self._h, 1 if symmetric else 0), "og_graph_set_symmetric")
+
+    def symmetric(self) -> bool:
+        """Whether every edge has its reverse (exact check on first use)."""
+        v = C.c_int()
+        _check(lib().og_graph_symmetric(self._h, C.byref(v)), "og_graph_symmetric")
+        return bool(v.value)
 
     def records(self) -> dict:
         """The packed edge records the engines read: words (borrowed view),

@@ -109,6 +109,7 @@ struct og_engine {
   unsigned long long *sum64_d = nullptr;  // result checksum scratch
 
   uint32_t sssp_delta = 0;  // near/far split width (0: plain frontier relaxation)
+  uint32_t cc_method = 0;   // OG_CC_AUTO / OG_CC_LABEL_PROPAGATION / OG_CC_UNION_FIND
 
   int last_algo = -1;
   uint64_t launches = 0;  // kernels launched since the query began
@@ -366,6 +367,7 @@ int clone(og_engine *parent, og_engine *e) {
   e->outdeg_d = parent->outdeg_d;
   e->tuned = parent->tuned;
   e->sssp_delta = parent->sssp_delta;
+  e->cc_method = parent->cc_method;
   CK(cudaSetDevice(e->dev));
   RC(create_query_state(e));
   parent->clones++;
@@ -1225,6 +1227,12 @@ extern "C" int og_engine_set_param(og_engine *e, int param, double value) {
     e->sssp_delta = (uint32_t)value;
     return OG_OK;
   }
+  if (param == OG_PARAM_CC_METHOD) {
+    if (value != OG_CC_AUTO && value != OG_CC_LABEL_PROPAGATION && value != OG_CC_UNION_FIND)
+      return fail(OG_E_ARG, "unknown CC method %g", value);
+    e->cc_method = (uint32_t)value;
+    return OG_OK;
+  }
   return fail(OG_E_ARG, "unknown parameter %d", param);
 }
 
@@ -1232,6 +1240,10 @@ extern "C" int og_engine_get_param(const og_engine *e, int param, double *value)
   if (!e || !value) return fail(OG_E_ARG, "og_engine_get_param: null argument");
   if (param == OG_PARAM_SSSP_DELTA) {
     *value = e->sssp_delta;
+    return OG_OK;
+  }
+  if (param == OG_PARAM_CC_METHOD) {
+    *value = e->cc_method;
     return OG_OK;
   }
   return fail(OG_E_ARG, "unknown parameter %d", param);
@@ -1271,10 +1283,108 @@ extern "C" int og_sssp(og_engine *e, uint32_t src, uint32_t *out_dist, og_stats 
   }, &src);
 }
 
+// ------------------------------------------------------------ union-find CC
+//
+// Symmetric graphs only (the result equals label propagation's there): two
+// sampling passes over every vertex's first two edges, compression, the giant
+// component picked from 1024 sampled roots, then one edge-balanced pass over
+// the edges of the vertices outside it (both regions, interleaved), and a
+// final compression.  parent[] lives in value_d and ends as the labels.
+int run_cc_uf(og_engine *e, og_stats &st) {
+  const uint32_t V = e->V;
+  cudaStream_t s = e->s_main;
+  const int g = grid_for(V, e->sms);
+  uint32_t *par = e->value_d;
+  unsigned long long *reads = e->sum64_d;  // [0] host records, [1] static records
+  uint32_t *roots_d = (uint32_t *)(e->sum64_d + 2);
+  constexpr uint32_t kRoots = 1024;
+  CK(cudaMemsetAsync(e->err_d, 0, 16, s));
+  CK(cudaMemsetAsync(reads, 0, 16, s));
+  k_iota_u32<<<g, kThreads, 0, s>>>(par, V);
+  e->launches++;
+  cudaEvent_t t0 = e->t_d0, t1 = e->ev_dyn_done;
+  CK(cudaEventRecord(t0, s));
+  for (uint32_t r = 0; r < 2; r++) {
+    k_uf_sample<EKU::PSrc><<<g, kThreads, 0, s>>>(e->off_d, V, e->plan.static_edges, EKU::stat(e),
+                                                  EKU::host(e), r, par, reads, e->err_d);
+    k_uf_compress<<<g, kThreads, 0, s>>>(par, V, e->err_d);
+    e->launches += 2;
+    st.iterations++;
+  }
+  k_uf_roots<<<(kRoots + kThreads - 1) / kThreads, kThreads, 0, s>>>(par, V, kRoots, roots_d);
+  e->launches++;
+  CK(cudaEventRecord(t1, s));
+  std::vector<uint32_t> roots(kRoots);
+  unsigned long long rd[2] = {0, 0};
+  CK(cudaMemcpyAsync(roots.data(), roots_d, 4 * kRoots, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(rd, reads, 16, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, t0, t1) == cudaSuccess) st.ms_dynamic += ms;
+  st.link_bytes += (rd[0] * e->bpe + 7) / 8;
+  st.edges_dynamic += rd[0];
+  st.edges_static += rd[1];
+  std::sort(roots.begin(), roots.end());
+  uint32_t c = roots[0], best = 0;
+  for (uint32_t i = 0; i < kRoots;) {
+    uint32_t j = i;
+    while (j < kRoots && roots[j] == roots[i]) j++;
+    if (j - i > best) {
+      best = j - i;
+      c = roots[i];
+    }
+    i = j;
+  }
+  // final pass over the vertices outside c
+  uint32_t *cur = e->bm[0];
+  k_uf_mark<<<grid_for(e->nwords * 32, e->sms), kThreads, 0, s>>>(e->off_d, par, V, c, cur, e->nwords);
+  e->launches++;
+  Timing tm;
+  uint64_t n = 0;
+  RC(compact_round(e, cur, st, tm, &n));
+  if (n) {
+    st.iterations++;
+    st.frontier_sum += n;
+    st.static_vertices += e->counts_h[0].n;
+    UnionOp op{par, e->err_d, V};
+    auto launch = [&](const LbsArgs &a, auto src, cudaStream_t ls) {
+      const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
+      if (grid) {
+        k_lbs<decltype(src), UnionOp><<<grid, kThreads, 0, ls>>>(a, src, op);
+        e->launches++;
+      }
+      return (int)OG_OK;
+    };
+    auto sfn = [&](const LbsArgs &a) { return launch(a, EKU::stat(e), e->s_main); };
+    auto pfn = [&](const LbsArgs &a0, auto s0, const LbsArgs &a1, auto s1, cudaStream_t ps) {
+      const uint64_t n0 = lbs_grid(a0.pos_begin, a0.pos_end), n1 = lbs_grid(a1.pos_begin, a1.pos_end);
+      if (n0 + n1 > 0x7fffffffull) return fail(OG_E_STATE, "relax grid too large");
+      k_lbs_pair<decltype(s0), decltype(s1), UnionOp><<<(unsigned)(n0 + n1), kThreads, 0, ps>>>(
+          a0, s0, a1, s1, op, n0, n0 + n1);
+      e->launches++;
+      return (int)OG_OK;
+    };
+    RC((run_regions<EKU>(e, st, tm, sfn, launch, pfn)));
+    CK(cudaStreamWaitEvent(e->s_main, e->ev_cd, 0));
+  }
+  k_uf_compress<<<g, kThreads, 0, s>>>(par, V, e->err_d);
+  e->launches++;
+  CK(cudaStreamSynchronize(s));
+  collect_timing(e, tm, &st);
+  CK(cudaMemcpy(e->err_h, e->err_d, 4, cudaMemcpyDeviceToHost));
+  RC(check_device_error(e));
+  e->last_algo = OG_ALGO_CC;
+  return OG_OK;
+}
+
 extern "C" int og_cc(og_engine *e, uint32_t *out_label, og_stats *st) {
   uint32_t dummy = 0;
   return query_common(e, OG_ALGO_CC, st, out_label, [](og_engine *en, og_stats &s, void *) {
-    return run_frontier<EKU>(en, OG_ALGO_CC, 0, s);
+    const bool uf = en->cc_method == OG_CC_UNION_FIND ||
+                    (en->cc_method == OG_CC_AUTO && en->g->symmetric == 1);
+    if (en->cc_method == OG_CC_UNION_FIND && en->g->symmetric != 1)
+      return fail(OG_E_ARG, "union-find CC needs a graph known to be symmetric (og_graph_symmetric)");
+    return uf ? run_cc_uf(en, s) : run_frontier<EKU>(en, OG_ALGO_CC, 0, s);
   }, &dummy);
 }
 

@@ -453,6 +453,58 @@ extern "C" int og_graph_save_bel(const og_graph *g, const char *prefix) {
   return ok ? OG_OK : fail(OG_E_IO, "writing %s.bel.* failed", prefix);
 }
 
+extern "C" int og_graph_set_symmetric(og_graph *g, int symmetric) {
+  clear_error();
+  if (!g || (symmetric != 0 && symmetric != 1)) return fail(OG_E_ARG, "og_graph_set_symmetric: bad argument");
+  g->symmetric = symmetric;
+  return OG_OK;
+}
+
+extern "C" int og_graph_symmetric(og_graph *g, int *symmetric) {
+  clear_error();
+  if (!g || !symmetric) return fail(OG_E_ARG, "og_graph_symmetric: null argument");
+  if (g->symmetric >= 0) {
+    *symmetric = g->symmetric;
+    return OG_OK;
+  }
+  const uint32_t V = g->V;
+  const uint32_t stride = g->kind == OG_GRAPH_WEIGHTED ? 2 : 1;
+  const uint32_t *ed = (const uint32_t *)g->edges;
+  const uint64_t *off = g->off;
+  std::atomic<int> bad{0};
+  const unsigned nt = hw_threads(0);
+  // sorted adjacency lists (strictly increasing columns)
+  parallel_for_threads(nt, [&](unsigned t, unsigned n) {
+    for (uint64_t u = (uint64_t)V * t / n, ue = (uint64_t)V * (t + 1) / n; u < ue && !bad.load(std::memory_order_relaxed); u++)
+      for (uint64_t e = off[u] + 1; e < off[u + 1]; e++)
+        if (ed[e * stride] <= ed[(e - 1) * stride]) {
+          bad.store(1);
+          break;
+        }
+  });
+  if (!bad.load()) {
+    parallel_for_threads(nt, [&](unsigned t, unsigned n) {
+      for (uint64_t u = (uint64_t)V * t / n, ue = (uint64_t)V * (t + 1) / n; u < ue && !bad.load(std::memory_order_relaxed); u++)
+        for (uint64_t e = off[u]; e < off[u + 1]; e++) {
+          const uint32_t v = ed[e * stride];
+          uint64_t lo = off[v], hi = off[v + 1];  // find u in adj(v)
+          while (lo < hi) {
+            const uint64_t mid = (lo + hi) / 2;
+            if (ed[mid * stride] < u) lo = mid + 1;
+            else hi = mid;
+          }
+          if (lo == off[v + 1] || ed[lo * stride] != u) {
+            bad.store(1);
+            break;
+          }
+        }
+    });
+  }
+  g->symmetric = bad.load() ? 0 : 1;
+  *symmetric = g->symmetric;
+  return OG_OK;
+}
+
 extern "C" int og_graph_records(og_graph *g, const uint32_t **words, uint64_t *nwords, uint32_t *bpe,
                                 uint32_t *bc, uint32_t *wmin) {
   clear_error();

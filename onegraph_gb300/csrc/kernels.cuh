@@ -1008,6 +1008,136 @@ __global__ void k_fill_u32(uint32_t *p, uint64_t n, uint32_t v) {
     p[i] = v;
 }
 
+// ------------------------------------------------------------ union-find CC
+//
+// Connected components of a symmetric graph by sampling union-find (the
+// Afforest scheme): hook every vertex with its first two neighbours, find the
+// giant component, then expand only the edges of vertices outside it.  A
+// root is hooked only under a smaller root (CAS on parent[hi] == hi), so
+// parent[x] <= x holds at all times and the root of every tree is the
+// smallest vertex id in it: after compression parent[] is exactly the
+// reference's CC label (minimum id of the component) with no relabelling.
+// Walks follow strictly decreasing ids, so they end within V steps; a broken
+// invariant sets kErrVertex instead of looping.
+
+__device__ __forceinline__ uint32_t uf_find(uint32_t *par, uint32_t x, uint32_t V, uint32_t *err) {
+  for (uint32_t steps = 0; steps <= V; steps++) {
+    const uint32_t p = __ldcg(par + x);
+    if (p == x) return x;
+    if (p > x) {
+      atomicOr(err, kErrVertex);
+      return x;
+    }
+    const uint32_t gp = __ldcg(par + p);
+    if (gp < p) __stcg(par + x, gp);  // path halving: gp is an ancestor of x
+    x = gp;
+  }
+  atomicOr(err, kErrVertex);
+  return x;
+}
+
+__device__ __forceinline__ void uf_link(uint32_t *par, uint32_t a, uint32_t b, uint32_t V, uint32_t *err) {
+  for (uint32_t tries = 0; tries <= V; tries++) {
+    const uint32_t ra = uf_find(par, a, V, err), rb = uf_find(par, b, V, err);
+    if (ra == rb) return;
+    const uint32_t hi = max(ra, rb), lo = min(ra, rb);
+    if (atomicCAS(par + hi, hi, lo) == hi) return;
+    a = ra;  // hi gained a parent meanwhile: retry from the two roots
+    b = rb;
+  }
+  atomicOr(err, kErrVertex);
+}
+
+// Sampling pass r: link every vertex of degree > r with its r-th neighbour
+// (edge off[v] + r, from the static region or from the host copy).
+template <class PS>
+__global__ void __launch_bounds__(kThreads) k_uf_sample(const uint64_t *off, uint32_t V, uint64_t static_edges,
+                                                        PS stat, PS host, uint32_t r, uint32_t *par,
+                                                        unsigned long long *reads, uint32_t *err) {
+  uint32_t nh = 0, ns = 0;  // records read from the host copy / the static region
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x) {
+    const uint64_t o = off[v];
+    if (off[v + 1] - o <= r) continue;
+    const uint64_t idx = o + r;
+    uint32_t u;
+    if (idx < static_edges) {
+      u = stat.load(idx);
+      ns++;
+    } else {
+      u = host.load(idx);
+      nh++;
+    }
+    if (u >= V) {
+      atomicOr(err, kErrVertex);
+      continue;
+    }
+    uf_link(par, (uint32_t)v, u, V, err);
+  }
+  nh = __reduce_add_sync(0xffffffffu, nh);
+  ns = __reduce_add_sync(0xffffffffu, ns);
+  if ((threadIdx.x & 31) == 0) {  // reads[0]: host records, reads[1]: static records
+    if (nh) atomicAdd(reads, (unsigned long long)nh);
+    if (ns) atomicAdd(reads + 1, (unsigned long long)ns);
+  }
+}
+
+// parent[v] = root of v for every vertex.
+__global__ void __launch_bounds__(kThreads) k_uf_compress(uint32_t *par, uint32_t V, uint32_t *err) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x)
+    __stcg(par + v, uf_find(par, (uint32_t)v, V, err));
+}
+
+// Roots of k pseudo-random vertices (after compression), for the host to
+// pick the most frequent one as the giant component.
+__global__ void k_uf_roots(const uint32_t *par, uint32_t V, uint32_t k, uint32_t *roots) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= k) return;
+  uint64_t z = 0x9e3779b97f4a7c15ull * (i + 1);
+  z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ull;
+  z = (z ^ (z >> 27)) * 0x94d049bb133111ebull;
+  z ^= z >> 31;
+  roots[i] = __ldcg(par + (uint32_t)(z % V));
+}
+
+// Frontier of the final pass: vertices of degree > 2 (their first two edges
+// are already linked) outside component c.  One thread per bitmap word.
+__global__ void __launch_bounds__(kThreads) k_uf_mark(const uint64_t *off, const uint32_t *par, uint32_t V,
+                                                      uint32_t c, uint32_t *bits, uint64_t nwords) {
+  for (uint64_t w = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; w < nwords; w += (uint64_t)gridDim.x * blockDim.x) {
+    uint32_t word = 0;
+    for (uint32_t b = 0; b < 32; b++) {
+      const uint64_t v = w * 32 + b;
+      if (v >= V) break;
+      if (off[v + 1] - off[v] > 2 && __ldcg(par + v) != c) word |= 1u << b;
+    }
+    bits[w] = word;
+  }
+}
+
+// LBS op of the final pass: link the source vertex with every neighbour.
+struct UnionOp {
+  using Val = uint32_t;
+  static constexpr bool kNeedVal = true;
+  uint32_t *par, *err;
+  uint32_t V;
+  __device__ uint32_t src_val(uint32_t v) const { return v; }
+  using Probe = uint32_t;  // the neighbour's parent (read early; links re-read it)
+  template <class Edge>
+  __device__ __forceinline__ Probe probe(Edge e) const {
+    const uint32_t v = edge_dst(e);
+    return v < V ? __ldcg(par + v) : 0u;
+  }
+  template <class Edge>
+  __device__ __forceinline__ void relax(Edge e, uint32_t sv, uint64_t, Probe) const {
+    const uint32_t v = edge_dst(e);
+    if (v >= V) {
+      atomicOr(err, kErrVertex);
+      return;
+    }
+    uf_link(par, sv, v, V, err);
+  }
+};
+
 __global__ void k_iota_u32(uint32_t *p, uint64_t n) {
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n;
        i += (uint64_t)gridDim.x * blockDim.x)

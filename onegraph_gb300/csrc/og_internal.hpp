@@ -20,6 +20,10 @@ struct og_graph {
   uint32_t *outdeg = nullptr;  // V (OG_GRAPH_PR only)
   int registered = 0;          // number of engines holding a registration
   bool host_pinned = false;    // allocated page-locked (cudaMallocHost)
+  // every edge (u, v) has its reverse (v, u): 1 yes, 0 no, -1 not known.
+  // Set by the symmetric R-MAT generator, asserted with og_graph_set_symmetric
+  // or checked by og_graph_symmetric; CC takes the union-find path only at 1.
+  int symmetric = -1;
   // Bit-packed edge records used by the engines (built once, on first use):
   // record e occupies bits [e*bpe, (e+1)*bpe) of the u32 word array `packed`
   // (little-endian bit order), low bc bits the column, the next bw bits the

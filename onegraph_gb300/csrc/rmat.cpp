@@ -106,6 +106,7 @@ extern "C" int og_rmat_generate(const og_rmat_params *p, og_graph **out) {
   const uint64_t E = ustart[nb];
   og_graph *g = graph_new((uint32_t)V, E, pr ? OG_GRAPH_PR : (weighted ? OG_GRAPH_WEIGHTED : OG_GRAPH_PLAIN));
   if (!g) return fail(OG_E_NOMEM, "cannot allocate host CSR (%llu edges)", (unsigned long long)E);
+  g->symmetric = sym ? 1 : -1;
   // 4. CSR: per-row counts, offsets, columns (and weights / out-degrees)
   std::vector<uint32_t> rowcnt(V, 0);
   if (pr) memset(g->outdeg, 0, 4 * V);

@@ -150,6 +150,7 @@ int rmat_generate_gpu(const og_rmat_params *p, og_graph **out) {
       rc = fail(OG_E_NOMEM, "cannot allocate host CSR (%llu edges)", (unsigned long long)E);
       goto done;
     }
+    g->symmetric = sym ? 1 : -1;
     GK(cudaMemcpyAsync(g->off, off_d, (V + 1) * 8, cudaMemcpyDeviceToHost, st));
     if (E) GK(cudaMemcpyAsync(g->edges, edges_d, E * (weighted ? 8 : 4), cudaMemcpyDeviceToHost, st));
     if (pr) GK(cudaMemcpyAsync(g->outdeg, outdeg_d, V * 4, cudaMemcpyDeviceToHost, st));

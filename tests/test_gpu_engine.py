@@ -57,6 +57,46 @@ def test_bfs_and_cc_match_reference_outputs(golden):
             e.close()
 
 
+def test_union_find_cc_matches_reference_outputs(golden):
+    """Sampling union-find CC (symmetric graphs) gives the reference CC/serial
+    labels on every golden graph and region layout; a symmetric R-MAT takes
+    it by default and agrees with label propagation."""
+    for n in golden_names(golden, "cc"):
+        g = og.Graph.from_arrays(golden[n + "/off"], golden[n + "/col"])
+        assert g.symmetric()  # exact check on first use
+        for cname, kw in configs(g):
+            e = engine(g, **kw)
+            assert e.get_param(og.PARAM_CC_METHOD) == og.CC_AUTO
+            np.testing.assert_array_equal(e.cc(), golden[n + "/cc"], err_msg="%s/%s auto" % (n, cname))
+            e.set_param(og.PARAM_CC_METHOD, og.CC_UNION_FIND)
+            np.testing.assert_array_equal(e.cc(), golden[n + "/cc"], err_msg="%s/%s uf" % (n, cname))
+            e.close()
+    for scale, kw in [(12, {}), (11, dict(weighted=True)), (12, dict(permute=False))]:
+        g = og.Graph.rmat(scale, 16, **kw)
+        for cname, ekw in configs(g):
+            e = engine(g, **ekw)
+            uf = e.cc()
+            st = e.stats
+            e.set_param(og.PARAM_CC_METHOD, og.CC_LABEL_PROPAGATION)
+            lp = e.cc()
+            np.testing.assert_array_equal(uf, lp, err_msg="rmat%d %s %s" % (scale, kw, cname))
+            np.testing.assert_array_equal(uf, oracle.cc(np.array(g.offsets), np.array(g.columns))[0])
+            assert st["link_bytes"] <= e.stats["link_bytes"]
+            e.close()
+
+
+def test_union_find_cc_needs_symmetry():
+    d = og.Graph.rmat(10, 16, pagerank=True, symmetric=False)
+    e = og.Engine(d, budget=1 << 28, advisek=1.0)
+    want, _ = oracle.cc(np.array(d.offsets), np.array(d.columns))
+    np.testing.assert_array_equal(e.cc(), want)  # auto: label propagation on a directed graph
+    e.set_param(og.PARAM_CC_METHOD, og.CC_UNION_FIND)
+    with pytest.raises(og.OGError) as ex:
+        e.cc()
+    assert ex.value.status == 1
+    e.close()
+
+
 def test_oom_configs_really_split_the_graph():
     g = og.Graph.rmat(12, 16)
     cfg = dict(configs(g))

@@ -341,3 +341,30 @@ def test_convert_uint_to_ulong(tmp_path):
     bad.write_bytes(np.array([V, E], np.uint32).tobytes() + off.tobytes())  # no edges
     with pytest.raises(og.OGError):
         og.convert_uint_to_ulong(str(bad), str(tmp_path / "x.lcsr"))
+
+
+def test_symmetry_flag_and_exact_check():
+    g = og.Graph.rmat(10, 16)  # symmetric generator: known without a check
+    assert g.symmetric()
+    d = og.Graph.rmat(10, 16, pagerank=True, symmetric=False)
+    assert not d.symmetric()
+    # loaded / built graphs are checked exactly: drop one reverse edge
+    off = np.array(g.offsets)
+    col = np.array(g.columns)
+    assert og.Graph.from_arrays(off, col).symmetric()
+    u = int(np.argmax(np.diff(off.astype(np.int64))))
+    keep = np.ones(col.size, bool)
+    keep[off[u]] = False  # remove u -> col[off[u]] but keep its reverse
+    off2 = off.copy()
+    off2[u + 1:] -= 1
+    assert not og.Graph.from_arrays(off2, col[keep]).symmetric()
+    # unsorted adjacency counts as not symmetric; an assertion overrides
+    col3 = col.copy()
+    col3[off[u]], col3[off[u] + 1] = col3[off[u] + 1], col3[off[u]]
+    g3 = og.Graph.from_arrays(off, col3)
+    assert not g3.symmetric()
+    g4 = og.Graph.from_arrays(off, col3)
+    g4.set_symmetric(True)
+    assert g4.symmetric()
+    w = og.Graph.rmat(9, 16, weighted=True)
+    assert og.Graph.from_arrays(np.array(w.offsets), np.array(w.edges), kind=og.WEIGHTED).symmetric()
