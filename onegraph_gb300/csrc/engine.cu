@@ -1047,7 +1047,15 @@ int pr_sums(og_engine *e, og_stats &st, Timing &tm) {
     }
     return (int)OG_OK;
   };
-  RC((run_regions<EKU>(e, st, tm, sfn, dfn)));
+  auto pfn = [&](const LbsArgs &a0, auto s0, const LbsArgs &a1, auto s1, cudaStream_t ps) {
+    const uint64_t n0 = lbs_grid(a0.pos_begin, a0.pos_end), n1 = lbs_grid(a1.pos_begin, a1.pos_end);
+    if (n0 + n1 > 0x7fffffffull) return fail(OG_E_STATE, "pull grid too large");
+    k_pr_pull_pair<decltype(s0), decltype(s1)><<<(unsigned)(n0 + n1), kThreads, 0, ps>>>(
+        a0, s0, args_for(0), a1, s1, args_for(1), n0, n0 + n1);
+    e->launches++;
+    return (int)OG_OK;
+  };
+  RC((run_regions<EKU>(e, st, tm, sfn, dfn, pfn)));
   for (int r = 0; r < 2; r++) {
     const Counts c = e->counts_h[r];
     if (!c.n) continue;

@@ -781,10 +781,8 @@ struct PrArgs {
 // memory in edge order and each vertex's segment is added sequentially, so the
 // result depends only on the tiling of the compacted list (deterministic).
 template <class Src>
-__global__ void __launch_bounds__(kThreads) k_pr_pull(LbsArgs a, Src src, PrArgs p) {
-  __shared__ LbsShared<uint32_t> sh;
-  __shared__ float s_c[kTile];
-  const uint64_t k = a.pos_begin / kTile + blockIdx.x;
+__device__ __forceinline__ void pr_tile(const LbsArgs &a, const Src &src, const PrArgs &p,
+                                        LbsShared<uint32_t> &sh, float *s_c, uint64_t k) {
   const uint64_t pos0 = k * kTile;
   if (pos0 >= a.pos_end) return;
   const uint64_t pend = min(pos0 + kTile, a.pos_end);
@@ -795,30 +793,97 @@ __global__ void __launch_bounds__(kThreads) k_pr_pull(LbsArgs a, Src src, PrArgs
   uint32_t i0;
   const uint32_t nl = lbs_setup<false>(a, nv, sh, k, pos0, i0);
   if (nl == 0) return;
+  // three phases, so that a thread keeps all eight record loads and then all
+  // eight contribution gathers in flight
+  uint32_t u[kItems];
 #pragma unroll
   for (int it = 0; it < (int)kItems; it++) {
     const uint32_t x = it * kThreads + threadIdx.x;
-    float c = 0.f;
+    u[it] = 0xffffffffu;  // no edge at this position
+    if (x < tlen) {
+      const uint64_t idx = sh.cb[sh.map[x]] + x;
+      if (idx < a.edge_bound) u[it] = edge_dst(src.load(idx));
+      else atomicOr(a.err, kErrEdgeIndex);
+    }
+  }
+  float c[kItems];
+#pragma unroll
+  for (int it = 0; it < (int)kItems; it++) {
+    c[it] = 0.f;
+    if (u[it] < p.V) c[it] = __ldg(p.contrib + u[it]);
+    else if (u[it] != 0xffffffffu) atomicOr(a.err, kErrVertex);
+  }
+#pragma unroll
+  for (int it = 0; it < (int)kItems; it++) s_c[it * kThreads + threadIdx.x] = c[it];
+  __syncthreads();
+  // Segmented reduction over the tile's positions: thread t sums positions
+  // [8t, 8t + 8) (restarting at every segment head), a block-wide segmented
+  // scan carries each thread's open segment into the next thread, and every
+  // segment's total is stored at its last position into s_tot[local vertex]
+  // (the per-vertex value table, unused by PageRank).  A high-degree vertex
+  // filling the tile is summed by all 256 threads instead of one.  The order
+  // of additions is fixed by the tiling, so sums are deterministic.
+  float *s_tot = reinterpret_cast<float *>(sh.val);
+  const uint32_t base = threadIdx.x * kItems;
+  float run = 0.f;
+  uint32_t head = 0;
+#pragma unroll
+  for (int it = 0; it < (int)kItems; it++) {
+    const uint32_t x = base + it;
+    if (x < tlen) {
+      if (x == 0 || sh.map[x] != sh.map[x - 1]) {
+        run = 0.f;
+        head = 1;
+      }
+      run += s_c[x];
+    }
+  }
+  // inclusive segmented scan of (head, run): (f1, v1) + (f2, v2) = (f1 | f2, f2 ? v2 : v1 + v2)
+  const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float iv = run;
+  uint32_t ifl = head;
+#pragma unroll
+  for (uint32_t d = 1; d < 32; d <<= 1) {
+    const float v2 = __shfl_up_sync(0xffffffffu, iv, d);
+    const uint32_t f2 = __shfl_up_sync(0xffffffffu, ifl, d);
+    if (lane >= d) {
+      if (!ifl) iv += v2;
+      ifl |= f2;
+    }
+  }
+  __shared__ float s_wv[kThreads / 32];
+  __shared__ uint32_t s_wf[kThreads / 32];
+  if (lane == 31) {
+    s_wv[warp] = iv;
+    s_wf[warp] = ifl;
+  }
+  __syncthreads();
+  // exclusive prefix of this thread: warps before it, then lanes before it
+  float cv = 0.f;
+  for (uint32_t w = 0; w < warp; w++) {
+    if (s_wf[w]) cv = s_wv[w];
+    else cv += s_wv[w];
+  }
+  const float lv = __shfl_up_sync(0xffffffffu, iv, 1);
+  const uint32_t lf = __shfl_up_sync(0xffffffffu, ifl, 1);
+  if (lane > 0) cv = lf ? lv : cv + lv;
+  run = cv;  // the open segment's sum before this thread's first position
+#pragma unroll
+  for (int it = 0; it < (int)kItems; it++) {
+    const uint32_t x = base + it;
     if (x < tlen) {
       const uint32_t l = sh.map[x];
-      const uint64_t idx = sh.cb[l] + x;
-      if (idx < a.edge_bound) {
-        const uint32_t u = edge_dst(src.load(idx));
-        if (u < p.V) c = __ldg(p.contrib + u);
-        else atomicOr(a.err, kErrVertex);
-      } else {
-        atomicOr(a.err, kErrEdgeIndex);
-      }
+      if (x == 0 || l != sh.map[x - 1]) run = 0.f;
+      run += s_c[x];
+      if (x + 1 == tlen || sh.map[x + 1] != l) s_tot[l] = run;
     }
-    s_c[x] = c;
   }
   __syncthreads();
   for (uint32_t j = threadIdx.x; j < nl; j += kThreads) {
     const uint32_t b = sh.rs[j];
     const uint32_t e = (j + 1 < nl) ? min(sh.rs[j + 1], tlen) : tlen;
     if (b >= e) continue;
-    float s = 0.f;
-    for (uint32_t x = b; x < e; x++) s += s_c[x];
+    const float s = s_tot[j];
     const uint32_t i = i0 + j;
     const bool before = (j == 0) && (a.pref[i] < pos0);
     const bool after = a.pref[i + 1] > pos0 + kTile;
@@ -831,6 +896,27 @@ __global__ void __launch_bounds__(kThreads) k_pr_pull(LbsArgs a, Src src, PrArgs
       p.sum[a.list[i]] = s;
     }
   }
+}
+
+template <class Src>
+__global__ void __launch_bounds__(kThreads) k_pr_pull(LbsArgs a, Src src, PrArgs p) {
+  __shared__ LbsShared<uint32_t> sh;
+  __shared__ float s_c[kTile];
+  pr_tile(a, src, p, sh, s_c, a.pos_begin / kTile + blockIdx.x);
+}
+
+// Both regions' pull sums in one launch, static and dynamic tiles interleaved
+// in CTA order as in k_lbs_pair (each region keeps its own carry arrays, so
+// the sums are the same as with two launches).
+template <class Src0, class Src1>
+__global__ void __launch_bounds__(kThreads) k_pr_pull_pair(LbsArgs a0, Src0 s0, PrArgs p0, LbsArgs a1, Src1 s1,
+                                                           PrArgs p1, uint64_t n0, uint64_t n) {
+  __shared__ LbsShared<uint32_t> sh;
+  __shared__ float s_c[kTile];
+  const uint64_t b = blockIdx.x;
+  const uint64_t lo = b * n0 / n, hi = (b + 1) * n0 / n;
+  if (hi > lo) pr_tile(a0, s0, p0, sh, s_c, a0.pos_begin / kTile + lo);
+  else pr_tile(a1, s1, p1, sh, s_c, a1.pos_begin / kTile + (b - hi));
 }
 
 // Completes the sums of vertices split over several tiles, in tile order.
