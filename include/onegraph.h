@@ -321,6 +321,16 @@ int og_engine_clone(og_engine *parent, og_engine **out);
 #define OG_CC_AUTO 0
 #define OG_CC_LABEL_PROPAGATION 1
 #define OG_CC_UNION_FIND 2
+/* OG_PARAM_BFS_DIRECTION: OG_BFS_AUTO (default) expands large BFS levels
+ *   bottom-up on graphs known to be symmetric: every unvisited vertex scans
+ *   its own neighbours and stops at the first one in the frontier (Beamer's
+ *   direction optimization: a level goes bottom-up when the frontier's edges
+ *   exceed the unexplored edges / 14, and back to top-down when the frontier
+ *   is below V / 24 and shrinking).  OG_BFS_TOP_DOWN expands every level from
+ *   the frontier, as the reference does.  Depths are identical either way. */
+#define OG_PARAM_BFS_DIRECTION 3
+#define OG_BFS_AUTO 0
+#define OG_BFS_TOP_DOWN 1
 int og_engine_set_param(og_engine *e, int param, double value);
 int og_engine_get_param(const og_engine *e, int param, double *value);
 

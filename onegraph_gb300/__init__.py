@@ -29,6 +29,8 @@ CFG_DIRECT, CFG_NO_PIN, CFG_PR, CFG_BATCH, CFG_BATCH_LEVELS, CFG_NO_STATIC = 1, 
 PARAM_SSSP_DELTA = 1
 PARAM_CC_METHOD = 2
 CC_AUTO, CC_LABEL_PROPAGATION, CC_UNION_FIND = 0, 1, 2
+PARAM_BFS_DIRECTION = 3
+BFS_AUTO, BFS_TOP_DOWN = 0, 1
 # R-MAT quadrant probabilities of the benchmark graphs
 RMAT_ABC = (0.57, 0.19, 0.19)
 

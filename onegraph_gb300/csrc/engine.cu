@@ -110,6 +110,7 @@ struct og_engine {
 
   uint32_t sssp_delta = 0;  // near/far split width (0: plain frontier relaxation)
   uint32_t cc_method = 0;   // OG_CC_AUTO / OG_CC_LABEL_PROPAGATION / OG_CC_UNION_FIND
+  uint32_t bfs_direction = 0;  // OG_BFS_AUTO / OG_BFS_TOP_DOWN
 
   int last_algo = -1;
   uint64_t launches = 0;  // kernels launched since the query began
@@ -368,6 +369,7 @@ int clone(og_engine *parent, og_engine *e) {
   e->tuned = parent->tuned;
   e->sssp_delta = parent->sssp_delta;
   e->cc_method = parent->cc_method;
+  e->bfs_direction = parent->bfs_direction;
   CK(cudaSetDevice(e->dev));
   RC(create_query_state(e));
   parent->clones++;
@@ -703,8 +705,48 @@ int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
   uint64_t thr = 1ull + e->sssp_delta;
   uint32_t far_min = 0xffffffffu;
   bool advance = false;
+  // Direction-optimizing BFS (symmetric graphs): a level is expanded bottom-up
+  // when its frontier's edges exceed unexplored / kAlpha (unexplored = the
+  // degrees of the vertices that have not been a frontier yet), and top-down
+  // again once the frontier falls below V / kBeta while shrinking.
+  constexpr uint64_t kAlpha = 14, kBeta = 24;
+  const bool dopt = algo == OG_ALGO_BFS && e->bfs_direction == OG_BFS_AUTO && e->g->symmetric == 1;
+  uint64_t unexplored = e->g->E;
+  bool bottom = false, counted = false;
+  uint64_t fn = 0;  // frontier size when it came from a bottom-up level
   for (;;) {
     uint64_t n = 0;
+    if (dopt && bottom) {
+      unsigned long long *cnt = e->sum64_d;  // reached, their degrees, host records, static records
+      CK(cudaMemsetAsync(cnt, 0, 32, s));  // next is all zero here, as at every level start
+      CK(cudaEventRecord(e->t_d0, s));
+      k_bfs_bottom_up<EKU::PSrc><<<grid_for(V, e->sms), kThreads, 0, s>>>(
+          e->off_d, (uint32_t)V, e->Vs, EKU::stat(e), EKU::host(e), cur, e->bm[2], next, e->value_d,
+          ro.level + 1, cnt, e->err_d);
+      e->launches++;
+      CK(cudaEventRecord(e->ev_dyn_done, s));
+      unsigned long long c4[4];
+      CK(cudaMemcpyAsync(c4, cnt, 32, cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(e->err_h, e->err_d, 4, cudaMemcpyDeviceToHost, s));
+      CK(cudaStreamSynchronize(s));
+      RC(check_device_error(e));
+      float ms = 0;
+      if (cudaEventElapsedTime(&ms, e->t_d0, e->ev_dyn_done) == cudaSuccess) st.ms_dynamic += ms;
+      st.iterations++;
+      st.frontier_sum += fn;
+      st.edges_dynamic += c4[2];
+      st.edges_static += c4[3];
+      st.link_bytes += (c4[2] * e->bpe + 7) / 8;
+      unexplored -= std::min<uint64_t>(unexplored, c4[1]);
+      std::swap(cur, next);
+      CK(cudaMemsetAsync(next, 0, 4 * e->nwords, s));  // the level just expanded
+      ro.level++;
+      if (c4[0] == 0) break;
+      if (c4[0] < V / kBeta && c4[0] < fn) bottom = false;  // next level: compaction + top-down
+      fn = c4[0];
+      counted = true;
+      continue;
+    }
     SplitArgs sp;
     sp.on = split;
     sp.thr = (uint32_t)std::min<uint64_t>(thr, 0xffffffffull);
@@ -722,6 +764,17 @@ int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
       continue;
     }
     advance = false;
+    if (dopt) {
+      const uint64_t mf = e->counts_h[0].total + e->counts_h[1].total;
+      if (!counted) unexplored -= std::min(unexplored, mf);
+      counted = false;
+      if (mf > unexplored / kAlpha) {  // expand this frontier bottom-up
+        bottom = true;
+        fn = n;
+        counted = true;
+        continue;
+      }
+    }
     st.iterations++;
     st.frontier_sum += n;
     st.static_vertices += e->counts_h[0].n;
@@ -1241,6 +1294,11 @@ extern "C" int og_engine_set_param(og_engine *e, int param, double value) {
     e->cc_method = (uint32_t)value;
     return OG_OK;
   }
+  if (param == OG_PARAM_BFS_DIRECTION) {
+    if (value != OG_BFS_AUTO && value != OG_BFS_TOP_DOWN) return fail(OG_E_ARG, "unknown BFS direction %g", value);
+    e->bfs_direction = (uint32_t)value;
+    return OG_OK;
+  }
   return fail(OG_E_ARG, "unknown parameter %d", param);
 }
 
@@ -1252,6 +1310,10 @@ extern "C" int og_engine_get_param(const og_engine *e, int param, double *value)
   }
   if (param == OG_PARAM_CC_METHOD) {
     *value = e->cc_method;
+    return OG_OK;
+  }
+  if (param == OG_PARAM_BFS_DIRECTION) {
+    *value = e->bfs_direction;
     return OG_OK;
   }
   return fail(OG_E_ARG, "unknown parameter %d", param);

@@ -1094,6 +1094,80 @@ __global__ void k_fill_u32(uint32_t *p, uint64_t n, uint32_t v) {
     p[i] = v;
 }
 
+// ---------------------------------------------------------- bottom-up BFS
+//
+// One bottom-up level of a direction-optimizing BFS (Beamer et al., 2012)
+// on a symmetric graph: every unvisited vertex scans its own neighbours, four
+// records at a time, and stops at the first one in the current frontier; it
+// then gets depth newdepth and joins the next frontier.  Valid because the
+// graph is symmetric (a neighbour u of v has the edge u -> v).  The depths
+// equal the top-down ones: a vertex is reached at level L + 1 exactly when
+// one of its neighbours has depth L.  Warps cover 32 consecutive vertices
+// (one bitmap word), so each word of next / visited has a single writer.
+// cnt[0] += vertices reached, cnt[1] += their degrees, cnt[2] += records read
+// from the host copy, cnt[3] += records read from the static region.
+template <class PS>
+__global__ void __launch_bounds__(kThreads) k_bfs_bottom_up(const uint64_t *off, uint32_t V, uint32_t Vs, PS stat,
+                                                            PS host, const uint32_t *cur, uint32_t *visited,
+                                                            uint32_t *next, uint32_t *depth, uint32_t newdepth,
+                                                            unsigned long long *cnt, uint32_t *err) {
+  const uint32_t lane = threadIdx.x & 31;
+  unsigned long long nn = 0, nm = 0, nh = 0, ns = 0;
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t base = (uint64_t)blockIdx.x * blockDim.x + (threadIdx.x & ~31u); base < V; base += stride) {
+    const uint64_t v = base + lane;
+    const uint32_t w = (uint32_t)(base >> 5);
+    const uint32_t vis = __ldcg(visited + w);
+    bool found = false;
+    uint64_t d = 0;
+    if (v < V && !((vis >> lane) & 1u)) {
+      const uint64_t o = off[v], e1 = off[v + 1];
+      d = e1 - o;
+      const bool st = v < Vs;
+      const PS &src = st ? stat : host;
+      for (uint64_t e = o; e < e1 && !found; e += 4) {
+        uint32_t u[4];
+#pragma unroll
+        for (int j = 0; j < 4; j++) u[j] = e + j < e1 ? src.load(e + j) : 0xffffffffu;
+        const uint64_t got = (e1 - e < 4) ? e1 - e : 4;
+        if (st) ns += got;
+        else nh += got;
+#pragma unroll
+        for (int j = 0; j < 4; j++) {
+          if (u[j] < V) {
+            if ((__ldcg(cur + (u[j] >> 5)) >> (u[j] & 31)) & 1u) found = true;
+          } else if (u[j] != 0xffffffffu) {
+            atomicOr(err, kErrVertex);
+          }
+        }
+      }
+    }
+    const uint32_t ball = __ballot_sync(0xffffffffu, found);
+    if (lane == 0 && ball) {
+      next[w] = ball;
+      visited[w] = vis | ball;
+    }
+    if (found) {
+      depth[v] = newdepth;
+      nn++;
+      nm += d;
+    }
+  }
+  nn = __reduce_add_sync(0xffffffffu, (uint32_t)nn);
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    nm += __shfl_xor_sync(0xffffffffu, nm, o);
+    nh += __shfl_xor_sync(0xffffffffu, nh, o);
+    ns += __shfl_xor_sync(0xffffffffu, ns, o);
+  }
+  if (lane == 0) {
+    if (nn) atomicAdd(cnt, nn);
+    if (nm) atomicAdd(cnt + 1, nm);
+    if (nh) atomicAdd(cnt + 2, nh);
+    if (ns) atomicAdd(cnt + 3, ns);
+  }
+}
+
 // ------------------------------------------------------------ union-find CC
 //
 // Connected components of a symmetric graph by sampling union-find (the

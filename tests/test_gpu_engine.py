@@ -104,6 +104,7 @@ def test_oom_configs_really_split_the_graph():
     p = e.plan
     assert 0 < p["static_edges"] < g.E and p["chunk_edges"] < p["dynamic_edges"]
     src = int(np.argmax(g.degrees()))
+    e.set_param(og.PARAM_BFS_DIRECTION, og.BFS_TOP_DOWN)  # the staged top-down path is under test
     e.bfs(src)
     st = e.stats
     assert st["chunks"] > st["iterations"]  # several chunks in some round
@@ -281,4 +282,38 @@ def test_sssp_delta_default_and_roundtrip():
     c = e.clone()
     assert c.get_param(og.PARAM_SSSP_DELTA) == 0
     c.close()
+    e.close()
+
+
+def test_direction_optimizing_bfs_matches_top_down():
+    """Bottom-up levels (symmetric graphs, the default) give the same depths as
+    the reference's top-down expansion in every region layout, and read fewer
+    edges on an R-MAT graph."""
+    for scale, kw in [(14, {}), (13, dict(weighted=True)), (12, dict(permute=False))]:
+        g = og.Graph.rmat(scale, 16, **kw)
+        off = np.array(g.offsets)
+        col = np.array(g.edges)[:, 0].copy() if g.kind == og.WEIGHTED else np.array(g.columns)
+        deg = np.diff(off.astype(np.int64))
+        srcs = [int(np.argmax(deg)), int(np.nonzero(deg)[0][7]), 3]
+        for cname, ekw in configs(g):
+            e = engine(g, **ekw)
+            assert e.get_param(og.PARAM_BFS_DIRECTION) == og.BFS_AUTO
+            for s in srcs:
+                d = e.bfs(s)
+                auto = dict(e.stats)
+                np.testing.assert_array_equal(oracle.normalise_bfs(d, g.V), oracle.bfs(off, col, s)[0],
+                                              err_msg="rmat%d %s %s src %d" % (scale, kw, cname, s))
+                e.set_param(og.PARAM_BFS_DIRECTION, og.BFS_TOP_DOWN)
+                np.testing.assert_array_equal(e.bfs(s), d)
+                td = dict(e.stats)
+                e.set_param(og.PARAM_BFS_DIRECTION, og.BFS_AUTO)
+                assert auto["iterations"] == td["iterations"]
+                if s == srcs[0] and deg[s] > 0:
+                    assert auto["edges_static"] + auto["edges_dynamic"] < td["edges_static"] + td["edges_dynamic"]
+            e.close()
+    # a directed graph is never expanded bottom-up
+    dg = og.Graph.rmat(11, 16, pagerank=True, symmetric=False)
+    e = og.Engine(dg, budget=1 << 28, advisek=1.0)
+    doff, dcol = np.array(dg.offsets), np.array(dg.columns)
+    np.testing.assert_array_equal(oracle.normalise_bfs(e.bfs(5), dg.V), oracle.bfs(doff, dcol, 5)[0])
     e.close()
