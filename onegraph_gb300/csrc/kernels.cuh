@@ -418,9 +418,27 @@ struct LbsShared {
   unsigned short map[kTile];   // tile position -> local vertex
 };
 
+// Shared tables of a PageRank pull tile, aliased by phase to fit 6 CTAs per
+// SM: the tile-relative starts (rs) are dead once the position map is built
+// and then hold the per-position contributions; the edge bases (cb) are dead
+// once every record load is issued and then hold the per-vertex sums.
+struct PrShared {
+  union {
+    uint32_t rs[kTile + 2];
+    float c[kTile + 2];
+  };
+  union {
+    unsigned long long cb[kTile + 1];
+    float tot[kTile + 1];
+  };
+  uint32_t val[1];  // no source value in PageRank (lbs_setup<false> never writes it)
+  unsigned short map[kTile];
+};
+
 // Builds the local-vertex tables of tile k; returns the local count (0 on error).
-template <bool kNeedVal, class Op, class Val>
-__device__ __forceinline__ uint32_t lbs_setup(const LbsArgs &a, const Op &op, LbsShared<Val> &sh,
+// Sh is LbsShared<Val> or PrShared.
+template <bool kNeedVal, class Op, class Sh>
+__device__ __forceinline__ uint32_t lbs_setup(const LbsArgs &a, const Op &op, Sh &sh,
                                               uint64_t k, uint64_t pos0, uint32_t &i0_out) {
   const uint64_t ntiles_total = (a.total + kTile - 1) / kTile;
   const uint32_t i0 = a.tile_first[k];
@@ -438,7 +456,7 @@ __device__ __forceinline__ uint32_t lbs_setup(const LbsArgs &a, const Op &op, Lb
     sh.rs[j] = p > pos0 ? (uint32_t)min(p - pos0, (uint64_t)kTile) : 0u;
     const uint64_t src = a.off ? a.off[v] - p : (0ull - a.stage_base);
     sh.cb[j] = src + pos0;
-    if (kNeedVal) sh.val[j] = op.src_val(v);
+    if constexpr (kNeedVal) sh.val[j] = op.src_val(v);
   }
   for (uint32_t x = threadIdx.x; x < kTile; x += kThreads) sh.map[x] = 0;
   __syncthreads();
@@ -781,8 +799,9 @@ struct PrArgs {
 // memory in edge order and each vertex's segment is added sequentially, so the
 // result depends only on the tiling of the compacted list (deterministic).
 template <class Src>
-__device__ __forceinline__ void pr_tile(const LbsArgs &a, const Src &src, const PrArgs &p,
-                                        LbsShared<uint32_t> &sh, float *s_c, uint64_t k) {
+__device__ __forceinline__ void pr_tile(const LbsArgs &a, const Src &src, const PrArgs &p, PrShared &sh,
+                                        uint64_t k) {
+  float *s_c = sh.c;
   const uint64_t pos0 = k * kTile;
   if (pos0 >= a.pos_end) return;
   const uint64_t pend = min(pos0 + kTile, a.pos_end);
@@ -823,7 +842,7 @@ __device__ __forceinline__ void pr_tile(const LbsArgs &a, const Src &src, const 
   // (the per-vertex value table, unused by PageRank).  A high-degree vertex
   // filling the tile is summed by all 256 threads instead of one.  The order
   // of additions is fixed by the tiling, so sums are deterministic.
-  float *s_tot = reinterpret_cast<float *>(sh.val);
+  float *s_tot = sh.tot;
   const uint32_t base = threadIdx.x * kItems;
   float run = 0.f;
   uint32_t head = 0;
@@ -880,11 +899,9 @@ __device__ __forceinline__ void pr_tile(const LbsArgs &a, const Src &src, const 
   }
   __syncthreads();
   for (uint32_t j = threadIdx.x; j < nl; j += kThreads) {
-    const uint32_t b = sh.rs[j];
-    const uint32_t e = (j + 1 < nl) ? min(sh.rs[j + 1], tlen) : tlen;
-    if (b >= e) continue;
-    const float s = s_tot[j];
     const uint32_t i = i0 + j;
+    if (j > 0 && a.pref[i] >= pend) continue;  // starts in the next tile: no position here
+    const float s = s_tot[j];
     const bool before = (j == 0) && (a.pref[i] < pos0);
     const bool after = a.pref[i + 1] > pos0 + kTile;
     if (before) {
@@ -899,24 +916,22 @@ __device__ __forceinline__ void pr_tile(const LbsArgs &a, const Src &src, const 
 }
 
 template <class Src>
-__global__ void __launch_bounds__(kThreads) k_pr_pull(LbsArgs a, Src src, PrArgs p) {
-  __shared__ LbsShared<uint32_t> sh;
-  __shared__ float s_c[kTile];
-  pr_tile(a, src, p, sh, s_c, a.pos_begin / kTile + blockIdx.x);
+__global__ void __launch_bounds__(kThreads, 6) k_pr_pull(LbsArgs a, Src src, PrArgs p) {
+  __shared__ PrShared sh;
+  pr_tile(a, src, p, sh, a.pos_begin / kTile + blockIdx.x);
 }
 
 // Both regions' pull sums in one launch, static and dynamic tiles interleaved
 // in CTA order as in k_lbs_pair (each region keeps its own carry arrays, so
 // the sums are the same as with two launches).
 template <class Src0, class Src1>
-__global__ void __launch_bounds__(kThreads) k_pr_pull_pair(LbsArgs a0, Src0 s0, PrArgs p0, LbsArgs a1, Src1 s1,
-                                                           PrArgs p1, uint64_t n0, uint64_t n) {
-  __shared__ LbsShared<uint32_t> sh;
-  __shared__ float s_c[kTile];
+__global__ void __launch_bounds__(kThreads, 6) k_pr_pull_pair(LbsArgs a0, Src0 s0, PrArgs p0, LbsArgs a1,
+                                                              Src1 s1, PrArgs p1, uint64_t n0, uint64_t n) {
+  __shared__ PrShared sh;
   const uint64_t b = blockIdx.x;
   const uint64_t lo = b * n0 / n, hi = (b + 1) * n0 / n;
-  if (hi > lo) pr_tile(a0, s0, p0, sh, s_c, a0.pos_begin / kTile + lo);
-  else pr_tile(a1, s1, p1, sh, s_c, a1.pos_begin / kTile + (b - hi));
+  if (hi > lo) pr_tile(a0, s0, p0, sh, a0.pos_begin / kTile + lo);
+  else pr_tile(a1, s1, p1, sh, a1.pos_begin / kTile + (b - hi));
 }
 
 // Completes the sums of vertices split over several tiles, in tile order.
