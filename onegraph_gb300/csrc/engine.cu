@@ -293,6 +293,13 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
                           cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
   CK(cudaFuncSetAttribute(k_gather<SrcP<true>, DstW<uint32_t>, kGatherMult>,
                           cudaFuncAttributeMaxDynamicSharedMemorySize, gsm));
+  // The SSSP relax reads each packed record as two overlapping words; the
+  // second mostly hits L1, so it runs best with a large L1: 58 % of the
+  // unified L1/shared storage as shared memory (3 CTAs of 38 KB per SM,
+  // ~124 KB of L1).  Measured on R-MAT 27: 9.55 queries/s with the driver's
+  // choice, 9.85 at 58 %, 6.77 at 86 %, 8.06 at 30 %.
+  CK(cudaFuncSetAttribute(k_lbs_pair<SrcP<true>, SrcP<true>, MinOp<true>>,
+                          cudaFuncAttributePreferredSharedMemoryCarveout, 58));
 
   // host CSR: page-lock so kernels can gather from it over the link
   if (P.dynamic_edges > 0) {
