@@ -1661,6 +1661,7 @@ int compact_args_ok(const uint32_t *bits, uint32_t v_begin, uint32_t v_end, cons
   if (v_end < v_begin) return fail(OG_E_ARG, "og_k_compact: v_end < v_begin");
   if (list_cap == 0 || tile_cap == 0) return fail(OG_E_ARG, "og_k_compact: zero capacity");
   static_assert(sizeof(og_counts) == sizeof(Counts), "og_counts layout");
+  static_assert(kCompactWords == kWordsPerCompactTile, "planner and kernel compaction tiles differ");
   return OG_OK;
 }
 

@@ -89,7 +89,7 @@ uint64_t engine_vertex_bytes(int kind, uint32_t flags);
 uint64_t engine_fixed_bytes(uint32_t V, uint64_t E, uint32_t flags);
 
 constexpr uint32_t kLbsTile = 2048;          // edge positions per LBS tile
-constexpr uint32_t kCompactWords = 256;      // bitmap words per compaction tile
+constexpr uint32_t kCompactWords = 1024;     // bitmap words per compaction tile (kWordsPerCompactTile)
 constexpr uint64_t kMinChunkEdges = 1u << 20;  // smallest staging buffer
 constexpr uint64_t kDefaultBudget = 12ull << 30;  // GraphMeta.h:305
 
