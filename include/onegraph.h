@@ -331,6 +331,14 @@ int og_engine_clone(og_engine *parent, og_engine **out);
 #define OG_PARAM_BFS_DIRECTION 3
 #define OG_BFS_AUTO 0
 #define OG_BFS_TOP_DOWN 1
+/* OG_PARAM_LEVEL_LOOP: OG_LOOP_AUTO (default) runs og_bfs's levels from two
+ *   CUDA graphs replayed back to back, with every per-level decision taken by
+ *   kernels (direct mode or a fully resident graph; staged engines keep the
+ *   host loop); the host checks for the end every few levels.  OG_LOOP_HOST
+ *   waits for each level's counts on the host.  Depths are identical. */
+#define OG_PARAM_LEVEL_LOOP 4
+#define OG_LOOP_AUTO 0
+#define OG_LOOP_HOST 1
 int og_engine_set_param(og_engine *e, int param, double value);
 int og_engine_get_param(const og_engine *e, int param, double *value);
 

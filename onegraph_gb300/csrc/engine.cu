@@ -19,6 +19,7 @@
 #include <vector>
 
 #include "batch_persist.cuh"
+#include "bfs_loop.cuh"
 #include "kernels.cuh"
 #include "og_internal.hpp"
 
@@ -99,6 +100,14 @@ struct og_engine {
   uint32_t *pmisc_h = nullptr;  // host copy of bar_d
   int tuned = -1;               // index into kPersistConfigs chosen by the autotuner
   cudaGraphExec_t graph = nullptr;
+  // device-driven BFS level loop: state, its host mirror, one graph per
+  // frontier parity (captured for the direction mode `bfs_exec_dopt`)
+  BfsLoop *loop_d = nullptr, *loop_h = nullptr;
+  cudaGraphExec_t bfs_exec[2] = {nullptr, nullptr};
+  int bfs_exec_dopt = -1;
+  uint32_t dev_epoch = 1u << 29;  // epochs of device-driven compactions: [2^29, 2^30)
+  uint32_t bfs_levels_hint = 4;   // levels of the last BFS (launched before the first check)
+  uint32_t level_loop = 0;        // OG_LOOP_AUTO / OG_LOOP_HOST
   uint32_t graph_n = 0;
   int graph_cfg = -1;
   bool graph_broken = false;
@@ -154,6 +163,9 @@ void destroy(og_engine *e) {
   if (e->srcs_h) cudaFreeHost(e->srcs_h);
   if (e->pmisc_h) cudaFreeHost(e->pmisc_h);
   if (e->graph) cudaGraphExecDestroy(e->graph);
+  for (int p = 0; p < 2; p++)
+    if (e->bfs_exec[p]) cudaGraphExecDestroy(e->bfs_exec[p]);
+  if (e->loop_h) cudaFreeHost(e->loop_h);
   if (e->err_h) cudaFreeHost(e->err_h);
   if (e->l1_h) cudaFreeHost(e->l1_h);
   cudaEvent_t evs[] = {e->ev_round, e->ev_cs, e->ev_cd, e->ev_dyn_done, e->ev_gat[0], e->ev_gat[1],
@@ -218,6 +230,8 @@ int create_query_state(og_engine *e) {
   e->active_d = e->err_d + 1;
   RC(dalloc(e, &e->sum64_d, 3ull * e->sms * 8 + 4));
   CK(cudaMallocHost(&e->counts_h, 3 * sizeof(Counts)));
+  RC(dalloc(e, (char **)&e->loop_d, sizeof(BfsLoop)));
+  CK(cudaMallocHost(&e->loop_h, sizeof(BfsLoop)));
   CK(cudaMallocHost(&e->err_h, 4 * sizeof(uint32_t)));
   CK(cudaMallocHost(&e->l1_h, sizeof(double)));
   if (P.chunk_edges && !(e->cfg.flags & OG_CFG_DIRECT)) {
@@ -383,6 +397,7 @@ int clone(og_engine *parent, og_engine *e) {
   e->sssp_delta = parent->sssp_delta;
   e->cc_method = parent->cc_method;
   e->bfs_direction = parent->bfs_direction;
+  e->level_loop = parent->level_loop;
   CK(cudaSetDevice(e->dev));
   RC(create_query_state(e));
   parent->clones++;
@@ -395,6 +410,9 @@ int clone(og_engine *parent, og_engine *e) {
 // waiting ones go to far_bits (when not null) and their minimum to the
 // region's Counts::far_min; listed ones are cleared from clear_bits.
 struct SplitArgs {
+  // device-driven loops: epoch read from device memory, launch gated by a flag
+  const uint32_t *epoch_ptr = nullptr;
+  const uint32_t *run_flag = nullptr;
   bool on = false;
   uint32_t thr = 0;
   uint32_t *far_bits = nullptr;
@@ -407,7 +425,7 @@ int launch_compact(og_engine *e, int r, const uint32_t *bits, uint32_t vb, uint3
     CK(cudaMemsetAsync(e->counts_d + r, 0, sizeof(Counts), s));
     return OG_OK;
   }
-  CompactArgs a;
+  CompactArgs a{};
   a.bits = bits;
   a.v_begin = vb;
   a.v_end = ve;
@@ -430,6 +448,8 @@ int launch_compact(og_engine *e, int r, const uint32_t *bits, uint32_t vb, uint3
   a.far_key = (unsigned long long *)(e->counts_d + 2) + r;
   a.clear_bits = sp.clear_bits;
   a.epoch = e->epoch;
+  a.epoch_ptr = sp.epoch_ptr;
+  a.run_flag = sp.run_flag;
   if (a.ntiles + 1 > e->lb_tiles) return fail(OG_E_STATE, "compaction scratch too small");
   k_compact<<<a.ntiles, kThreads, 0, s>>>(a);
   e->launches++;
@@ -809,6 +829,122 @@ int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
   CK(cudaMemcpy(e->err_h, e->err_d, 4, cudaMemcpyDeviceToHost));
   RC(check_device_error(e));
   e->last_algo = algo;
+  return OG_OK;
+}
+
+// ------------------------------------------------------- device-driven BFS
+
+// Captures one BFS level for the frontier in bm[p] (next in bm[1 - p]).
+int capture_bfs_level(og_engine *e, int p, int dopt, cudaGraphExec_t *out) {
+  cudaStream_t s = e->s_main;
+  uint32_t *cur = e->bm[p], *next = e->bm[1 - p];
+  BfsLoop *L = e->loop_d;
+  cudaGraph_t gr = nullptr;
+  const uint64_t before = e->launches;
+  int per_sm = 0;  // fixed grid of the top-down relax: every CTA resident
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lbs_pair_dev<EKU::PSrc, EKU::PSrc>, kThreads, 0));
+  const unsigned grid = (unsigned)std::max(1, per_sm) * (unsigned)e->sms;
+  CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  int rc = OG_OK;
+  auto body = [&]() -> int {
+    SplitArgs sp;
+    sp.epoch_ptr = &L->epoch;
+    sp.run_flag = &L->compact_go;
+    CK(cudaEventRecord(e->ev_round, s));
+    CK(cudaStreamWaitEvent(e->s_dyn, e->ev_round, 0));
+    RC(launch_compact(e, 0, cur, 0, e->Vs, s, sp));
+    RC(launch_compact(e, 1, cur, e->Vs, e->V, e->s_dyn, sp));
+    CK(cudaEventRecord(e->ev_cd, e->s_dyn));
+    CK(cudaStreamWaitEvent(s, e->ev_cd, 0));
+    k_bfs_ctl_mid<<<1, 32, 0, s>>>(L, e->counts_d, dopt);
+    BfsOp op{e->bm[2], next, e->value_d, e->err_d, e->V, 0};
+    k_lbs_pair_dev<EKU::PSrc, EKU::PSrc><<<grid, kThreads, 0, s>>>(
+        lbs_args(e, 0, 0, 0, true, e->plan.static_edges), EKU::stat(e), lbs_args(e, 1, 0, 0, true, e->g->E),
+        EKU::host(e), op, e->counts_d, &L->td_go, &L->level);
+    k_bfs_bottom_up<EKU::PSrc><<<grid_for(e->V, e->sms), kThreads, 0, s>>>(
+        e->off_d, e->V, e->Vs, EKU::stat(e), EKU::host(e), cur, e->bm[2], next, e->value_d, 0, L->bu,
+        e->err_d, &L->bu_go, &L->level);
+    k_bfs_ctl_end<<<1, 32, 0, s>>>(L, e->V);
+    CK(cudaMemsetAsync(cur, 0, 4 * e->nwords, s));  // the expanded frontier: next level's "next"
+    return OG_OK;
+  };
+  rc = body();
+  const cudaError_t ce = cudaStreamEndCapture(s, &gr);
+  e->launches = before;  // captured, not launched
+  if (rc != OG_OK || ce != cudaSuccess) {
+    if (gr) cudaGraphDestroy(gr);
+    cudaGetLastError();
+    return rc != OG_OK ? rc : fail(OG_E_CUDA, "BFS level capture: %s", cudaGetErrorString(ce));
+  }
+  const cudaError_t ie = cudaGraphInstantiate(out, gr, 0);
+  cudaGraphDestroy(gr);
+  if (ie != cudaSuccess) return fail(OG_E_CUDA, "BFS level graph: %s", cudaGetErrorString(ie));
+  return OG_OK;
+}
+
+// Single-source BFS with the device-driven level loop (see bfs_loop.cuh):
+// the two level graphs alternate; the host checks the done flag after as many
+// levels as the previous query took, then every two levels.
+int run_bfs_dev(og_engine *e, uint32_t src, og_stats &st) {
+  const uint64_t V = e->V;
+  cudaStream_t s = e->s_main;
+  const int g = grid_for(V, e->sms);
+  const int dopt = e->bfs_direction == OG_BFS_AUTO && e->g->symmetric == 1;
+  if (dopt != e->bfs_exec_dopt) {
+    for (int p = 0; p < 2; p++)
+      if (e->bfs_exec[p]) {
+        cudaGraphExecDestroy(e->bfs_exec[p]);
+        e->bfs_exec[p] = nullptr;
+      }
+    for (int p = 0; p < 2; p++) RC(capture_bfs_level(e, p, dopt, &e->bfs_exec[p]));
+    e->bfs_exec_dopt = dopt;
+  }
+  if (e->dev_epoch > (1u << 30) - (1u << 20)) {  // epoch wrap: clear the status words once
+    for (int r = 0; r < 2; r++)
+      CK(cudaMemsetAsync(e->lb[r].status, 0, sizeof(uint32_t) * e->lb_tiles, s));
+    e->dev_epoch = 1u << 29;
+  }
+  CK(cudaMemsetAsync(e->err_d, 0, 16, s));
+  CK(cudaMemsetAsync(e->bm[0], 0, 4 * e->nwords, s));
+  CK(cudaMemsetAsync(e->bm[1], 0, 4 * e->nwords, s));
+  CK(cudaMemsetAsync(e->bm[2], 0, 4 * e->nwords, s));
+  k_fill_u32<<<g, kThreads, 0, s>>>(e->value_d, V, (uint32_t)(V + 1));  // GraphMeta.h:378
+  k_set_source<<<1, 1, 0, s>>>(e->value_d, src, 1u, e->bm[0], e->bm[2]);
+  BfsLoop &h = *e->loop_h;
+  memset(&h, 0, sizeof h);
+  h.level = 1;
+  h.need_compact = 1;
+  h.compact_go = 1;
+  h.epoch = e->dev_epoch;
+  h.unexplored = e->g->E;
+  CK(cudaMemcpyAsync(e->loop_d, &h, sizeof h, cudaMemcpyHostToDevice, s));
+  CK(cudaEventRecord(e->t_d0, s));
+  uint32_t launched = 0, batch = std::max<uint32_t>(2, e->bfs_levels_hint + 1);
+  for (;;) {
+    for (uint32_t i = 0; i < batch; i++, launched++) CK(cudaGraphLaunch(e->bfs_exec[launched & 1], s));
+    CK(cudaMemcpyAsync(&h.done, &e->loop_d->done, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (h.done) break;
+    if (launched > 4 * V + 64) return fail(OG_E_STATE, "BFS did not end after %u levels", launched);
+    batch = 2;
+  }
+  CK(cudaEventRecord(e->ev_dyn_done, s));
+  CK(cudaMemcpyAsync(&h, e->loop_d, sizeof h, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(e->err_h, e->err_d, 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  RC(check_device_error(e));
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, e->t_d0, e->ev_dyn_done) == cudaSuccess) st.ms_dynamic += ms;
+  st.iterations += (uint32_t)h.iterations;
+  st.frontier_sum += h.frontier_sum;
+  st.edges_static += h.edges_static;
+  st.edges_dynamic += h.edges_dynamic;
+  st.link_bytes += (h.edges_dynamic * e->bpe + 7) / 8;
+  st.chunks += (uint32_t)h.iterations;
+  e->launches += 2 + 7ull * launched;
+  e->bfs_levels_hint = (uint32_t)h.iterations;
+  e->dev_epoch = h.epoch + 1;
+  e->last_algo = OG_ALGO_BFS;
   return OG_OK;
 }
 
@@ -1312,6 +1448,11 @@ extern "C" int og_engine_set_param(og_engine *e, int param, double value) {
     e->bfs_direction = (uint32_t)value;
     return OG_OK;
   }
+  if (param == OG_PARAM_LEVEL_LOOP) {
+    if (value != OG_LOOP_AUTO && value != OG_LOOP_HOST) return fail(OG_E_ARG, "unknown level loop %g", value);
+    e->level_loop = (uint32_t)value;
+    return OG_OK;
+  }
   return fail(OG_E_ARG, "unknown parameter %d", param);
 }
 
@@ -1327,6 +1468,10 @@ extern "C" int og_engine_get_param(const og_engine *e, int param, double *value)
   }
   if (param == OG_PARAM_BFS_DIRECTION) {
     *value = e->bfs_direction;
+    return OG_OK;
+  }
+  if (param == OG_PARAM_LEVEL_LOOP) {
+    *value = e->level_loop;
     return OG_OK;
   }
   return fail(OG_E_ARG, "unknown parameter %d", param);
@@ -1351,7 +1496,11 @@ extern "C" int og_bfs(og_engine *e, uint32_t src, uint32_t *out_depth, og_stats 
   if (e && src >= e->V) return fail(OG_E_ARG, "source %u >= V %u", src, e->V);
   return query_common(e, OG_ALGO_BFS, st, out_depth, [](og_engine *en, og_stats &s, void *c) {
     const uint32_t src_ = *(uint32_t *)c;
-    return run_frontier<EKU>(en, OG_ALGO_BFS, src_, s);
+    // the device-driven loop needs no staging pipeline: direct mode or a
+    // fully resident graph
+    const bool dev = en->level_loop == OG_LOOP_AUTO &&
+                     (en->plan.dynamic_edges == 0 || (en->cfg.flags & OG_CFG_DIRECT));
+    return dev ? run_bfs_dev(en, src_, s) : run_frontier<EKU>(en, OG_ALGO_BFS, src_, s);
   }, &src);
 }
 
@@ -1607,7 +1756,7 @@ void compact_launch(const uint32_t *bits, uint32_t v_begin, uint32_t v_end, cons
                     uint32_t *list, uint64_t *pref, uint64_t list_cap, uint32_t *tile,
                     uint64_t tile_cap, Counts *counts, const Lookback &lb, uint32_t *err,
                     cudaStream_t s) {
-  CompactArgs a;
+  CompactArgs a{};
   a.bits = bits;
   a.v_begin = v_begin;
   a.v_end = v_end;

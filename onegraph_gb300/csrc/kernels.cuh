@@ -86,6 +86,11 @@ struct CompactArgs {
   // the status array needs no clearing between launches.  The CTA that takes
   // the last ticket resets the ticket counter for the next launch.
   uint32_t epoch;
+  // Device-driven loops (launches replayed from a CUDA graph): when not null,
+  // the epoch is read from *epoch_ptr and the launch does nothing while
+  // *run_flag is 0.
+  const uint32_t *epoch_ptr;
+  const uint32_t *run_flag;
 };
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
@@ -155,6 +160,8 @@ __global__ void __launch_bounds__(kThreads) k_compact(CompactArgs a) {
   __shared__ uint32_t s_excl_n;
   __shared__ uint64_t s_excl_e;
   __shared__ int s_bad;
+  if (a.run_flag && *a.run_flag == 0u) return;  // every CTA of the launch reads the same flag
+  if (a.epoch_ptr) a.epoch = *a.epoch_ptr;
   if (threadIdx.x == 0) {
     s_tile = atomicAdd(a.lb.ticket, 1u);
     if (s_tile == a.ntiles - 1) *a.lb.ticket = 0u;  // every CTA of this launch has its ticket
@@ -1125,7 +1132,12 @@ template <class PS>
 __global__ void __launch_bounds__(kThreads) k_bfs_bottom_up(const uint64_t *off, uint32_t V, uint32_t Vs, PS stat,
                                                             PS host, const uint32_t *cur, uint32_t *visited,
                                                             uint32_t *next, uint32_t *depth, uint32_t newdepth,
-                                                            unsigned long long *cnt, uint32_t *err) {
+                                                            unsigned long long *cnt, uint32_t *err,
+                                                            const uint32_t *go = nullptr,
+                                                            const uint32_t *level = nullptr) {
+  // device-driven loops: run only when *go, at depth *level + 1
+  if (go && *go == 0u) return;
+  if (level) newdepth = *level + 1;
   const uint32_t lane = threadIdx.x & 31;
   unsigned long long nn = 0, nm = 0, nh = 0, ns = 0;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;

@@ -317,3 +317,32 @@ def test_direction_optimizing_bfs_matches_top_down():
     doff, dcol = np.array(dg.offsets), np.array(dg.columns)
     np.testing.assert_array_equal(oracle.normalise_bfs(e.bfs(5), dg.V), oracle.bfs(doff, dcol, 5)[0])
     e.close()
+
+
+def test_device_level_loop_matches_host_loop():
+    """og_bfs's device-driven level loop (CUDA graphs, decisions on the GPU)
+    gives the host loop's depths and statistics, for both directions, on
+    resident and out-of-memory (direct) engines, over repeated queries."""
+    for scale, kw in [(13, {}), (12, dict(weighted=True)), (11, dict(pagerank=True, symmetric=False))]:
+        g = og.Graph.rmat(scale, 16, **kw)
+        off = np.array(g.offsets)
+        col = np.array(g.edges)[:, 0].copy() if g.kind == og.WEIGHTED else np.array(g.columns)
+        deg = np.diff(off.astype(np.int64))
+        T = max(int(0.3 * g.E), 3 * 2048)
+        for ekw in [dict(budget=1 << 30, advisek=1.0),
+                    dict(budget=budget_for(g, T, og.CFG_DIRECT), advisek=0.5, direct=True)]:
+            e = engine(g, **ekw)
+            assert e.get_param(og.PARAM_LEVEL_LOOP) == og.LOOP_AUTO
+            for direction in (og.BFS_AUTO, og.BFS_TOP_DOWN):
+                e.set_param(og.PARAM_BFS_DIRECTION, direction)
+                for s in [int(np.argmax(deg)), 3, int(np.nonzero(deg)[0][-1]), int(np.argmax(deg))]:
+                    e.set_param(og.PARAM_LEVEL_LOOP, og.LOOP_AUTO)
+                    d = e.bfs(s)
+                    dev = dict(e.stats)
+                    e.set_param(og.PARAM_LEVEL_LOOP, og.LOOP_HOST)
+                    np.testing.assert_array_equal(e.bfs(s), d)
+                    host = dict(e.stats)
+                    np.testing.assert_array_equal(oracle.normalise_bfs(d, g.V), oracle.bfs(off, col, s)[0])
+                    for k in ("iterations", "frontier_sum", "edges_static", "edges_dynamic"):
+                        assert dev[k] == host[k], (scale, kw, ekw, direction, s, k, dev[k], host[k])
+            e.close()
