@@ -331,11 +331,12 @@ int og_engine_clone(og_engine *parent, og_engine **out);
 #define OG_PARAM_BFS_DIRECTION 3
 #define OG_BFS_AUTO 0
 #define OG_BFS_TOP_DOWN 1
-/* OG_PARAM_LEVEL_LOOP: OG_LOOP_AUTO (default) runs og_bfs's levels from two
- *   CUDA graphs replayed back to back, with every per-level decision taken by
- *   kernels (direct mode or a fully resident graph; staged engines keep the
- *   host loop); the host checks for the end every few levels.  OG_LOOP_HOST
- *   waits for each level's counts on the host.  Depths are identical. */
+/* OG_PARAM_LEVEL_LOOP: OG_LOOP_AUTO (default) runs the levels / rounds of
+ *   og_bfs, og_sssp and label-propagation og_cc from two CUDA graphs replayed
+ *   back to back, with every per-round decision taken by kernels (direct mode
+ *   or a fully resident graph; staged engines keep the host loop); the host
+ *   checks for the end every few rounds.  OG_LOOP_HOST waits for each round's
+ *   counts on the host.  Results are identical. */
 #define OG_PARAM_LEVEL_LOOP 4
 #define OG_LOOP_AUTO 0
 #define OG_LOOP_HOST 1

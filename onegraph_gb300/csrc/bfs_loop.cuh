@@ -16,6 +16,8 @@
 // BFS of Beamer et al. 2012 on symmetric graphs, top-down otherwise), so the
 // depths are the same.
 #pragma once
+#include <type_traits>
+
 #include "kernels.cuh"
 
 namespace og {
@@ -30,7 +32,8 @@ struct BfsLoop {
   uint32_t td_go;
   uint32_t bu_go;
   uint32_t epoch;         // compaction epoch of the current level
-  uint32_t pad[7];
+  uint32_t tile_next;     // tile counter of the top-down relax
+  uint32_t pad[6];
   unsigned long long unexplored;  // degrees of the vertices never in a frontier
   unsigned long long fn;          // size of the current frontier
   unsigned long long bu[4];       // bottom-up: reached, their degrees, host / static records
@@ -70,6 +73,7 @@ __global__ void k_bfs_ctl_mid(BfsLoop *st, const Counts *counts, int dopt) {
   }
   st->td_go = st->bottom ? 0u : 1u;
   st->bu_go = st->bottom;
+  st->tile_next = 0;
   if (st->bottom) st->bu[0] = st->bu[1] = st->bu[2] = st->bu[3] = 0;
 }
 
@@ -107,33 +111,145 @@ __global__ void k_bfs_ctl_end(BfsLoop *st, uint64_t V) {
   st->compact_go = st->need_compact;
 }
 
-// Top-down relax of both regions over a fixed grid: tile counts come from
-// the level's compaction (device memory); CTAs loop over the interleaved
-// static / dynamic tiles as k_lbs_pair does.  Runs only when *go; the BFS
-// depth written is *level + 1.
-template <class Src0, class Src1>
-__global__ void __launch_bounds__(kThreads) k_lbs_pair_dev(LbsArgs a0, Src0 s0, LbsArgs a1, Src1 s1, BfsOp op,
+// Per-level op fields taken from device memory: the BFS depth of the level.
+__device__ __forceinline__ void dev_prepare(BfsOp &op, const uint32_t *level) {
+  if (level) op.newdepth = *level + 1;
+}
+template <bool W>
+__device__ __forceinline__ void dev_prepare(MinOp<W> &, const uint32_t *) {}
+
+// Relax of both regions over a fixed grid: tile counts come from the level's
+// compaction (device memory); CTAs loop over the interleaved static / dynamic
+// tiles as k_lbs_pair does.  Runs only when *go.
+//
+// Tiles are handed out by an atomic counter (*tile_next, zeroed by the
+// control kernel that sets *go), not by a grid stride: a CTA that becomes
+// resident late only finds fewer tiles, so the fixed grid may exceed what
+// fits on the GPU at once without a second wave doing half the work.
+template <class Src0, class Src1, class Op>
+__global__ void __launch_bounds__(kThreads) k_lbs_pair_dev(LbsArgs a0, Src0 s0, LbsArgs a1, Src1 s1, Op op,
                                                            const Counts *counts, const uint32_t *go,
-                                                           const uint32_t *level) {
+                                                           const uint32_t *level, uint32_t *tile_next) {
+  static_assert(std::is_same<Src0, Src1>::value, "one tile body for both regions");
   if (*go == 0u) return;
-  __shared__ LbsShared<BfsOp::Val> sh;
-  op.newdepth = *level + 1;
-  a0.n = counts[0].n;
-  a0.total = counts[0].total;
-  a0.pos_begin = 0;
-  a0.pos_end = a0.total;
-  a1.n = counts[1].n;
-  a1.total = counts[1].total;
-  a1.pos_begin = 0;
-  a1.pos_end = a1.total;
-  const uint64_t n0 = (a0.total + kTile - 1) / kTile, n1 = (a1.total + kTile - 1) / kTile;
-  const uint64_t n = n0 + n1;
-  for (uint64_t b = blockIdx.x; b < n; b += gridDim.x) {
-    const uint64_t lo = b * n0 / n, hi = (b + 1) * n0 / n;
-    if (hi > lo) lbs_tile(a0, s0, op, sh, lo);
-    else lbs_tile(a1, s1, op, sh, b - hi);
-    __syncthreads();  // the tile tables are rebuilt for the next tile
+  __shared__ LbsShared<typename Op::Val> sh;
+  __shared__ uint32_t s_b[2];
+  // Both regions' arguments live in shared memory and one tile body serves
+  // both: kept in registers across the tile loop they cost 98 registers per
+  // thread (2 CTAs per SM) against 46 for the one-tile-per-CTA kernel.
+  __shared__ LbsArgs s_a[2];
+  __shared__ Src0 s_s[2];
+  if (threadIdx.x == 0) {
+    a0.n = counts[0].n;
+    a0.total = counts[0].total;
+    a0.pos_begin = 0;
+    a0.pos_end = a0.total;
+    a1.n = counts[1].n;
+    a1.total = counts[1].total;
+    a1.pos_begin = 0;
+    a1.pos_end = a1.total;
+    s_a[0] = a0;
+    s_a[1] = a1;
+    s_s[0] = s0;
+    s_s[1] = s1;
   }
+  dev_prepare(op, level);
+  __syncthreads();
+  const uint64_t n0 = (s_a[0].total + kTile - 1) / kTile, n1 = (s_a[1].total + kTile - 1) / kTile;
+  const uint64_t n = n0 + n1;
+  // the next tile's index is fetched while the current tile runs (two slots)
+  if (threadIdx.x == 0) s_b[0] = atomicAdd(tile_next, 1u);
+  __syncthreads();
+  for (int slot = 0;; slot ^= 1) {
+    const uint64_t b = s_b[slot];
+    if (b >= n) break;
+    if (threadIdx.x == 0) s_b[slot ^ 1] = atomicAdd(tile_next, 1u);
+    const uint64_t lo = b * n0 / n, hi = (b + 1) * n0 / n;
+    const int r = hi > lo ? 0 : 1;
+    lbs_tile(s_a[r], s_s[r], op, sh, r == 0 ? lo : b - hi);
+    __syncthreads();  // the tile tables are rebuilt and the next slot is read after this
+  }
+}
+
+// --------------------------------------------------- device-driven SSSP / CC
+//
+// Rounds of the min-relax algorithms (SSSP with or without the near/far
+// split, CC by label propagation), driven the same way.  A round graph:
+// compaction of the frontier (gated by round_go), k_min_ctl_a, compaction of
+// the waiting set (gated by adv_go), k_min_ctl_b, the relax (gated by
+// relax_go), k_min_ctl_end, the clear of the frontier.  A round that relaxes
+// nothing hands an empty bitmap to the next parity, whose frontier
+// compaction then finds nothing and moves on to the waiting set, as the host
+// loop does.
+
+struct MinLoop {
+  uint32_t done;
+  uint32_t epoch;      // epoch of the next compaction launch
+  uint32_t thr;        // near threshold (SSSP split)
+  uint32_t round_go;   // gates
+  uint32_t adv_go;
+  uint32_t relax_go;
+  uint32_t far_min;    // smallest waiting distance (running, see the host loop)
+  uint32_t delta;
+  uint32_t split;
+  uint32_t rounds;     // rounds that did work (the host's launch hint for the next query)
+  uint32_t tile_next;  // tile counter of the relax
+  uint32_t pad[5];
+  unsigned long long iterations, frontier_sum, edges_static, edges_dynamic;
+};
+
+// smallest waiting value a compaction of this epoch saw in its two regions
+__device__ __forceinline__ uint32_t far_of_dev(const unsigned long long *keys, uint32_t epoch) {
+  uint32_t m = 0xffffffffu;
+  for (int r = 0; r < 2; r++)
+    if ((uint32_t)(keys[r] >> 32) == epoch) m = min(m, ~(uint32_t)keys[r]);
+  return m;
+}
+
+__device__ __forceinline__ void min_account(MinLoop *st, const Counts *counts) {
+  st->iterations++;
+  st->frontier_sum += (uint64_t)counts[0].n + counts[1].n;
+  st->edges_static += counts[0].total;
+  st->edges_dynamic += counts[1].total;
+}
+
+// After the frontier's compaction (epoch st->epoch).
+__global__ void k_min_ctl_a(MinLoop *st, const Counts *counts, const unsigned long long *keys) {
+  if (threadIdx.x != 0) return;
+  st->adv_go = 0;
+  st->relax_go = 0;
+  st->tile_next = 0;
+  if (st->done) return;
+  st->rounds++;
+  const uint64_t n = (uint64_t)counts[0].n + counts[1].n;
+  if (st->split) st->far_min = min(st->far_min, far_of_dev(keys, st->epoch));
+  st->epoch++;
+  if (n) {
+    st->relax_go = 1;
+    min_account(st, counts);
+  } else if (!st->split || st->far_min == 0xffffffffu) {
+    st->done = 1;
+  } else {
+    const uint64_t t = (uint64_t)st->far_min + st->delta;
+    st->thr = t > 0xffffffffull ? 0xffffffffu : (uint32_t)t;
+    st->adv_go = 1;
+  }
+}
+
+// After the waiting set's compaction (when it ran): its minimum is now exact.
+__global__ void k_min_ctl_b(MinLoop *st, const Counts *counts, const unsigned long long *keys) {
+  if (threadIdx.x != 0 || !st->adv_go) return;
+  st->far_min = far_of_dev(keys, st->epoch);
+  st->epoch++;
+  if ((uint64_t)counts[0].n + counts[1].n) {
+    st->relax_go = 1;
+    min_account(st, counts);
+  }
+}
+
+__global__ void k_min_ctl_end(MinLoop *st) {
+  if (threadIdx.x != 0) return;
+  st->round_go = st->done ? 0u : 1u;
 }
 
 }  // namespace og

@@ -108,6 +108,12 @@ struct og_engine {
   uint32_t dev_epoch = 1u << 29;  // epochs of device-driven compactions: [2^29, 2^30)
   uint32_t bfs_levels_hint = 4;   // levels of the last BFS (launched before the first check)
   uint32_t level_loop = 0;        // OG_LOOP_AUTO / OG_LOOP_HOST
+  // device-driven SSSP / CC rounds: state, host mirror, round graphs captured
+  // for (algorithm, split) = min_exec_key
+  MinLoop *mloop_d = nullptr, *mloop_h = nullptr;
+  cudaGraphExec_t min_exec[2] = {nullptr, nullptr};
+  int min_exec_key = -1;
+  uint32_t min_rounds_hint[2] = {16, 4};  // SSSP, CC
   uint32_t graph_n = 0;
   int graph_cfg = -1;
   bool graph_broken = false;
@@ -166,6 +172,9 @@ void destroy(og_engine *e) {
   for (int p = 0; p < 2; p++)
     if (e->bfs_exec[p]) cudaGraphExecDestroy(e->bfs_exec[p]);
   if (e->loop_h) cudaFreeHost(e->loop_h);
+  for (int p = 0; p < 2; p++)
+    if (e->min_exec[p]) cudaGraphExecDestroy(e->min_exec[p]);
+  if (e->mloop_h) cudaFreeHost(e->mloop_h);
   if (e->err_h) cudaFreeHost(e->err_h);
   if (e->l1_h) cudaFreeHost(e->l1_h);
   cudaEvent_t evs[] = {e->ev_round, e->ev_cs, e->ev_cd, e->ev_dyn_done, e->ev_gat[0], e->ev_gat[1],
@@ -232,6 +241,8 @@ int create_query_state(og_engine *e) {
   CK(cudaMallocHost(&e->counts_h, 3 * sizeof(Counts)));
   RC(dalloc(e, (char **)&e->loop_d, sizeof(BfsLoop)));
   CK(cudaMallocHost(&e->loop_h, sizeof(BfsLoop)));
+  RC(dalloc(e, (char **)&e->mloop_d, sizeof(MinLoop)));
+  CK(cudaMallocHost(&e->mloop_h, sizeof(MinLoop)));
   CK(cudaMallocHost(&e->err_h, 4 * sizeof(uint32_t)));
   CK(cudaMallocHost(&e->l1_h, sizeof(double)));
   if (P.chunk_edges && !(e->cfg.flags & OG_CFG_DIRECT)) {
@@ -313,6 +324,8 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
   // ~124 KB of L1).  Measured on R-MAT 27: 9.55 queries/s with the driver's
   // choice, 9.85 at 58 %, 6.77 at 86 %, 8.06 at 30 %.
   CK(cudaFuncSetAttribute(k_lbs_pair<SrcP<true>, SrcP<true>, MinOp<true>>,
+                          cudaFuncAttributePreferredSharedMemoryCarveout, 58));
+  CK(cudaFuncSetAttribute(k_lbs_pair_dev<SrcP<true>, SrcP<true>, MinOp<true>>,
                           cudaFuncAttributePreferredSharedMemoryCarveout, 58));
   // Same for the PageRank pull (29 KB tiles: 4 CTAs per SM at 58 %).  R-MAT 26
   // directed: 58.5 iterations/s with the driver's choice, 69.6 at 58 %,
@@ -413,6 +426,7 @@ struct SplitArgs {
   // device-driven loops: epoch read from device memory, launch gated by a flag
   const uint32_t *epoch_ptr = nullptr;
   const uint32_t *run_flag = nullptr;
+  const uint32_t *thr_ptr = nullptr;
   bool on = false;
   uint32_t thr = 0;
   uint32_t *far_bits = nullptr;
@@ -450,6 +464,7 @@ int launch_compact(og_engine *e, int r, const uint32_t *bits, uint32_t vb, uint3
   a.epoch = e->epoch;
   a.epoch_ptr = sp.epoch_ptr;
   a.run_flag = sp.run_flag;
+  a.thr_ptr = sp.thr_ptr;
   if (a.ntiles + 1 > e->lb_tiles) return fail(OG_E_STATE, "compaction scratch too small");
   k_compact<<<a.ntiles, kThreads, 0, s>>>(a);
   e->launches++;
@@ -713,6 +728,9 @@ int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
     e->launches += 2;
   } else if (algo == OG_ALGO_SSSP) {
     if (e->sssp_delta > 0) CK(cudaMemsetAsync(e->bm[2], 0, 4 * e->nwords, s));  // waiting set
+    // far keys: a device-driven query leaves keys of higher epochs, which
+    // atomicMax would keep over this query's
+    CK(cudaMemsetAsync(e->counts_d + 2, 0, sizeof(Counts), s));
     k_fill_u32<<<g, kThreads, 0, s>>>(e->value_d, V, 0xFFFFFFFFu);  // SSSP GraphMeta.h:377
     k_set_source<<<1, 1, 0, s>>>(e->value_d, src, 1u, cur, nullptr);
     e->launches += 2;
@@ -842,7 +860,7 @@ int capture_bfs_level(og_engine *e, int p, int dopt, cudaGraphExec_t *out) {
   cudaGraph_t gr = nullptr;
   const uint64_t before = e->launches;
   int per_sm = 0;  // fixed grid of the top-down relax: every CTA resident
-  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lbs_pair_dev<EKU::PSrc, EKU::PSrc>, kThreads, 0));
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_lbs_pair_dev<EKU::PSrc, EKU::PSrc, BfsOp>, kThreads, 0));
   const unsigned grid = (unsigned)std::max(1, per_sm) * (unsigned)e->sms;
   CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
   int rc = OG_OK;
@@ -858,9 +876,9 @@ int capture_bfs_level(og_engine *e, int p, int dopt, cudaGraphExec_t *out) {
     CK(cudaStreamWaitEvent(s, e->ev_cd, 0));
     k_bfs_ctl_mid<<<1, 32, 0, s>>>(L, e->counts_d, dopt);
     BfsOp op{e->bm[2], next, e->value_d, e->err_d, e->V, 0};
-    k_lbs_pair_dev<EKU::PSrc, EKU::PSrc><<<grid, kThreads, 0, s>>>(
+    k_lbs_pair_dev<EKU::PSrc, EKU::PSrc, BfsOp><<<grid, kThreads, 0, s>>>(
         lbs_args(e, 0, 0, 0, true, e->plan.static_edges), EKU::stat(e), lbs_args(e, 1, 0, 0, true, e->g->E),
-        EKU::host(e), op, e->counts_d, &L->td_go, &L->level);
+        EKU::host(e), op, e->counts_d, &L->td_go, &L->level, &L->tile_next);
     k_bfs_bottom_up<EKU::PSrc><<<grid_for(e->V, e->sms), kThreads, 0, s>>>(
         e->off_d, e->V, e->Vs, EKU::stat(e), EKU::host(e), cur, e->bm[2], next, e->value_d, 0, L->bu,
         e->err_d, &L->bu_go, &L->level);
@@ -945,6 +963,147 @@ int run_bfs_dev(og_engine *e, uint32_t src, og_stats &st) {
   e->bfs_levels_hint = (uint32_t)h.iterations;
   e->dev_epoch = h.epoch + 1;
   e->last_algo = OG_ALGO_BFS;
+  return OG_OK;
+}
+
+// Captures one SSSP / CC round for the frontier in bm[p] (next in bm[1 - p],
+// waiting set in bm[2]); see bfs_loop.cuh.
+template <class K, bool kW>
+int capture_min_round(og_engine *e, int p, bool split, cudaGraphExec_t *out) {
+  cudaStream_t s = e->s_main;
+  uint32_t *cur = e->bm[p], *next = e->bm[1 - p], *waiting = e->bm[2];
+  MinLoop *L = e->mloop_d;
+  const unsigned long long *keys = (const unsigned long long *)(e->counts_d + 2);
+  int per_sm = 0;
+  CK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+      &per_sm, k_lbs_pair_dev<typename K::PSrc, typename K::PSrc, MinOp<kW>>, kThreads, 0));
+  const unsigned grid = (unsigned)std::max(1, per_sm) * (unsigned)e->sms;
+  cudaGraph_t gr = nullptr;
+  const uint64_t before = e->launches;
+  CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+  auto compact_both = [&](const uint32_t *bits, const SplitArgs &sp) -> int {
+    CK(cudaEventRecord(e->ev_round, s));
+    CK(cudaStreamWaitEvent(e->s_dyn, e->ev_round, 0));
+    RC(launch_compact(e, 0, bits, 0, e->Vs, s, sp));
+    RC(launch_compact(e, 1, bits, e->Vs, e->V, e->s_dyn, sp));
+    CK(cudaEventRecord(e->ev_cd, e->s_dyn));
+    CK(cudaStreamWaitEvent(s, e->ev_cd, 0));
+    return OG_OK;
+  };
+  auto body = [&]() -> int {
+    SplitArgs sr;
+    sr.epoch_ptr = &L->epoch;
+    sr.run_flag = &L->round_go;
+    sr.thr_ptr = &L->thr;
+    sr.on = split;
+    sr.far_bits = split ? waiting : nullptr;
+    sr.clear_bits = split ? waiting : nullptr;
+    RC(compact_both(cur, sr));
+    k_min_ctl_a<<<1, 32, 0, s>>>(L, e->counts_d, keys);
+    if (split) {
+      SplitArgs sa = sr;
+      sa.run_flag = &L->adv_go;
+      sa.far_bits = nullptr;
+      RC(compact_both(waiting, sa));
+      k_min_ctl_b<<<1, 32, 0, s>>>(L, e->counts_d, keys);
+    }
+    MinOp<kW> op{e->value_d, next, e->err_d, e->V};
+    k_lbs_pair_dev<typename K::PSrc, typename K::PSrc, MinOp<kW>><<<grid, kThreads, 0, s>>>(
+        lbs_args(e, 0, 0, 0, true, e->plan.static_edges), K::stat(e), lbs_args(e, 1, 0, 0, true, e->g->E),
+        K::host(e), op, e->counts_d, &L->relax_go, nullptr, &L->tile_next);
+    k_min_ctl_end<<<1, 32, 0, s>>>(L);
+    CK(cudaMemsetAsync(cur, 0, 4 * e->nwords, s));
+    return OG_OK;
+  };
+  const int rc = body();
+  const cudaError_t ce = cudaStreamEndCapture(s, &gr);
+  e->launches = before;  // captured, not launched
+  if (rc != OG_OK || ce != cudaSuccess) {
+    if (gr) cudaGraphDestroy(gr);
+    cudaGetLastError();
+    return rc != OG_OK ? rc : fail(OG_E_CUDA, "round capture: %s", cudaGetErrorString(ce));
+  }
+  const cudaError_t ie = cudaGraphInstantiate(out, gr, 0);
+  cudaGraphDestroy(gr);
+  if (ie != cudaSuccess) return fail(OG_E_CUDA, "round graph: %s", cudaGetErrorString(ie));
+  return OG_OK;
+}
+
+// SSSP (algo OG_ALGO_SSSP) or label-propagation CC with device-driven rounds.
+int run_min_dev(og_engine *e, int algo, uint32_t src, og_stats &st) {
+  const uint64_t V = e->V;
+  cudaStream_t s = e->s_main;
+  const int g = grid_for(V, e->sms);
+  const bool sssp = algo == OG_ALGO_SSSP;
+  const bool split = sssp && e->sssp_delta > 0;
+  const int key = (sssp ? 2 : 0) + (split ? 1 : 0);
+  if (key != e->min_exec_key) {
+    for (int p = 0; p < 2; p++)
+      if (e->min_exec[p]) {
+        cudaGraphExecDestroy(e->min_exec[p]);
+        e->min_exec[p] = nullptr;
+      }
+    for (int p = 0; p < 2; p++)
+      RC((sssp ? capture_min_round<EK<uint8_t>, true>(e, p, split, &e->min_exec[p])
+               : capture_min_round<EKU, false>(e, p, false, &e->min_exec[p])));
+    e->min_exec_key = key;
+  }
+  if (e->dev_epoch > (1u << 30) - (1u << 20)) {  // epoch wrap: clear the status words once
+    for (int r = 0; r < 2; r++)
+      CK(cudaMemsetAsync(e->lb[r].status, 0, sizeof(uint32_t) * e->lb_tiles, s));
+    CK(cudaMemsetAsync(e->counts_d + 2, 0, sizeof(Counts), s));
+    e->dev_epoch = 1u << 29;
+  }
+  CK(cudaMemsetAsync(e->err_d, 0, 16, s));
+  CK(cudaMemsetAsync(e->bm[0], 0, 4 * e->nwords, s));
+  CK(cudaMemsetAsync(e->bm[1], 0, 4 * e->nwords, s));
+  if (sssp) {
+    if (split) CK(cudaMemsetAsync(e->bm[2], 0, 4 * e->nwords, s));  // waiting set
+    CK(cudaMemsetAsync(e->counts_d + 2, 0, sizeof(Counts), s));    // far keys of earlier queries
+    k_fill_u32<<<g, kThreads, 0, s>>>(e->value_d, V, 0xFFFFFFFFu);  // SSSP GraphMeta.h:377
+    k_set_source<<<1, 1, 0, s>>>(e->value_d, src, 1u, e->bm[0], nullptr);
+  } else {
+    k_iota_u32<<<g, kThreads, 0, s>>>(e->value_d, V);  // CC GraphMeta.h:341-345
+    k_fill_bits<<<g, kThreads, 0, s>>>(e->bm[0], e->nwords, V);
+  }
+  MinLoop &h = *e->mloop_h;
+  memset(&h, 0, sizeof h);
+  h.epoch = e->dev_epoch;
+  const uint64_t thr = 1ull + e->sssp_delta;
+  h.thr = thr > 0xffffffffull ? 0xffffffffu : (uint32_t)thr;
+  h.round_go = 1;
+  h.far_min = 0xffffffffu;
+  h.delta = e->sssp_delta;
+  h.split = split ? 1 : 0;
+  CK(cudaMemcpyAsync(e->mloop_d, &h, sizeof h, cudaMemcpyHostToDevice, s));
+  CK(cudaEventRecord(e->t_d0, s));
+  uint32_t &hint = e->min_rounds_hint[sssp ? 0 : 1];
+  uint32_t launched = 0, batch = std::max<uint32_t>(2, hint + 2);
+  for (;;) {
+    for (uint32_t i = 0; i < batch; i++, launched++) CK(cudaGraphLaunch(e->min_exec[launched & 1], s));
+    CK(cudaMemcpyAsync(&h.done, &e->mloop_d->done, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    if (h.done) break;
+    if (launched > 8 * V + 64) return fail(OG_E_STATE, "rounds did not end after %u", launched);
+    batch = 8;
+  }
+  CK(cudaEventRecord(e->ev_dyn_done, s));
+  CK(cudaMemcpyAsync(&h, e->mloop_d, sizeof h, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(e->err_h, e->err_d, 4, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  RC(check_device_error(e));
+  float ms = 0;
+  if (cudaEventElapsedTime(&ms, e->t_d0, e->ev_dyn_done) == cudaSuccess) st.ms_dynamic += ms;
+  st.iterations += (uint32_t)h.iterations;
+  st.frontier_sum += h.frontier_sum;
+  st.edges_static += h.edges_static;
+  st.edges_dynamic += h.edges_dynamic;
+  st.link_bytes += (h.edges_dynamic * e->bpe + 7) / 8;
+  st.chunks += (uint32_t)h.iterations;
+  e->launches += 2 + (split ? 11ull : 7ull) * launched;
+  hint = h.rounds;  // rounds this query needed (the next one is launched that far before its first check)
+  e->dev_epoch = h.epoch + 1;
+  e->last_algo = algo;
   return OG_OK;
 }
 
@@ -1509,6 +1668,8 @@ extern "C" int og_sssp(og_engine *e, uint32_t src, uint32_t *out_dist, og_stats 
   if (e && e->g->kind != OG_GRAPH_WEIGHTED) return fail(OG_E_UNSUPPORTED, "SSSP needs a weighted graph");
   return query_common(e, OG_ALGO_SSSP, st, out_dist, [](og_engine *en, og_stats &s, void *c) {
     const uint32_t src_ = *(uint32_t *)c;
+    if (en->level_loop == OG_LOOP_AUTO && (en->plan.dynamic_edges == 0 || (en->cfg.flags & OG_CFG_DIRECT)))
+      return run_min_dev(en, OG_ALGO_SSSP, src_, s);
     if (en->wbytes == 1) return run_frontier<EK<uint8_t>>(en, OG_ALGO_SSSP, src_, s);
     if (en->wbytes == 2) return run_frontier<EK<uint16_t>>(en, OG_ALGO_SSSP, src_, s);
     return run_frontier<EK<uint32_t>>(en, OG_ALGO_SSSP, src_, s);
@@ -1616,7 +1777,10 @@ extern "C" int og_cc(og_engine *e, uint32_t *out_label, og_stats *st) {
                     (en->cc_method == OG_CC_AUTO && en->g->symmetric == 1);
     if (en->cc_method == OG_CC_UNION_FIND && en->g->symmetric != 1)
       return fail(OG_E_ARG, "union-find CC needs a graph known to be symmetric (og_graph_symmetric)");
-    return uf ? run_cc_uf(en, s) : run_frontier<EKU>(en, OG_ALGO_CC, 0, s);
+    if (uf) return run_cc_uf(en, s);
+    if (en->level_loop == OG_LOOP_AUTO && (en->plan.dynamic_edges == 0 || (en->cfg.flags & OG_CFG_DIRECT)))
+      return run_min_dev(en, OG_ALGO_CC, 0, s);
+    return run_frontier<EKU>(en, OG_ALGO_CC, 0, s);
   }, &dummy);
 }
 

@@ -91,6 +91,7 @@ struct CompactArgs {
   // *run_flag is 0.
   const uint32_t *epoch_ptr;
   const uint32_t *run_flag;
+  const uint32_t *thr_ptr;  // when not null, thr is read from *thr_ptr
 };
 
 __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p) {
@@ -162,6 +163,7 @@ __global__ void __launch_bounds__(kThreads) k_compact(CompactArgs a) {
   __shared__ int s_bad;
   if (a.run_flag && *a.run_flag == 0u) return;  // every CTA of the launch reads the same flag
   if (a.epoch_ptr) a.epoch = *a.epoch_ptr;
+  if (a.thr_ptr) a.thr = *a.thr_ptr;
   if (threadIdx.x == 0) {
     s_tile = atomicAdd(a.lb.ticket, 1u);
     if (s_tile == a.ntiles - 1) *a.lb.ticket = 0u;  // every CTA of this launch has its ticket

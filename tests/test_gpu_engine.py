@@ -346,3 +346,35 @@ def test_device_level_loop_matches_host_loop():
                     for k in ("iterations", "frontier_sum", "edges_static", "edges_dynamic"):
                         assert dev[k] == host[k], (scale, kw, ekw, direction, s, k, dev[k], host[k])
             e.close()
+
+
+def test_device_rounds_sssp_cc_match_host_loop():
+    """Device-driven SSSP (several near/far widths, including 0) and
+    label-propagation CC rounds equal the host loop's results and statistics."""
+    for scale in (12, 13):
+        g = og.Graph.rmat(scale, 16, weighted=True, seed=scale)
+        off, pairs = np.array(g.offsets), np.array(g.edges)
+        deg = np.diff(off.astype(np.int64))
+        T = max(int(0.3 * g.E), 3 * 2048)
+        for ekw in [dict(budget=1 << 30, advisek=1.0),
+                    dict(budget=budget_for(g, T, og.CFG_DIRECT), advisek=0.5, direct=True)]:
+            e = engine(g, **ekw)
+            for delta in (4, 0, 1, 37):
+                e.set_param(og.PARAM_SSSP_DELTA, delta)
+                for s in [int(np.argmax(deg)), 9, int(np.argmax(deg))]:
+                    e.set_param(og.PARAM_LEVEL_LOOP, og.LOOP_AUTO)
+                    d = e.sssp(s)
+                    dev = dict(e.stats)
+                    e.set_param(og.PARAM_LEVEL_LOOP, og.LOOP_HOST)
+                    np.testing.assert_array_equal(e.sssp(s), d)
+                    host = dict(e.stats)
+                    np.testing.assert_array_equal(d, oracle.sssp_dijkstra(off, pairs, s))
+                    for k in ("iterations", "frontier_sum", "edges_static", "edges_dynamic"):
+                        assert dev[k] == host[k], (scale, ekw, delta, s, k)
+            e.set_param(og.PARAM_CC_METHOD, og.CC_LABEL_PROPAGATION)
+            e.set_param(og.PARAM_LEVEL_LOOP, og.LOOP_AUTO)
+            lab = e.cc()
+            np.testing.assert_array_equal(lab, oracle.cc(off, pairs[:, 0].copy())[0])
+            e.set_param(og.PARAM_LEVEL_LOOP, og.LOOP_HOST)
+            np.testing.assert_array_equal(e.cc(), lab)
+            e.close()
