@@ -7,7 +7,11 @@
 // --method/-method <0 OneGraph | 1 Subway | 2 USM> (parsed but unused by the
 // reference), --adviseK/-adviseK/--advisek/-advisek <ratio>,
 // plus --budget <bytes|NNG|NNM>, --dump <file>, --sources <n>,
-// --direct <0|1>, --json <0|1>, --threshold <pr delta>, --device <ordinal>.
+// --direct <0|1>, --json <0|1>, --threshold <pr delta>, --device <ordinal>,
+// --symmetric <1|0|check> (1 asserts that every edge has its reverse, which
+// lets CC use union-find and BFS expand large levels bottom-up; "check"
+// verifies it on the host first; without the flag a loaded file counts as
+// not known to be symmetric and the reference's algorithms run).
 // Differences from the reference, on purpose: a --type naming another
 // algorithm is an error (exit 2) instead of a silent exit 0 (main.cpp:9-13),
 // and -r is honoured by BFS when given (the reference BFS always walks
@@ -36,7 +40,7 @@ static uint64_t parse_bytes(const char *s) {
 }
 
 struct Args {
-  std::string input, algo, dump;
+  std::string input, algo, dump, symmetric;
   int source = 0;
   bool has_source = false;
   double advisek = 0.0;
@@ -67,6 +71,7 @@ static bool parse(int argc, char **argv, Args &a) {
     else if (!strcmp(k, "--json")) a.json = atoi(v);
     else if (!strcmp(k, "--threshold")) a.threshold = atof(v);
     else if (!strcmp(k, "--device")) a.device = atoi(v);
+    else if (!strcmp(k, "--symmetric")) a.symmetric = v;
     else {
       fprintf(stderr, "unknown flag %s\n", k);
       return false;
@@ -120,6 +125,17 @@ int main(int argc, char **argv) {
   og_graph *g = nullptr;
   int rc = og_graph_load(a.input.c_str(), kind, &g);
   if (rc) return die("og_graph_load", rc);
+  if (a.symmetric == "1" || a.symmetric == "0") {
+    og_graph_set_symmetric(g, a.symmetric == "1" ? 1 : 0);
+  } else if (a.symmetric == "check") {
+    int sym = 0;
+    rc = og_graph_symmetric(g, &sym);
+    if (rc) return die("og_graph_symmetric", rc);
+    printf("symmetric %d\n", sym);
+  } else if (!a.symmetric.empty()) {
+    fprintf(stderr, "--symmetric takes 1, 0 or check\n");
+    return 2;
+  }
   uint64_t V = 0, E = 0;
   og_graph_info(g, &V, &E, nullptr, nullptr, nullptr, nullptr);
   printf("vertexArrSize = %llu edgeArrSize = %llu\n", (unsigned long long)V, (unsigned long long)E);

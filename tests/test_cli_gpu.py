@@ -52,8 +52,14 @@ def test_sssp_cc_pr_cli(tmp_path):
     g.save(p)
     out = str(tmp_path / "cc.bin")
     run("CC_OneGraph", "-f", p, "--advisek", "0.5", "--budget", "300K", "--dump", out, "--direct", "1")
-    np.testing.assert_array_equal(np.fromfile(out, np.uint32),
-                                  oracle.cc(np.array(g.offsets), np.array(g.columns))[0])
+    want_cc = oracle.cc(np.array(g.offsets), np.array(g.columns))[0]
+    np.testing.assert_array_equal(np.fromfile(out, np.uint32), want_cc)
+    # the same through union-find, with the symmetry checked or asserted
+    for flag in ("check", "1"):
+        o = run("CC_OneGraph", "-f", p, "--advisek", "0.5", "--budget", "300K", "--dump", out,
+                "--direct", "1", "--symmetric", flag)
+        assert flag == "1" or "symmetric 1" in o
+        np.testing.assert_array_equal(np.fromfile(out, np.uint32), want_cc)
     gp = og.Graph.rmat(11, 16, pagerank=True, symmetric=False)
     p = str(tmp_path / "pr.csr")
     gp.save(p)
