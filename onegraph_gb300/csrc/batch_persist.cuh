@@ -9,6 +9,16 @@
 // tile (CTA size x items) is also the split granularity of high-degree
 // vertices.  No reference counterpart: the reference runs sources one by one
 // (BFS/oneGraph_BFS/CalculateOpt.h:55-209).
+//
+// On a symmetric graph a level may instead be expanded bottom-up: every
+// vertex that some active source has not reached scans its own records and
+// ORs in its neighbours' frontier masks, stopping as soon as every missing
+// active source is found.  The choice per level is the direction-optimizing
+// rule of Beamer et al. (SC 2012) on batch totals: bottom-up once the
+// frontier's edges exceed 1/14 of the edges of the vertices still missing an
+// active source; top-down again when the frontier is under V/24 vertices and
+// shrinking.  Every CTA computes the same totals, so all take the same
+// branch.  The masks produced are the same in both directions.
 // Data written by other CTAs during the launch (list, prefix, tile map,
 // frontier words and masks) is read with __ldcg: L1 is not coherent within a
 // kernel, so a plain load could return a line cached in an earlier level.
@@ -43,9 +53,18 @@ struct PersistArgs {
   uint32_t n_src;
   uint32_t *err;
   uint32_t *levels;           // number of expanded levels (out)
-  unsigned long long *stat;   // [0] listed vertices, [1] edges expanded, [2] of them dynamic
+  unsigned long long *stat;   // [0] listed vertices, [1] edges expanded, [2] of them dynamic,
+                              // [3] bottom-up levels, [4..5] OR of the frontier masks by level parity
+  unsigned long long *cta_mu; // per-CTA degree sums of the vertices missing an active source
+  uint32_t *defer;            // bottom-up vertices handed to the pull pass (bitmap, zero between levels)
   uint32_t Vs;                // first dynamic vertex
+  uint32_t dopt;              // bottom-up levels allowed (the graph is symmetric)
+  __device__ __forceinline__ unsigned long long *act_slot(uint32_t level) const {
+    return stat + 4 + (level & 1u);
+  }
 };
+
+constexpr uint64_t kBatchAlpha = 14, kBatchBeta = 24;
 
 __device__ __forceinline__ bool grid_barrier(unsigned int *bar, uint32_t *err) {
   __shared__ int s_ok;
@@ -86,8 +105,23 @@ struct PersistShared {
   unsigned long long wsum_e[BLOCK / 32];
   uint32_t cnt[64];
   uint32_t red_n;
-  unsigned long long red_e, red_tn, red_te;
+  unsigned long long red_e, red_tn, red_te, red_mu;
+  unsigned long long act;
 };
+
+// block-wide sum of a u64 (BLOCK threads); every thread gets the total
+template <int BLOCK, class SH>
+__device__ __forceinline__ uint64_t block_sum(SH &sh, uint64_t x) {
+#pragma unroll
+  for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+  if ((threadIdx.x & 31) == 0) sh.wsum_e[threadIdx.x >> 5] = x;
+  __syncthreads();
+  uint64_t t = 0;
+#pragma unroll
+  for (int w = 0; w < BLOCK / 32; w++) t += sh.wsum_e[w];
+  __syncthreads();
+  return t;
+}
 
 // block-wide exclusive scan of (u32, u64) with totals; BLOCK threads
 template <int BLOCK, class SH>
@@ -135,173 +169,200 @@ __device__ __forceinline__ void pscan(SH &sh, uint32_t c, uint64_t e, uint32_t &
   __syncthreads();
 }
 
-template <int BLOCK, int ITEMS>
-__global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
-  using SH = PersistShared<BLOCK, ITEMS>;
-  constexpr uint32_t TILE = SH::TILE;
-  __shared__ SH sh;
-  unsigned long long *cur = a.cur, *next = a.next;
-  uint32_t *cur_any = a.cur_any, *next_any = a.next_any;
-  // contiguous word range of this CTA, split into contiguous per-thread runs
-  const uint64_t wper_cta = (a.nwords + gridDim.x - 1) / gridDim.x;
-  const uint64_t wper_thr = (wper_cta + BLOCK - 1) / BLOCK;
-  const uint64_t wb = min(a.nwords, blockIdx.x * wper_cta + threadIdx.x * wper_thr);
-  const uint64_t we = min(min(a.nwords, (blockIdx.x + 1) * wper_cta), wb + wper_thr);
-  uint32_t level = 1;
-  for (;; level++) {
-    // ---- 1. count the frontier (vertices with edges) in this thread's words
-    uint32_t c = 0;
-    uint64_t e = 0, dyn = 0;
-    for (uint64_t w = wb; w < we; w++)
-      for (uint32_t m = __ldcg(cur_any + w); m; m &= m - 1) {
-        const uint64_t v = w * 32 + (__ffs(m) - 1);
-        const uint64_t d = a.off[v + 1] - a.off[v];
-        c += d ? 1u : 0u;
-        e += d;
-        if (v >= a.Vs) dyn += d;
-      }
-    if (dyn) atomicAdd(a.stat + 2, (unsigned long long)dyn);
-    uint32_t exc, totc;
-    uint64_t exe, tote;
-    pscan<BLOCK>(sh, c, e, exc, exe, totc, tote);
-    if (threadIdx.x == 0) {
-      a.cta_n[blockIdx.x] = totc;
-      a.cta_e[blockIdx.x] = tote;
+// Records of vertex v beyond its first `skip`.
+__device__ __forceinline__ uint64_t rest_deg(const PersistArgs &a, uint64_t v, uint64_t skip) {
+  const uint64_t d = a.off[v + 1] - a.off[v];
+  return d > skip ? d - skip : 0;
+}
+
+// Count the listed vertices of this thread's words of `bits` (those with
+// records beyond `skip`) and their record sums; publish the CTA's totals.
+template <int BLOCK, class SH>
+__device__ __forceinline__ void count_list(const PersistArgs &a, SH &sh, const uint32_t *bits, uint64_t wb,
+                                           uint64_t we, uint64_t skip, uint32_t &exc, uint64_t &exe,
+                                           uint64_t &dyn) {
+  uint32_t c = 0;
+  uint64_t e = 0;
+  dyn = 0;
+  for (uint64_t w = wb; w < we; w++)
+    for (uint32_t m = __ldcg(bits + w); m; m &= m - 1) {
+      const uint64_t v = w * 32 + (__ffs(m) - 1);
+      const uint64_t d = rest_deg(a, v, skip);
+      c += d ? 1u : 0u;
+      e += d;
+      if (v >= a.Vs) dyn += d;
     }
-    if (!grid_barrier(a.bar, a.err)) return;
-    // ---- 2. this CTA's offset and the grand totals, then write the list
+  uint32_t totc;
+  uint64_t tote;
+  pscan<BLOCK>(sh, c, e, exc, exe, totc, tote);
+  if (threadIdx.x == 0) {
+    a.cta_n[blockIdx.x] = totc;
+    a.cta_e[blockIdx.x] = tote;
+  }
+}
+
+// After count_list and a grid barrier: this CTA's list offset (sh.red_n,
+// sh.red_e), the grid totals (sh.red_tn, sh.red_te) and, when with_mu, the
+// grid sum of cta_mu (sh.red_mu).  Every CTA computes the same totals.
+template <int BLOCK, class SH>
+__device__ __forceinline__ void grid_totals(const PersistArgs &a, SH &sh, bool with_mu) {
+  uint32_t pn = 0, tn = 0;
+  uint64_t pe = 0, te = 0, tmu = 0;
+  for (uint32_t b = threadIdx.x; b < gridDim.x; b += BLOCK) {
+    const uint32_t bn = __ldcg(a.cta_n + b);
+    const uint64_t be = __ldcg(a.cta_e + b);
+    tn += bn;
+    te += be;
+    if (with_mu) tmu += __ldcg(a.cta_mu + b);
+    if (b < blockIdx.x) {
+      pn += bn;
+      pe += be;
+    }
+  }
+  tmu = block_sum<BLOCK>(sh, tmu);
+  uint32_t x0, y0;
+  uint64_t x1, y1;
+  pscan<BLOCK>(sh, pn, pe, x0, x1, y0, y1);  // block sums of the predecessor parts
+  uint32_t z0, z1;
+  uint64_t z2, z3;
+  pscan<BLOCK>(sh, tn, te, z0, z2, z1, z3);
+  if (threadIdx.x == 0) {
+    sh.red_n = y0;
+    sh.red_e = y1;
+    sh.red_tn = z1;
+    sh.red_te = z3;
+    sh.red_mu = tmu;
+  }
+  __syncthreads();
+}
+
+// Write the list (vertex, record prefix) of this thread's words of `bits` and
+// the first list entry of every tile; positions come from count_list's scan.
+template <uint32_t TILE>
+__device__ __forceinline__ void write_list(const PersistArgs &a, const uint32_t *bits, uint64_t wb, uint64_t we,
+                                           uint64_t skip, uint32_t pos, uint64_t ep, uint64_t total_n,
+                                           uint64_t total_e) {
+  for (uint64_t w = wb; w < we; w++)
+    for (uint32_t m = __ldcg(bits + w); m; m &= m - 1) {
+      const uint64_t v = w * 32 + (__ffs(m) - 1);
+      const uint64_t d = rest_deg(a, v, skip);
+      if (!d) continue;
+      a.list[pos] = (uint32_t)v;
+      a.pref[pos] = ep;
+      for (uint64_t t = (ep + TILE - 1) / TILE; t * TILE < ep + d; t++) a.tile_first[t] = pos;
+      pos++;
+      ep += d;
+    }
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == blockDim.x - 1) a.pref[total_n] = total_e;
+}
+
+// Edge-balanced pass over the listed vertices' records (from record `skip` of
+// each), TILE records per CTA tile.
+//  push (top-down): a listed vertex's frontier mask goes to every neighbour
+//    that a source of the mask has not reached (visited / next / next_any by
+//    atomicOr).
+//  pull (the deferred vertices of a bottom-up level): every neighbour's
+//    frontier mask, restricted to the sources the listed vertex still lacks,
+//    is ORed into a per-vertex accumulator in shared memory and then into the
+//    vertex's next mask; visited and next_any are settled afterwards.
+template <int BLOCK, int ITEMS, bool PULL>
+__device__ __forceinline__ void expand_tiles(const PersistArgs &a, PersistShared<BLOCK, ITEMS> &sh,
+                                             uint64_t total_n, uint64_t total_e, uint64_t skip,
+                                             unsigned long long act, const unsigned long long *cur,
+                                             unsigned long long *next, uint32_t *next_any) {
+  constexpr uint32_t TILE = BLOCK * ITEMS;
+  const uint64_t ntiles = (total_e + TILE - 1) / TILE;
+  for (uint64_t k = blockIdx.x; k < ntiles; k += gridDim.x) {
+    const uint64_t pos0 = k * TILE;
+    const uint32_t tlen = (uint32_t)min((uint64_t)TILE, total_e - pos0);
+    const uint32_t i0 = __ldcg(a.tile_first + k);
+    const uint32_t i1 = (k + 1 < ntiles) ? __ldcg(a.tile_first + k + 1) : (uint32_t)(total_n - 1);
+    const uint32_t nl = i1 - i0 + 1;
+    if (i1 < i0 || nl > TILE + 1) {  // uniform per tile
+      if (threadIdx.x == 0) atomicOr(a.err, kErrTileMap);
+      continue;
+    }
+    for (uint32_t j = threadIdx.x; j < nl; j += BLOCK) {
+      const uint32_t v = __ldcg(a.list + i0 + j);
+      const uint64_t p = __ldcg(a.pref + i0 + j);
+      sh.rs[j] = p > pos0 ? (uint32_t)min(p - pos0, (uint64_t)TILE) : 0u;
+      sh.cb[j] = a.off[v] + skip - p + pos0;
+      if (PULL) sh.val[j] = ~__ldcg(a.visited + v) & act & ~__ldcg(next + v);
+      else sh.val[j] = __ldcg(cur + v);
+    }
+    for (uint32_t x = threadIdx.x; x < TILE; x += BLOCK) sh.map[x] = 0;
+    __syncthreads();
+    for (uint32_t j = 1 + threadIdx.x; j < nl; j += BLOCK)
+      if (sh.rs[j] < TILE) sh.map[sh.rs[j]] = 1;
+    __syncthreads();
     {
-      uint32_t pn = 0, tn = 0;
-      uint64_t pe = 0, te = 0;
-      for (uint32_t b = threadIdx.x; b < gridDim.x; b += BLOCK) {
-        const uint32_t bn = __ldcg(a.cta_n + b);
-        const uint64_t be = __ldcg(a.cta_e + b);
-        tn += bn;
-        te += be;
-        if (b < blockIdx.x) {
-          pn += bn;
-          pe += be;
-        }
-      }
-      uint32_t x0, y0;
-      uint64_t x1, y1;
-      pscan<BLOCK>(sh, pn, pe, x0, x1, y0, y1);  // block sums of the predecessor parts
-      uint32_t z0, z1;
-      uint64_t z2, z3;
-      pscan<BLOCK>(sh, tn, te, z0, z2, z1, z3);
-      if (threadIdx.x == 0) {
-        sh.red_n = y0;
-        sh.red_e = y1;
-        sh.red_tn = z1;
-        sh.red_te = z3;
-      }
-      __syncthreads();
-    }
-    const uint64_t total_n = sh.red_tn, total_e = sh.red_te;
-    if (total_n == 0) break;  // every CTA sees the same totals
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      a.stat[0] += total_n;
-      a.stat[1] += total_e;
-    }
-    if (level >= kMaxBatchLevels) {
-      if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.err, kErrLevels);
-      break;
-    }
-    if (total_n > a.list_cap || total_e / TILE + 1 >= a.tile_cap) {
-      if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.err, kErrTileMap);
-      break;
-    }
-    {
-      uint32_t pos = sh.red_n + exc;
-      uint64_t ep = sh.red_e + exe;
-      for (uint64_t w = wb; w < we; w++)
-        for (uint32_t m = __ldcg(cur_any + w); m; m &= m - 1) {
-          const uint64_t v = w * 32 + (__ffs(m) - 1);
-          const uint64_t d = a.off[v + 1] - a.off[v];
-          if (!d) continue;
-          a.list[pos] = (uint32_t)v;
-          a.pref[pos] = ep;
-          for (uint64_t t = (ep + TILE - 1) / TILE; t * TILE < ep + d; t++) a.tile_first[t] = pos;
-          pos++;
-          ep += d;
-        }
-      if (blockIdx.x == gridDim.x - 1 && threadIdx.x == BLOCK - 1) a.pref[total_n] = total_e;
-    }
-    if (!grid_barrier(a.bar, a.err)) return;
-    // ---- 3. edge-balanced expansion of all listed vertices
-    const uint64_t ntiles = (total_e + TILE - 1) / TILE;
-    for (uint64_t k = blockIdx.x; k < ntiles; k += gridDim.x) {
-      const uint64_t pos0 = k * TILE;
-      const uint32_t tlen = (uint32_t)min((uint64_t)TILE, total_e - pos0);
-      const uint32_t i0 = __ldcg(a.tile_first + k);
-      const uint32_t i1 = (k + 1 < ntiles) ? __ldcg(a.tile_first + k + 1) : (uint32_t)(total_n - 1);
-      const uint32_t nl = i1 - i0 + 1;
-      if (i1 < i0 || nl > TILE + 1) {  // uniform per tile
-        if (threadIdx.x == 0) atomicOr(a.err, kErrTileMap);
-        continue;
-      }
-      for (uint32_t j = threadIdx.x; j < nl; j += BLOCK) {
-        const uint32_t v = __ldcg(a.list + i0 + j);
-        const uint64_t p = __ldcg(a.pref + i0 + j);
-        sh.rs[j] = p > pos0 ? (uint32_t)min(p - pos0, (uint64_t)TILE) : 0u;
-        sh.cb[j] = a.off[v] - p + pos0;
-        sh.val[j] = __ldcg(cur + v);
-      }
-      for (uint32_t x = threadIdx.x; x < TILE; x += BLOCK) sh.map[x] = 0;
-      __syncthreads();
-      for (uint32_t j = 1 + threadIdx.x; j < nl; j += BLOCK)
-        if (sh.rs[j] < TILE) sh.map[sh.rs[j]] = 1;
-      __syncthreads();
-      {
-        uint32_t f[ITEMS], s = 0;
+      uint32_t f[ITEMS], s = 0;
 #pragma unroll
-        for (int i = 0; i < ITEMS; i++) {
-          f[i] = sh.map[threadIdx.x * ITEMS + i];
-          s += f[i];
-        }
-        uint32_t ex, tot;
-        uint64_t ex64, tot64;
-        pscan<BLOCK>(sh, s, 0, ex, ex64, tot, tot64);
+      for (int i = 0; i < ITEMS; i++) {
+        f[i] = sh.map[threadIdx.x * ITEMS + i];
+        s += f[i];
+      }
+      uint32_t ex, tot;
+      uint64_t ex64, tot64;
+      pscan<BLOCK>(sh, s, 0, ex, ex64, tot, tot64);
 #pragma unroll
-        for (int i = 0; i < ITEMS; i++) {
-          ex += f[i];
-          sh.map[threadIdx.x * ITEMS + i] = (unsigned short)ex;
+      for (int i = 0; i < ITEMS; i++) {
+        ex += f[i];
+        sh.map[threadIdx.x * ITEMS + i] = (unsigned short)ex;
+      }
+    }
+    __syncthreads();
+    uint32_t ev[ITEMS];
+    uint32_t lv[ITEMS];
+    uint32_t okm = 0;
+#pragma unroll
+    for (int it = 0; it < ITEMS; it++) {
+      const uint32_t x = it * BLOCK + threadIdx.x;
+      lv[it] = 0;
+      if (x < tlen) {
+        const uint32_t l = sh.map[x];
+        const uint64_t idx = sh.cb[l] + x;
+        lv[it] = l;
+        if (idx < a.static_edges) {
+          ev[it] = a.ssrc.load(idx);
+          okm |= 1u << it;
+        } else if (idx < a.E && a.hsrc.words) {
+          ev[it] = a.hsrc.load(idx);
+          okm |= 1u << it;
+        } else {
+          atomicOr(a.err, kErrEdgeIndex);
         }
       }
+    }
+    // probe every target before the first atomic (the reads overlap; a stale
+    // visited probe only costs an extra atomic)
+    unsigned long long pv[ITEMS];
+#pragma unroll
+    for (int it = 0; it < ITEMS; it++) {
+      pv[it] = PULL ? 0ull : ~0ull;
+      if ((okm >> it) & 1u) {
+        const uint32_t v = edge_dst(ev[it]);
+        if (v < a.V) pv[it] = __ldcg((PULL ? cur : a.visited) + v);
+      }
+    }
+    if (PULL) {
+      __syncthreads();  // the record bases are no longer needed: cb becomes the accumulator
+      for (uint32_t j = threadIdx.x; j < nl; j += BLOCK) sh.cb[j] = 0ull;
       __syncthreads();
-      uint32_t ev[ITEMS];
-      uint32_t lv[ITEMS];
-      uint32_t okm = 0;
 #pragma unroll
       for (int it = 0; it < ITEMS; it++) {
-        const uint32_t x = it * BLOCK + threadIdx.x;
-        lv[it] = 0;
-        if (x < tlen) {
-          const uint32_t l = sh.map[x];
-          const uint64_t idx = sh.cb[l] + x;
-          lv[it] = l;
-          if (idx < a.static_edges) {
-            ev[it] = a.ssrc.load(idx);
-            okm |= 1u << it;
-          } else if (idx < a.E && a.hsrc.words) {
-            ev[it] = a.hsrc.load(idx);
-            okm |= 1u << it;
-          } else {
-            atomicOr(a.err, kErrEdgeIndex);
-          }
+        if (!(okm & (1u << it))) continue;
+        if (edge_dst(ev[it]) >= a.V) {
+          atomicOr(a.err, kErrVertex);
+          continue;
         }
+        const unsigned long long x = pv[it] & sh.val[lv[it]];
+        if (x) atomicOr(&sh.cb[lv[it]], x);
       }
-      // probe every target's visited mask before the first atomic (the reads
-      // overlap; a stale probe only costs an extra atomic)
-      unsigned long long pv[ITEMS];
-#pragma unroll
-      for (int it = 0; it < ITEMS; it++) {
-        pv[it] = ~0ull;
-        if ((okm >> it) & 1u) {
-          const uint32_t v = edge_dst(ev[it]);
-          if (v < a.V) pv[it] = __ldcg(a.visited + v);
-        }
-      }
+      __syncthreads();
+      for (uint32_t j = threadIdx.x; j < nl; j += BLOCK)
+        if (sh.cb[j]) atomicOr(next + __ldcg(a.list + i0 + j), sh.cb[j]);
+    } else {
 #pragma unroll
       for (int it = 0; it < ITEMS; it++) {
         if (!(okm & (1u << it))) continue;
@@ -316,17 +377,204 @@ __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
         if (!nb) continue;
         if (atomicOr(next + v, nb) == 0ull) atomicOr(next_any + (v >> 5), 1u << (v & 31));
       }
-      __syncthreads();  // shared tables are rebuilt for the next tile
+    }
+    __syncthreads();  // shared tables are rebuilt for the next tile
+  }
+}
+
+// Records a lane scans for one vertex in a bottom-up level before it hands
+// the rest of the vertex's list to the edge-balanced pull pass.
+constexpr uint64_t kBuLaneRecords = 32;
+
+// First part of a bottom-up level.  A warp owns 32-vertex words of the
+// bitmaps; each lane scans its vertex's records (HBM for the static prefix,
+// page-locked host memory beyond it) four at a time and ORs in its
+// neighbours' frontier masks, restricted to the active sources that have not
+// reached the vertex, until every one of them is found or kBuLaneRecords
+// records are read.  A vertex with records left and sources still missing is
+// deferred: its partial mask goes to next[v] and its bit to `defer`, and the
+// pull pass scans the rest of its list in parallel, so no lane walks a long
+// list alone.  A lane writes only its own vertex's masks and lane 0 its
+// warp's words of next_any and defer, so nothing here needs an atomic.
+template <int BLOCK>
+__device__ __forceinline__ void bottom_up_scan(const PersistArgs &a, unsigned long long act,
+                                               const unsigned long long *cur, unsigned long long *next,
+                                               uint32_t *next_any) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nwarps = (uint64_t)gridDim.x * (BLOCK / 32);
+  unsigned long long ns = 0, nd = 0;  // static / dynamic records read
+  for (uint64_t w = ((uint64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5; w < a.nwords; w += nwarps) {
+    const uint64_t v = w * 32 + lane;
+    unsigned long long found = 0;
+    bool defer = false;
+    if (v < a.V) {
+      const unsigned long long vis = __ldcg(a.visited + v);
+      const unsigned long long need = ~vis & act;
+      if (need) {
+        const uint64_t e0 = a.off[v], e1 = a.off[v + 1];
+        const uint64_t lim = min(e1, e0 + kBuLaneRecords);
+        for (uint64_t e = e0; e < lim && found != need; e += 4) {
+          uint32_t u[4];
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            const uint64_t i = e + j;
+            u[j] = 0xffffffffu;
+            if (i >= lim) continue;
+            if (i < a.static_edges) {
+              u[j] = a.ssrc.load(i);
+              ns++;
+            } else if (i < a.E && a.hsrc.words) {
+              u[j] = a.hsrc.load(i);
+              nd++;
+            } else {
+              atomicOr(a.err, kErrEdgeIndex);
+            }
+          }
+#pragma unroll
+          for (int j = 0; j < 4; j++) {
+            if (u[j] < a.V) found |= __ldcg(cur + u[j]) & need;
+            else if (u[j] != 0xffffffffu) atomicOr(a.err, kErrVertex);
+          }
+        }
+        defer = found != need && lim < e1;
+        if (defer) {
+          next[v] = found;
+        } else if (found) {
+          next[v] = found;
+          a.visited[v] = vis | found;
+        }
+      }
+    }
+    const uint32_t ball = __ballot_sync(0xffffffffu, found != 0ull && !defer);
+    const uint32_t dball = __ballot_sync(0xffffffffu, defer);
+    if (lane == 0) {
+      if (ball) next_any[w] = ball;
+      if (dball) a.defer[w] = dball;
+    }
+  }
+#pragma unroll
+  for (int o = 16; o; o >>= 1) {
+    ns += __shfl_xor_sync(0xffffffffu, ns, o);
+    nd += __shfl_xor_sync(0xffffffffu, nd, o);
+  }
+  if (lane == 0 && (ns | nd)) {
+    atomicAdd(a.stat + 1, ns + nd);
+    if (nd) atomicAdd(a.stat + 2, nd);
+  }
+}
+
+template <int BLOCK, int ITEMS>
+__global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
+  using SH = PersistShared<BLOCK, ITEMS>;
+  constexpr uint32_t TILE = SH::TILE;
+  __shared__ SH sh;
+  unsigned long long *cur = a.cur, *next = a.next;
+  uint32_t *cur_any = a.cur_any, *next_any = a.next_any;
+  // contiguous word range of this CTA, split into contiguous per-thread runs
+  const uint64_t wper_cta = (a.nwords + gridDim.x - 1) / gridDim.x;
+  const uint64_t wper_thr = (wper_cta + BLOCK - 1) / BLOCK;
+  const uint64_t wb = min(a.nwords, blockIdx.x * wper_cta + threadIdx.x * wper_thr);
+  const uint64_t we = min(min(a.nwords, (blockIdx.x + 1) * wper_cta), wb + wper_thr);
+  const unsigned long long all_src = a.n_src >= 64 ? ~0ull : (1ull << a.n_src) - 1ull;
+  bool bottom = false;   // this level is expanded bottom-up
+  uint64_t prev_n = 0;   // frontier size of the previous level
+  uint32_t level = 1;
+  for (;; level++) {
+    // sources whose frontier is not empty
+    const unsigned long long act = level == 1 ? all_src : __ldcg(a.act_slot(level));
+    // ---- 0. (top-down levels of a symmetric graph) degrees of the vertices
+    //         still missing an active source: the bottom-up work bound
+    const bool with_mu = a.dopt && !bottom;
+    if (with_mu) {
+      uint64_t mu = 0;
+      const uint64_t nthr = (uint64_t)gridDim.x * BLOCK;
+      for (uint64_t v = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; v < a.V; v += nthr)
+        if (~__ldcg(a.visited + v) & act) mu += a.off[v + 1] - a.off[v];
+      mu = block_sum<BLOCK>(sh, mu);
+      if (threadIdx.x == 0) a.cta_mu[blockIdx.x] = mu;
+    }
+    // ---- 1. count the frontier (vertices with edges) in this thread's words
+    uint32_t exc;
+    uint64_t exe, dyn;
+    count_list<BLOCK>(a, sh, cur_any, wb, we, 0, exc, exe, dyn);
+    if (!grid_barrier(a.bar, a.err)) return;
+    // ---- 2. grand totals, the level's direction, and its expansion
+    grid_totals<BLOCK>(a, sh, with_mu);
+    const uint64_t total_n = sh.red_tn, total_e = sh.red_te;
+    if (total_n == 0) break;  // every CTA sees the same totals
+    if (a.dopt) {
+      if (!bottom) bottom = total_e > sh.red_mu / kBatchAlpha;
+      else bottom = !(total_n < a.V / kBatchBeta && total_n < prev_n);
+    }
+    prev_n = total_n;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      a.stat[0] += total_n;
+      if (bottom) a.stat[3]++;
+      else a.stat[1] += total_e;
+      *a.act_slot(level + 1) = 0ull;  // last read in phase 0 of the previous level
+    }
+    if (level >= kMaxBatchLevels) {
+      if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.err, kErrLevels);
+      break;
+    }
+    if (!bottom) {
+      if (dyn) atomicAdd(a.stat + 2, (unsigned long long)dyn);
+      if (total_n > a.list_cap || total_e / TILE + 1 >= a.tile_cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.err, kErrTileMap);
+        break;
+      }
+      write_list<TILE>(a, cur_any, wb, we, 0, sh.red_n + exc, sh.red_e + exe, total_n, total_e);
+      if (!grid_barrier(a.bar, a.err)) return;
+      expand_tiles<BLOCK, ITEMS, false>(a, sh, total_n, total_e, 0, act, cur, next, next_any);
+    } else {
+      bottom_up_scan<BLOCK>(a, act, cur, next, next_any);
+      if (!grid_barrier(a.bar, a.err)) return;
+      // the deferred vertices' remaining records, edge-balanced
+      count_list<BLOCK>(a, sh, a.defer, wb, we, kBuLaneRecords, exc, exe, dyn);
+      if (!grid_barrier(a.bar, a.err)) return;
+      grid_totals<BLOCK>(a, sh, false);
+      const uint64_t dn = sh.red_tn, de = sh.red_te;
+      if (dn) {
+        if (dyn) atomicAdd(a.stat + 2, (unsigned long long)dyn);
+        if (blockIdx.x == 0 && threadIdx.x == 0) a.stat[1] += de;
+        if (dn > a.list_cap || de / TILE + 1 >= a.tile_cap) {
+          if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.err, kErrTileMap);
+          break;
+        }
+        write_list<TILE>(a, a.defer, wb, we, kBuLaneRecords, sh.red_n + exc, sh.red_e + exe, dn, de);
+        if (!grid_barrier(a.bar, a.err)) return;
+        expand_tiles<BLOCK, ITEMS, true>(a, sh, dn, de, kBuLaneRecords, act, cur, next, next_any);
+      }
     }
     if (!grid_barrier(a.bar, a.err)) return;
-    // ---- 4. per-source counts of the newly reached vertices, depths, and
-    //         clearing of the consumed frontier
+    // ---- 4. settle the deferred vertices; per-source counts of the newly
+    //         reached vertices, depths, and clearing of the consumed frontier
     if (threadIdx.x < 64) sh.cnt[threadIdx.x] = 0;
+    if (threadIdx.x == 0) sh.act = 0ull;
     __syncthreads();
+    unsigned long long nact = 0;  // sources with a vertex in the next frontier
     for (uint64_t w = wb; w < we; w++) {
+      if (bottom) {
+        const uint32_t dm = __ldcg(a.defer + w);
+        if (dm) {
+          uint32_t nb = 0;
+          for (uint32_t m = dm; m; m &= m - 1) {
+            const uint64_t v = w * 32 + (__ffs(m) - 1);
+            const unsigned long long f = __ldcg(next + v);
+            if (f) {
+              a.visited[v] = __ldcg(a.visited + v) | f;
+              nb |= m & (0u - m);
+            }
+          }
+          if (nb) next_any[w] = __ldcg(next_any + w) | nb;
+          a.defer[w] = 0u;
+        }
+      }
       for (uint32_t m = __ldcg(next_any + w); m; m &= m - 1) {
         const uint64_t v = w * 32 + (__ffs(m) - 1);
-        for (unsigned long long b = __ldcg(next + v); b; b &= b - 1) {
+        const unsigned long long nv = __ldcg(next + v);
+        nact |= nv;
+        for (unsigned long long b = nv; b; b &= b - 1) {
           const uint32_t s = __ffsll((long long)b) - 1;
           if (s < a.n_src) {
             atomicAdd(&sh.cnt[s], 1u);
@@ -337,9 +585,13 @@ __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
       for (uint32_t m = __ldcg(cur_any + w); m; m &= m - 1) cur[w * 32 + (__ffs(m) - 1)] = 0ull;
       cur_any[w] = 0u;
     }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) nact |= __shfl_xor_sync(0xffffffffu, nact, o);
+    if ((threadIdx.x & 31) == 0 && nact) atomicOr(&sh.act, nact);
     __syncthreads();
     if (threadIdx.x < 64 && sh.cnt[threadIdx.x])
       atomicAdd(a.hist + (uint64_t)level * 64 + threadIdx.x, (unsigned long long)sh.cnt[threadIdx.x]);
+    if (threadIdx.x == 0 && sh.act) atomicOr(a.act_slot(level + 1), sh.act);
     // the next level reads the counts and masks written above by other CTAs
     if (!grid_barrier(a.bar, a.err)) return;
     unsigned long long *tm = cur;

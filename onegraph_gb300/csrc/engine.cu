@@ -116,6 +116,7 @@ struct og_engine {
   uint32_t min_rounds_hint[2] = {16, 4};  // SSSP, CC
   uint32_t graph_n = 0;
   int graph_cfg = -1;
+  int graph_dopt = -1;
   bool graph_broken = false;
 
   og_engine *parent = nullptr;  // set on clones: resident state belongs to the parent
@@ -269,8 +270,8 @@ int create_query_state(og_engine *e) {
     e->ptile_cap = e->g->E / 1024 + 8;
     RC(dalloc(e, &e->ptile_d, e->ptile_cap));
     RC(dalloc(e, &e->cta_n, kMaxPersistCtas));
-    RC(dalloc(e, &e->cta_e, kMaxPersistCtas));
-    RC(dalloc(e, &e->bar_d, 16));  // barrier (2), error, levels, stats (4 u64)
+    RC(dalloc(e, &e->cta_e, 2 * kMaxPersistCtas));  // frontier degree sums, then missing-source degree sums
+    RC(dalloc(e, &e->bar_d, 16));  // barrier (2), error, levels, stats (6 u64)
     CK(cudaMallocHost(&e->hist_h, (size_t)kMaxBatchLevels * 64 * sizeof(unsigned long long)));
     CK(cudaMallocHost(&e->srcs_h, 64 * sizeof(uint32_t)));
     CK(cudaMallocHost(&e->pmisc_h, 16 * sizeof(uint32_t)));
@@ -1233,6 +1234,12 @@ int launch_persist(og_engine *e, int ci, const PersistArgs &a, cudaStream_t s) {
   }
 }
 
+// Bottom-up levels need the graph's reverse edges: only a symmetric graph has
+// them in its own records.
+uint32_t batch_dopt(const og_engine *e) {
+  return e->bfs_direction == OG_BFS_AUTO && e->g->symmetric == 1 ? 1u : 0u;
+}
+
 // Enqueues one whole batch on s_main: clear state, upload the sources from the
 // page-locked buffer, seed, run every level in one cooperative kernel, copy
 // the per-level counts and the status words back to page-locked memory.
@@ -1242,6 +1249,7 @@ int enqueue_persist(og_engine *e, uint32_t n, int ci, uint32_t *depth_d) {
   for (int i = 0; i < 3; i++) CK(cudaMemsetAsync(e->bmask[i], 0, 8 * (V + 1), s));
   CK(cudaMemsetAsync(e->bm[0], 0, 4 * e->nwords, s));
   CK(cudaMemsetAsync(e->bm[1], 0, 4 * e->nwords, s));
+  CK(cudaMemsetAsync(e->bm[2], 0, 4 * e->nwords, s));  // deferred bottom-up vertices
   CK(cudaMemsetAsync(e->hist_d, 0, 8ull * kMaxBatchLevels * 64, s));
   CK(cudaMemsetAsync(e->bar_d, 0, 64, s));
   CK(cudaMemcpyAsync(e->srcs_d, e->srcs_h, 4 * n, cudaMemcpyHostToDevice, s));
@@ -1274,7 +1282,10 @@ int enqueue_persist(og_engine *e, uint32_t n, int ci, uint32_t *depth_d) {
   a.err = e->bar_d + 2;
   a.levels = e->bar_d + 3;
   a.stat = (unsigned long long *)(e->bar_d + 4);
+  a.cta_mu = e->cta_e + kMaxPersistCtas;
+  a.defer = e->bm[2];
   a.Vs = e->Vs;
+  a.dopt = batch_dopt(e);
   RC(launch_persist(e, ci, a, s));
   CK(cudaMemcpyAsync(e->hist_h, e->hist_d, 8ull * kMaxBatchLevels * 64, cudaMemcpyDeviceToHost, s));
   CK(cudaMemcpyAsync(e->pmisc_h, e->bar_d, 64, cudaMemcpyDeviceToHost, s));
@@ -1284,7 +1295,9 @@ int enqueue_persist(og_engine *e, uint32_t n, int ci, uint32_t *depth_d) {
 // Captures enqueue_persist for (n, config) as a CUDA graph once and replays it.
 int run_persist_graph(og_engine *e, uint32_t n, int ci, bool *used_graph) {
   *used_graph = false;
-  if (!e->graph_broken && !(e->graph && e->graph_n == n && e->graph_cfg == ci)) {
+  const int dopt = (int)batch_dopt(e);
+  if (!e->graph_broken &&
+      !(e->graph && e->graph_n == n && e->graph_cfg == ci && e->graph_dopt == dopt)) {
     if (e->graph) {
       cudaGraphExecDestroy(e->graph);
       e->graph = nullptr;
@@ -1304,6 +1317,7 @@ int run_persist_graph(og_engine *e, uint32_t n, int ci, bool *used_graph) {
     } else {
       e->graph_n = n;
       e->graph_cfg = ci;
+      e->graph_dopt = dopt;
     }
   }
   if (e->graph) {

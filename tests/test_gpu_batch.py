@@ -97,3 +97,40 @@ def test_batch_errors():
     with pytest.raises(og.OGError) as ex:
         b.bfs_batch([g.V])
     assert ex.value.status == 1
+
+
+@pytest.mark.parametrize("scale", [10, 13])
+def test_batch_bottom_up_levels(scale):
+    """On a symmetric graph the persistent kernel expands the wide levels
+    bottom-up; its depths equal the top-down-only kernel's and single-source
+    runs, in every region layout, and it examines fewer edges.  A directed
+    graph (no reverse edges) stays top-down."""
+    g = og.Graph.rmat(scale, 16, seed=11)
+    assert g.symmetric()
+    deg = g.degrees()
+    rng = np.random.default_rng(scale)
+    srcs = rng.integers(0, g.V, 64).astype(np.uint32)
+    srcs[0] = np.argmax(deg)
+    for cname, kw in batch_configs(g):
+        e = og.Engine(g, batch=True, **kw)
+        got, ck = e.bfs_batch(srcs)
+        _, ck_r = e.bfs_batch(srcs, out=False)  # captured graph
+        auto_edges = e.stats["edges_static"] + e.stats["edges_dynamic"]
+        e.set_param(og.PARAM_BFS_DIRECTION, og.BFS_TOP_DOWN)
+        want, wck = e.bfs_batch(srcs)
+        _, ck_t = e.bfs_batch(srcs, out=False)  # recaptured for the new direction
+        td_edges = e.stats["edges_static"] + e.stats["edges_dynamic"]
+        np.testing.assert_array_equal(got, want, err_msg=cname)
+        np.testing.assert_array_equal(ck, wck)
+        np.testing.assert_array_equal(ck_r, wck)
+        np.testing.assert_array_equal(ck_t, wck)
+        assert auto_edges < td_edges, (cname, auto_edges, td_edges)
+        for i in (0, 1, 63):
+            np.testing.assert_array_equal(got[i], e.bfs(int(srcs[i])), err_msg="%s source %d" % (cname, i))
+        e.close()
+    gd = og.Graph.rmat(scale, 16, seed=11, symmetric=False)
+    e = og.Engine(gd, batch=True, budget=1 << 30, advisek=1.0)
+    got, _ = e.bfs_batch(srcs)
+    for i in (0, 1, 63):
+        np.testing.assert_array_equal(got[i], e.bfs(int(srcs[i])))
+    e.close()
