@@ -10,15 +10,19 @@
 // vertices.  No reference counterpart: the reference runs sources one by one
 // (BFS/oneGraph_BFS/CalculateOpt.h:55-209).
 //
-// On a symmetric graph a level may instead be expanded bottom-up: every
-// vertex that some active source has not reached scans its own records and
-// ORs in its neighbours' frontier masks, stopping as soon as every missing
-// active source is found.  The choice per level is the direction-optimizing
-// rule of Beamer et al. (SC 2012) on batch totals: bottom-up once the
-// frontier's edges exceed 1/14 of the edges of the vertices still missing an
-// active source; top-down again when the frontier is under V/24 vertices and
-// shrinking.  Every CTA computes the same totals, so all take the same
-// branch.  The masks produced are the same in both directions.
+// On a symmetric graph each source chooses its direction per level (the
+// direction-optimizing rule of Beamer et al., SC 2012, applied to every
+// source's own frontier): bottom-up once the source's frontier edges exceed
+// 1/14 of the edges of the vertices it has not reached, top-down again when
+// its frontier is under V/24 vertices and shrinking.  A level then runs the
+// bottom-up sources first (every vertex that one of them has not reached
+// scans its own records and ORs in its neighbours' frontier masks,
+// restricted to those sources, until all are found) and the top-down
+// sources after (the frontier vertices of those sources push their masks,
+// restricted to them).  A source whose frontier is small stays top-down, so
+// it never forces full scans on the vertices it does not reach.  Every CTA
+// computes the same per-source statistics and so the same choice; the masks
+// produced are the same in every direction.
 // Data written by other CTAs during the launch (list, prefix, tile map,
 // frontier words and masks) is read with __ldcg: L1 is not coherent within a
 // kernel, so a plain load could return a line cached in an earlier level.
@@ -54,13 +58,17 @@ struct PersistArgs {
   uint32_t *err;
   uint32_t *levels;           // number of expanded levels (out)
   unsigned long long *stat;   // [0] listed vertices, [1] edges expanded, [2] of them dynamic,
-                              // [3] bottom-up levels, [4..5] OR of the frontier masks by level parity
-  unsigned long long *cta_mu; // per-CTA degree sums of the vertices missing an active source
+                              // [3] levels with bottom-up sources, [4..5] OR of the frontier masks
+                              // by level parity
+  unsigned long long *smf;    // [2][64] per-source frontier degree sums by level parity
   uint32_t *defer;            // bottom-up vertices handed to the pull pass (bitmap, zero between levels)
   uint32_t Vs;                // first dynamic vertex
-  uint32_t dopt;              // bottom-up levels allowed (the graph is symmetric)
+  uint32_t dopt;              // bottom-up sources allowed (the graph is symmetric)
   __device__ __forceinline__ unsigned long long *act_slot(uint32_t level) const {
     return stat + 4 + (level & 1u);
+  }
+  __device__ __forceinline__ unsigned long long *smf_slot(uint32_t level) const {
+    return smf + 64 * (level & 1u);
   }
 };
 
@@ -105,23 +113,11 @@ struct PersistShared {
   unsigned long long wsum_e[BLOCK / 32];
   uint32_t cnt[64];
   uint32_t red_n;
-  unsigned long long red_e, red_tn, red_te, red_mu;
+  unsigned long long red_e, red_tn, red_te;
   unsigned long long act;
+  unsigned long long msum[64];  // per-source degree sums of the newly reached vertices
+  uint32_t bu_w[2];             // this level's bottom-up sources
 };
-
-// block-wide sum of a u64 (BLOCK threads); every thread gets the total
-template <int BLOCK, class SH>
-__device__ __forceinline__ uint64_t block_sum(SH &sh, uint64_t x) {
-#pragma unroll
-  for (int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
-  if ((threadIdx.x & 31) == 0) sh.wsum_e[threadIdx.x >> 5] = x;
-  __syncthreads();
-  uint64_t t = 0;
-#pragma unroll
-  for (int w = 0; w < BLOCK / 32; w++) t += sh.wsum_e[w];
-  __syncthreads();
-  return t;
-}
 
 // block-wide exclusive scan of (u32, u64) with totals; BLOCK threads
 template <int BLOCK, class SH>
@@ -177,9 +173,11 @@ __device__ __forceinline__ uint64_t rest_deg(const PersistArgs &a, uint64_t v, u
 
 // Count the listed vertices of this thread's words of `bits` (those with
 // records beyond `skip`) and their record sums; publish the CTA's totals.
+// With `masks`, only vertices whose mask shares a bit with `sel` count.
 template <int BLOCK, class SH>
 __device__ __forceinline__ void count_list(const PersistArgs &a, SH &sh, const uint32_t *bits, uint64_t wb,
-                                           uint64_t we, uint64_t skip, uint32_t &exc, uint64_t &exe,
+                                           uint64_t we, uint64_t skip, const unsigned long long *masks,
+                                           unsigned long long sel, uint32_t &exc, uint64_t &exe,
                                            uint64_t &dyn) {
   uint32_t c = 0;
   uint64_t e = 0;
@@ -187,6 +185,7 @@ __device__ __forceinline__ void count_list(const PersistArgs &a, SH &sh, const u
   for (uint64_t w = wb; w < we; w++)
     for (uint32_t m = __ldcg(bits + w); m; m &= m - 1) {
       const uint64_t v = w * 32 + (__ffs(m) - 1);
+      if (masks && !(__ldcg(masks + v) & sel)) continue;
       const uint64_t d = rest_deg(a, v, skip);
       c += d ? 1u : 0u;
       e += d;
@@ -202,24 +201,22 @@ __device__ __forceinline__ void count_list(const PersistArgs &a, SH &sh, const u
 }
 
 // After count_list and a grid barrier: this CTA's list offset (sh.red_n,
-// sh.red_e), the grid totals (sh.red_tn, sh.red_te) and, when with_mu, the
-// grid sum of cta_mu (sh.red_mu).  Every CTA computes the same totals.
+// sh.red_e) and the grid totals (sh.red_tn, sh.red_te).  Every CTA computes
+// the same totals.
 template <int BLOCK, class SH>
-__device__ __forceinline__ void grid_totals(const PersistArgs &a, SH &sh, bool with_mu) {
+__device__ __forceinline__ void grid_totals(const PersistArgs &a, SH &sh) {
   uint32_t pn = 0, tn = 0;
-  uint64_t pe = 0, te = 0, tmu = 0;
+  uint64_t pe = 0, te = 0;
   for (uint32_t b = threadIdx.x; b < gridDim.x; b += BLOCK) {
     const uint32_t bn = __ldcg(a.cta_n + b);
     const uint64_t be = __ldcg(a.cta_e + b);
     tn += bn;
     te += be;
-    if (with_mu) tmu += __ldcg(a.cta_mu + b);
     if (b < blockIdx.x) {
       pn += bn;
       pe += be;
     }
   }
-  tmu = block_sum<BLOCK>(sh, tmu);
   uint32_t x0, y0;
   uint64_t x1, y1;
   pscan<BLOCK>(sh, pn, pe, x0, x1, y0, y1);  // block sums of the predecessor parts
@@ -231,7 +228,6 @@ __device__ __forceinline__ void grid_totals(const PersistArgs &a, SH &sh, bool w
     sh.red_e = y1;
     sh.red_tn = z1;
     sh.red_te = z3;
-    sh.red_mu = tmu;
   }
   __syncthreads();
 }
@@ -240,11 +236,13 @@ __device__ __forceinline__ void grid_totals(const PersistArgs &a, SH &sh, bool w
 // the first list entry of every tile; positions come from count_list's scan.
 template <uint32_t TILE>
 __device__ __forceinline__ void write_list(const PersistArgs &a, const uint32_t *bits, uint64_t wb, uint64_t we,
-                                           uint64_t skip, uint32_t pos, uint64_t ep, uint64_t total_n,
-                                           uint64_t total_e) {
+                                           uint64_t skip, const unsigned long long *masks,
+                                           unsigned long long sel, uint32_t pos, uint64_t ep,
+                                           uint64_t total_n, uint64_t total_e) {
   for (uint64_t w = wb; w < we; w++)
     for (uint32_t m = __ldcg(bits + w); m; m &= m - 1) {
       const uint64_t v = w * 32 + (__ffs(m) - 1);
+      if (masks && !(__ldcg(masks + v) & sel)) continue;
       const uint64_t d = rest_deg(a, v, skip);
       if (!d) continue;
       a.list[pos] = (uint32_t)v;
@@ -257,7 +255,7 @@ __device__ __forceinline__ void write_list(const PersistArgs &a, const uint32_t 
 }
 
 // Edge-balanced pass over the listed vertices' records (from record `skip` of
-// each), TILE records per CTA tile.
+// each), TILE records per CTA tile, for the sources in `sel`.
 //  push (top-down): a listed vertex's frontier mask goes to every neighbour
 //    that a source of the mask has not reached (visited / next / next_any by
 //    atomicOr).
@@ -268,7 +266,7 @@ __device__ __forceinline__ void write_list(const PersistArgs &a, const uint32_t 
 template <int BLOCK, int ITEMS, bool PULL>
 __device__ __forceinline__ void expand_tiles(const PersistArgs &a, PersistShared<BLOCK, ITEMS> &sh,
                                              uint64_t total_n, uint64_t total_e, uint64_t skip,
-                                             unsigned long long act, const unsigned long long *cur,
+                                             unsigned long long sel, const unsigned long long *cur,
                                              unsigned long long *next, uint32_t *next_any) {
   constexpr uint32_t TILE = BLOCK * ITEMS;
   const uint64_t ntiles = (total_e + TILE - 1) / TILE;
@@ -287,8 +285,8 @@ __device__ __forceinline__ void expand_tiles(const PersistArgs &a, PersistShared
       const uint64_t p = __ldcg(a.pref + i0 + j);
       sh.rs[j] = p > pos0 ? (uint32_t)min(p - pos0, (uint64_t)TILE) : 0u;
       sh.cb[j] = a.off[v] + skip - p + pos0;
-      if (PULL) sh.val[j] = ~__ldcg(a.visited + v) & act & ~__ldcg(next + v);
-      else sh.val[j] = __ldcg(cur + v);
+      if (PULL) sh.val[j] = ~__ldcg(a.visited + v) & sel & ~__ldcg(next + v);
+      else sh.val[j] = __ldcg(cur + v) & sel;
     }
     for (uint32_t x = threadIdx.x; x < TILE; x += BLOCK) sh.map[x] = 0;
     __syncthreads();
@@ -386,18 +384,18 @@ __device__ __forceinline__ void expand_tiles(const PersistArgs &a, PersistShared
 // the rest of the vertex's list to the edge-balanced pull pass.
 constexpr uint64_t kBuLaneRecords = 32;
 
-// First part of a bottom-up level.  A warp owns 32-vertex words of the
-// bitmaps; each lane scans its vertex's records (HBM for the static prefix,
-// page-locked host memory beyond it) four at a time and ORs in its
-// neighbours' frontier masks, restricted to the active sources that have not
-// reached the vertex, until every one of them is found or kBuLaneRecords
+// Bottom-up part of a level, for the sources in `sel`.  A warp owns 32-vertex
+// words of the bitmaps; each lane scans its vertex's records (HBM for the
+// static prefix, page-locked host memory beyond it) four at a time and ORs in
+// its neighbours' frontier masks, restricted to the sources of `sel` that
+// have not reached the vertex, until every one of them is found or kBuLaneRecords
 // records are read.  A vertex with records left and sources still missing is
 // deferred: its partial mask goes to next[v] and its bit to `defer`, and the
 // pull pass scans the rest of its list in parallel, so no lane walks a long
 // list alone.  A lane writes only its own vertex's masks and lane 0 its
 // warp's words of next_any and defer, so nothing here needs an atomic.
 template <int BLOCK>
-__device__ __forceinline__ void bottom_up_scan(const PersistArgs &a, unsigned long long act,
+__device__ __forceinline__ void bottom_up_scan(const PersistArgs &a, unsigned long long sel,
                                                const unsigned long long *cur, unsigned long long *next,
                                                uint32_t *next_any) {
   const uint32_t lane = threadIdx.x & 31;
@@ -409,7 +407,7 @@ __device__ __forceinline__ void bottom_up_scan(const PersistArgs &a, unsigned lo
     bool defer = false;
     if (v < a.V) {
       const unsigned long long vis = __ldcg(a.visited + v);
-      const unsigned long long need = ~vis & act;
+      const unsigned long long need = ~vis & sel;
       if (need) {
         const uint64_t e0 = a.off[v], e1 = a.off[v + 1];
         const uint64_t lim = min(e1, e0 + kBuLaneRecords);
@@ -463,8 +461,11 @@ __device__ __forceinline__ void bottom_up_scan(const PersistArgs &a, unsigned lo
   }
 }
 
+// Resident threads per SM asked of the register allocator: 1024 (64
+// registers a thread) for the short tiles; the long tiles keep more items in
+// flight per thread and get 128 registers.
 template <int BLOCK, int ITEMS>
-__global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
+__global__ void __launch_bounds__(BLOCK, (ITEMS <= 4 ? 1024 : 512) / BLOCK) k_batch_persistent(PersistArgs a) {
   using SH = PersistShared<BLOCK, ITEMS>;
   constexpr uint32_t TILE = SH::TILE;
   __shared__ SH sh;
@@ -476,63 +477,68 @@ __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
   const uint64_t wb = min(a.nwords, blockIdx.x * wper_cta + threadIdx.x * wper_thr);
   const uint64_t we = min(min(a.nwords, (blockIdx.x + 1) * wper_cta), wb + wper_thr);
   const unsigned long long all_src = a.n_src >= 64 ? ~0ull : (1ull << a.n_src) - 1ull;
-  bool bottom = false;   // this level is expanded bottom-up
-  uint64_t prev_n = 0;   // frontier size of the previous level
+  // direction state of source threadIdx.x (threads 0..63 of every CTA)
+  bool src_bu = false;       // the source expands bottom-up
+  uint64_t src_prev_n = 0;   // its previous frontier size
+  uint64_t src_explored = 0; // record count of the vertices it has reached
   uint32_t level = 1;
   for (;; level++) {
     // sources whose frontier is not empty
     const unsigned long long act = level == 1 ? all_src : __ldcg(a.act_slot(level));
-    // ---- 0. (top-down levels of a symmetric graph) degrees of the vertices
-    //         still missing an active source: the bottom-up work bound
-    const bool with_mu = a.dopt && !bottom;
-    if (with_mu) {
-      uint64_t mu = 0;
-      const uint64_t nthr = (uint64_t)gridDim.x * BLOCK;
-      for (uint64_t v = (uint64_t)blockIdx.x * BLOCK + threadIdx.x; v < a.V; v += nthr)
-        if (~__ldcg(a.visited + v) & act) mu += a.off[v + 1] - a.off[v];
-      mu = block_sum<BLOCK>(sh, mu);
-      if (threadIdx.x == 0) a.cta_mu[blockIdx.x] = mu;
-    }
-    // ---- 1. count the frontier (vertices with edges) in this thread's words
-    uint32_t exc;
-    uint64_t exe, dyn;
-    count_list<BLOCK>(a, sh, cur_any, wb, we, 0, exc, exe, dyn);
-    if (!grid_barrier(a.bar, a.err)) return;
-    // ---- 2. grand totals, the level's direction, and its expansion
-    grid_totals<BLOCK>(a, sh, with_mu);
-    const uint64_t total_n = sh.red_tn, total_e = sh.red_te;
-    if (total_n == 0) break;  // every CTA sees the same totals
+    // ---- 0. each source's direction for this level (symmetric graphs)
+    unsigned long long bu = 0;
     if (a.dopt) {
-      if (!bottom) bottom = total_e > sh.red_mu / kBatchAlpha;
-      else bottom = !(total_n < a.V / kBatchBeta && total_n < prev_n);
+      if (threadIdx.x < 64) {
+        bool b = false;
+        if (level > 1 && ((act >> threadIdx.x) & 1ull)) {
+          const uint64_t mf = __ldcg(a.smf_slot(level) + threadIdx.x);
+          const uint64_t nf = __ldcg(a.hist + (uint64_t)(level - 1) * 64 + threadIdx.x);
+          const uint64_t mu = a.E > src_explored ? a.E - src_explored : 0;
+          if (!src_bu) src_bu = mf > mu / kBatchAlpha;
+          else src_bu = !(nf < a.V / kBatchBeta && nf < src_prev_n);
+          src_prev_n = nf;
+          src_explored += mf;
+          b = src_bu;
+        }
+        const uint32_t ball = __ballot_sync(0xffffffffu, b);
+        if ((threadIdx.x & 31) == 0) sh.bu_w[threadIdx.x >> 5] = ball;
+      }
+      __syncthreads();
+      bu = (((unsigned long long)sh.bu_w[1] << 32) | sh.bu_w[0]) & act;
     }
-    prev_n = total_n;
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-      a.stat[0] += total_n;
-      if (bottom) a.stat[3]++;
-      else a.stat[1] += total_e;
-      *a.act_slot(level + 1) = 0ull;  // last read in phase 0 of the previous level
+    const unsigned long long td = act & ~bu;
+    // ---- 1. count the frontier vertices of the top-down sources in this
+    //         thread's words
+    uint32_t exc;
+    uint64_t exe, dyn_td;
+    count_list<BLOCK>(a, sh, cur_any, wb, we, 0, a.dopt ? cur : nullptr, td, exc, exe, dyn_td);
+    if (!grid_barrier(a.bar, a.err)) return;
+    // ---- 2. grand totals, then the bottom-up and the top-down sources
+    grid_totals<BLOCK>(a, sh);
+    const uint64_t total_n = sh.red_tn, total_e = sh.red_te;
+    const uint32_t td_pos = sh.red_n + exc;
+    const uint64_t td_ep = sh.red_e + exe;
+    if (total_n == 0 && bu == 0) break;  // every CTA sees the same totals
+    if (blockIdx.x == 0) {
+      if (threadIdx.x == 0) {
+        a.stat[0] += total_n;
+        if (bu) a.stat[3]++;
+        *a.act_slot(level + 1) = 0ull;  // last read in phase 0 of the previous level
+      }
+      if (threadIdx.x < 64) a.smf_slot(level + 1)[threadIdx.x] = 0ull;
     }
     if (level >= kMaxBatchLevels) {
       if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.err, kErrLevels);
       break;
     }
-    if (!bottom) {
-      if (dyn) atomicAdd(a.stat + 2, (unsigned long long)dyn);
-      if (total_n > a.list_cap || total_e / TILE + 1 >= a.tile_cap) {
-        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.err, kErrTileMap);
-        break;
-      }
-      write_list<TILE>(a, cur_any, wb, we, 0, sh.red_n + exc, sh.red_e + exe, total_n, total_e);
-      if (!grid_barrier(a.bar, a.err)) return;
-      expand_tiles<BLOCK, ITEMS, false>(a, sh, total_n, total_e, 0, act, cur, next, next_any);
-    } else {
-      bottom_up_scan<BLOCK>(a, act, cur, next, next_any);
+    if (bu) {
+      bottom_up_scan<BLOCK>(a, bu, cur, next, next_any);
       if (!grid_barrier(a.bar, a.err)) return;
       // the deferred vertices' remaining records, edge-balanced
-      count_list<BLOCK>(a, sh, a.defer, wb, we, kBuLaneRecords, exc, exe, dyn);
+      uint64_t dyn;
+      count_list<BLOCK>(a, sh, a.defer, wb, we, kBuLaneRecords, nullptr, 0, exc, exe, dyn);
       if (!grid_barrier(a.bar, a.err)) return;
-      grid_totals<BLOCK>(a, sh, false);
+      grid_totals<BLOCK>(a, sh);
       const uint64_t dn = sh.red_tn, de = sh.red_te;
       if (dn) {
         if (dyn) atomicAdd(a.stat + 2, (unsigned long long)dyn);
@@ -541,20 +547,37 @@ __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
           if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.err, kErrTileMap);
           break;
         }
-        write_list<TILE>(a, a.defer, wb, we, kBuLaneRecords, sh.red_n + exc, sh.red_e + exe, dn, de);
+        write_list<TILE>(a, a.defer, wb, we, kBuLaneRecords, nullptr, 0, sh.red_n + exc, sh.red_e + exe, dn,
+                         de);
         if (!grid_barrier(a.bar, a.err)) return;
-        expand_tiles<BLOCK, ITEMS, true>(a, sh, dn, de, kBuLaneRecords, act, cur, next, next_any);
+        expand_tiles<BLOCK, ITEMS, true>(a, sh, dn, de, kBuLaneRecords, bu, cur, next, next_any);
+        // the list buffers are rebuilt for the top-down sources below
+        if (!grid_barrier(a.bar, a.err)) return;
       }
+    }
+    if (total_n) {
+      if (dyn_td) atomicAdd(a.stat + 2, (unsigned long long)dyn_td);
+      if (blockIdx.x == 0 && threadIdx.x == 0) a.stat[1] += total_e;
+      if (total_n > a.list_cap || total_e / TILE + 1 >= a.tile_cap) {
+        if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.err, kErrTileMap);
+        break;
+      }
+      write_list<TILE>(a, cur_any, wb, we, 0, a.dopt ? cur : nullptr, td, td_pos, td_ep, total_n, total_e);
+      if (!grid_barrier(a.bar, a.err)) return;
+      expand_tiles<BLOCK, ITEMS, false>(a, sh, total_n, total_e, 0, td, cur, next, next_any);
     }
     if (!grid_barrier(a.bar, a.err)) return;
     // ---- 4. settle the deferred vertices; per-source counts of the newly
     //         reached vertices, depths, and clearing of the consumed frontier
-    if (threadIdx.x < 64) sh.cnt[threadIdx.x] = 0;
+    if (threadIdx.x < 64) {
+      sh.cnt[threadIdx.x] = 0;
+      sh.msum[threadIdx.x] = 0;
+    }
     if (threadIdx.x == 0) sh.act = 0ull;
     __syncthreads();
     unsigned long long nact = 0;  // sources with a vertex in the next frontier
     for (uint64_t w = wb; w < we; w++) {
-      if (bottom) {
+      if (bu) {
         const uint32_t dm = __ldcg(a.defer + w);
         if (dm) {
           uint32_t nb = 0;
@@ -573,11 +596,13 @@ __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
       for (uint32_t m = __ldcg(next_any + w); m; m &= m - 1) {
         const uint64_t v = w * 32 + (__ffs(m) - 1);
         const unsigned long long nv = __ldcg(next + v);
+        const uint64_t d = a.dopt ? a.off[v + 1] - a.off[v] : 0;
         nact |= nv;
         for (unsigned long long b = nv; b; b &= b - 1) {
           const uint32_t s = __ffsll((long long)b) - 1;
           if (s < a.n_src) {
             atomicAdd(&sh.cnt[s], 1u);
+            if (d) atomicAdd(&sh.msum[s], (unsigned long long)d);
             if (a.depth) a.depth[(uint64_t)s * a.V + v] = level + 1;
           }
         }
@@ -591,6 +616,8 @@ __global__ void __launch_bounds__(BLOCK) k_batch_persistent(PersistArgs a) {
     __syncthreads();
     if (threadIdx.x < 64 && sh.cnt[threadIdx.x])
       atomicAdd(a.hist + (uint64_t)level * 64 + threadIdx.x, (unsigned long long)sh.cnt[threadIdx.x]);
+    if (threadIdx.x < 64 && sh.msum[threadIdx.x])
+      atomicAdd(a.smf_slot(level + 1) + threadIdx.x, sh.msum[threadIdx.x]);
     if (threadIdx.x == 0 && sh.act) atomicOr(a.act_slot(level + 1), sh.act);
     // the next level reads the counts and masks written above by other CTAs
     if (!grid_barrier(a.bar, a.err)) return;

@@ -96,6 +96,7 @@ struct og_engine {
   uint64_t ptile_cap = 0;
   uint32_t *cta_n = nullptr;
   unsigned long long *cta_e = nullptr;
+  unsigned long long *smf_d = nullptr;  // batched BFS: per-source frontier degree sums
   uint32_t *bar_d = nullptr;   // [0..1] barrier, [2] error, [3] levels, [4..11] 4 x u64 stats
   uint32_t *pmisc_h = nullptr;  // host copy of bar_d
   int tuned = -1;               // index into kPersistConfigs chosen by the autotuner
@@ -270,7 +271,8 @@ int create_query_state(og_engine *e) {
     e->ptile_cap = e->g->E / 1024 + 8;
     RC(dalloc(e, &e->ptile_d, e->ptile_cap));
     RC(dalloc(e, &e->cta_n, kMaxPersistCtas));
-    RC(dalloc(e, &e->cta_e, 2 * kMaxPersistCtas));  // frontier degree sums, then missing-source degree sums
+    RC(dalloc(e, &e->cta_e, kMaxPersistCtas));
+    RC(dalloc(e, &e->smf_d, 2 * 64));
     RC(dalloc(e, &e->bar_d, 16));  // barrier (2), error, levels, stats (6 u64)
     CK(cudaMallocHost(&e->hist_h, (size_t)kMaxBatchLevels * 64 * sizeof(unsigned long long)));
     CK(cudaMallocHost(&e->srcs_h, 64 * sizeof(uint32_t)));
@@ -1250,6 +1252,7 @@ int enqueue_persist(og_engine *e, uint32_t n, int ci, uint32_t *depth_d) {
   CK(cudaMemsetAsync(e->bm[0], 0, 4 * e->nwords, s));
   CK(cudaMemsetAsync(e->bm[1], 0, 4 * e->nwords, s));
   CK(cudaMemsetAsync(e->bm[2], 0, 4 * e->nwords, s));  // deferred bottom-up vertices
+  CK(cudaMemsetAsync(e->smf_d, 0, 8 * 2 * 64, s));
   CK(cudaMemsetAsync(e->hist_d, 0, 8ull * kMaxBatchLevels * 64, s));
   CK(cudaMemsetAsync(e->bar_d, 0, 64, s));
   CK(cudaMemcpyAsync(e->srcs_d, e->srcs_h, 4 * n, cudaMemcpyHostToDevice, s));
@@ -1282,7 +1285,7 @@ int enqueue_persist(og_engine *e, uint32_t n, int ci, uint32_t *depth_d) {
   a.err = e->bar_d + 2;
   a.levels = e->bar_d + 3;
   a.stat = (unsigned long long *)(e->bar_d + 4);
-  a.cta_mu = e->cta_e + kMaxPersistCtas;
+  a.smf = e->smf_d;
   a.defer = e->bm[2];
   a.Vs = e->Vs;
   a.dopt = batch_dopt(e);
