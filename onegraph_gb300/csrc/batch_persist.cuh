@@ -383,10 +383,11 @@ __device__ __forceinline__ void expand_tiles(const PersistArgs &a, PersistShared
 // Records a lane scans for one vertex in a bottom-up level before it hands
 // the rest of the vertex's list to the edge-balanced pull pass.
 constexpr uint64_t kBuLaneRecords = 32;
+constexpr int kBuStep = 8;  // records loaded (and probed) together
 
 // Bottom-up part of a level, for the sources in `sel`.  A warp owns 32-vertex
 // words of the bitmaps; each lane scans its vertex's records (HBM for the
-// static prefix, page-locked host memory beyond it) four at a time and ORs in
+// static prefix, page-locked host memory beyond it) kBuStep at a time and ORs in
 // its neighbours' frontier masks, restricted to the sources of `sel` that
 // have not reached the vertex, until every one of them is found or kBuLaneRecords
 // records are read.  A vertex with records left and sources still missing is
@@ -411,10 +412,10 @@ __device__ __forceinline__ void bottom_up_scan(const PersistArgs &a, unsigned lo
       if (need) {
         const uint64_t e0 = a.off[v], e1 = a.off[v + 1];
         const uint64_t lim = min(e1, e0 + kBuLaneRecords);
-        for (uint64_t e = e0; e < lim && found != need; e += 4) {
-          uint32_t u[4];
+        for (uint64_t e = e0; e < lim && found != need; e += kBuStep) {
+          uint32_t u[kBuStep];
 #pragma unroll
-          for (int j = 0; j < 4; j++) {
+          for (int j = 0; j < kBuStep; j++) {
             const uint64_t i = e + j;
             u[j] = 0xffffffffu;
             if (i >= lim) continue;
@@ -429,7 +430,7 @@ __device__ __forceinline__ void bottom_up_scan(const PersistArgs &a, unsigned lo
             }
           }
 #pragma unroll
-          for (int j = 0; j < 4; j++) {
+          for (int j = 0; j < kBuStep; j++) {
             if (u[j] < a.V) found |= __ldcg(cur + u[j]) & need;
             else if (u[j] != 0xffffffffu) atomicOr(a.err, kErrVertex);
           }
@@ -459,6 +460,128 @@ __device__ __forceinline__ void bottom_up_scan(const PersistArgs &a, unsigned lo
     atomicAdd(a.stat + 1, ns + nd);
     if (nd) atomicAdd(a.stat + 2, nd);
   }
+}
+
+// Transpose of the 32 x 32 bit matrix whose row i is lane i's x: lane c
+// gets column c (bit i = bit c of lane i's x).  Butterfly exchange of
+// 16-, 8-, 4-, 2- and 1-bit blocks.
+__device__ __forceinline__ uint32_t warp_transpose32(uint32_t x) {
+  const uint32_t lane = threadIdx.x & 31;
+  uint32_t m = 0x0000ffffu;
+#pragma unroll
+  for (int j = 16; j; j >>= 1, m ^= m << j) {
+    const uint32_t y = __shfl_xor_sync(0xffffffffu, x, j);
+    x = (lane & j) ? ((x & ~m) | ((y >> j) & m)) : ((x & m) | ((y << j) & ~m));
+  }
+  return x;
+}
+
+// Adds to lane c's count the vertices of this word (one per lane, masks `x`)
+// that carry source c.  A transpose when many sources are present, a ballot
+// per source otherwise.
+__device__ __forceinline__ uint32_t word_counts(uint32_t x, uint32_t present) {
+  const uint32_t lane = threadIdx.x & 31;
+  if (__popc(present) > 12) return __popc(warp_transpose32(x));
+  uint32_t c = 0;
+  for (uint32_t m = present; m; m &= m - 1) {
+    const uint32_t src = __ffs(m) - 1;
+    const uint32_t n = __popc(__ballot_sync(0xffffffffu, (x >> src) & 1u));
+    if (lane == src) c = n;
+  }
+  return c;
+}
+
+// Phase 4 of a level.  A warp takes kTallyWords consecutive 32-vertex words
+// at a time (lane = vertex) and issues their loads together.  Deferred
+// bottom-up vertices get their final mask into visited and next_any; the
+// newly reached vertices are counted per source (hist), and for the sources
+// in `msum_sel` their degrees are summed (the next level's direction
+// choice); the consumed frontier is cleared.
+constexpr int kTallyWords = 4;
+template <int BLOCK, class SH>
+__device__ __forceinline__ void level_tally(const PersistArgs &a, SH &sh, unsigned long long bu,
+                                            unsigned long long msum_sel, unsigned long long all_src,
+                                            uint32_t level, unsigned long long *cur,
+                                            unsigned long long *next, uint32_t *cur_any, uint32_t *next_any) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint64_t nwarps = (uint64_t)gridDim.x * (BLOCK / 32);
+  uint32_t cnt_lo = 0, cnt_hi = 0;  // sources lane and lane + 32
+  unsigned long long ms_lo = 0, ms_hi = 0, nact = 0;
+  for (uint64_t g = (((uint64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5) * kTallyWords; g < a.nwords;
+       g += nwarps * kTallyWords) {
+    uint32_t nw[kTallyWords], cw[kTallyWords];
+#pragma unroll
+    for (int j = 0; j < kTallyWords; j++) {
+      const bool ok = g + j < a.nwords;
+      nw[j] = ok ? __ldcg(next_any + g + j) : 0u;
+      cw[j] = ok ? __ldcg(cur_any + g + j) : 0u;
+      const uint32_t dm = (bu && ok) ? __ldcg(a.defer + g + j) : 0u;
+      if (dm) {  // uniform: the word is the same for every lane
+        const uint64_t v = (g + j) * 32 + lane;
+        unsigned long long f = 0;
+        if ((dm >> lane) & 1u) {
+          f = __ldcg(next + v);
+          if (f) a.visited[v] = __ldcg(a.visited + v) | f;
+        }
+        const uint32_t nb = __ballot_sync(0xffffffffu, f != 0ull);
+        if (lane == 0) {
+          if (nb & ~nw[j]) next_any[g + j] = nw[j] | nb;
+          a.defer[g + j] = 0u;
+        }
+        nw[j] |= nb;
+      }
+    }
+    unsigned long long nv[kTallyWords];
+#pragma unroll
+    for (int j = 0; j < kTallyWords; j++)
+      nv[j] = ((nw[j] >> lane) & 1u) ? __ldcg(next + (g + j) * 32 + lane) : 0ull;
+    uint64_t d[kTallyWords];
+#pragma unroll
+    for (int j = 0; j < kTallyWords; j++) {
+      const uint64_t v = (g + j) * 32 + lane;
+      d[j] = (nv[j] & msum_sel) ? a.off[v + 1] - a.off[v] : 0;
+    }
+#pragma unroll
+    for (int j = 0; j < kTallyWords; j++) {
+      if (!nw[j]) continue;  // uniform
+      const unsigned long long x = nv[j] & all_src;
+      nact |= x;
+      const uint32_t plo = __reduce_or_sync(0xffffffffu, (uint32_t)x);
+      const uint32_t phi = __reduce_or_sync(0xffffffffu, (uint32_t)(x >> 32));
+      cnt_lo += word_counts((uint32_t)x, plo);
+      cnt_hi += word_counts((uint32_t)(x >> 32), phi);
+      const unsigned long long ms = (((unsigned long long)phi << 32) | plo) & msum_sel;
+      if (ms) {
+        const uint32_t dlo = (uint32_t)(d[j] & 0xffffu), dhi = (uint32_t)(d[j] >> 16);
+        for (unsigned long long m = ms; m; m &= m - 1) {
+          const uint32_t src = __ffsll((long long)m) - 1;
+          const bool bit = (x >> src) & 1ull;
+          const unsigned long long sum = __reduce_add_sync(0xffffffffu, bit ? dlo : 0u) +
+                                         ((unsigned long long)__reduce_add_sync(0xffffffffu, bit ? dhi : 0u) << 16);
+          if (lane == (src & 31u)) {
+            if (src < 32) ms_lo += sum;
+            else ms_hi += sum;
+          }
+        }
+      }
+      if (a.depth)
+        for (unsigned long long b = x; b; b &= b - 1)
+          a.depth[(uint64_t)(__ffsll((long long)b) - 1) * a.V + (g + j) * 32 + lane] = level + 1;
+    }
+#pragma unroll
+    for (int j = 0; j < kTallyWords; j++) {
+      if (!cw[j]) continue;  // uniform
+      if ((cw[j] >> lane) & 1u) cur[(g + j) * 32 + lane] = 0ull;
+      if (lane == 0) cur_any[g + j] = 0u;
+    }
+  }
+  if (cnt_lo) atomicAdd(&sh.cnt[lane], cnt_lo);
+  if (cnt_hi) atomicAdd(&sh.cnt[lane + 32], cnt_hi);
+  if (ms_lo) atomicAdd(&sh.msum[lane], ms_lo);
+  if (ms_hi) atomicAdd(&sh.msum[lane + 32], ms_hi);
+#pragma unroll
+  for (int o = 16; o; o >>= 1) nact |= __shfl_xor_sync(0xffffffffu, nact, o);
+  if (lane == 0 && nact) atomicOr(&sh.act, nact);
 }
 
 // Resident threads per SM asked of the register allocator: 1024 (64
@@ -568,51 +691,15 @@ __global__ void __launch_bounds__(BLOCK, (ITEMS <= 4 ? 1024 : 512) / BLOCK) k_ba
     }
     if (!grid_barrier(a.bar, a.err)) return;
     // ---- 4. settle the deferred vertices; per-source counts of the newly
-    //         reached vertices, depths, and clearing of the consumed frontier
+    //         reached vertices (and, for top-down sources, their degree
+    //         sums), depths, and clearing of the consumed frontier
     if (threadIdx.x < 64) {
       sh.cnt[threadIdx.x] = 0;
       sh.msum[threadIdx.x] = 0;
     }
     if (threadIdx.x == 0) sh.act = 0ull;
     __syncthreads();
-    unsigned long long nact = 0;  // sources with a vertex in the next frontier
-    for (uint64_t w = wb; w < we; w++) {
-      if (bu) {
-        const uint32_t dm = __ldcg(a.defer + w);
-        if (dm) {
-          uint32_t nb = 0;
-          for (uint32_t m = dm; m; m &= m - 1) {
-            const uint64_t v = w * 32 + (__ffs(m) - 1);
-            const unsigned long long f = __ldcg(next + v);
-            if (f) {
-              a.visited[v] = __ldcg(a.visited + v) | f;
-              nb |= m & (0u - m);
-            }
-          }
-          if (nb) next_any[w] = __ldcg(next_any + w) | nb;
-          a.defer[w] = 0u;
-        }
-      }
-      for (uint32_t m = __ldcg(next_any + w); m; m &= m - 1) {
-        const uint64_t v = w * 32 + (__ffs(m) - 1);
-        const unsigned long long nv = __ldcg(next + v);
-        const uint64_t d = a.dopt ? a.off[v + 1] - a.off[v] : 0;
-        nact |= nv;
-        for (unsigned long long b = nv; b; b &= b - 1) {
-          const uint32_t s = __ffsll((long long)b) - 1;
-          if (s < a.n_src) {
-            atomicAdd(&sh.cnt[s], 1u);
-            if (d) atomicAdd(&sh.msum[s], (unsigned long long)d);
-            if (a.depth) a.depth[(uint64_t)s * a.V + v] = level + 1;
-          }
-        }
-      }
-      for (uint32_t m = __ldcg(cur_any + w); m; m &= m - 1) cur[w * 32 + (__ffs(m) - 1)] = 0ull;
-      cur_any[w] = 0u;
-    }
-#pragma unroll
-    for (int o = 16; o; o >>= 1) nact |= __shfl_xor_sync(0xffffffffu, nact, o);
-    if ((threadIdx.x & 31) == 0 && nact) atomicOr(&sh.act, nact);
+    level_tally<BLOCK>(a, sh, bu, a.dopt ? td & all_src : 0ull, all_src, level, cur, next, cur_any, next_any);
     __syncthreads();
     if (threadIdx.x < 64 && sh.cnt[threadIdx.x])
       atomicAdd(a.hist + (uint64_t)level * 64 + threadIdx.x, (unsigned long long)sh.cnt[threadIdx.x]);
