@@ -270,6 +270,7 @@ __device__ __forceinline__ void expand_tiles(const PersistArgs &a, PersistShared
                                              unsigned long long *next, uint32_t *next_any) {
   constexpr uint32_t TILE = BLOCK * ITEMS;
   const uint64_t ntiles = (total_e + TILE - 1) / TILE;
+  unsigned long long pulled_s = 0, pulled_d = 0;  // pull: static / dynamic records read
   for (uint64_t k = blockIdx.x; k < ntiles; k += gridDim.x) {
     const uint64_t pos0 = k * TILE;
     const uint32_t tlen = (uint32_t)min((uint64_t)TILE, total_e - pos0);
@@ -321,12 +322,16 @@ __device__ __forceinline__ void expand_tiles(const PersistArgs &a, PersistShared
         const uint32_t l = sh.map[x];
         const uint64_t idx = sh.cb[l] + x;
         lv[it] = l;
-        if (idx < a.static_edges) {
+        if (PULL && sh.val[l] == 0ull) {
+          // every source this vertex lacked was found by an earlier tile
+        } else if (idx < a.static_edges) {
           ev[it] = a.ssrc.load(idx);
           okm |= 1u << it;
+          if (PULL) pulled_s++;
         } else if (idx < a.E && a.hsrc.words) {
           ev[it] = a.hsrc.load(idx);
           okm |= 1u << it;
+          if (PULL) pulled_d++;
         } else {
           atomicOr(a.err, kErrEdgeIndex);
         }
@@ -378,11 +383,22 @@ __device__ __forceinline__ void expand_tiles(const PersistArgs &a, PersistShared
     }
     __syncthreads();  // shared tables are rebuilt for the next tile
   }
+  if (PULL) {
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      pulled_s += __shfl_xor_sync(0xffffffffu, pulled_s, o);
+      pulled_d += __shfl_xor_sync(0xffffffffu, pulled_d, o);
+    }
+    if ((threadIdx.x & 31) == 0 && (pulled_s | pulled_d)) {
+      atomicAdd(a.stat + 1, pulled_s + pulled_d);
+      if (pulled_d) atomicAdd(a.stat + 2, pulled_d);
+    }
+  }
 }
 
 // Records a lane scans for one vertex in a bottom-up level before it hands
 // the rest of the vertex's list to the edge-balanced pull pass.
-constexpr uint64_t kBuLaneRecords = 32;
+constexpr uint64_t kBuLaneRecords = 64;
 constexpr int kBuStep = 8;  // records loaded (and probed) together
 
 // Bottom-up part of a level, for the sources in `sel`.  A warp owns 32-vertex
@@ -402,15 +418,31 @@ __device__ __forceinline__ void bottom_up_scan(const PersistArgs &a, unsigned lo
   const uint32_t lane = threadIdx.x & 31;
   const uint64_t nwarps = (uint64_t)gridDim.x * (BLOCK / 32);
   unsigned long long ns = 0, nd = 0;  // static / dynamic records read
-  for (uint64_t w = ((uint64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5; w < a.nwords; w += nwarps) {
+  // a vertex's visited mask and list bounds are fetched one word ahead, so
+  // their latency overlaps the scan of the current word
+  uint64_t w = ((uint64_t)blockIdx.x * BLOCK + threadIdx.x) >> 5;
+  unsigned long long vis_n = ~0ull;
+  uint64_t e0_n = 0, e1_n = 0;
+  auto fetch = [&](uint64_t wn) {
+    const uint64_t vn = wn * 32 + lane;
+    vis_n = ~0ull;
+    if (wn < a.nwords && vn < a.V) {
+      vis_n = __ldcg(a.visited + vn);
+      e0_n = a.off[vn];
+      e1_n = a.off[vn + 1];
+    }
+  };
+  fetch(w);
+  for (; w < a.nwords; w += nwarps) {
     const uint64_t v = w * 32 + lane;
+    const unsigned long long vis = vis_n;
+    const uint64_t e0 = e0_n, e1 = e1_n;
+    fetch(w + nwarps);
     unsigned long long found = 0;
     bool defer = false;
     if (v < a.V) {
-      const unsigned long long vis = __ldcg(a.visited + v);
       const unsigned long long need = ~vis & sel;
       if (need) {
-        const uint64_t e0 = a.off[v], e1 = a.off[v + 1];
         const uint64_t lim = min(e1, e0 + kBuLaneRecords);
         for (uint64_t e = e0; e < lim && found != need; e += kBuStep) {
           uint32_t u[kBuStep];
@@ -657,15 +689,14 @@ __global__ void __launch_bounds__(BLOCK, (ITEMS <= 4 ? 1024 : 512) / BLOCK) k_ba
     if (bu) {
       bottom_up_scan<BLOCK>(a, bu, cur, next, next_any);
       if (!grid_barrier(a.bar, a.err)) return;
-      // the deferred vertices' remaining records, edge-balanced
+      // the deferred vertices' remaining records, edge-balanced (the pull
+      // pass counts the records it reads)
       uint64_t dyn;
       count_list<BLOCK>(a, sh, a.defer, wb, we, kBuLaneRecords, nullptr, 0, exc, exe, dyn);
       if (!grid_barrier(a.bar, a.err)) return;
       grid_totals<BLOCK>(a, sh);
       const uint64_t dn = sh.red_tn, de = sh.red_te;
       if (dn) {
-        if (dyn) atomicAdd(a.stat + 2, (unsigned long long)dyn);
-        if (blockIdx.x == 0 && threadIdx.x == 0) a.stat[1] += de;
         if (dn > a.list_cap || de / TILE + 1 >= a.tile_cap) {
           if (blockIdx.x == 0 && threadIdx.x == 0) atomicOr(a.err, kErrTileMap);
           break;
