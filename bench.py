@@ -591,6 +591,22 @@ def run_bfs_resident(args, rank, world, local):
     # (bottom-up); 20 B per frontier vertex
     eb = eng.plan["edge_bits"] / 8
     gbs = ((eb + 4) * examined + 20 * fverts) / (k_ms / 1e3) / 1e9 if k_ms else 0.0
+    # the same query with every level top-down: every edge of the component
+    # is read once, so this leg shows the kernels' bandwidth on the resident
+    # region (direction optimisation reads a small fraction of the edges)
+    eng.set_param(og.PARAM_BFS_DIRECTION, og.BFS_TOP_DOWN)
+    eng.bfs(src, out=False)
+    tstats = []
+
+    def topdown(k):
+        eng.bfs(src, out=False)
+        tstats.append(dict(eng.stats))
+    ttd, _ = timed(topdown, args.steps)
+    eng.set_param(og.PARAM_BFS_DIRECTION, og.BFS_AUTO)
+    td_ms = sum(x["ms_static"] + x["ms_dynamic"] for x in tstats)
+    td_ex = sum(x["edges_static"] + x["edges_dynamic"] for x in tstats)
+    td_fv = sum(x["frontier_sum"] for x in tstats)
+    td_gbs = ((eb + 4) * td_ex + 20 * td_fv) / (td_ms / 1e3) / 1e9 if td_ms else 0.0
     c0 = time.perf_counter()
     oracle.bfs(np.array(g.offsets), np.array(g.columns), src)
     cpu_s = time.perf_counter() - c0
@@ -603,6 +619,11 @@ def run_bfs_resident(args, rank, world, local):
                    "advisek": 1.0, "l2": "graph %.0f MB" % (g.E * 4 / 1e6)},
         "persistent_ms_per_query": tb / args.steps * 1e3,
         "persistent_gteps": comp_edges * args.steps / tb / 1e9,
+        "top_down_only": {"ms_per_query": ttd / args.steps * 1e3,
+                          "gteps": comp_edges * args.steps / ttd / 1e9,
+                          "edges_examined_per_query": td_ex / args.steps,
+                          "achieved_gbs": td_gbs, "frac": td_gbs / peaks["hbm_gbs"],
+                          "graph_vs_l2": "packed records %.0f MB, L2 129 MB" % (g.E * eb / 1e6)},
         "bit_exact_vs_runCPUBFS": exact, "levels": stats[0]["iterations"],
         "edges_examined_per_query": examined / args.steps,
         "roofline": {"bound": "hbm", "kernel": "device-driven level loop (compaction, top-down k_lbs_pair_dev, "
