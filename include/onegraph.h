@@ -326,7 +326,10 @@ int og_engine_clone(og_engine *parent, og_engine **out);
  *   its own neighbours and stops at the first one in the frontier (Beamer's
  *   direction optimization: a level goes bottom-up when the frontier's edges
  *   exceed the unexplored edges / 14, and back to top-down when the frontier
- *   is below V / 24 and shrinking).  OG_BFS_TOP_DOWN expands every level from
+ *   is below V / 24 and shrinking).  og_bfs_batch applies the same rule to
+ *   each source of the batch separately: in one level the bottom-up sources
+ *   are found by scans of the vertices missing them and the top-down sources
+ *   by pushes from their frontiers.  OG_BFS_TOP_DOWN expands every level from
  *   the frontier, as the reference does.  Depths are identical either way. */
 #define OG_PARAM_BFS_DIRECTION 3
 #define OG_BFS_AUTO 0
