@@ -134,3 +134,59 @@ def test_batch_bottom_up_levels(scale):
     for i in (0, 1, 63):
         np.testing.assert_array_equal(got[i], e.bfs(int(srcs[i])))
     e.close()
+
+
+def _irregular_symmetric_graph():
+    """V = 1000 (not a multiple of 32): a 300-leaf star whose hub (vertex 950)
+    lies in the dynamic region and has a longer list than a bottom-up lane
+    scans, so it goes to the pull pass; a 200-vertex path hanging off a leaf
+    (many levels); random edges among 501..940; isolated vertices."""
+    rng = np.random.default_rng(17)
+    V = 1000
+    edges = set()
+    for leaf in range(1, 301):
+        edges.add((950, leaf))
+    prev = 5
+    for v in range(301, 501):
+        edges.add((prev, v))
+        prev = v
+    for _ in range(1500):
+        a, b = rng.integers(501, 941, 2)
+        if a != b:
+            edges.add((int(a), int(b)))
+    edges.add((700, 37))  # joins the random part to the star
+    edges = {(min(a, b), max(a, b)) for a, b in edges}
+    adj = [[] for _ in range(V)]
+    for a, b in edges:
+        adj[a].append(b)
+        adj[b].append(a)
+    off = np.zeros(V + 1, np.uint64)
+    for v in range(V):
+        off[v + 1] = off[v] + len(adj[v])
+    col = np.array([u for v in range(V) for u in sorted(adj[v])], np.uint32)
+    return off, col
+
+
+def test_batch_irregular_graph_directions():
+    off, col = _irregular_symmetric_graph()
+    g = og.Graph.from_arrays(off, col)
+    g.set_symmetric(True)
+    V = off.size - 1
+    rng = np.random.default_rng(3)
+    srcs = rng.integers(0, V, 64).astype(np.uint32)
+    srcs[:6] = [950, 500, 999, 150, 301, 37]  # hub, path end, isolated, leaf, path start, star-side
+    for cname, kw in [("resident", dict(budget=1 << 30, advisek=1.0)),
+                      ("direct", dict(budget=budget_for(g, 400, og.CFG_BATCH | og.CFG_DIRECT),
+                                      advisek=0.5, direct=True))]:
+        e = og.Engine(g, batch=True, **kw)
+        single = np.stack([e.bfs(int(s)) for s in srcs])
+        for direction in (og.BFS_AUTO, og.BFS_TOP_DOWN):
+            e.set_param(og.PARAM_BFS_DIRECTION, direction)
+            for n in (64, 7):
+                got, ck = e.bfs_batch(srcs[:n])
+                np.testing.assert_array_equal(got, single[:n], err_msg="%s direction %d n %d" % (cname, direction, n))
+                _, ck2 = e.bfs_batch(srcs[:n], out=False)
+                np.testing.assert_array_equal(ck2, ck)
+        for i in (0, 1, 2):
+            np.testing.assert_array_equal(oracle.normalise_bfs(single[i], V), oracle.bfs(off, col, int(srcs[i]))[0])
+        e.close()
