@@ -1874,7 +1874,7 @@ extern "C" int og_bfs_batch_tune(og_engine *e, const uint32_t *srcs, int n, int 
     r.items[i] = kPersistConfigs[i].items;
     float tmin = 1e30f;
     for (int k = 0; k <= reps; k++) {  // the first run warms up
-      og_stats st;
+      og_stats st{};
       BatchCtx c{srcs, (uint32_t)n, nullptr, nullptr, 2 + i};
       RC(query_common(e, OG_ALGO_BFS, &st, nullptr, batch_body, &c));
       if (k > 0) tmin = std::min(tmin, (float)st.ms_static);
