@@ -491,7 +491,9 @@ def run_pr_precision(args, rank, world, local):
     out-degrees, 6 GiB budget; FP32 ranks with FP32 pull sums and the FP64 L1
     delta reduced on the GPU, stopped at L1 < 1e-6 (normalised ranks),
     against the multi-threaded FP64 host oracle; the reference's delta form
-    (og_pr, per-vertex 1e-3) is timed beside it."""
+    (og_pr, per-vertex 1e-3) is timed beside it, and so is the push form
+    (og_pr_l1_push over the out-edge CSR from og_graph_transpose, same budget),
+    with its own errors against the same oracle."""
     import torch
     import onegraph_gb300 as og
     import oracle
@@ -513,6 +515,17 @@ def run_pr_precision(args, rank, world, local):
     rank32 = outs[0].astype(np.float64)
     t1, _ = timed(lambda k: eng.pr(0.001, 0, out=False), 1)
     st_delta = dict(eng.stats)
+    eng.close()
+    c0 = time.time()
+    gt = g.transpose()
+    tr_s = time.time() - c0
+    peng = og.Engine(gt, budget=int(args.budget_gib * GIB), advisek=args.advisek,
+                     direct=bool(args.direct), pagerank=True, device=local)
+    peng.pr_l1_push(0.85, 1e-6, 3, out=False)  # warm-up
+    tpush, pouts = timed(lambda k: peng.pr_l1_push(0.85, 1e-6, 500), 1)
+    st_push = dict(peng.stats)
+    push64 = pouts[0].astype(np.float64)
+    peng.close()
     threads = os.cpu_count() or 1
     ref = np.empty(g.V)
     c0 = time.perf_counter()
@@ -520,7 +533,9 @@ def run_pr_precision(args, rank, world, local):
                                          threads, ref)
     cpu_s = time.perf_counter() - c0
     err = np.abs(rank32 - ref)
+    perr = np.abs(push64 - ref)
     iters = max(st["iterations"], 1)
+    piters = max(st_push["iterations"], 1)
     line = {
         "metric": "pagerank iterations/s", "value": iters / t, "unit": "iterations/s",
         "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": t * 1e3 / iters,
@@ -535,13 +550,19 @@ def run_pr_precision(args, rank, world, local):
         "oracle": {"iterations": it_ref, "residual_l1": l1_ref, "seconds": cpu_s, "threads": threads},
         "link_gb_per_iter": st["link_bytes"] / iters / 1e9,
         "delta_form": {"rounds": st_delta["iterations"], "ms": t1 * 1e3},
+        "push": {"iterations_per_s": piters / tpush, "iterations": st_push["iterations"],
+                 "ms_per_iter": tpush * 1e3 / piters, "residual_l1": st_push["residual"],
+                 "max_abs_err": float(perr.max()), "l1_err": float(perr.sum()),
+                 "max_rel_err": float((perr / ref).max()),
+                 "max_abs_diff_vs_pull": float(np.abs(push64 - rank32).max()),
+                 "link_gb_per_iter": st_push["link_bytes"] / piters / 1e9,
+                 "transpose_s": tr_s},
         "cpu_baseline": {"value": it_ref / cpu_s, "unit": "iterations/s", "cores": threads, "kind": "port",
                          "sample": "FP64 pull PageRank oracle, full run to L1 < 1e-6"},
         "clocks": clocks, "setup_s": {"generate": gen_s},
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
-    eng.close()
 
 
 def run_bfs_resident(args, rank, world, local):

@@ -102,6 +102,13 @@ int og_graph_save_bel(const og_graph *g, const char *prefix);
  * input path without its last four characters, plus "lcsr". */
 int og_convert_uint_to_ulong(const char *in_path, const char *out_path);
 
+/* The reverse graph as a new OG_GRAPH_PLAIN CSR: list u holds, sorted, every
+ * v whose list contains u.  For the reference's PageRank files, whose lists
+ * are in-neighbours (PR/OneGraph/GraphMeta.h:131-149), this is the out-edge
+ * CSR that og_pr_l1_push traverses.  Weighted graphs are not supported.  No
+ * reference counterpart (the reference pulls only). */
+int og_graph_transpose(const og_graph *g, og_graph **out);
+
 /* Symmetry of the edge set (every (u, v) has its reverse (v, u)), which lets
  * og_cc use its union-find path.  og_graph_set_symmetric records the caller's
  * assertion (1 or 0) without checking it; a wrong 1 gives wrong components.
@@ -255,6 +262,15 @@ int og_pr(og_engine *e, float *out_rank, double threshold, int max_rounds,
  * No reference counterpart beyond the pr_cal_cpu formula (PR/usm/pr.cpp:149-187). */
 int og_pr_l1(og_engine *e, float *out_rank, double damping, double tol,
              int max_iter, og_stats *st);
+/* The same L1-stopped PageRank by push: the engine's graph holds OUT-edges
+ * (og_graph_transpose of an in-edge PR graph; out-degrees are the list
+ * lengths), every vertex adds rank / out-degree to each out-neighbour's sum
+ * with an FP32 atomicAdd, then the update and the FP64 L1 reduction of
+ * og_pr_l1 follow.  The summation order of atomics varies from run to run, so
+ * results agree with og_pr_l1 to FP32 rounding, not bit for bit.  Needs
+ * OG_CFG_PR. */
+int og_pr_l1_push(og_engine *e, float *out_rank, double damping, double tol, int max_iter,
+                  og_stats *st);
 
 /* Multi-source BFS: up to 64 sources in one level-synchronous pass over
  * per-vertex 64-bit visited / frontier masks, so every edge read (including

@@ -134,6 +134,7 @@ SIGNATURES = [
     ("og_graph_findbignode", C.c_uint32, [_P, C.c_uint32]),
     ("og_graph_save_bel", C.c_int, [_P, C.c_char_p]),
     ("og_convert_uint_to_ulong", C.c_int, [C.c_char_p, C.c_char_p]),
+    ("og_graph_transpose", C.c_int, [_P, C.POINTER(_P)]),
     ("og_graph_set_symmetric", C.c_int, [_P, C.c_int]),
     ("og_graph_symmetric", C.c_int, [_P, C.POINTER(C.c_int)]),
     ("og_graph_records", C.c_int, [_P, C.POINTER(_P), C.POINTER(C.c_uint64), C.POINTER(C.c_uint32),
@@ -150,6 +151,7 @@ SIGNATURES = [
     ("og_cc", C.c_int, [_P, _P, C.POINTER(Stats)]),
     ("og_pr", C.c_int, [_P, _P, C.c_double, C.c_int, C.POINTER(Stats)]),
     ("og_pr_l1", C.c_int, [_P, _P, C.c_double, C.c_double, C.c_int, C.POINTER(Stats)]),
+    ("og_pr_l1_push", C.c_int, [_P, _P, C.c_double, C.c_double, C.c_int, C.POINTER(Stats)]),
     ("og_bfs_batch", C.c_int, [_P, _P, C.c_int, _P, _P, C.POINTER(Stats)]),
     ("og_bfs_batch_tune", C.c_int, [_P, _P, C.c_int, C.c_int, C.POINTER(TuneResult)]),
     ("og_bfs_batch_set_config", C.c_int, [_P, C.c_int]),
@@ -258,6 +260,12 @@ class Graph:
 
     def save_bel(self, prefix: str):
         _check(lib().og_graph_save_bel(self._h, prefix.encode()), "og_graph_save_bel")
+
+    def transpose(self) -> "Graph":
+        """The reverse graph (PLAIN): the out-edge CSR of an in-edge PageRank graph."""
+        h = _P()
+        _check(lib().og_graph_transpose(self._h, C.byref(h)), "og_graph_transpose")
+        return Graph(h)
 
     @property
     def offsets(self) -> np.ndarray:
@@ -418,6 +426,16 @@ class Engine:
         o = self._out(out, np.float32)
         st = Stats()
         _check(lib().og_pr_l1(self._h, _ptr(o), damping, tol, max_iter, C.byref(st)), "og_pr_l1")
+        self.stats = st.as_dict()
+        return o
+
+    def pr_l1_push(self, damping: float = 0.85, tol: float = 1e-6, max_iter: int = 200,
+                   out=None) -> np.ndarray | None:
+        """pr_l1 by push; the engine's graph must hold out-edges (Graph.transpose)."""
+        o = self._out(out, np.float32)
+        st = Stats()
+        _check(lib().og_pr_l1_push(self._h, _ptr(o), damping, tol, max_iter, C.byref(st)),
+               "og_pr_l1_push")
         self.stats = st.as_dict()
         return o
 

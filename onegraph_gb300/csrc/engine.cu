@@ -1520,6 +1520,64 @@ int run_pr_l1(og_engine *e, float damping, double tol, int max_iter, og_stats &s
   return OG_OK;
 }
 
+// og_pr_l1_push: the graph holds out-edges; sums by scattered atomic adds.
+int run_pr_l1_push(og_engine *e, float damping, double tol, int max_iter, og_stats &st) {
+  const uint64_t V = e->V;
+  uint32_t *cur = e->bm[0];
+  cudaStream_t s = e->s_main;
+  const int g = grid_for(V, e->sms);
+  CK(cudaMemsetAsync(e->err_d, 0, 16, s));
+  k_pr_init<<<g, kThreads, 0, s>>>(V, (float *)e->value_d, e->contrib_d, e->sum_d, e->outdeg_d,
+                                   (float)(1.0 / (double)V));
+  e->launches++;
+  k_fill_bits<<<g, kThreads, 0, s>>>(cur, e->nwords, V);
+  e->launches++;
+  CK(cudaGetLastError());
+  Timing tm;
+  uint64_t n = 0;
+  RC(compact_round(e, cur, st, tm, &n));  // every vertex with out-edges, once
+  const float teleport = (float)((1.0 - (double)damping) / (double)V);
+  const PushOp op{e->contrib_d, e->sum_d, e->err_d, (uint32_t)V};
+  auto launch = [&](const LbsArgs &a, auto src, cudaStream_t ls) {
+    const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
+    if (grid) {
+      k_lbs<decltype(src), PushOp><<<grid, kThreads, 0, ls>>>(a, src, op);
+      e->launches++;
+    }
+    return (int)OG_OK;
+  };
+  auto sfn = [&](const LbsArgs &a) { return launch(a, EKU::stat(e), e->s_main); };
+  auto pfn = [&](const LbsArgs &a0, auto s0, const LbsArgs &a1, auto s1, cudaStream_t ps) {
+    const uint64_t n0 = lbs_grid(a0.pos_begin, a0.pos_end), n1 = lbs_grid(a1.pos_begin, a1.pos_end);
+    if (n0 + n1 > 0x7fffffffull) return fail(OG_E_STATE, "push grid too large");
+    k_lbs_pair<decltype(s0), decltype(s1), PushOp><<<(unsigned)(n0 + n1), kThreads, 0, ps>>>(a0, s0, a1, s1, op,
+                                                                                        n0, n0 + n1);
+    e->launches++;
+    return (int)OG_OK;
+  };
+  for (int it = 0; it < max_iter; it++) {
+    st.iterations++;
+    st.frontier_sum += n;
+    st.static_vertices += e->counts_h[0].n;
+    CK(cudaMemsetAsync(e->sum_d, 0, 4 * V, s));
+    RC((run_regions<EKU>(e, st, tm, sfn, launch, pfn)));
+    k_pr_update_l1<<<e->part_n, kThreads, 0, s>>>(V, (float *)e->value_d, e->contrib_d, e->sum_d,
+                                                  e->outdeg_d, teleport, damping, e->part_d);
+    e->launches++;
+    k_reduce_f64<<<1, kThreads, 0, s>>>(e->part_d, e->part_n, e->l1_d);
+    e->launches++;
+    CK(cudaMemcpyAsync(e->l1_h, e->l1_d, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(e->err_h, e->err_d, 4, cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+    RC(check_device_error(e));
+    collect_timing(e, tm, &st);
+    st.residual = *e->l1_h;
+    if (*e->l1_h < tol) break;
+  }
+  e->last_algo = OG_ALGO_PR;
+  return OG_OK;
+}
+
 double now_ms() {
   return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now().time_since_epoch())
       .count();
@@ -1825,6 +1883,17 @@ extern "C" int og_pr_l1(og_engine *e, float *out_rank, double damping, double to
   return query_common(e, OG_ALGO_PR, st, out_rank, [](og_engine *en, og_stats &s, void *cx) {
     const PrCtx &p = *(PrCtx *)cx;
     return run_pr_l1(en, (float)p.a, p.b, p.n, s);
+  }, &c);
+}
+
+extern "C" int og_pr_l1_push(og_engine *e, float *out_rank, double damping, double tol, int max_iter,
+                             og_stats *st) {
+  if (e && !e->pr_enabled) return fail(OG_E_UNSUPPORTED, "engine has no PageRank state (OG_CFG_PR)");
+  if (max_iter <= 0) return fail(OG_E_ARG, "max_iter must be positive");
+  PrCtx c{damping, tol, max_iter};
+  return query_common(e, OG_ALGO_PR, st, out_rank, [](og_engine *en, og_stats &s, void *cx) {
+    const PrCtx &p = *(PrCtx *)cx;
+    return run_pr_l1_push(en, (float)p.a, p.b, p.n, s);
   }, &c);
 }
 

@@ -6,8 +6,10 @@
 #include <cstdarg>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <thread>
+#include <vector>
 
 #include "og_internal.hpp"
 
@@ -380,6 +382,63 @@ extern "C" int og_graph_from_arrays(uint64_t V, uint64_t E, const uint64_t *offs
     return rc;
   }
   *out = g;
+  return OG_OK;
+}
+
+extern "C" int og_graph_transpose(const og_graph *g, og_graph **out) {
+  clear_error();
+  if (!g || !out) return fail(OG_E_ARG, "og_graph_transpose: null argument");
+  if (g->kind == OG_GRAPH_WEIGHTED) return fail(OG_E_UNSUPPORTED, "og_graph_transpose: weighted graph");
+  *out = nullptr;
+  const uint32_t V = g->V;
+  const uint64_t E = g->E;
+  og_graph *t = graph_new(V, E, OG_GRAPH_PLAIN);
+  std::unique_ptr<std::atomic<uint64_t>[]> cur(new (std::nothrow) std::atomic<uint64_t>[(size_t)V]);
+  if (!t || !cur) {
+    if (t) graph_delete(t);
+    return fail(OG_E_NOMEM, "og_graph_transpose: cannot allocate %llu edges", (unsigned long long)E);
+  }
+  const uint32_t *col = (const uint32_t *)g->edges;
+  uint32_t *tcol = (uint32_t *)t->edges;
+  const unsigned nt = hw_threads(0);
+  auto parallel = [&](uint64_t n, auto body) {  // body(lo, hi) over nt contiguous ranges
+    std::vector<std::thread> th;
+    for (unsigned k = 0; k < nt; k++) {
+      const uint64_t lo = n * k / nt, hi = n * (k + 1) / nt;
+      th.emplace_back([=, &body] { body(lo, hi); });
+    }
+    for (auto &x : th) x.join();
+  };
+  // 1. list lengths of the reverse graph
+  parallel(V, [&](uint64_t lo, uint64_t hi) {
+    for (uint64_t u = lo; u < hi; u++) cur[u].store(0, std::memory_order_relaxed);
+  });
+  parallel(E, [&](uint64_t lo, uint64_t hi) {
+    for (uint64_t i = lo; i < hi; i++) cur[col[i]].fetch_add(1, std::memory_order_relaxed);
+  });
+  t->off[0] = 0;
+  for (uint64_t u = 0; u < V; u++) {
+    const uint64_t n = cur[u].load(std::memory_order_relaxed);
+    cur[u].store(t->off[u], std::memory_order_relaxed);
+    t->off[u + 1] = t->off[u] + n;
+  }
+  // 2. scatter (v, u) into list u, then sort each list: the result does not
+  //    depend on the threads' interleaving
+  parallel(V, [&](uint64_t lo, uint64_t hi) {
+    for (uint64_t v = lo; v < hi; v++)
+      for (uint64_t i = g->off[v]; i < g->off[v + 1]; i++)
+        tcol[cur[col[i]].fetch_add(1, std::memory_order_relaxed)] = (uint32_t)v;
+  });
+  parallel(V, [&](uint64_t lo, uint64_t hi) {
+    for (uint64_t u = lo; u < hi; u++) std::sort(tcol + t->off[u], tcol + t->off[u + 1]);
+  });
+  t->symmetric = g->symmetric;
+  const int rc = graph_validate(t);
+  if (rc != OG_OK) {
+    graph_delete(t);
+    return rc;
+  }
+  *out = t;
   return OG_OK;
 }
 

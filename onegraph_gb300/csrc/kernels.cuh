@@ -749,6 +749,33 @@ struct BatchOp {
   }
 };
 
+// PageRank by push over an out-edge CSR: the listed vertex u adds its
+// contribution (rank / out-degree, the LBS source value) to the sum of every
+// out-neighbour with an FP32 atomicAdd.  Nothing to probe.
+struct PushOp {
+  using Val = float;
+  static constexpr bool kNeedVal = true;
+  const float *contrib;
+  float *sum;
+  uint32_t *err;
+  uint32_t V;
+  __device__ Val src_val(uint32_t u) const { return contrib[u]; }
+  using Probe = uint32_t;
+  template <class Edge>
+  __device__ __forceinline__ Probe probe(Edge) const {
+    return 0u;
+  }
+  template <class Edge>
+  __device__ __forceinline__ void relax(Edge e, Val c, uint64_t, Probe) const {
+    const uint32_t v = edge_dst(e);
+    if (v >= V) {
+      atomicOr(err, kErrVertex);
+      return;
+    }
+    if (c != 0.f) atomicAdd(sum + v, c);
+  }
+};
+
 __global__ void k_batch_init(const uint32_t *srcs, uint32_t n, unsigned long long *visited,
                              unsigned long long *cur, uint32_t *cur_any, uint32_t *depth,
                              uint64_t V) {

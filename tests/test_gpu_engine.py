@@ -191,6 +191,26 @@ def test_pagerank_l1_precision_vs_fp64_oracle():
         e.close()
 
 
+def test_pagerank_push_vs_fp64_oracle_and_pull():
+    """Push over the transposed (out-edge) graph: the same tolerances against
+    the FP64 oracle as the pull kernel, and within FP32 rounding of it."""
+    g, off, col, od = _pr_graph()
+    want, it_ref, _ = oracle.pr_l1(off, col, od, 0.85, 1e-6, 200)
+    pull = og.Engine(g, budget=1 << 30, advisek=1.0).pr_l1(0.85, 1e-6, 200)
+    t = g.transpose()
+    for cname, kw in configs(t, og.CFG_PR):
+        e = og.Engine(t, pagerank=True, **kw)
+        r = e.pr_l1_push(0.85, 1e-6, 200)
+        err = np.abs(r.astype(np.float64) - want)
+        assert err.max() < 1e-6, (cname, err.max())
+        assert err.sum() < 1e-5, (cname, err.sum())
+        assert e.stats["residual"] < 1e-6
+        assert abs(e.stats["iterations"] - it_ref) <= 2
+        assert np.abs(r - pull).max() < 1e-6, cname
+        assert e.stats["edges_static"] + e.stats["edges_dynamic"] == t.E * e.stats["iterations"], cname
+        e.close()
+
+
 def test_pagerank_delta_form_vs_reference_semantics():
     g, off, col, od = _pr_graph()
     want, rounds = oracle.pr_onegraph(off, col, od, 0.001)

@@ -368,3 +368,29 @@ def test_symmetry_flag_and_exact_check():
     assert g4.symmetric()
     w = og.Graph.rmat(9, 16, weighted=True)
     assert og.Graph.from_arrays(np.array(w.offsets), np.array(w.edges), kind=og.WEIGHTED).symmetric()
+
+
+def test_transpose_is_the_reverse_graph():
+    """og_graph_transpose: list u of the result holds, sorted, every v whose
+    list holds u; a PageRank in-edge graph becomes its out-edge CSR, a
+    symmetric graph maps to itself, a weighted graph is refused."""
+    g = og.Graph.rmat(10, 16, pagerank=True, symmetric=False)
+    off, col, od = np.array(g.offsets), np.array(g.columns), np.array(g.outdeg)
+    t = g.transpose()
+    toff, tcol = np.array(t.offsets), np.array(t.columns)
+    assert t.kind == og.PLAIN and t.V == g.V and t.E == g.E
+    v_of = np.repeat(np.arange(g.V, dtype=np.uint32), np.diff(off).astype(np.int64))
+    order = np.lexsort((v_of, col))  # by source u, then destination v
+    np.testing.assert_array_equal(tcol, v_of[order])
+    np.testing.assert_array_equal(np.diff(toff), np.bincount(col, minlength=g.V))
+    np.testing.assert_array_equal(np.diff(toff), od)  # the file's out-degrees
+    tt = t.transpose()
+    np.testing.assert_array_equal(np.array(tt.offsets), off)
+    np.testing.assert_array_equal(np.array(tt.columns), col)
+    s = og.Graph.rmat(9, 8)
+    st = s.transpose()
+    np.testing.assert_array_equal(np.array(st.offsets), np.array(s.offsets))
+    np.testing.assert_array_equal(np.array(st.columns), np.array(s.columns))
+    with pytest.raises(og.OGError) as ex:
+        og.Graph.rmat(8, 8, weighted=True).transpose()
+    assert ex.value.status == 9
