@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define OG_ABI_VERSION 2
+#define OG_ABI_VERSION 3
 
 typedef enum og_status {
   OG_OK = 0,
@@ -232,6 +232,10 @@ typedef struct og_stats {
   double residual;           /* PR: last L1 delta; otherwise 0              */
   uint64_t launches;         /* kernels launched for the query              */
   double ms_gather;          /* device time of the dynamic gather kernels   */
+  double ms_relax;           /* device-driven rounds: time of the (top-down)
+                                relax launches, each measured inside the
+                                kernel from its first CTA start to its last
+                                CTA end; 0 for host-driven rounds           */
 } og_stats;
 
 /* initGraphHost + getMaxPartitionSize + initGraphDevice

@@ -84,7 +84,7 @@ class Stats(C.Structure):
                 ("edges_dynamic", C.c_uint64), ("link_bytes", C.c_uint64),
                 ("ms_total", C.c_double), ("ms_static", C.c_double), ("ms_dynamic", C.c_double),
                 ("ms_compact", C.c_double), ("residual", C.c_double), ("launches", C.c_uint64),
-                ("ms_gather", C.c_double)]
+                ("ms_gather", C.c_double), ("ms_relax", C.c_double)]
 
     def as_dict(self):
         return {f: getattr(self, f) for f, _ in self._fields_}
@@ -177,7 +177,7 @@ SIGNATURES = [
 ]
 
 
-ABI_VERSION = 2  # OG_ABI_VERSION of include/onegraph.h these bindings follow
+ABI_VERSION = 3  # OG_ABI_VERSION of include/onegraph.h these bindings follow
 
 
 def lib():

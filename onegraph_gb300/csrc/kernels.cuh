@@ -39,6 +39,34 @@ constexpr uint32_t kErrTileMap = 8u;     // LBS tile map inconsistent
 
 constexpr uint32_t kSpinLimit = 1u << 24;
 
+// Nanosecond global timer (the same clock on every SM).
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// In-kernel launch timer: kt[0] earliest CTA start (~0 between launches),
+// kt[1] CTAs finished, kt[2] accumulated ns.  Each CTA stamps its start; the
+// last CTA to finish adds (its end - the earliest start) to kt[2] and resets
+// kt[0..1] for the next launch.  Host-side gaps before a launch are excluded.
+__device__ __forceinline__ void ktimer_start(unsigned long long *kt) {
+  if (kt && threadIdx.x == 0) {
+    atomicMin(kt, globaltimer_ns());
+    __threadfence();
+  }
+}
+__device__ __forceinline__ void ktimer_end(unsigned long long *kt) {
+  if (kt && threadIdx.x == 0) {
+    __threadfence();
+    if (atomicAdd(kt + 1, 1ull) == gridDim.x - 1ull) {
+      const unsigned long long t0 = atomicExch(kt, ~0ull);
+      atomicAdd(kt + 2, globaltimer_ns() - t0);
+      atomicExch(kt + 1, 0ull);
+    }
+  }
+}
+
 struct Counts {
   uint32_t n;        // compacted vertices
   uint32_t far_min;  // near/far split: smallest value left for later rounds

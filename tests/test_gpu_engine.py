@@ -391,6 +391,9 @@ def test_device_rounds_sssp_cc_match_host_loop():
                     np.testing.assert_array_equal(d, oracle.sssp_dijkstra(off, pairs, s))
                     for k in ("iterations", "frontier_sum", "edges_static", "edges_dynamic"):
                         assert dev[k] == host[k], (scale, ekw, delta, s, k)
+                    # the relax launches time themselves inside the device loop
+                    assert 0.0 < dev["ms_relax"] <= dev["ms_dynamic"], (dev["ms_relax"], dev["ms_dynamic"])
+                    assert host["ms_relax"] == 0.0
             e.set_param(og.PARAM_CC_METHOD, og.CC_LABEL_PROPAGATION)
             e.set_param(og.PARAM_LEVEL_LOOP, og.LOOP_AUTO)
             lab = e.cc()
