@@ -232,10 +232,11 @@ typedef struct og_stats {
   double residual;           /* PR: last L1 delta; otherwise 0              */
   uint64_t launches;         /* kernels launched for the query              */
   double ms_gather;          /* device time of the dynamic gather kernels   */
-  double ms_relax;           /* device-driven rounds: time of the (top-down)
+  double ms_relax;           /* device-driven rounds with
+                                OG_PARAM_RELAX_TIMER: time of the (top-down)
                                 relax launches, each measured inside the
                                 kernel from its first CTA start to its last
-                                CTA end; 0 for host-driven rounds           */
+                                CTA end; otherwise 0                        */
 } og_stats;
 
 /* initGraphHost + getMaxPartitionSize + initGraphDevice
@@ -363,6 +364,10 @@ int og_engine_clone(og_engine *parent, og_engine **out);
 #define OG_PARAM_LEVEL_LOOP 4
 #define OG_LOOP_AUTO 0
 #define OG_LOOP_HOST 1
+/* OG_PARAM_RELAX_TIMER: 1 makes the relax launches of the device-driven
+ *   rounds time themselves (og_stats.ms_relax); 0 (default) leaves the timer
+ *   out of the kernels, which saves a few per cent of query time. */
+#define OG_PARAM_RELAX_TIMER 5
 int og_engine_set_param(og_engine *e, int param, double value);
 int og_engine_get_param(const og_engine *e, int param, double *value);
 

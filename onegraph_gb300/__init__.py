@@ -33,6 +33,7 @@ PARAM_BFS_DIRECTION = 3
 BFS_AUTO, BFS_TOP_DOWN = 0, 1
 PARAM_LEVEL_LOOP = 4
 LOOP_AUTO, LOOP_HOST = 0, 1
+PARAM_RELAX_TIMER = 5
 # R-MAT quadrant probabilities of the benchmark graphs
 RMAT_ABC = (0.57, 0.19, 0.19)
 

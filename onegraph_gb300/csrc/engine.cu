@@ -109,6 +109,7 @@ struct og_engine {
   uint32_t dev_epoch = 1u << 29;  // epochs of device-driven compactions: [2^29, 2^30)
   uint32_t bfs_levels_hint = 4;   // levels of the last BFS (launched before the first check)
   uint32_t level_loop = 0;        // OG_LOOP_AUTO / OG_LOOP_HOST
+  uint32_t relax_timer = 0;       // OG_PARAM_RELAX_TIMER
   // device-driven SSSP / CC rounds: state, host mirror, round graphs captured
   // for (algorithm, split) = min_exec_key
   MinLoop *mloop_d = nullptr, *mloop_h = nullptr;
@@ -414,6 +415,7 @@ int clone(og_engine *parent, og_engine *e) {
   e->cc_method = parent->cc_method;
   e->bfs_direction = parent->bfs_direction;
   e->level_loop = parent->level_loop;
+  e->relax_timer = parent->relax_timer;
   CK(cudaSetDevice(e->dev));
   RC(create_query_state(e));
   parent->clones++;
@@ -881,7 +883,8 @@ int capture_bfs_level(og_engine *e, int p, int dopt, cudaGraphExec_t *out) {
     BfsOp op{e->bm[2], next, e->value_d, e->err_d, e->V, 0};
     k_lbs_pair_dev<EKU::PSrc, EKU::PSrc, BfsOp><<<grid, kThreads, 0, s>>>(
         lbs_args(e, 0, 0, 0, true, e->plan.static_edges), EKU::stat(e), lbs_args(e, 1, 0, 0, true, e->g->E),
-        EKU::host(e), op, e->counts_d, &L->td_go, &L->level, &L->tile_next, L->relax_timer);
+        EKU::host(e), op, e->counts_d, &L->td_go, &L->level, &L->tile_next,
+        e->relax_timer ? L->relax_timer : nullptr);
     k_bfs_bottom_up<EKU::PSrc><<<grid_for(e->V, e->sms), kThreads, 0, s>>>(
         e->off_d, e->V, e->Vs, EKU::stat(e), EKU::host(e), cur, e->bm[2], next, e->value_d, 0, L->bu,
         e->err_d, &L->bu_go, &L->level);
@@ -910,14 +913,15 @@ int run_bfs_dev(og_engine *e, uint32_t src, og_stats &st) {
   const uint64_t V = e->V;
   cudaStream_t s = e->s_main;
   const int g = grid_for(V, e->sms);
-  const int dopt = e->bfs_direction == OG_BFS_AUTO && e->g->symmetric == 1;
+  // the captured graphs depend on the direction mode and the relax timer
+  const int dopt = (e->bfs_direction == OG_BFS_AUTO && e->g->symmetric == 1) | (e->relax_timer ? 2 : 0);
   if (dopt != e->bfs_exec_dopt) {
     for (int p = 0; p < 2; p++)
       if (e->bfs_exec[p]) {
         cudaGraphExecDestroy(e->bfs_exec[p]);
         e->bfs_exec[p] = nullptr;
       }
-    for (int p = 0; p < 2; p++) RC(capture_bfs_level(e, p, dopt, &e->bfs_exec[p]));
+    for (int p = 0; p < 2; p++) RC(capture_bfs_level(e, p, dopt & 1, &e->bfs_exec[p]));
     e->bfs_exec_dopt = dopt;
   }
   if (e->dev_epoch > (1u << 30) - (1u << 20)) {  // epoch wrap: clear the status words once
@@ -1015,7 +1019,8 @@ int capture_min_round(og_engine *e, int p, bool split, cudaGraphExec_t *out) {
     MinOp<kW> op{e->value_d, next, e->err_d, e->V};
     k_lbs_pair_dev<typename K::PSrc, typename K::PSrc, MinOp<kW>><<<grid, kThreads, 0, s>>>(
         lbs_args(e, 0, 0, 0, true, e->plan.static_edges), K::stat(e), lbs_args(e, 1, 0, 0, true, e->g->E),
-        K::host(e), op, e->counts_d, &L->relax_go, nullptr, &L->tile_next, L->relax_timer);
+        K::host(e), op, e->counts_d, &L->relax_go, nullptr, &L->tile_next,
+        e->relax_timer ? L->relax_timer : nullptr);
     k_min_ctl_end<<<1, 32, 0, s>>>(L);
     CK(cudaMemsetAsync(cur, 0, 4 * e->nwords, s));
     return OG_OK;
@@ -1041,7 +1046,7 @@ int run_min_dev(og_engine *e, int algo, uint32_t src, og_stats &st) {
   const int g = grid_for(V, e->sms);
   const bool sssp = algo == OG_ALGO_SSSP;
   const bool split = sssp && e->sssp_delta > 0;
-  const int key = (sssp ? 2 : 0) + (split ? 1 : 0);
+  const int key = (sssp ? 2 : 0) + (split ? 1 : 0) + (e->relax_timer ? 4 : 0);
   if (key != e->min_exec_key) {
     for (int p = 0; p < 2; p++)
       if (e->min_exec[p]) {
@@ -1691,6 +1696,11 @@ extern "C" int og_engine_set_param(og_engine *e, int param, double value) {
     e->level_loop = (uint32_t)value;
     return OG_OK;
   }
+  if (param == OG_PARAM_RELAX_TIMER) {
+    if (value != 0 && value != 1) return fail(OG_E_ARG, "relax timer must be 0 or 1, not %g", value);
+    e->relax_timer = (uint32_t)value;
+    return OG_OK;
+  }
   return fail(OG_E_ARG, "unknown parameter %d", param);
 }
 
@@ -1710,6 +1720,10 @@ extern "C" int og_engine_get_param(const og_engine *e, int param, double *value)
   }
   if (param == OG_PARAM_LEVEL_LOOP) {
     *value = e->level_loop;
+    return OG_OK;
+  }
+  if (param == OG_PARAM_RELAX_TIMER) {
+    *value = e->relax_timer;
     return OG_OK;
   }
   return fail(OG_E_ARG, "unknown parameter %d", param);

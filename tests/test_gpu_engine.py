@@ -370,7 +370,11 @@ def test_device_level_loop_matches_host_loop():
 
 def test_device_rounds_sssp_cc_match_host_loop():
     """Device-driven SSSP (several near/far widths, including 0) and
-    label-propagation CC rounds equal the host loop's results and statistics."""
+    label-propagation CC rounds equal the host loop's results.  Their round
+    counters agree within 1 %: inside a round, whether a tile reads a vertex's
+    distance before or after another tile lowers it depends on timing, which
+    moves vertices between consecutive frontiers without changing the fixed
+    point (BFS level sets have no such freedom and are compared exactly)."""
     for scale in (12, 13):
         g = og.Graph.rmat(scale, 16, weighted=True, seed=scale)
         off, pairs = np.array(g.offsets), np.array(g.edges)
@@ -379,6 +383,7 @@ def test_device_rounds_sssp_cc_match_host_loop():
         for ekw in [dict(budget=1 << 30, advisek=1.0),
                     dict(budget=budget_for(g, T, og.CFG_DIRECT), advisek=0.5, direct=True)]:
             e = engine(g, **ekw)
+            e.set_param(og.PARAM_RELAX_TIMER, 1)
             for delta in (4, 0, 1, 37):
                 e.set_param(og.PARAM_SSSP_DELTA, delta)
                 for s in [int(np.argmax(deg)), 9, int(np.argmax(deg))]:
@@ -389,11 +394,16 @@ def test_device_rounds_sssp_cc_match_host_loop():
                     np.testing.assert_array_equal(e.sssp(s), d)
                     host = dict(e.stats)
                     np.testing.assert_array_equal(d, oracle.sssp_dijkstra(off, pairs, s))
-                    for k in ("iterations", "frontier_sum", "edges_static", "edges_dynamic"):
-                        assert dev[k] == host[k], (scale, ekw, delta, s, k)
+                    assert abs(dev["iterations"] - host["iterations"]) <= 2, (scale, ekw, delta, s)
+                    for k in ("frontier_sum", "edges_static", "edges_dynamic"):
+                        assert abs(dev[k] - host[k]) <= 0.01 * host[k] + 64, (scale, ekw, delta, s, k, dev[k], host[k])
                     # the relax launches time themselves inside the device loop
                     assert 0.0 < dev["ms_relax"] <= dev["ms_dynamic"], (dev["ms_relax"], dev["ms_dynamic"])
                     assert host["ms_relax"] == 0.0
+            e.set_param(og.PARAM_RELAX_TIMER, 0)
+            e.set_param(og.PARAM_LEVEL_LOOP, og.LOOP_AUTO)
+            e.sssp(9)
+            assert e.stats["ms_relax"] == 0.0 and e.get_param(og.PARAM_RELAX_TIMER) == 0
             e.set_param(og.PARAM_CC_METHOD, og.CC_LABEL_PROPAGATION)
             e.set_param(og.PARAM_LEVEL_LOOP, og.LOOP_AUTO)
             lab = e.cc()
