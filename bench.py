@@ -323,8 +323,8 @@ def run_ours(args, rank, world, local):
     h2d = h2d_peak_gbs()
     # Kernel-level timing of the dominant kernel: the same queries again with
     # the relax timer on, so that every relax launch of the device-driven
-    # rounds measures itself (first CTA start to last CTA end,
-    # og_stats.ms_relax); the timed queries above run without it.  The
+    # rounds is bracketed by two stamp kernels reading the GPU's global timer
+    # (og_stats.ms_relax); the timed queries above run without them.  The
     # host-driven loop is timed beside it with CUDA events around each round's
     # relax launch, for comparison: those intervals also hold any host delay
     # between the start event and the launch.
@@ -359,7 +359,7 @@ def run_ours(args, rank, world, local):
     roof_link = {"bound": "host-link", "kernel": kname, "achieved": link_gbs, "peak": h2d, "unit": "GB/s",
                  "frac": link_gbs / h2d if h2d else None, "traffic": None,
                  "peak_source": "measured pinned H2D copy in this run",
-                 "timing": "in-kernel globaltimer over every relax launch of %d device-driven queries "
+                 "timing": "globaltimer stamps around every relax launch of %d device-driven queries "
                            "(the timed queries' sources, timer on)" % len(tstats)}
     roof_static = {"bound": "hbm", "kernel": kname + ", its HBM side", "achieved": static_gbs,
                    "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": static_gbs / peaks["hbm_gbs"],

@@ -234,9 +234,9 @@ typedef struct og_stats {
   double ms_gather;          /* device time of the dynamic gather kernels   */
   double ms_relax;           /* device-driven rounds with
                                 OG_PARAM_RELAX_TIMER: time of the (top-down)
-                                relax launches, each measured inside the
-                                kernel from its first CTA start to its last
-                                CTA end; otherwise 0                        */
+                                relax launches, between stamp kernels
+                                enqueued right before and after each;
+                                otherwise 0                                 */
 } og_stats;
 
 /* initGraphHost + getMaxPartitionSize + initGraphDevice
@@ -364,9 +364,9 @@ int og_engine_clone(og_engine *parent, og_engine **out);
 #define OG_PARAM_LEVEL_LOOP 4
 #define OG_LOOP_AUTO 0
 #define OG_LOOP_HOST 1
-/* OG_PARAM_RELAX_TIMER: 1 makes the relax launches of the device-driven
- *   rounds time themselves (og_stats.ms_relax); 0 (default) leaves the timer
- *   out of the kernels, which saves a few per cent of query time. */
+/* OG_PARAM_RELAX_TIMER: 1 brackets every relax launch of the device-driven
+ *   rounds with two one-thread stamp kernels that read the GPU's global timer
+ *   (og_stats.ms_relax); 0 (default) leaves them out of the captured rounds. */
 #define OG_PARAM_RELAX_TIMER 5
 int og_engine_set_param(og_engine *e, int param, double value);
 int og_engine_get_param(const og_engine *e, int param, double *value);

@@ -38,7 +38,7 @@ struct BfsLoop {
   unsigned long long fn;          // size of the current frontier
   unsigned long long bu[4];       // bottom-up: reached, their degrees, host / static records
   unsigned long long iterations, frontier_sum, edges_static, edges_dynamic;
-  unsigned long long relax_timer[3];  // ktimer of the top-down relax (kt[0] starts at ~0)
+  unsigned long long relax_timer[2];  // k_stamp slots of the top-down relax
 };
 
 constexpr uint64_t kBfsAlpha = 14, kBfsBeta = 24;
@@ -130,11 +130,9 @@ __device__ __forceinline__ void dev_prepare(MinOp<W> &, const uint32_t *) {}
 template <class Src0, class Src1, class Op>
 __global__ void __launch_bounds__(kThreads) k_lbs_pair_dev(LbsArgs a0, Src0 s0, LbsArgs a1, Src1 s1, Op op,
                                                            const Counts *counts, const uint32_t *go,
-                                                           const uint32_t *level, uint32_t *tile_next,
-                                                           unsigned long long *ktime) {
+                                                           const uint32_t *level, uint32_t *tile_next) {
   static_assert(std::is_same<Src0, Src1>::value, "one tile body for both regions");
   if (*go == 0u) return;
-  ktimer_start(ktime);
   __shared__ LbsShared<typename Op::Val> sh;
   __shared__ uint32_t s_b[2];
   // Both regions' arguments live in shared memory and one tile body serves
@@ -172,7 +170,6 @@ __global__ void __launch_bounds__(kThreads) k_lbs_pair_dev(LbsArgs a0, Src0 s0, 
     lbs_tile(s_a[r], s_s[r], op, sh, r == 0 ? lo : b - hi);
     __syncthreads();  // the tile tables are rebuilt and the next slot is read after this
   }
-  ktimer_end(ktime);
 }
 
 // --------------------------------------------------- device-driven SSSP / CC
@@ -200,7 +197,7 @@ struct MinLoop {
   uint32_t tile_next;  // tile counter of the relax
   uint32_t pad[5];
   unsigned long long iterations, frontier_sum, edges_static, edges_dynamic;
-  unsigned long long relax_timer[3];  // ktimer of the relax (kt[0] starts at ~0)
+  unsigned long long relax_timer[2];  // k_stamp slots of the relax
 };
 
 // smallest waiting value a compaction of this epoch saw in its two regions

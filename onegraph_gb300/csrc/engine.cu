@@ -881,10 +881,11 @@ int capture_bfs_level(og_engine *e, int p, int dopt, cudaGraphExec_t *out) {
     CK(cudaStreamWaitEvent(s, e->ev_cd, 0));
     k_bfs_ctl_mid<<<1, 32, 0, s>>>(L, e->counts_d, dopt);
     BfsOp op{e->bm[2], next, e->value_d, e->err_d, e->V, 0};
+    if (e->relax_timer) k_stamp<<<1, 1, 0, s>>>(&L->td_go, L->relax_timer, 0);
     k_lbs_pair_dev<EKU::PSrc, EKU::PSrc, BfsOp><<<grid, kThreads, 0, s>>>(
         lbs_args(e, 0, 0, 0, true, e->plan.static_edges), EKU::stat(e), lbs_args(e, 1, 0, 0, true, e->g->E),
-        EKU::host(e), op, e->counts_d, &L->td_go, &L->level, &L->tile_next,
-        e->relax_timer ? L->relax_timer : nullptr);
+        EKU::host(e), op, e->counts_d, &L->td_go, &L->level, &L->tile_next);
+    if (e->relax_timer) k_stamp<<<1, 1, 0, s>>>(&L->td_go, L->relax_timer, 1);
     k_bfs_bottom_up<EKU::PSrc><<<grid_for(e->V, e->sms), kThreads, 0, s>>>(
         e->off_d, e->V, e->Vs, EKU::stat(e), EKU::host(e), cur, e->bm[2], next, e->value_d, 0, L->bu,
         e->err_d, &L->bu_go, &L->level);
@@ -937,7 +938,6 @@ int run_bfs_dev(og_engine *e, uint32_t src, og_stats &st) {
   k_set_source<<<1, 1, 0, s>>>(e->value_d, src, 1u, e->bm[0], e->bm[2]);
   BfsLoop &h = *e->loop_h;
   memset(&h, 0, sizeof h);
-  h.relax_timer[0] = ~0ull;
   h.level = 1;
   h.need_compact = 1;
   h.compact_go = 1;
@@ -967,8 +967,8 @@ int run_bfs_dev(og_engine *e, uint32_t src, og_stats &st) {
   st.edges_dynamic += h.edges_dynamic;
   st.link_bytes += (h.edges_dynamic * e->bpe + 7) / 8;
   st.chunks += (uint32_t)h.iterations;
-  st.ms_relax += h.relax_timer[2] / 1e6;
-  e->launches += 2 + 7ull * launched;
+  st.ms_relax += h.relax_timer[1] / 1e6;
+  e->launches += 2 + (7ull + (e->relax_timer ? 2 : 0)) * launched;
   e->bfs_levels_hint = (uint32_t)h.iterations;
   e->dev_epoch = h.epoch + 1;
   e->last_algo = OG_ALGO_BFS;
@@ -1017,10 +1017,11 @@ int capture_min_round(og_engine *e, int p, bool split, cudaGraphExec_t *out) {
       k_min_ctl_b<<<1, 32, 0, s>>>(L, e->counts_d, keys);
     }
     MinOp<kW> op{e->value_d, next, e->err_d, e->V};
+    if (e->relax_timer) k_stamp<<<1, 1, 0, s>>>(&L->relax_go, L->relax_timer, 0);
     k_lbs_pair_dev<typename K::PSrc, typename K::PSrc, MinOp<kW>><<<grid, kThreads, 0, s>>>(
         lbs_args(e, 0, 0, 0, true, e->plan.static_edges), K::stat(e), lbs_args(e, 1, 0, 0, true, e->g->E),
-        K::host(e), op, e->counts_d, &L->relax_go, nullptr, &L->tile_next,
-        e->relax_timer ? L->relax_timer : nullptr);
+        K::host(e), op, e->counts_d, &L->relax_go, nullptr, &L->tile_next);
+    if (e->relax_timer) k_stamp<<<1, 1, 0, s>>>(&L->relax_go, L->relax_timer, 1);
     k_min_ctl_end<<<1, 32, 0, s>>>(L);
     CK(cudaMemsetAsync(cur, 0, 4 * e->nwords, s));
     return OG_OK;
@@ -1078,7 +1079,6 @@ int run_min_dev(og_engine *e, int algo, uint32_t src, og_stats &st) {
   }
   MinLoop &h = *e->mloop_h;
   memset(&h, 0, sizeof h);
-  h.relax_timer[0] = ~0ull;
   h.epoch = e->dev_epoch;
   const uint64_t thr = 1ull + e->sssp_delta;
   h.thr = thr > 0xffffffffull ? 0xffffffffu : (uint32_t)thr;
@@ -1111,8 +1111,8 @@ int run_min_dev(og_engine *e, int algo, uint32_t src, og_stats &st) {
   st.edges_dynamic += h.edges_dynamic;
   st.link_bytes += (h.edges_dynamic * e->bpe + 7) / 8;
   st.chunks += (uint32_t)h.iterations;
-  st.ms_relax += h.relax_timer[2] / 1e6;
-  e->launches += 2 + (split ? 11ull : 7ull) * launched;
+  st.ms_relax += h.relax_timer[1] / 1e6;
+  e->launches += 2 + ((split ? 11ull : 7ull) + (e->relax_timer ? 2 : 0)) * launched;
   hint = h.rounds;  // rounds this query needed (the next one is launched that far before its first check)
   e->dev_epoch = h.epoch + 1;
   e->last_algo = algo;

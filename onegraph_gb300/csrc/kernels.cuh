@@ -46,26 +46,18 @@ __device__ __forceinline__ unsigned long long globaltimer_ns() {
   return t;
 }
 
-// In-kernel launch timer: kt[0] earliest CTA start (~0 between launches),
-// kt[1] CTAs finished, kt[2] accumulated ns.  Each CTA stamps its start; the
-// last CTA to finish adds (its end - the earliest start) to kt[2] and resets
-// kt[0..1] for the next launch.  Host-side gaps before a launch are excluded.
-__device__ __forceinline__ void ktimer_start(unsigned long long *kt) {
-  if (kt && threadIdx.x == 0) {
-    atomicMin(kt, globaltimer_ns());
-    __threadfence();
-  }
+// Launch timer of the device-driven rounds: a one-thread kernel enqueued
+// right before (end = 0) and right after (end = 1) a gated launch, in the
+// same captured stream.  Stream order puts the first stamp before the launch
+// starts and the second after it ends; kt[0] holds the start, kt[1] the
+// accumulated ns.  Rounds whose gate is closed add nothing.
+__global__ void k_stamp(const uint32_t *go, unsigned long long *kt, int end) {
+  if (*go == 0u) return;
+  const unsigned long long t = globaltimer_ns();
+  if (end) kt[1] += t - kt[0];
+  else kt[0] = t;
 }
-__device__ __forceinline__ void ktimer_end(unsigned long long *kt) {
-  if (kt && threadIdx.x == 0) {
-    __threadfence();
-    if (atomicAdd(kt + 1, 1ull) == gridDim.x - 1ull) {
-      const unsigned long long t0 = atomicExch(kt, ~0ull);
-      atomicAdd(kt + 2, globaltimer_ns() - t0);
-      atomicExch(kt + 1, 0ull);
-    }
-  }
-}
+
 
 struct Counts {
   uint32_t n;        // compacted vertices
