@@ -38,6 +38,8 @@ def lib():
                                 C.POINTER(C.c_double)]
         L.ora_pr_l1_mt.argtypes = [u32, _P, _P, _P, C.c_double, C.c_double, C.c_int, C.c_int, _P,
                                    C.POINTER(C.c_double)]
+        L.ora_path_certify.argtypes = [u32, _P, _P, u32, C.c_int, _P, u32, u32, C.c_int, _P]
+        L.ora_path_certify.restype = u64
         for f in ("ora_bfs", "ora_cc", "ora_sssp_frontier", "ora_pr_cpu", "ora_pr_onegraph",
                   "ora_pr_l1", "ora_pr_l1_mt"):
             getattr(L, f).restype = C.c_int
@@ -135,3 +137,14 @@ def normalise_bfs(depth, V):
     d = np.array(depth, dtype=np.uint32, copy=True)
     d[d == np.uint32(V + 1)] = np.uint32(0xFFFFFFFF)
     return d
+
+
+def path_certify_raw(V, off_ptr, edges_ptr, stride, unit, dist, src, unreached, threads):
+    """Shortest-path certificate (ora_path_certify) on a graph given by
+    pointers (no copies of large graphs).  Returns (violations, first bad
+    vertex or V)."""
+    fb = C.c_uint32()
+    d = np.ascontiguousarray(dist, dtype=np.uint32)
+    bad = lib().ora_path_certify(V, off_ptr, edges_ptr, stride, 1 if unit else 0, _p(d), src, unreached,
+                                 threads, C.byref(fb))
+    return int(bad), int(fb.value)

@@ -386,3 +386,94 @@ int ora_pr_l1_mt(uint32_t V, const uint64_t *off, const uint32_t *col,
   free(tid);
   return it;
 }
+
+/* ---------------------------------------------------- path certificates */
+
+typedef struct {
+  uint32_t V, stride, src, unreached, b, e;
+  int unit;
+  const uint64_t *off;
+  const uint32_t *edges, *dist;
+  uint64_t bad;
+  uint32_t first_bad;
+} cert_job;
+
+/* weight of edge (u, v): v searched in u's sorted list; 0 if absent */
+static uint64_t cert_weight(const cert_job *j, uint32_t u, uint32_t v, int *found) {
+  uint64_t lo = j->off[u], hi = j->off[(uint64_t)u + 1];
+  while (lo < hi) {
+    const uint64_t mid = lo + (hi - lo) / 2;
+    const uint32_t x = j->edges[mid * j->stride];
+    if (x < v) lo = mid + 1;
+    else hi = mid;
+  }
+  *found = lo < j->off[(uint64_t)u + 1] && j->edges[lo * j->stride] == v;
+  if (!*found) return 0;
+  return j->unit ? 1u : j->edges[lo * j->stride + 1];
+}
+
+static void *cert_worker(void *arg) {
+  cert_job *j = (cert_job *)arg;
+  j->bad = 0;
+  j->first_bad = j->V;
+  for (uint32_t u = j->b; u < j->e; u++) {
+    const uint32_t du = j->dist[u];
+    int ok = 1;
+    if (u == j->src && du != 1) ok = 0;
+    if (du != j->unreached) {
+      int tight = u == j->src;
+      for (uint64_t i = j->off[u]; i < j->off[(uint64_t)u + 1]; i++) {
+        const uint32_t v = j->edges[i * j->stride];
+        const uint64_t w = j->unit ? 1u : j->edges[i * j->stride + 1];
+        const uint32_t dv = j->dist[v];
+        if (dv == j->unreached || (uint64_t)dv > (uint64_t)du + w) ok = 0;  /* u -> v could improve v */
+        if (!tight && dv != j->unreached) {  /* v -> u is an in-edge of u (symmetric edge set) */
+          int found = 0;
+          const uint64_t wvu = cert_weight(j, v, u, &found);
+          if (!found) ok = 0;
+          else if ((uint64_t)dv + wvu == (uint64_t)du) tight = 1;
+        }
+      }
+      if (!tight) ok = 0;
+    }
+    if (!ok) {
+      if (j->bad == 0) j->first_bad = u;
+      j->bad++;
+    }
+  }
+  return NULL;
+}
+
+uint64_t ora_path_certify(uint32_t V, const uint64_t *off, const uint32_t *edges, uint32_t stride,
+                          int unit, const uint32_t *dist, uint32_t src, uint32_t unreached,
+                          int threads, uint32_t *first_bad) {
+  if (threads < 1) threads = 1;
+  cert_job *jobs = (cert_job *)calloc((size_t)threads, sizeof(cert_job));
+  pthread_t *tid = (pthread_t *)calloc((size_t)threads, sizeof(pthread_t));
+  uint64_t bad = 0;
+  uint32_t fb = V;
+  if (src >= V) bad = 1;
+  for (int t = 0; t < threads && src < V; t++) {
+    cert_job *j = &jobs[t];
+    j->V = V;
+    j->stride = stride;
+    j->src = src;
+    j->unreached = unreached;
+    j->unit = unit;
+    j->off = off;
+    j->edges = edges;
+    j->dist = dist;
+    j->b = (uint32_t)((uint64_t)V * t / threads);
+    j->e = (uint32_t)((uint64_t)V * (t + 1) / threads);
+    pthread_create(&tid[t], NULL, cert_worker, j);
+  }
+  for (int t = 0; t < threads && src < V; t++) {
+    pthread_join(tid[t], NULL);
+    bad += jobs[t].bad;
+    if (jobs[t].bad && fb == V) fb = jobs[t].first_bad;
+  }
+  free(jobs);
+  free(tid);
+  if (first_bad) *first_bad = fb;
+  return bad;
+}

@@ -84,6 +84,23 @@ int ora_pr_l1_mt(uint32_t V, const uint64_t *off, const uint32_t *col,
                  const uint32_t *outdeg, double damping, double tol, int max_iter,
                  int threads, double *out, double *final_l1);
 
+/* Shortest-path certificate of a BFS depth or SSSP distance array on a graph
+ * whose edge set is symmetric with sorted lists (the symmetric R-MAT graphs):
+ * dist[src] == 1; no edge (u, v, w) out of a reached u can lower dist[v]
+ * (dist[v] <= dist[u] + w); every reached v != src has an in-edge (u, v, w)
+ * with dist[u] + w == dist[v], the in-edge's weight found by binary search of
+ * v in u's list.  With weights >= 1 these prove that dist holds the exact
+ * shortest distances (a tight in-edge chain strictly decreases to the
+ * source).  edges: V-indexed u32 entries, `stride` per edge (1 columns, 2
+ * {dst, w} pairs); unit != 0 takes every weight as 1 (BFS depths).  Vertices
+ * with dist == unreached are unreached.  Runs on `threads` host threads;
+ * returns the number of violations (0: certified) and the first violating
+ * vertex in *first_bad (V if none).  Not a restatement of reference code: a
+ * size-independent check for inputs too large to run the oracle on. */
+uint64_t ora_path_certify(uint32_t V, const uint64_t *off, const uint32_t *edges, uint32_t stride,
+                          int unit, const uint32_t *dist, uint32_t src, uint32_t unreached,
+                          int threads, uint32_t *first_bad);
+
 #ifdef __cplusplus
 }
 #endif

@@ -7,6 +7,7 @@ CC/serial and PR/cpu compiled from the reference sources
 import numpy as np
 import pytest
 
+import onegraph_gb300 as og
 import oracle
 
 from conftest import golden_names
@@ -138,3 +139,25 @@ def test_cc_round_bounded_is_the_first_round():
                 want[v] = lab
     np.testing.assert_array_equal(out, want)
     assert oracle.cc_round_bounded_raw(g.V, g._off_p, g._edges_p, 2, 100, out) < g.E
+
+
+def test_path_certificate_accepts_exact_and_rejects_planted_errors():
+    """ora_path_certify: exact SSSP distances and BFS depths pass; a distance
+    raised or lowered by one (planted here, in the oracle's output) fails."""
+    g = og.Graph.rmat(11, 16, weighted=True, seed=4)
+    off, pairs = np.array(g.offsets), np.array(g.edges)
+    s = int(np.argmax(np.diff(off.astype(np.int64))))
+    d = oracle.sssp_dijkstra(off, pairs, s)
+    assert oracle.path_certify_raw(g.V, g._off_p, g._edges_p, 2, False, d, s, 0xFFFFFFFF, 4) == (0, g.V)
+    b, _ = oracle.bfs(off, pairs[:, 0].copy(), s)
+    assert oracle.path_certify_raw(g.V, g._off_p, g._edges_p, 2, True, b, s, 0xFFFFFFFF, 4)[0] == 0
+    reached = np.nonzero((d != 0xFFFFFFFF) & (np.arange(g.V) != s))[0]
+    for delta in (1, -1):
+        bad = d.copy()
+        v = int(reached[len(reached) // 2])
+        bad[v] = np.uint32(int(bad[v]) + delta)
+        n, first = oracle.path_certify_raw(g.V, g._off_p, g._edges_p, 2, False, bad, s, 0xFFFFFFFF, 4)
+        assert n > 0
+    wrong_src = d.copy()
+    wrong_src[s] = 2
+    assert oracle.path_certify_raw(g.V, g._off_p, g._edges_p, 2, False, wrong_src, s, 0xFFFFFFFF, 4)[0] > 0
