@@ -332,6 +332,9 @@ def run_ours(args, rank, world, local):
     # relax launch, for comparison: those intervals also hold any host delay
     # between the start event and the launch.
     eng.set_param(og.PARAM_RELAX_TIMER, 1)
+    # one untimed query first: a mode switch recaptures the round graphs, and
+    # the first replay pays for loading kernels used for the first time
+    eng.sssp(srcs[0], out=False)
     tstats = []
     for k in range(min(args.steps, 8)):
         eng.sssp(srcs[(args.warmup + k) % len(srcs)], out=False)
@@ -341,6 +344,7 @@ def run_ours(args, rank, world, local):
     link_dev = statistics.mean(s["link_bytes"] for s in tstats)
     static_dev = statistics.mean(s["edges_static"] for s in tstats)
     eng.set_param(og.PARAM_LEVEL_LOOP, og.LOOP_HOST)
+    eng.sssp(srcs[0], out=False)  # untimed, as above
     kstats = []
     for k in range(min(4, len(srcs))):
         eng.sssp(srcs[k], out=False)
