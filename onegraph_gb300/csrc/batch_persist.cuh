@@ -635,7 +635,11 @@ __global__ void __launch_bounds__(BLOCK, (ITEMS <= 4 ? 1024 : 512) / BLOCK) k_ba
   // direction state of source threadIdx.x (threads 0..63 of every CTA)
   bool src_bu = false;       // the source expands bottom-up
   uint64_t src_prev_n = 0;   // its previous frontier size
-  uint64_t src_explored = 0; // record count of the vertices it has reached
+  // record count of the vertices it has reached in its top-down levels (the
+  // bookkeeping sums degrees only for top-down sources, so after a bottom-up
+  // stretch this undercounts and the unexplored estimate E - src_explored is
+  // high: a source that has gone back to top-down is slow to switch again)
+  uint64_t src_explored = 0;
   uint32_t level = 1;
   for (;; level++) {
     // sources whose frontier is not empty
