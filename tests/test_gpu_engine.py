@@ -365,6 +365,15 @@ def test_device_level_loop_matches_host_loop():
                     np.testing.assert_array_equal(oracle.normalise_bfs(d, g.V), oracle.bfs(off, col, s)[0])
                     for k in ("iterations", "frontier_sum", "edges_static", "edges_dynamic"):
                         assert dev[k] == host[k], (scale, kw, ekw, direction, s, k, dev[k], host[k])
+            # the relax timer's stamp kernels change nothing but ms_relax
+            e.set_param(og.PARAM_LEVEL_LOOP, og.LOOP_AUTO)
+            e.set_param(og.PARAM_BFS_DIRECTION, og.BFS_TOP_DOWN)
+            s = int(np.argmax(deg))
+            want = e.bfs(s)
+            e.set_param(og.PARAM_RELAX_TIMER, 1)
+            np.testing.assert_array_equal(e.bfs(s), want)
+            assert 0.0 < e.stats["ms_relax"] <= e.stats["ms_dynamic"]
+            e.set_param(og.PARAM_RELAX_TIMER, 0)
             e.close()
 
 
