@@ -325,14 +325,14 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
   // The SSSP relax reads each packed record as two overlapping words; the
   // second mostly hits L1, so it runs best with a large L1: 58 % of the
   // unified L1/shared storage as shared memory (3 CTAs of 38 KB per SM,
-  // ~124 KB of L1).  Measured on R-MAT 27: 9.55 queries/s with the driver's
+  // ~124 KB of L1).  Measured on R-MAT 27: 9.55 queries/s with the CUDA driver's
   // choice, 9.85 at 58 %, 6.77 at 86 %, 8.06 at 30 %.
   CK(cudaFuncSetAttribute(k_lbs_pair<SrcP<true>, SrcP<true>, MinOp<true>>,
                           cudaFuncAttributePreferredSharedMemoryCarveout, 58));
   CK(cudaFuncSetAttribute(k_lbs_pair_dev<SrcP<true>, SrcP<true>, MinOp<true>>,
                           cudaFuncAttributePreferredSharedMemoryCarveout, 58));
   // Same for the PageRank pull (29 KB tiles: 4 CTAs per SM at 58 %).  R-MAT 26
-  // directed: 58.5 iterations/s with the driver's choice, 69.6 at 58 %,
+  // directed: 58.5 iterations/s with the CUDA driver's choice, 69.6 at 58 %,
   // 68.4 at 44 %, 63.2 at 30 %, 34.0 at 86 %.
   CK(cudaFuncSetAttribute(k_pr_pull<SrcP<false>>, cudaFuncAttributePreferredSharedMemoryCarveout, 58));
   CK(cudaFuncSetAttribute(k_pr_pull_pair<SrcP<false>, SrcP<false>>,
@@ -2128,7 +2128,7 @@ extern "C" int og_k_compact(const uint32_t *bits, uint32_t v_begin, uint32_t v_e
 //
 // og_k_compact_noalloc runs the same compaction with its look-back scratch in
 // a fixed array that is part of the loaded library instead of memory it asks
-// the driver for.  Limit: kNoAllocTiles compaction tiles of 32768 vertices,
+// the CUDA runtime for.  Limit: kNoAllocTiles compaction tiles of 32768 vertices,
 // i.e. a range of at most 2^28 vertices per call.  The array lives on every
 // device that loads the library, for as long as the process runs.
 

@@ -1,5 +1,5 @@
 """bench.py's JSON contract, on the CPU: the reference arm (the CPU baseline
-of the path, no GPU needed) prints one line with the keys the driver reads."""
+of the path, no GPU needed) prints one JSON line with the benchmark keys."""
 import json
 import os
 import subprocess
