@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define OG_ABI_VERSION 3
+#define OG_ABI_VERSION 4
 
 typedef enum og_status {
   OG_OK = 0,
@@ -212,6 +212,12 @@ typedef struct og_config {
                                  is the Subway scheme (BFS/sbw_BFS/main.cpp:323-506),
                                  with OG_CFG_DIRECT|OG_CFG_NO_PIN the unified-
                                  memory scheme (BFS/usm_BFS/main.cpp:120-222) */
+/* Also hold the state of og_sssp_batch for up to k sources per pass
+ * (1 <= k <= 32): a row of 8, 16 or 32 u32 distances per vertex (k rounded
+ * up), a pending-source mask per vertex and a near-source mask per list
+ * entry, 4 B x row + 8 B per vertex, sharing one allocation with the
+ * OG_CFG_BATCH masks.  Weighted graphs only. */
+#define OG_CFG_SSSP_BATCH(k) ((uint32_t)(k) << 8)
 #define OG_CFG_PR 4u      /* also hold PageRank state for a PLAIN/WEIGHTED
                              graph, read as symmetric (in-edges = out-edges,
                              outDegree = degree); implied for OG_GRAPH_PR    */
@@ -288,6 +294,37 @@ int og_pr_l1_push(og_engine *e, float *out_rank, double damping, double tol, int
  * NULL.  Depths are identical to n separate og_bfs calls. */
 int og_bfs_batch(og_engine *e, const uint32_t *srcs, int n, uint32_t *out,
                  uint64_t *checks, og_stats *st);
+/* Multi-source SSSP: up to k sources (the engine's OG_CFG_SSSP_BATCH(k)) in
+ * one pass.  Every round compacts the vertices whose distance from some
+ * source improved, and one edge-balanced relax serves every source active at
+ * a vertex, so an edge record read from HBM or over the host link is read once
+ * for all of them; the sources share the near/far threshold of og_sssp
+ * (OG_PARAM_SSSP_DELTA).  No reference counterpart: the reference runs
+ * sssp_opt once per source (SSSP/oneGraph/CalculateOpt.h:12-30).
+ * out: n x V distances, source-major, same convention as og_sssp, or NULL;
+ * checks: 2n values, {vertices reached, sum of their distances} per source,
+ * or NULL.  Distances are identical to n separate og_sssp calls. */
+int og_sssp_batch(og_engine *e, const uint32_t *srcs, int n, uint32_t *out, uint64_t *checks,
+                  og_stats *st);
+
+/* og_sssp_batch round by round, so that sources can join a pass in flight
+ * (the server's continuous batching).  Slots are 0..k-1.
+ * og_sssp_batch_begin clears every slot.  og_sssp_batch_join seeds slots[i]
+ * with source srcs[i], at any round boundary: a late source starts below the
+ * shared threshold and is expanded every round until it has caught up, with
+ * the same distances.  og_sssp_batch_step runs one round; *pending receives
+ * the slots that still have work (a joined slot outside it holds its final
+ * distances and may be read and joined again), *done = 1 once nothing is
+ * left.  og_sssp_batch_checks writes {reached, sum of distances} of every
+ * slot in the mask `slots` to out[2 s], out[2 s + 1] (64 values).
+ * og_sssp_batch_fetch copies slot `slot`'s V distances to host memory.
+ * No reference counterpart. */
+int og_sssp_batch_begin(og_engine *e);
+int og_sssp_batch_join(og_engine *e, const uint32_t *srcs, const uint32_t *slots, int n);
+int og_sssp_batch_step(og_engine *e, uint32_t *pending, int *done, og_stats *st);
+int og_sssp_batch_checks(og_engine *e, uint32_t slots, uint64_t *out);
+int og_sssp_batch_fetch(og_engine *e, uint32_t slot, uint32_t *out);
+
 /* og_bfs_batch runs all levels in one persistent cooperative kernel (static
  * edges from HBM, dynamic edges read straight from page-locked host memory);
  * with out == NULL the whole batch is captured once as a CUDA graph and
@@ -368,6 +405,14 @@ int og_engine_clone(og_engine *parent, og_engine **out);
  *   rounds with two one-thread stamp kernels that read the GPU's global timer
  *   (og_stats.ms_relax); 0 (default) leaves them out of the captured rounds. */
 #define OG_PARAM_RELAX_TIMER 5
+/* OG_PARAM_SSSP_BATCH_DELTA: near/far width of og_sssp_batch, shared by its
+ *   sources.  0 (default) expands every improved (vertex, source) pair every
+ *   round, as the reference's SSSP rounds do: the sources then advance in
+ *   lockstep by hops and one edge read serves many of them at once; d > 0
+ *   applies og_sssp's split with one threshold for all sources (fewer
+ *   re-expansions per source, less sharing).  Distances are exact for every
+ *   value.  Clones inherit it. */
+#define OG_PARAM_SSSP_BATCH_DELTA 6
 int og_engine_set_param(og_engine *e, int param, double value);
 int og_engine_get_param(const og_engine *e, int param, double *value);
 

@@ -26,6 +26,13 @@ PLAIN, WEIGHTED, PR = 0, 1, 2
 ALGO_BFS, ALGO_SSSP, ALGO_CC, ALGO_PR = 0, 1, 2, 3
 RMAT_SYMMETRIC, RMAT_PERMUTE, RMAT_WEIGHTED, RMAT_PR, RMAT_ON_GPU = 1, 2, 4, 8, 16
 CFG_DIRECT, CFG_NO_PIN, CFG_PR, CFG_BATCH, CFG_BATCH_LEVELS, CFG_NO_STATIC = 1, 2, 4, 8, 16, 32
+
+
+def CFG_SSSP_BATCH(k: int) -> int:
+    """OG_CFG_SSSP_BATCH(k): hold og_sssp_batch state for up to k (1..32) sources."""
+    return (int(k) & 63) << 8
+
+
 PARAM_SSSP_DELTA = 1
 PARAM_CC_METHOD = 2
 CC_AUTO, CC_LABEL_PROPAGATION, CC_UNION_FIND = 0, 1, 2
@@ -34,6 +41,7 @@ BFS_AUTO, BFS_TOP_DOWN = 0, 1
 PARAM_LEVEL_LOOP = 4
 LOOP_AUTO, LOOP_HOST = 0, 1
 PARAM_RELAX_TIMER = 5
+PARAM_SSSP_BATCH_DELTA = 6
 # R-MAT quadrant probabilities of the benchmark graphs
 RMAT_ABC = (0.57, 0.19, 0.19)
 
@@ -154,6 +162,12 @@ SIGNATURES = [
     ("og_pr_l1", C.c_int, [_P, _P, C.c_double, C.c_double, C.c_int, C.POINTER(Stats)]),
     ("og_pr_l1_push", C.c_int, [_P, _P, C.c_double, C.c_double, C.c_int, C.POINTER(Stats)]),
     ("og_bfs_batch", C.c_int, [_P, _P, C.c_int, _P, _P, C.POINTER(Stats)]),
+    ("og_sssp_batch", C.c_int, [_P, _P, C.c_int, _P, _P, C.POINTER(Stats)]),
+    ("og_sssp_batch_begin", C.c_int, [_P]),
+    ("og_sssp_batch_join", C.c_int, [_P, _P, _P, C.c_int]),
+    ("og_sssp_batch_step", C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_int), C.POINTER(Stats)]),
+    ("og_sssp_batch_checks", C.c_int, [_P, C.c_uint32, _P]),
+    ("og_sssp_batch_fetch", C.c_int, [_P, C.c_uint32, _P]),
     ("og_bfs_batch_tune", C.c_int, [_P, _P, C.c_int, C.c_int, C.POINTER(TuneResult)]),
     ("og_bfs_batch_set_config", C.c_int, [_P, C.c_int]),
     ("og_result_fetch", C.c_int, [_P, C.c_int, _P]),
@@ -178,7 +192,7 @@ SIGNATURES = [
 ]
 
 
-ABI_VERSION = 3  # OG_ABI_VERSION of include/onegraph.h these bindings follow
+ABI_VERSION = 4  # OG_ABI_VERSION of include/onegraph.h these bindings follow
 
 
 def lib():
@@ -370,12 +384,13 @@ class Engine:
 
     def __init__(self, graph: Graph, budget: int = 0, advisek: float = 0.0, direct: bool = False,
                  pagerank: bool = False, no_pin: bool = False, batch: bool = False,
-                 batch_levels: bool = False, no_static: bool = False, device: int = 0):
+                 batch_levels: bool = False, no_static: bool = False, sssp_batch: int = 0,
+                 device: int = 0):
         self.graph = graph
         cfg = Config(budget, advisek, (CFG_DIRECT if direct else 0) | (CFG_PR if pagerank else 0) |
                      (CFG_NO_PIN if no_pin else 0) | (CFG_BATCH if batch or batch_levels else 0) |
                      (CFG_BATCH_LEVELS if batch_levels else 0) |
-                     (CFG_NO_STATIC if no_static else 0), device)
+                     (CFG_NO_STATIC if no_static else 0) | CFG_SSSP_BATCH(sssp_batch), device)
         h = _P()
         _check(lib().og_engine_create(graph._h, C.byref(cfg), C.byref(h)), "og_engine_create")
         self._h = h
@@ -452,6 +467,47 @@ class Engine:
                "og_bfs_batch")
         self.stats = st.as_dict()
         return o, ck
+
+    def sssp_batch(self, srcs, out=None, checks: bool = True):
+        """Up to k SSSP sources (Engine(sssp_batch=k)) in one pass.  Returns
+        (distances n x V or None, checks n x 2 {reached, distance sum} or None);
+        out=False skips the distances."""
+        s = np.ascontiguousarray(srcs, dtype=np.uint32)
+        n = s.size
+        o = None if out is False else (np.empty((n, self.graph.V), np.uint32) if out is None else out)
+        ck = np.empty((n, 2), np.uint64) if checks else None
+        st = Stats()
+        _check(lib().og_sssp_batch(self._h, _ptr(s), n, _ptr(o), _ptr(ck), C.byref(st)),
+               "og_sssp_batch")
+        self.stats = st.as_dict()
+        return o, ck
+
+    # og_sssp_batch round by round (sources may join a pass in flight)
+    def sssp_batch_begin(self):
+        _check(lib().og_sssp_batch_begin(self._h), "og_sssp_batch_begin")
+
+    def sssp_batch_join(self, srcs, slots):
+        s = np.ascontiguousarray(srcs, dtype=np.uint32)
+        k = np.ascontiguousarray(slots, dtype=np.uint32)
+        assert s.size == k.size
+        _check(lib().og_sssp_batch_join(self._h, _ptr(s), _ptr(k), s.size), "og_sssp_batch_join")
+
+    def sssp_batch_step(self) -> tuple:
+        """One round: (slots still pending as a bit mask, done)."""
+        p, d, st = C.c_uint32(), C.c_int(), Stats()
+        _check(lib().og_sssp_batch_step(self._h, C.byref(p), C.byref(d), C.byref(st)), "og_sssp_batch_step")
+        self.stats = st.as_dict()
+        return p.value, bool(d.value)
+
+    def sssp_batch_checks(self, slots: int) -> np.ndarray:
+        out = np.zeros((32, 2), np.uint64)
+        _check(lib().og_sssp_batch_checks(self._h, slots, _ptr(out)), "og_sssp_batch_checks")
+        return out
+
+    def sssp_batch_fetch(self, slot: int) -> np.ndarray:
+        o = np.empty(self.graph.V, np.uint32)
+        _check(lib().og_sssp_batch_fetch(self._h, slot, _ptr(o)), "og_sssp_batch_fetch")
+        return o
 
     def bfs_batch_tune(self, srcs, reps: int = 2) -> dict:
         s = np.ascontiguousarray(srcs, dtype=np.uint32)

@@ -22,6 +22,7 @@
 #include "bfs_loop.cuh"
 #include "kernels.cuh"
 #include "og_internal.hpp"
+#include "sssp_batch.cuh"
 
 using namespace og;
 
@@ -121,6 +122,21 @@ struct og_engine {
   int graph_dopt = -1;
   bool graph_broken = false;
 
+  // multi-source SSSP (og_sssp_batch, sssp_batch.cuh): sb_k sources per pass
+  // in rows of sb_ks slots; its rows, pending masks and near masks share
+  // `arena` with the batched BFS masks
+  uint32_t sb_k = 0, sb_ks = 0;
+  unsigned char *arena = nullptr;
+  uint32_t *sb_dist = nullptr, *sb_pend = nullptr, *sb_lmask = nullptr;
+  uint32_t *sb_masks = nullptr;  // device: [0] pending slots seen, [1] waiting slots, [2..3] spare
+  uint32_t *sb_io_h = nullptr;   // page-locked: sources [0, 32), slots [32, 64), masks [64, 68)
+  uint32_t *sb_io_d = nullptr;
+  unsigned long long *sb_ck_d = nullptr, *sb_ck_h = nullptr;  // per-slot checks (2 x 32)
+  uint32_t sb_thr = 0, sb_far_min = 0;
+  uint32_t sb_delta = 0;  // OG_PARAM_SSSP_BATCH_DELTA: near/far width of the batch (0: every round)
+  bool sb_advance = false;
+  uint32_t sb_dirty = 0;  // slots whose distances are not all unreached
+
   og_engine *parent = nullptr;  // set on clones: resident state belongs to the parent
   int clones = 0;               // live clones of this engine
   uint64_t resident_bytes = 0;  // device bytes of the shared resident state
@@ -170,6 +186,8 @@ void destroy(og_engine *e) {
   if (e->counts_h) cudaFreeHost(e->counts_h);
   if (e->hist_h) cudaFreeHost(e->hist_h);
   if (e->srcs_h) cudaFreeHost(e->srcs_h);
+  if (e->sb_io_h) cudaFreeHost(e->sb_io_h);
+  if (e->sb_ck_h) cudaFreeHost(e->sb_ck_h);
   if (e->pmisc_h) cudaFreeHost(e->pmisc_h);
   if (e->graph) cudaGraphExecDestroy(e->graph);
   for (int p = 0; p < 2; p++)
@@ -265,8 +283,26 @@ int create_query_state(og_engine *e) {
     RC(dalloc(e, &e->part_d, e->part_n));
     RC(dalloc(e, &e->l1_d, 1));
   }
+  if (e->batch_enabled || e->sb_k) {
+    // one arena for the batched BFS masks (24 B per vertex) and the
+    // multi-source SSSP rows (4 sb_ks + 8 B per vertex): a context runs one
+    // at a time
+    const uint64_t per = std::max<uint64_t>(e->batch_enabled ? 24 : 0, e->sb_k ? 4ull * e->sb_ks + 8 : 0);
+    RC(dalloc(e, &e->arena, per * (V + 1)));
+    if (e->batch_enabled)
+      for (int i = 0; i < 3; i++) e->bmask[i] = (unsigned long long *)e->arena + (uint64_t)i * (V + 1);
+    if (e->sb_k) {
+      e->sb_dist = (uint32_t *)e->arena;
+      e->sb_pend = e->sb_dist + (V + 1) * e->sb_ks;
+      e->sb_lmask = e->sb_pend + (V + 1);  // list_cap[0] + list_cap[1] <= V + 1 entries
+      RC(dalloc(e, &e->sb_masks, 4));
+      RC(dalloc(e, &e->sb_io_d, 128));
+      RC(dalloc(e, &e->sb_ck_d, 2 * kSbMaxSources));
+      CK(cudaMallocHost(&e->sb_io_h, 128 * sizeof(uint32_t)));
+      CK(cudaMallocHost(&e->sb_ck_h, 2 * kSbMaxSources * sizeof(unsigned long long)));
+    }
+  }
   if (e->batch_enabled) {
-    for (int i = 0; i < 3; i++) RC(dalloc(e, &e->bmask[i], V + 1));
     RC(dalloc(e, &e->hist_d, (uint64_t)kMaxBatchLevels * 64));
     RC(dalloc(e, &e->srcs_d, 64));
     e->ptile_cap = e->g->E / 1024 + 8;
@@ -291,6 +327,10 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
   e->V = g->V;
   e->pr_enabled = g->kind == OG_GRAPH_PR || (cfg->flags & OG_CFG_PR);
   e->batch_enabled = (cfg->flags & OG_CFG_BATCH) != 0;
+  e->sb_k = sb_sources(cfg->flags);
+  if (e->sb_k > kSbMaxSources) return fail(OG_E_ARG, "OG_CFG_SSSP_BATCH(%u): at most %u sources", e->sb_k, kSbMaxSources);
+  if (e->sb_k && g->kind != OG_GRAPH_WEIGHTED) return fail(OG_E_UNSUPPORTED, "multi-source SSSP needs a weighted graph");
+  e->sb_ks = e->sb_k ? sb_row_slots(e->sb_k) : 0;
   CK(cudaSetDevice(e->dev));
   CK(cudaDeviceGetAttribute(&e->sms, cudaDevAttrMultiProcessorCount, e->dev));
   RC(graph_prepare(g));
@@ -399,6 +439,9 @@ int clone(og_engine *parent, og_engine *e) {
   e->sms = parent->sms;
   e->pr_enabled = parent->pr_enabled;
   e->batch_enabled = parent->batch_enabled;
+  e->sb_k = parent->sb_k;
+  e->sb_ks = parent->sb_ks;
+  e->sb_delta = parent->sb_delta;
   e->V = parent->V;
   e->Vs = parent->Vs;
   e->nwords = parent->nwords;
@@ -1398,6 +1441,249 @@ int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *
   return OG_OK;
 }
 
+// ------------------------------------------------------------ multi-source SSSP
+
+// Launches k_compact_sb for region r over the active (scan_wait = false) or
+// waiting bitmap.
+int launch_compact_sb(og_engine *e, int r, uint32_t *bits, uint32_t vb, uint32_t ve, bool scan_wait,
+                      cudaStream_t s) {
+  if (ve <= vb) {
+    CK(cudaMemsetAsync(e->counts_d + r, 0, sizeof(Counts), s));
+    return OG_OK;
+  }
+  SbCompactArgs a{};
+  a.bits = bits;
+  a.wait = e->bm[2];
+  a.v_begin = vb;
+  a.v_end = ve;
+  a.w_begin = vb / 32;
+  a.w_end = (uint32_t)(((uint64_t)ve + 31) / 32);
+  a.ntiles = (a.w_end - a.w_begin + kWordsPerCompactTile - 1) / kWordsPerCompactTile;
+  a.off = e->off_d;
+  a.list = e->list_d[r];
+  a.pref = e->pref_d[r];
+  a.tile_first = e->tile_d[r];
+  a.lmask = e->sb_lmask + (e->list_d[r] - e->list_d[0]);
+  a.counts = e->counts_d + r;
+  a.lb = e->lb[r];
+  a.err = e->err_d;
+  a.list_cap = e->list_cap[r];
+  a.tile_cap = e->tile_cap[r];
+  a.pend = e->sb_pend;
+  a.dist = e->sb_dist;
+  a.ks = e->sb_ks;
+  a.thr = e->sb_thr;
+  a.scan_wait = scan_wait ? 1u : 0u;
+  a.far_key = (unsigned long long *)(e->counts_d + 2) + r;
+  a.masks = e->sb_masks;
+  a.epoch = e->epoch;
+  if (a.ntiles + 1 > e->lb_tiles) return fail(OG_E_STATE, "compaction scratch too small");
+  k_compact_sb<<<a.ntiles, kThreads, 0, s>>>(a);
+  e->launches++;
+  return OG_OK;
+}
+
+// Clears the batch: no slot in use, no vertex active or waiting.
+int sb_reset(og_engine *e) {
+  if (!e->sb_k) return fail(OG_E_STATE, "engine created without OG_CFG_SSSP_BATCH");
+  const uint64_t V = e->V;
+  cudaStream_t s = e->s_main;
+  CK(cudaMemsetAsync(e->err_d, 0, 16, s));
+  CK(cudaMemsetAsync(e->bm[0], 0, 4 * e->nwords, s));  // active
+  CK(cudaMemsetAsync(e->bm[2], 0, 4 * e->nwords, s));  // waiting
+  CK(cudaMemsetAsync(e->sb_pend, 0, 4 * (V + 1), s));
+  CK(cudaMemsetAsync(e->sb_masks, 0, 16, s));
+  CK(cudaMemsetAsync(e->counts_d + 2, 0, sizeof(Counts), s));  // far keys of earlier queries
+  k_fill_u32<<<grid_for((V + 1) * e->sb_ks, e->sms), kThreads, 0, s>>>(e->sb_dist, (V + 1) * e->sb_ks,
+                                                                      0xffffffffu);
+  e->launches++;
+  const uint64_t thr = 1ull + e->sb_delta;
+  e->sb_thr = e->sb_delta == 0 || thr > 0xffffffffull ? 0xffffffffu : (uint32_t)thr;
+  e->sb_far_min = 0xffffffffu;
+  e->sb_advance = false;
+  e->sb_dirty = 0;
+  CK(cudaGetLastError());
+  return OG_OK;
+}
+
+// Seeds slots[i] with srcs[i] (their columns are reset first when a finished
+// source left distances there).  A source may join while others are in
+// flight: its distances start below any threshold, so it is expanded every
+// round until it has caught up; the result is the same.
+int sb_join_impl(og_engine *e, const uint32_t *srcs, const uint32_t *slots, uint32_t n) {
+  if (n == 0) return OG_OK;
+  if (n > e->sb_k) return fail(OG_E_ARG, "%u sources joined, the engine holds %u", n, e->sb_k);
+  uint32_t cols = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    if (srcs[i] >= e->V) return fail(OG_E_ARG, "source %u >= V %u", srcs[i], e->V);
+    if (slots[i] >= e->sb_k) return fail(OG_E_ARG, "slot %u >= %u", slots[i], e->sb_k);
+    if (cols & (1u << slots[i])) return fail(OG_E_ARG, "slot %u joined twice", slots[i]);
+    cols |= 1u << slots[i];
+  }
+  cudaStream_t s = e->s_main;
+  if (cols & e->sb_dirty) {
+    k_sb_clear_cols<<<grid_for(e->V + 1, e->sms), kThreads, 0, s>>>(e->sb_dist, e->V + 1, e->sb_ks,
+                                                                   cols & e->sb_dirty);
+    e->launches++;
+  }
+  e->sb_dirty |= cols;
+  // the page-locked buffer is rewritten only after the previous upload ran
+  CK(cudaStreamSynchronize(s));
+  memcpy(e->sb_io_h, srcs, 4 * n);
+  memcpy(e->sb_io_h + 32, slots, 4 * n);
+  CK(cudaMemcpyAsync(e->sb_io_d, e->sb_io_h, 256, cudaMemcpyHostToDevice, s));
+  k_sb_seed<<<1, 32, 0, s>>>(e->sb_io_d, e->sb_io_d + 32, n, e->sb_dist, e->sb_ks, e->sb_pend, e->bm[0],
+                             e->V, e->err_d);
+  e->launches++;
+  CK(cudaGetLastError());
+  return OG_OK;
+}
+
+// One round: compaction of the active set (or of the waiting set after a
+// threshold advance) in both regions, then the relax of the listed near
+// pairs.  *pending receives the slots that still have work as of this
+// round's compaction (a slot outside it has final distances); *done is set
+// when nothing is active or waiting.
+template <class K>
+int sb_round(og_engine *e, og_stats &st, Timing &tm, uint32_t *pending, bool *done) {
+  *done = false;
+  if (++e->epoch >= (1u << 30)) {  // epoch wrap: clear the status words and far keys once
+    for (int r = 0; r < 2; r++)
+      CK(cudaMemsetAsync(e->lb[r].status, 0, sizeof(uint32_t) * e->lb_tiles, e->s_main));
+    CK(cudaMemsetAsync(e->counts_d + 2, 0, sizeof(Counts), e->s_main));
+    e->epoch = 1;
+  }
+  const bool adv = e->sb_advance;
+  uint32_t *bits = adv ? e->bm[2] : e->bm[0];
+  // masks[0] is per round; masks[1] (slots waiting) accumulates until the
+  // waiting set is scanned again
+  CK(cudaMemsetAsync(e->sb_masks, 0, adv ? 8 : 4, e->s_main));
+  CK(cudaEventRecord(e->ev_round, e->s_main));
+  RC(launch_compact_sb(e, 0, bits, 0, e->Vs, adv, e->s_main));
+  CK(cudaEventRecord(e->ev_cs, e->s_main));
+  CK(cudaStreamWaitEvent(e->s_dyn, e->ev_round, 0));
+  RC(launch_compact_sb(e, 1, bits, e->Vs, e->V, adv, e->s_dyn));
+  CK(cudaEventRecord(e->ev_cd, e->s_dyn));
+  CK(cudaStreamWaitEvent(e->s_dyn, e->ev_cs, 0));
+  CK(cudaMemcpyAsync(e->counts_h, e->counts_d, 3 * sizeof(Counts), cudaMemcpyDeviceToHost, e->s_dyn));
+  CK(cudaMemcpyAsync(e->sb_io_h + 64, e->sb_masks, 8, cudaMemcpyDeviceToHost, e->s_dyn));
+  CK(cudaMemcpyAsync(e->err_h, e->err_d, 4, cudaMemcpyDeviceToHost, e->s_dyn));
+  CK(cudaStreamSynchronize(e->s_dyn));
+  collect_timing(e, tm, &st);
+  float ms;
+  if (cudaEventElapsedTime(&ms, e->ev_round, e->ev_cd) == cudaSuccess) st.ms_compact += ms;
+  RC(check_device_error(e));
+  *pending = e->sb_io_h[64] | e->sb_io_h[65];
+  const uint32_t fm = std::min(far_of(e, 0), far_of(e, 1));
+  e->sb_far_min = adv ? fm : std::min(e->sb_far_min, fm);
+  const uint64_t n = (uint64_t)e->counts_h[0].n + e->counts_h[1].n;
+  if (n == 0) {
+    if (e->sb_far_min == 0xffffffffu) {
+      *done = true;
+      *pending = 0;
+      return OG_OK;
+    }
+    const uint64_t t = (uint64_t)e->sb_far_min + e->sb_delta;
+    e->sb_thr = t > 0xffffffffull ? 0xffffffffu : (uint32_t)t;
+    e->sb_advance = true;
+    return OG_OK;
+  }
+  e->sb_advance = false;
+  st.iterations++;
+  st.frontier_sum += n;
+  st.static_vertices += e->counts_h[0].n;
+  SbOp op{e->list_d[0], e->sb_lmask, e->sb_dist, e->sb_pend, e->bm[0], e->err_d, e->V, e->sb_ks};
+  auto launch = [&](const LbsArgs &a, auto src, cudaStream_t ls) {
+    const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
+    if (grid) {
+      using S = decltype(src);
+      if (e->sb_ks == 8) k_sb_relax<S, 8><<<grid, kThreads, 0, ls>>>(a, src, op);
+      else if (e->sb_ks == 16) k_sb_relax<S, 16><<<grid, kThreads, 0, ls>>>(a, src, op);
+      else k_sb_relax<S, 32><<<grid, kThreads, 0, ls>>>(a, src, op);
+      e->launches++;
+    }
+    return (int)OG_OK;
+  };
+  auto sfn = [&](const LbsArgs &a) { return launch(a, K::stat(e), e->s_main); };
+  auto pfn = [&](const LbsArgs &a0, auto s0, const LbsArgs &a1, auto s1, cudaStream_t ps) {
+    const uint64_t n0 = lbs_grid(a0.pos_begin, a0.pos_end), n1 = lbs_grid(a1.pos_begin, a1.pos_end);
+    if (n0 + n1 > 0x7fffffffull) return fail(OG_E_STATE, "relax grid too large");
+    using S0 = decltype(s0);
+    using S1 = decltype(s1);
+    const unsigned grid = (unsigned)(n0 + n1);
+    if (e->sb_ks == 8) k_sb_relax_pair<S0, S1, 8><<<grid, kThreads, 0, ps>>>(a0, s0, a1, s1, op, n0, n0 + n1);
+    else if (e->sb_ks == 16) k_sb_relax_pair<S0, S1, 16><<<grid, kThreads, 0, ps>>>(a0, s0, a1, s1, op, n0, n0 + n1);
+    else k_sb_relax_pair<S0, S1, 32><<<grid, kThreads, 0, ps>>>(a0, s0, a1, s1, op, n0, n0 + n1);
+    e->launches++;
+    return (int)OG_OK;
+  };
+  RC((run_regions<K>(e, st, tm, sfn, launch, pfn)));
+  CK(cudaStreamWaitEvent(e->s_main, e->ev_cd, 0));
+  CK(cudaGetLastError());
+  return OG_OK;
+}
+
+int sb_round_any(og_engine *e, og_stats &st, Timing &tm, uint32_t *pending, bool *done) {
+  if (e->wbytes == 1) return sb_round<EK<uint8_t>>(e, st, tm, pending, done);
+  if (e->wbytes == 2) return sb_round<EK<uint16_t>>(e, st, tm, pending, done);
+  return sb_round<EK<uint32_t>>(e, st, tm, pending, done);
+}
+
+// {reached, sum of distances} of every slot in cols, indexed by slot.
+int sb_checks_impl(og_engine *e, uint32_t cols, uint64_t *out) {
+  cudaStream_t s = e->s_main;
+  CK(cudaMemsetAsync(e->sb_ck_d, 0, 16 * kSbMaxSources, s));
+  k_sb_checks<<<(unsigned)e->sms * 4, kThreads, 0, s>>>(e->sb_dist, e->V, e->sb_ks, cols, e->sb_ck_d);
+  e->launches++;
+  CK(cudaMemcpyAsync(e->sb_ck_h, e->sb_ck_d, 16 * kSbMaxSources, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  for (uint32_t i = 0; i < 2 * kSbMaxSources; i++) out[i] = e->sb_ck_h[i];
+  return OG_OK;
+}
+
+// Distances of slot `slot` into out (V entries of host memory), through the
+// engine's value array.
+int sb_fetch_impl(og_engine *e, uint32_t slot, uint32_t *out) {
+  if (slot >= e->sb_k) return fail(OG_E_ARG, "slot %u >= %u", slot, e->sb_k);
+  cudaStream_t s = e->s_main;
+  k_sb_column<<<grid_for(e->V, e->sms), kThreads, 0, s>>>(e->sb_dist, e->V, e->sb_ks, slot, e->value_d);
+  e->launches++;
+  CK(cudaMemcpyAsync(out, e->value_d, 4ull * e->V, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  e->last_algo = -1;  // the value array holds no single-source result
+  return OG_OK;
+}
+
+int run_sssp_batch(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *out, uint64_t *checks,
+                   og_stats &st) {
+  RC(sb_reset(e));
+  uint32_t slots[kSbMaxSources];
+  for (uint32_t i = 0; i < n; i++) slots[i] = i;
+  RC(sb_join_impl(e, srcs, slots, n));
+  Timing tm;
+  for (uint64_t r = 0;; r++) {
+    uint32_t pending = 0;
+    bool done = false;
+    RC(sb_round_any(e, st, tm, &pending, &done));
+    if (done) break;
+    if (r > 16ull * e->V + 64) return fail(OG_E_STATE, "multi-source SSSP did not end after %llu rounds",
+                                           (unsigned long long)r);
+  }
+  CK(cudaStreamSynchronize(e->s_main));
+  collect_timing(e, tm, &st);
+  CK(cudaMemcpy(e->err_h, e->err_d, 4, cudaMemcpyDeviceToHost));
+  RC(check_device_error(e));
+  if (checks) {
+    uint64_t ck[2 * kSbMaxSources];
+    RC(sb_checks_impl(e, (n >= 32 ? 0xffffffffu : (1u << n) - 1u), ck));
+    for (uint32_t i = 0; i < 2 * n; i++) checks[i] = ck[i];
+  }
+  if (out)
+    for (uint32_t i = 0; i < n; i++) RC(sb_fetch_impl(e, i, out + (uint64_t)i * e->V));
+  e->last_algo = -1;
+  return OG_OK;
+}
+
 // ------------------------------------------------------------------ PageRank
 
 int pr_sums(og_engine *e, og_stats &st, Timing &tm) {
@@ -1701,6 +1987,11 @@ extern "C" int og_engine_set_param(og_engine *e, int param, double value) {
     e->relax_timer = (uint32_t)value;
     return OG_OK;
   }
+  if (param == OG_PARAM_SSSP_BATCH_DELTA) {
+    if (value < 0 || value > 4294967295.0) return fail(OG_E_ARG, "delta out of range");
+    e->sb_delta = (uint32_t)value;
+    return OG_OK;
+  }
   return fail(OG_E_ARG, "unknown parameter %d", param);
 }
 
@@ -1724,6 +2015,10 @@ extern "C" int og_engine_get_param(const og_engine *e, int param, double *value)
   }
   if (param == OG_PARAM_RELAX_TIMER) {
     *value = e->relax_timer;
+    return OG_OK;
+  }
+  if (param == OG_PARAM_SSSP_BATCH_DELTA) {
+    *value = e->sb_delta;
     return OG_OK;
   }
   return fail(OG_E_ARG, "unknown parameter %d", param);
@@ -1982,6 +2277,92 @@ extern "C" int og_bfs_batch_set_config(og_engine *e, int config) {
   if (config < -1 || config >= kNumPersistConfigs) return fail(OG_E_ARG, "config %d out of range", config);
   e->tuned = config;
   return OG_OK;
+}
+
+extern "C" int og_sssp_batch(og_engine *e, const uint32_t *srcs, int n, uint32_t *out, uint64_t *checks,
+                             og_stats *st) {
+  if (!e || !srcs) return fail(OG_E_ARG, "og_sssp_batch: null argument");
+  if (e->g->kind != OG_GRAPH_WEIGHTED) return fail(OG_E_UNSUPPORTED, "SSSP needs a weighted graph");
+  if (!e->sb_k) return fail(OG_E_STATE, "engine created without OG_CFG_SSSP_BATCH");
+  if (n < 1 || n > (int)e->sb_k) return fail(OG_E_ARG, "n = %d, the engine holds 1..%u sources", n, e->sb_k);
+  for (int i = 0; i < n; i++)
+    if (srcs[i] >= e->V) return fail(OG_E_ARG, "source %u >= V %u", srcs[i], e->V);
+  struct Ctx {
+    const uint32_t *srcs;
+    uint32_t n;
+    uint32_t *out;
+    uint64_t *checks;
+  } c{srcs, (uint32_t)n, out, checks};
+  return query_common(e, OG_ALGO_SSSP, st, nullptr, [](og_engine *en, og_stats &s, void *cx) {
+    Ctx &q = *(Ctx *)cx;
+    return run_sssp_batch(en, q.srcs, q.n, q.out, q.checks, s);
+  }, &c);
+}
+
+extern "C" int og_sssp_batch_begin(og_engine *e) {
+  if (!e) return fail(OG_E_ARG, "null engine");
+  return guarded([&]() -> int {
+    clear_error();
+    CK(cudaSetDevice(e->dev));
+    e->launches = 0;
+    return sb_reset(e);
+  });
+}
+
+extern "C" int og_sssp_batch_join(og_engine *e, const uint32_t *srcs, const uint32_t *slots, int n) {
+  if (!e || n < 0 || (n && (!srcs || !slots))) return fail(OG_E_ARG, "og_sssp_batch_join: bad argument");
+  if (!e->sb_k) return fail(OG_E_STATE, "engine created without OG_CFG_SSSP_BATCH");
+  return guarded([&]() -> int {
+    clear_error();
+    CK(cudaSetDevice(e->dev));
+    return sb_join_impl(e, srcs, slots, (uint32_t)n);
+  });
+}
+
+extern "C" int og_sssp_batch_step(og_engine *e, uint32_t *pending, int *done, og_stats *st) {
+  if (!e || !pending || !done) return fail(OG_E_ARG, "og_sssp_batch_step: null argument");
+  if (!e->sb_k) return fail(OG_E_STATE, "engine created without OG_CFG_SSSP_BATCH");
+  return guarded([&]() -> int {
+    clear_error();
+    CK(cudaSetDevice(e->dev));
+    og_stats s;
+    memset(&s, 0, sizeof s);
+    const uint64_t l0 = e->launches;
+    const double t0 = now_ms();
+    Timing tm;
+    bool d = false;
+    RC(sb_round_any(e, s, tm, pending, &d));
+    CK(cudaStreamSynchronize(e->s_main));
+    collect_timing(e, tm, &s);
+    CK(cudaMemcpy(e->err_h, e->err_d, 4, cudaMemcpyDeviceToHost));
+    RC(check_device_error(e));
+    s.launches = e->launches - l0;
+    s.ms_total = now_ms() - t0;
+    if (st) *st = s;
+    *done = d ? 1 : 0;
+    e->last_algo = -1;
+    return OG_OK;
+  });
+}
+
+extern "C" int og_sssp_batch_checks(og_engine *e, uint32_t slots, uint64_t *out) {
+  if (!e || !out) return fail(OG_E_ARG, "og_sssp_batch_checks: null argument");
+  if (!e->sb_k) return fail(OG_E_STATE, "engine created without OG_CFG_SSSP_BATCH");
+  return guarded([&]() -> int {
+    clear_error();
+    CK(cudaSetDevice(e->dev));
+    return sb_checks_impl(e, slots, out);
+  });
+}
+
+extern "C" int og_sssp_batch_fetch(og_engine *e, uint32_t slot, uint32_t *out) {
+  if (!e || !out) return fail(OG_E_ARG, "og_sssp_batch_fetch: null argument");
+  if (!e->sb_k) return fail(OG_E_STATE, "engine created without OG_CFG_SSSP_BATCH");
+  return guarded([&]() -> int {
+    clear_error();
+    CK(cudaSetDevice(e->dev));
+    return sb_fetch_impl(e, slot, out);
+  });
 }
 
 extern "C" int og_result_checksum(og_engine *e, int algo, uint64_t *out) {

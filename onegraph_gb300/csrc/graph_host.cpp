@@ -184,8 +184,12 @@ uint64_t engine_vertex_bytes(int kind, uint32_t flags) {
   // sum f32 and outdeg u32.
   uint64_t b = 8 + 4 + 4 + 8;
   if (kind == OG_GRAPH_PR || (flags & OG_CFG_PR)) b += 12;
-  if (flags & OG_CFG_BATCH) b += 24;  // visited, frontier, next u64 masks
-  return b;
+  // batched BFS: visited, frontier, next u64 masks; multi-source SSSP: a row
+  // of distances, a pending-slot mask and a near-slot mask per list entry.
+  // The two share one allocation (a query context runs one at a time).
+  uint64_t batch = (flags & OG_CFG_BATCH) ? 24 : 0;
+  if (sb_sources(flags)) batch = std::max<uint64_t>(batch, 4ull * sb_row_slots(sb_sources(flags)) + 8);
+  return b + batch;
 }
 
 uint64_t engine_fixed_bytes(uint32_t V, uint64_t E, uint32_t flags) {

@@ -172,6 +172,85 @@ __device__ __forceinline__ void block_scan_pair(uint32_t cnt, uint64_t sum, uint
   __syncthreads();  // shared arrays are reused by the next call
 }
 
+// Warp-wide decoupled look-back of compaction tile `tile` (called by all 32
+// lanes of warp 0): publishes the tile's totals (tot_n, tot_e) and returns in
+// (pn, pe) the exclusive prefix of the tiles before it.  Each pass reads the
+// status of the 32 nearest unaccounted predecessors at once, sums their
+// aggregates up to the nearest one holding an inclusive prefix, and stops
+// there; tiles before the first count as an inclusive prefix of 0.  Waits
+// are bounded by `spin_limit` polls: a status that never appears sets
+// kErrLookback in *err and bad = 1 (the caller then writes nothing), and the
+// tile still publishes an inclusive prefix so that successors never wait
+// forever.
+__device__ __forceinline__ void lookback_prefix(const Lookback &lb, uint32_t tile, uint32_t epoch,
+                                                uint32_t tot_n, uint64_t tot_e, uint32_t *err,
+                                                uint32_t &pn, uint64_t &pe, int &bad,
+                                                uint32_t spin_limit = kSpinLimit) {
+  const int lane = threadIdx.x & 31;
+  pn = 0;
+  pe = 0;
+  bad = 0;
+  if (tile == 0) {
+    if (lane == 0) {
+      lb.inc_n[0] = tot_n;
+      lb.inc_e[0] = tot_e;
+      __threadfence();
+      st_release(&lb.status[0], (epoch << 2) | 2u);
+    }
+    return;
+  }
+  if (lane == 0) {
+    lb.agg_n[tile] = tot_n;
+    lb.agg_e[tile] = tot_e;
+    __threadfence();
+    st_release(&lb.status[tile], (epoch << 2) | 1u);
+  }
+  for (int p = (int)tile - 1;; p -= 32) {
+    const int q = p - lane;  // lane 0: nearest predecessor of the window
+    uint32_t st = 2u;
+    if (q >= 0) {
+      uint32_t spins = 0;
+      for (;;) {
+        const uint32_t raw = ld_acquire(&lb.status[q]);
+        st = (raw >> 2) == epoch ? (raw & 3u) : 0u;
+        if (st != 0u || ++spins > spin_limit) break;
+        __nanosleep(64);
+      }
+    }
+    __syncwarp();
+    if (__any_sync(0xffffffffu, st == 0u)) {  // bounded wait expired: report, never hang
+      if (lane == 0) atomicOr(err, kErrLookback);
+      bad = 1;
+      break;
+    }
+    const unsigned incl = __ballot_sync(0xffffffffu, st == 2u);
+    const int k = incl ? __ffs(incl) - 1 : 32;
+    uint32_t vn = 0;
+    uint64_t ve = 0;
+    if (q >= 0 && lane < k) {
+      vn = __ldcg(&lb.agg_n[q]);
+      ve = __ldcg(&lb.agg_e[q]);
+    } else if (q >= 0 && lane == k) {
+      vn = __ldcg(&lb.inc_n[q]);
+      ve = __ldcg(&lb.inc_e[q]);
+    }
+#pragma unroll
+    for (int o = 16; o; o >>= 1) {
+      vn += __shfl_xor_sync(0xffffffffu, vn, o);
+      ve += __shfl_xor_sync(0xffffffffu, ve, o);
+    }
+    pn += vn;
+    pe += ve;
+    if (k < 32) break;
+  }
+  if (lane == 0) {
+    lb.inc_n[tile] = pn + tot_n;
+    lb.inc_e[tile] = pe + tot_e;
+    __threadfence();
+    st_release(&lb.status[tile], (epoch << 2) | 2u);  // published even when bad
+  }
+}
+
 // Frontier compaction for the vertex range [v_begin, v_end).  Four
 // consecutive bitmap words (128 vertices) per thread, 1024 words per CTA
 // tile, tiles ordered by a ticket so that every predecessor a tile waits for
@@ -249,75 +328,12 @@ __global__ void __launch_bounds__(kThreads) k_compact(CompactArgs a) {
     for (int i = 0; i < kThreads / 32; i++) m = min(m, s_wmin[i]);
     if (m != 0xffffffffu) atomicMax(a.far_key, ((unsigned long long)a.epoch << 32) | (~m & 0xffffffffu));
   }
-  // Warp-wide decoupled look-back (warp 0): each pass reads the status of the
-  // 32 nearest unaccounted predecessors at once, sums their aggregates up to
-  // the nearest one holding an inclusive prefix, and stops there; tiles
-  // before the first count as an inclusive prefix of 0.  Waits are bounded:
-  // a status that never appears sets kErrLookback and the tile writes nothing.
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;
     uint32_t pn = 0;
     uint64_t pe = 0;
     int bad = 0;
-    if (tile == 0) {
-      if (lane == 0) {
-        a.lb.inc_n[0] = tot_n;
-        a.lb.inc_e[0] = tot_e;
-        __threadfence();
-        st_release(&a.lb.status[0], (a.epoch << 2) | 2u);
-      }
-    } else {
-      if (lane == 0) {
-        a.lb.agg_n[tile] = tot_n;
-        a.lb.agg_e[tile] = tot_e;
-        __threadfence();
-        st_release(&a.lb.status[tile], (a.epoch << 2) | 1u);
-      }
-      for (int p = (int)tile - 1;; p -= 32) {
-        const int q = p - lane;  // lane 0: nearest predecessor of the window
-        uint32_t st = 2u;
-        if (q >= 0) {
-          uint32_t spins = 0;
-          for (;;) {
-            const uint32_t raw = ld_acquire(&a.lb.status[q]);
-            st = (raw >> 2) == a.epoch ? (raw & 3u) : 0u;
-            if (st != 0u || ++spins > kSpinLimit) break;
-            __nanosleep(64);
-          }
-        }
-        __syncwarp();
-        if (__any_sync(0xffffffffu, st == 0u)) {  // bounded wait expired: report, never hang
-          if (lane == 0) atomicOr(a.err, kErrLookback);
-          bad = 1;
-          break;
-        }
-        const unsigned incl = __ballot_sync(0xffffffffu, st == 2u);
-        const int k = incl ? __ffs(incl) - 1 : 32;
-        uint32_t vn = 0;
-        uint64_t ve = 0;
-        if (q >= 0 && lane < k) {
-          vn = __ldcg(&a.lb.agg_n[q]);
-          ve = __ldcg(&a.lb.agg_e[q]);
-        } else if (q >= 0 && lane == k) {
-          vn = __ldcg(&a.lb.inc_n[q]);
-          ve = __ldcg(&a.lb.inc_e[q]);
-        }
-#pragma unroll
-        for (int o = 16; o; o >>= 1) {
-          vn += __shfl_xor_sync(0xffffffffu, vn, o);
-          ve += __shfl_xor_sync(0xffffffffu, ve, o);
-        }
-        pn += vn;
-        pe += ve;
-        if (k < 32) break;
-      }
-      if (lane == 0) {
-        a.lb.inc_n[tile] = pn + tot_n;
-        a.lb.inc_e[tile] = pe + tot_e;
-        __threadfence();
-        st_release(&a.lb.status[tile], (a.epoch << 2) | 2u);  // published even when bad: successors never wait forever
-      }
-    }
+    lookback_prefix(a.lb, tile, a.epoch, tot_n, tot_e, a.err, pn, pe, bad);
     if (lane == 0) {
       if (!bad && (uint64_t)pn + tot_n > a.list_cap) {
         atomicOr(a.err, kErrTileMap);
@@ -464,6 +480,20 @@ struct PrShared {
   unsigned short map[kTile];
 };
 
+// Optional op hooks, detected at compile time:
+//  list_val(v, e)   the source value belongs to the list entry at address e
+//                   (an array parallel to the compacted list) instead of
+//                   src_val(v);
+//  probe_v(e, val)  the probe also sees the source value.
+template <class T, class = void>
+struct HasListVal : std::false_type {};
+template <class T>
+struct HasListVal<T, std::void_t<decltype(&T::list_val)>> : std::true_type {};
+template <class T, class = void>
+struct HasProbeVal : std::false_type {};
+template <class T>
+struct HasProbeVal<T, std::void_t<decltype(T::kProbeVal)>> : std::true_type {};
+
 // Builds the local-vertex tables of tile k; returns the local count (0 on error).
 // Sh is LbsShared<Val> or PrShared.
 template <bool kNeedVal, class Op, class Sh>
@@ -485,7 +515,8 @@ __device__ __forceinline__ uint32_t lbs_setup(const LbsArgs &a, const Op &op, Sh
     sh.rs[j] = p > pos0 ? (uint32_t)min(p - pos0, (uint64_t)kTile) : 0u;
     const uint64_t src = a.off ? a.off[v] - p : (0ull - a.stage_base);
     sh.cb[j] = src + pos0;
-    if constexpr (kNeedVal) sh.val[j] = op.src_val(v);
+    if constexpr (HasListVal<Op>::value) sh.val[j] = op.list_val(v, a.list + i);
+    else if constexpr (kNeedVal) sh.val[j] = op.src_val(v);
   }
   for (uint32_t x = threadIdx.x; x < kTile; x += kThreads) sh.map[x] = 0;
   __syncthreads();
@@ -558,11 +589,14 @@ __device__ __forceinline__ void lbs_tile(const LbsArgs &a, const Src &src, const
   typename Op::Probe pr[kItems];
 #pragma unroll
   for (int it = 0; it < (int)kItems; it++)
-    if (okmask & (1u << it)) pr[it] = op.probe(ev[it]);
+    if (okmask & (1u << it)) {
+      if constexpr (HasProbeVal<Op>::value) pr[it] = op.probe_v(ev[it], sh.val[lv[it]]);
+      else pr[it] = op.probe(ev[it]);
+    }
 #pragma unroll
   for (int it = 0; it < (int)kItems; it++) {
     if (okmask & (1u << it))
-      op.relax(ev[it], Op::kNeedVal ? sh.val[lv[it]] : typename Op::Val(0),
+      op.relax(ev[it], Op::kNeedVal ? sh.val[lv[it]] : typename Op::Val{},
                pos0 + it * kThreads + threadIdx.x, pr[it]);
   }
 }

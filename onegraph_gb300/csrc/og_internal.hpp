@@ -84,6 +84,12 @@ inline uint32_t bits_for(uint64_t x) {
   return b;
 }
 
+// Slots of one multi-source SSSP row for k sources: 8, 16 or 32 (a divisor
+// of the warp size, so a warp covers whole rows in the reduction kernels).
+inline uint32_t sb_row_slots(uint32_t k) { return k <= 8 ? 8u : (k <= 16 ? 16u : 32u); }
+// Sources per multi-source SSSP pass requested by og_config flags (0: none).
+inline uint32_t sb_sources(uint32_t flags) { return (flags >> 8) & 63u; }
+
 // Per-vertex / fixed device bytes the engine allocates (planner inputs).
 uint64_t engine_vertex_bytes(int kind, uint32_t flags);
 uint64_t engine_fixed_bytes(uint32_t V, uint64_t E, uint32_t flags);
