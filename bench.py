@@ -1,21 +1,26 @@
 #!/usr/bin/env python
-"""Benchmark of the out-of-memory SSSP path on one GB300.
+"""Benchmarks of the GB300 out-of-memory graph engine.
 
-Workload (the reference's out-of-memory configuration): R-MAT scale 27,
-edge factor 16, a,b,c,d = .57/.19/.19/.05, symmetrised, deduplicated, no
-self-loops, seeded vertex permutation (seed 1), uint32 weights uniform in
-[1, 64] (seed 2); device budget 8 GiB, advisek 0.8; SSSP from 32 seeded random
-sources (seed 3) with edges.  The graph is synthetic (no datasets offline).
+Default workload (`serving`, the headline metric "served queries/s + p50/p99
+latency vs plain per-query path"): four resident weighted R-MAT graphs
+(scales 22, 24, 26, 27; edge factor 16, a,b,c,d = .57/.19/.19/.05,
+symmetrised, deduplicated, no self-loops, seeded vertex permutation (seed 1),
+uint32 weights uniform in [1, 64] (seed 2)) under a 24 GiB device budget;
+400 requests with Poisson arrivals at 2000/s (seed 4), 60 % BFS / 30 % SSSP /
+10 % PageRank (5 iterations), graph chosen by Zipf(1.1).  One step = one
+pass of the mix through og_server; `value` = served queries/s with results
+left on the device, `e2e` = the same with every result read into page-locked
+host memory; the plain per-query path and the CPU baseline are in the line.
+The graphs are synthetic (no datasets offline).
 
-One step = one SSSP query (the next source, cycling over the 32) through the
-engine: static prefix relaxed from HBM, the dynamic region gathered from
-page-locked host memory every round.  `value` = queries/s with the result left
-in device memory; `e2e` = queries/s through the C ABI writing the distances
-into a page-locked host buffer (D2H of 4V bytes per query inside the timing).
+--workload sssp-oom: one out-of-memory SSSP query per step on R-MAT 27 with
+an 8 GiB budget, advisek 0.8, 32 seeded sources (seed 3).  Other workloads:
+cc-oom, bfs-batch, bfs-resident, pr-precision (see run_* below).
 
---impl reference times the reference's CPU path on the host cores: the
-reference ships no CPU SSSP, so its stand-in is the oracle's serial Dijkstra
-(one query per host thread, bounded samples, extrapolated per query).
+--impl reference times the reference's CPU path on the host cores (the
+oracle's restatement; the reference's GPU path needs a SYCL compiler this
+image lacks), on graphs the oracle builds on the CPU: the engine is not
+loaded.  The reference ships no CPU SSSP; its stand-in is a serial Dijkstra.
 """
 from __future__ import annotations
 
@@ -52,9 +57,9 @@ def parse_args():
     ap.add_argument("--advisek", type=float, default=0.8)
     ap.add_argument("--sources", type=int, default=32)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
-    ap.add_argument("--workload", default="sssp-oom",
-                    choices=["sssp-oom", "cc-oom", "bfs-batch", "bfs-resident", "pr-precision", "serving"],
-                    help="sssp-oom (default headline), or another measured configuration")
+    ap.add_argument("--workload", default="serving",
+                    choices=["serving", "sssp-oom", "cc-oom", "bfs-batch", "bfs-resident", "pr-precision"],
+                    help="serving (default: the served-queries/s headline), or another measured configuration")
     ap.add_argument("--tune", type=int, default=1, help="bfs-batch: run the autotuner first")
     ap.add_argument("--serving-scales", default="22,24,26,27")
     ap.add_argument("--serving-budget-gib", type=float, default=24.0)
@@ -70,6 +75,8 @@ def parse_args():
     a = ap.parse_args()
     if a.scale is None:
         a.scale = {"pr-precision": 26, "bfs-resident": 20}.get(a.workload, 27)
+    if a.workload == "serving":
+        a.steps = max(1, a.steps)
     if a.budget_gib is None:
         a.budget_gib = 6.0 if a.workload == "pr-precision" else 8.0
     return a
@@ -189,7 +196,7 @@ def cpu_dijkstra_sample(g, srcs, deg, target_s, threads, per_query_edges):
     extrapolated from edges scanned per second to each query's edge count."""
     import oracle
     V = g.V
-    offp, edp = g._off_p, g._edges_p
+    offp, edp = getattr(g, "_off_p", None) or g.off_p, getattr(g, "_edges_p", None) or g.edges_p
 
     def one(i, max_edges):
         s = srcs[i % len(srcs)]
@@ -213,11 +220,24 @@ def cpu_dijkstra_sample(g, srcs, deg, target_s, threads, per_query_edges):
             "rate_edges_per_s_1core": rate}
 
 
+def oracle_graph(scale: int):
+    """The benchmark graph built on the CPU by the oracle (the reference arm
+    must not load the engine); bit-identical to make_graph's."""
+    import oracle
+    t0 = time.time()
+    g = oracle.RmatGraph(scale, 16, seed=1, weight_seed=2, weighted=True)
+    return g, time.time() - t0
+
+
 def run_reference(args, rank, world):
+    """The reference's CPU path on the host cores (the oracle's restatement
+    of it; the reference's GPU path needs a SYCL compiler this image lacks),
+    on this arm's workload and config.  Loads nothing from onegraph_gb300."""
     if rank != 0:
         return
-    import onegraph_gb300 as og  # graph synthesis only; the timed path is the CPU oracle
-    g, gen_s = make_graph(args.scale)
+    if args.workload == "serving":
+        return run_reference_serving(args, world)
+    g, gen_s = oracle_graph(args.scale)
     deg = g.degrees()
     srcs = pick_sources(deg, args.sources)
     threads = os.cpu_count() or 1
@@ -250,13 +270,56 @@ def run_reference(args, rank, world):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_serving(args, world):
+    scales = [int(x) for x in args.serving_scales.split(",")]
+    graphs, gen_s = [], 0.0
+    for sc in scales:
+        g, t = oracle_graph(sc)
+        graphs.append(g)
+        gen_s += t
+    n = args.requests
+    arrivals, gsel, algos, srcs = serving_requests([g.degrees() for g in graphs], n, args.rate)
+    views = [(g.V, g.E, g.off_p, g.edges_p) for g in graphs]
+    threads = os.cpu_count() or 1
+    target = max(1.0, args.cpu_seconds / 6)
+    samples = []
+    for step in range(args.warmup + args.steps):
+        r = cpu_serving_estimate(views, gsel, algos, srcs, target, threads)
+        if step >= args.warmup:
+            samples.append(r)
+    val = statistics.median(s["value"] for s in samples)
+    wall = sum(s["wall_s"] for s in samples)
+    line = {
+        "impl": "reference", "metric": "served queries/s", "value": val, "unit": "queries/s",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": wall / len(samples) * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32/f32", "data": "synthetic",
+        "config": serving_config(args, scales, [(g.V, g.E) for g in graphs], algos),
+        "cpu_baseline": {"value": val, "unit": "queries/s", "cores": threads, "kind": "port",
+                         "sample": "per step, one bounded sample (~%.1f s) of every (graph, algorithm) class of "
+                                   "the %d-request mix, all classes at once on the host threads: runCPUBFS, "
+                                   "serial Dijkstra (no CPU SSSP in the reference), pr_cal pull iterations; "
+                                   "extrapolated to E (BFS, SSSP) or 5E (PR5) edges per request, requests "
+                                   "spread over %d threads" % (target, n, threads)},
+        "e2e": {"value": val, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "setup_s": gen_s,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def packed_bits(V: int, wmin: int = 1, wmax: int = 64) -> int:
+    """Bits of one packed edge record: column bits(V - 1) + weight bits(wmax - wmin)."""
+    return int(V - 1).bit_length() + int(wmax - wmin).bit_length()
+
+
 def config_dict(args, g):
+    delta = args.delta if args.delta is not None else max(1, (1 + 64) // 16)  # the engine's default
     return {"workload": "oom-sssp-rmat%d-%gGiB-%dsrc" % (args.scale, args.budget_gib, args.sources),
             "graph": "R-MAT scale %d ef16 a,b,c=.57,.19,.19 symmetric dedup weights U[1,64]" % args.scale,
             "V": g.V, "E": g.E, "budget_bytes": int(args.budget_gib * GIB), "advisek": args.advisek,
             "sources": args.sources, "seeds": {"graph": 1, "weights": 2, "sources": 3},
-            "l2": "inputs larger than L2 (packed graph %.1f GB)" % (g.E * g.plan(1 << 40)["edge_bits"] / 8e9),
-            "dynamic_mode": "direct" if args.direct else "staged", "sssp_delta": args.delta}
+            "l2": "inputs larger than L2 (packed graph %.1f GB)" % (g.E * packed_bits(g.V) / 8e9),
+            "dynamic_mode": "direct" if args.direct else "staged", "sssp_delta": float(delta)}
 
 
 def run_ours(args, rank, world, local):
@@ -394,8 +457,9 @@ def run_ours(args, rank, world, local):
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32",
         "data": "synthetic", "config": config_dict(args, g),
         "gteps": comp_edges * args.steps * world / t_dev / 1e9,
-        "gteps_traversed": (st_edges + sum(s["edges_dynamic"] for s in stats)) / t_dev / 1e9,
-        "p50_ms": p50, "p99_ms": p99,
+        "gteps_traversed": sum(s["edges_static"] + s["edges_dynamic"] for s in stats) / t_dev / 1e9,
+        "p50_ms": p50, ("p99_ms" if len(lat) >= 100 else "latency_max_ms"): p99,
+        "latency_samples": len(lat),
         "e2e": {"value": args.steps / e2e_s, "unit": "queries/s", "h2d_bytes_per_step":
                 int(4 + e2e_stats["link_bytes"]), "d2h_bytes_per_step": 4 * g.V},
         "roofline": dominant, "roofline_static": roof_static, "roofline_link": roof_link,
@@ -795,129 +859,326 @@ def run_cc_oom(args, rank, world, local):
     eng.close()
 
 
-SERVING_BUDGETS_GIB = {22: 1.5, 24: 3.0, 26: 6.5, 27: 10.0}  # resident graph + first context
+# Serving mix: per graph scale, the device budget (GiB) of its resident state
+# and first query context, and the sources of one multi-source SSSP pass.
+# The four budgets hold 22.5 of the 24 GiB; the rest admits extra contexts.
+SERVING_GRAPHS = {22: (1.0, 16), 24: (3.75, 16), 26: (6.75, 8), 27: (11.0, 4)}
+
+
+def serving_graph(sc: int):
+    """(budget GiB, SSSP sources per pass) of a serving graph; smaller test
+    graphs get 1 GiB and 8 sources."""
+    return SERVING_GRAPHS.get(sc, (1.0, 8))
+# direct mode keeps no staging buffers, so the whole edge share is static
+SERVING_ADVISEK = 1.0
+ALGO_BFS, ALGO_SSSP, ALGO_PR = 0, 1, 3  # og_algo values (the reference arm loads no engine)
+
+
+def serving_requests(degrees, n, rate, seed=4):
+    """The request mix: Poisson arrivals at `rate`/s, graph by Zipf(1.1) with
+    the smallest graph most popular, 60 % BFS / 30 % SSSP / 10 % PageRank
+    (5 iterations), sources uniform over each graph's vertices with edges."""
+    rng = np.random.default_rng(seed)
+    z = np.array([1.0 / (k + 1) ** 1.1 for k in range(len(degrees))])
+    z /= z.sum()
+    arrivals = np.cumsum(rng.exponential(1.0 / rate, n))
+    gsel = rng.choice(len(degrees), n, p=z)
+    u = rng.random(n)
+    algos = np.where(u < 0.6, ALGO_BFS, np.where(u < 0.9, ALGO_SSSP, ALGO_PR))
+    nz = [np.nonzero(d)[0] for d in degrees]
+    srcs = [int(nz[gi][rng.integers(0, nz[gi].size)]) for gi in gsel]
+    return arrivals, gsel, algos, srcs
+
+
+def serving_config(args, scales, VE, gsel_algos):
+    algos = gsel_algos
+    return {"workload": "serving-rmat%s-%gGiB" % ("-".join(map(str, scales)), args.serving_budget_gib),
+            "graphs": {str(sc): {"V": V, "E": E, "budget_bytes": int(serving_graph(sc)[0] * GIB),
+                                 "sssp_sources_per_pass": serving_graph(sc)[1]}
+                       for sc, (V, E) in zip(scales, VE)},
+            "graph": "R-MAT ef16 a,b,c=.57,.19,.19 symmetric dedup weights U[1,64], seeds graph 1 weights 2",
+            "budget_bytes": int(args.serving_budget_gib * GIB), "advisek": SERVING_ADVISEK,
+            "arrivals": "Poisson %g/s, seed 4" % args.rate, "requests_per_pass": args.requests,
+            "mix": {"bfs": int((algos == ALGO_BFS).sum()), "sssp": int((algos == ALGO_SSSP).sum()),
+                    "pr5": int((algos == ALGO_PR).sum())},
+            "zipf": "1.1, smallest graph most popular", "workers": args.workers,
+            "l2": "inputs larger than L2 (R-MAT 26/27 packed records 8.4 / 17.4 GB)"}
+
+
+def cpu_serving_estimate(views, gsel, algos, srcs, target_s, threads):
+    """Served queries/s of the reference's CPU paths on the host cores for the
+    request mix.  views[g] = (V, E, offsets pointer, {dst, w} pairs pointer).
+    Every (graph, algorithm) class of the mix gets one bounded sample of its
+    CPU algorithm, all classes at once on the host threads (so the samples
+    share memory bandwidth as concurrent requests would): runCPUBFS for BFS,
+    serial Dijkstra for SSSP (the reference ships no CPU SSSP), pr_cal pull
+    iterations for PageRank.  Each class's edges/s extrapolate to its
+    per-request edges (E for BFS and SSSP, 5 E for five PageRank iterations);
+    requests are independent, so the mix's CPU time is their sum spread over
+    the threads."""
+    import oracle
+    classes = sorted(set(zip(gsel.tolist(), algos.tolist())))
+    first = {}
+    for i, c in enumerate(zip(gsel.tolist(), algos.tolist())):
+        first.setdefault(c, srcs[i])
+
+    def sample(c, max_edges):
+        gi, a = c
+        V, E, offp, edp = views[gi]
+        t = time.perf_counter()
+        if a == ALGO_BFS:
+            out = np.empty(V, np.uint32)
+            n = oracle.bfs_bounded_raw(V, offp, edp, 2, first[c], max_edges, out)
+        elif a == ALGO_SSSP:
+            out = np.empty(V, np.uint32)
+            n = oracle.sssp_dijkstra_bounded_raw(V, offp, edp, first[c], max_edges, out)
+        else:
+            out = np.empty(V, np.float64)
+            n = oracle.pr_pull_bounded_raw(V, offp, edp, 2, max_edges, out)
+        return max(n, 1), time.perf_counter() - t
+
+    # calibration: a short sample of each class on its own
+    rate0 = {c: (lambda r: r[0] / max(r[1], 1e-6))(sample(c, 2_000_000)) for c in classes}
+    with cf.ThreadPoolExecutor(max_workers=threads) as ex:
+        t0 = time.perf_counter()
+        res = dict(zip(classes, ex.map(lambda c: sample(c, max(int(rate0[c] * target_s), 1)), classes)))
+        wall = time.perf_counter() - t0
+    rate = {c: res[c][0] / res[c][1] for c in classes}
+    total_s = 0.0
+    for c in zip(gsel.tolist(), algos.tolist()):
+        work = views[c[0]][1] * (5 if c[1] == ALGO_PR else 1)
+        total_s += work / rate[c]
+    n = len(gsel)
+    return {"value": n / (total_s / threads), "cores": threads, "wall_s": wall,
+            "rates_edges_per_s": {"g%d/a%d" % c: r for c, r in rate.items()}}
+
+
+def serve_pass(srv, arrivals, gsel, algos, srcs, outs=None):
+    """Submits the mix at its arrival times (client thread) and collects every
+    response; returns (responses by request, span in ms from the first
+    submission to the last response, server clock)."""
+    import threading
+    n = len(gsel)
+    t0 = time.perf_counter()
+    err = []
+
+    def client():
+        try:
+            for i in range(n):
+                dt = arrivals[i] - (time.perf_counter() - t0)
+                if dt > 0:
+                    time.sleep(dt)
+                srv.submit(int(gsel[i]), int(algos[i]), srcs[i], iterations=5,
+                           out=None if outs is None else outs[i], user=i)
+        except Exception as ex:  # reported below
+            err.append(ex)
+    th = threading.Thread(target=client)
+    th.start()
+    resp = {}
+    while len(resp) < n and (th.is_alive() or len(resp) < srv.stats()["submitted"]):
+        for r in srv.poll(1024, wait_ms=200):
+            resp[r["user"]] = r
+    th.join()
+    if err:
+        raise err[0]
+    span = max(r["t_done_ms"] for r in resp.values()) - min(r["t_submit_ms"] for r in resp.values())
+    return resp, span
 
 
 def run_serving(args, rank, world, local):
     """Serving mix: four resident weighted R-MAT graphs (scales 22/24/26/27)
     under a 24 GiB budget, Poisson arrivals at 2000 requests/s (seed 4),
     60 % BFS / 30 % SSSP / 10 % PageRank (5 iterations), graph by Zipf(1.1)
-    with the smallest graph most popular; the same requests are then run one
-    at a time through the plain per-query path."""
-    import threading
+    with the smallest graph most popular.  A step is one pass of the 400
+    requests through og_server (continuous batching: multi-source SSSP passes
+    that requests join in flight, fused BFS passes, shared PageRank).  Then
+    the same requests end to end (every result into page-locked host memory),
+    and one at a time through the plain per-query path (og_bfs / og_sssp /
+    og_pr_l1 on an engine per graph with the same budget and no batch state)."""
     import torch
     import onegraph_gb300 as og
     torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
     scales = [int(x) for x in args.serving_scales.split(",")]
     graphs, gen_s = [], 0.0
     for sc in scales:
         g, t = make_graph(sc)
         graphs.append(g)
         gen_s += t
-    rng = np.random.default_rng(4)
-    z = np.array([1.0 / (k + 1) ** 1.1 for k in range(len(graphs))])
-    z /= z.sum()
     n = args.requests
-    arrivals = np.cumsum(rng.exponential(1.0 / args.rate, n))
-    gsel = rng.choice(len(graphs), n, p=z)
-    u = rng.random(n)
-    algos = np.where(u < 0.6, og.ALGO_BFS, np.where(u < 0.9, og.ALGO_SSSP, og.ALGO_PR))
-    nz = [np.nonzero(g.degrees())[0] for g in graphs]
-    srcs = [int(nz[gi][rng.integers(0, nz[gi].size)]) for gi in gsel]
-    budgets = [int(SERVING_BUDGETS_GIB.get(sc, 2.0) * GIB) for sc in scales]
+    arrivals, gsel, algos, srcs = serving_requests([g.degrees() for g in graphs], n, args.rate)
+    budgets = [int(serving_graph(sc)[0] * GIB) for sc in scales]
+    slots = [serving_graph(sc)[1] for sc in scales]
+    # page-locked result buffers of the end-to-end passes (one per request),
+    # allocated before any query: large page-locked allocations made between
+    # queries have slowed the queries after them
+    words = [graphs[gi].V for gi in gsel]
+    pool = torch.empty(int(sum(words)), dtype=torch.int32, pin_memory=True).numpy()
+    outs, o = [], 0
+    for i, w in enumerate(words):
+        v = pool[o:o + w]
+        outs.append(v.view(np.float32) if algos[i] == ALGO_PR else v.view(np.uint32))
+        o += w
+    h2d = h2d_peak_gbs()
     srv = og.Server(budget=int(args.serving_budget_gib * GIB), workers=args.workers, max_batch=64,
                     device=local)
-    for g, b in zip(graphs, budgets):
-        srv.add_graph(g, budget=b, advisek=args.advisek, direct=True, pagerank=True)
+    for g, b, k in zip(graphs, budgets, slots):
+        srv.add_graph(g, budget=b, advisek=SERVING_ADVISEK, direct=True, pagerank=True, sssp_batch=k)
+    # warm-up: every (graph, algorithm) once per warm-up step
+    for w in range(args.warmup):
+        for gi, g in enumerate(graphs):
+            for a in (ALGO_BFS, ALGO_SSSP, ALGO_PR):
+                srv.submit(gi, a, srcs[int(np.nonzero(gsel == gi)[0][0])], iterations=5, user=1 << 40)
+        srv.drain()
+        srv.poll(1 << 16, wait_ms=0)
+    st0 = srv.stats()
     sampler = ClockSampler(local)
     sampler.start()
-    t0 = time.perf_counter()
-
-    def client():
-        for i in range(n):
-            dt = arrivals[i] - (time.perf_counter() - t0)
-            if dt > 0:
-                time.sleep(dt)
-            srv.submit(int(gsel[i]), int(algos[i]), srcs[i], iterations=5, user=i)
-    th = threading.Thread(target=client)
-    th.start()
-    resp = {}
-    while len(resp) < n:
-        for r in srv.poll(1024, wait_ms=200):
-            resp[r["user"]] = r
-    th.join()
-    wall = time.perf_counter() - t0
+    lat, spans, ref_resp = [], [], None
+    replicas.barrier(world)
+    for k in range(args.steps):
+        resp, span = serve_pass(srv, arrivals, gsel, algos, srcs)
+        spans.append(span)
+        lat.extend(resp[i]["t_done_ms"] - resp[i]["t_submit_ms"] for i in range(n))
+        if ref_resp is None:
+            ref_resp = resp
+        elif any(resp[i]["checksum"] != ref_resp[i]["checksum"] for i in range(n)):
+            raise RuntimeError("a served result changed between passes")
+    replicas.barrier(world)
     clocks = sampler.stop()
-    st = srv.stats()
+    st1 = srv.stats()
+    t_srv = replicas.max_over_ranks(sum(spans) / 1e3, world)
+    value = replicas.whole_job_rate(args.steps * n, world, t_srv)
+    # end to end: the same passes with every result in page-locked host memory
+    e2e_passes = max(1, min(args.steps, 3))
+    e2e_spans = []
+    for k in range(e2e_passes):
+        resp, span = serve_pass(srv, arrivals, gsel, algos, srcs, outs=outs)
+        e2e_spans.append(span)
+        bad = [i for i in range(n) if resp[i]["checksum"] != ref_resp[i]["checksum"] or resp[i]["status"]]
+        if bad:
+            raise RuntimeError("end-to-end results differ from the device-resident pass: %s" % bad[:5])
+    e2e_qps = replicas.whole_job_rate(e2e_passes * n, world, replicas.max_over_ranks(sum(e2e_spans) / 1e3, world))
     srv.close()
-    lat = np.array([resp[i]["t_done_ms"] - resp[i]["t_submit_ms"] for i in range(n)])
-    span_ms = max(r["t_done_ms"] for r in resp.values()) - min(r["t_submit_ms"] for r in resp.values())
-    served_qps = n / (span_ms / 1e3)
-    bad = [r for r in resp.values() if r["status"] != 0]
-    # plain per-query path: one engine per graph, requests one after another
-    engines = [og.Engine(g, budget=b, advisek=args.advisek, direct=True, pagerank=True, batch=True)
+    batch_of = {i: ref_resp[i]["batch"] for i in range(n)}
+    run_ms = {i: ref_resp[i]["t_done_ms"] - ref_resp[i]["t_start_ms"] for i in range(n)}
+    # plain per-query path: an engine per graph with the same budget and no
+    # batch state, requests one after another in arrival order
+    engines = [og.Engine(g, budget=b, advisek=SERVING_ADVISEK, direct=True, pagerank=True, device=local)
                for g, b in zip(graphs, budgets)]
+    for gi, e in enumerate(engines):  # warm-up
+        s0 = srcs[int(np.nonzero(gsel == gi)[0][0])]
+        e.bfs(s0, out=False)
+        e.sssp(s0, out=False)
+        e.pr_l1(0.85, 0.0, 5, out=False)
     mism = 0
+    plain_lat, plain_svc = [], []
     p0 = time.perf_counter()
-    plain_lat = []
-    plain_svc = []
     for i in range(n):
-        e = engines[gsel[i]]
-        a = int(algos[i])
+        e, a = engines[gsel[i]], int(algos[i])
         q0 = time.perf_counter()
-        if a == og.ALGO_BFS:
+        if a == ALGO_BFS:
             e.bfs(srcs[i], out=False)
-        elif a == og.ALGO_SSSP:
+        elif a == ALGO_SSSP:
             e.sssp(srcs[i], out=False)
         else:
             e.pr_l1(0.85, 0.0, 5, out=False)
-        done = time.perf_counter() - p0
-        plain_svc.append((time.perf_counter() - q0) * 1e3)
-        plain_lat.append(max(0.0, done - arrivals[i]) * 1e3)
-        mism += e.checksum(a) != resp[i]["checksum"]
+        now = time.perf_counter()
+        plain_svc.append((now - q0) * 1e3)
+        plain_lat.append(max(0.0, (now - p0) - arrivals[i]) * 1e3)
+        mism += e.checksum(a) != ref_resp[i]["checksum"]
     plain_wall = time.perf_counter() - p0
     for e in engines:
         e.close()
-    plain_lat = np.array(plain_lat)
+    plain_qps = n / plain_wall
     plain_svc = np.array(plain_svc)
-    # per (graph, algorithm): request count, plain service time, served latency
-    # and the mean fused batch the server ran the request in
-    names = {og.ALGO_BFS: "bfs", og.ALGO_SSSP: "sssp", og.ALGO_PR: "pr5"}
+    lat = np.array(lat)
+    names = {ALGO_BFS: "bfs", ALGO_SSSP: "sssp", ALGO_PR: "pr5"}
     breakdown = {}
     for gi, sc in enumerate(scales):
         for a, nm in names.items():
             idx = [i for i in range(n) if gsel[i] == gi and algos[i] == a]
-            if not idx:
-                continue
-            breakdown["rmat%d/%s" % (sc, nm)] = {
-                "requests": len(idx),
-                "plain_service_ms_mean": float(plain_svc[idx].mean()),
-                "plain_service_ms_total": float(plain_svc[idx].sum()),
-                "served_p50_ms": float(np.percentile(lat[idx], 50)),
-                "served_batch_mean": float(np.mean([resp[i]["batch"] for i in idx])),
-                "served_run_ms_mean": float(np.mean([resp[i]["t_done_ms"] - resp[i]["t_start_ms"]
-                                                     for i in idx])),
-            }
+            if idx:
+                breakdown["rmat%d/%s" % (sc, nm)] = {
+                    "requests": len(idx), "plain_service_ms_mean": float(plain_svc[idx].mean()),
+                    "plain_service_ms_total": float(plain_svc[idx].sum()),
+                    "served_batch_mean": float(np.mean([batch_of[i] for i in idx])),
+                    "served_run_ms_mean": float(np.mean([run_ms[i] for i in idx]))}
+    # the dominant kernels measured alone on the R-MAT 27 graph's configuration
+    roof = serving_rooflines(og, graphs[-1], budgets[-1], slots[-1], srcs, gsel, algos, len(graphs) - 1, h2d,
+                             local)
+    cpu = None
+    if rank == 0 and world == 1:
+        try:
+            views = [(g.V, g.E, g._off_p, g._edges_p) for g in graphs]
+            threads = os.cpu_count() or 1
+            c = cpu_serving_estimate(views, gsel, algos, srcs, max(2.0, args.cpu_seconds / 3), threads)
+            cpu = {"value": c["value"], "unit": "queries/s", "cores": threads, "kind": "port",
+                   "sample": "one bounded sample (~%.0f s) per (graph, algorithm) class of the mix, all classes "
+                             "at once: runCPUBFS, serial Dijkstra (no CPU SSSP in the reference), pr_cal pull "
+                             "iterations; extrapolated to E (BFS, SSSP) or 5E (PR5) edges per request"
+                             % max(2.0, args.cpu_seconds / 3), "rates_edges_per_s": c["rates_edges_per_s"]}
+        except Exception as ex:
+            cpu = {"value": None, "unit": "queries/s", "cores": 0, "kind": "port", "sample": "failed: %s" % ex}
+    d2h = float(np.mean([4 * graphs[gi].V for gi in gsel]))
     line = {
-        "metric": "served queries/s", "value": served_qps, "unit": "queries/s", "n_gpus": world,
-        "steps": n, "warmup": 0, "ms_per_step": span_ms / n, "higher_is_better": True,
-        "scaling": "weak", "vs_baseline": None, "dtype": "u32/f32", "data": "synthetic",
-        "config": {"workload": "serving-rmat%s-%gGiB" % ("-".join(map(str, scales)), args.serving_budget_gib),
-                   "graphs": {str(sc): {"V": g.V, "E": g.E, "budget_bytes": b}
-                              for sc, g, b in zip(scales, graphs, budgets)},
-                   "arrivals": "Poisson %g/s, seed 4" % args.rate, "requests": n,
-                   "mix": {"bfs": int((algos == og.ALGO_BFS).sum()), "sssp": int((algos == og.ALGO_SSSP).sum()),
-                           "pr5": int((algos == og.ALGO_PR).sum())},
-                   "zipf": "1.1, smallest graph most popular", "workers": args.workers},
+        "metric": "served queries/s", "value": value, "unit": "queries/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": sum(spans) / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32/f32",
+        "data": "synthetic", "config": serving_config(args, scales, [(g.V, g.E) for g in graphs], algos),
+        "step": "one pass of the %d-request mix through og_server" % n,
         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-        "plain_queries_per_s": n / plain_wall,
-        "plain_p50_ms": float(np.percentile(plain_lat, 50)), "plain_p99_ms": float(np.percentile(plain_lat, 99)),
-        "speedup_vs_plain": served_qps / (n / plain_wall),
-        "results_identical_to_plain": mism == 0, "failed_requests": len(bad),
-        "breakdown": breakdown, "server": st, "clocks": clocks, "setup_s": {"generate": gen_s}, "wall_s": wall,
+        "latency_samples": int(lat.size),
+        "plain_queries_per_s": plain_qps, "plain_p50_ms": float(np.percentile(plain_lat, 50)),
+        "plain_p99_ms": float(np.percentile(plain_lat, 99)),
+        "speedup_vs_plain": value / plain_qps, "results_identical_to_plain": mism == 0,
+        "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step":
+                int(d2h * n), "passes": e2e_passes,
+                "note": "a step is one pass of the mix; every request's V results read into page-locked host "
+                        "memory, the request (graph, algorithm, source) sent from the host"},
+        "roofline": roof["dominant"], "rooflines": roof["all"],
+        "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": st1["launches"] - st0["launches"],
+        "server": {k: st1[k] - st0.get(k, 0) if k != "used_bytes" else st1[k] for k in st1},
+        "breakdown": breakdown, "setup_s": {"generate": gen_s},
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+def serving_rooflines(og, g, budget, slots, srcs, gsel, algos, gi, h2d, local):
+    """Link-side rooflines of the serving mix's dominant kernels on the
+    largest graph, in the server's engine configuration: the multi-source
+    SSSP relax (k_sb_relax_pair) over one pass of `slots` sources, and the
+    PageRank pull (k_pr_pull_pair) over five iterations.  Achieved = packed
+    records read over the host link (og_stats.link_bytes) / the kernels'
+    CUDA-event time on the engine's stream (og_stats.ms_dynamic); peak = the
+    pinned host-to-device copy measured in this run."""
+    e = og.Engine(g, budget=budget, advisek=SERVING_ADVISEK, direct=True, pagerank=True, batch=True,
+                  sssp_batch=slots, device=local)
+    idx = [i for i in range(len(gsel)) if gsel[i] == gi and algos[i] == ALGO_SSSP][:slots]
+    ss = [srcs[i] for i in idx] or [srcs[0]]
+    e.sssp_batch(ss, out=False)  # untimed first pass
+    e.sssp_batch(ss, out=False)
+    sb = dict(e.stats)
+    e.pr_l1(0.85, 0.0, 5, out=False)
+    e.pr_l1(0.85, 0.0, 5, out=False)
+    pr = dict(e.stats)
+    e.close()
+
+    def roof(kernel, st, unit_note):
+        ach = st["link_bytes"] / (st["ms_dynamic"] / 1e3) / 1e9 if st["ms_dynamic"] else 0.0
+        return {"bound": "host-link", "kernel": kernel, "achieved": ach, "peak": h2d, "unit": "GB/s",
+                "frac": ach / h2d if h2d else None, "traffic": None,
+                "peak_source": "measured pinned H2D copy in this run", "bytes_per_launch_note": unit_note,
+                "link_gb": st["link_bytes"] / 1e9, "kernel_ms": st["ms_dynamic"]}
+    a = roof("k_sb_relax_pair<SrcP<true>,SrcP<true>,%d> (multi-source SSSP relax, R-MAT %d pass of %d sources)"
+             % (4 if slots <= 4 else 8, 27, len(ss)), sb, "packed 33-bit records of the dynamic region")
+    b = roof("k_pr_pull_pair<SrcP<false>,SrcP<false>> (PageRank pull, R-MAT 27, 5 iterations)", pr,
+             "packed records of the dynamic region per iteration")
+    dom = a if sb["ms_dynamic"] >= pr["ms_dynamic"] else b
+    return {"dominant": dom, "all": [a, b]}
 
 
 def main():

@@ -213,10 +213,11 @@ typedef struct og_config {
                                  with OG_CFG_DIRECT|OG_CFG_NO_PIN the unified-
                                  memory scheme (BFS/usm_BFS/main.cpp:120-222) */
 /* Also hold the state of og_sssp_batch for up to k sources per pass
- * (1 <= k <= 32): a row of 8, 16 or 32 u32 distances per vertex (k rounded
- * up), a pending-source mask per vertex and a near-source mask per list
- * entry, 4 B x row + 8 B per vertex, sharing one allocation with the
- * OG_CFG_BATCH masks.  Weighted graphs only. */
+ * (1 <= k <= 32): a row of 4, 8, 16 or 32 u32 distances per vertex (k
+ * rounded up), a pending-source mask per vertex and a near-source mask per
+ * list entry, 4 B x row + 8 B per vertex, sharing one allocation with the
+ * OG_CFG_BATCH masks (24 B per vertex: k <= 4 adds nothing to them).
+ * Weighted graphs only. */
 #define OG_CFG_SSSP_BATCH(k) ((uint32_t)(k) << 8)
 #define OG_CFG_PR 4u      /* also hold PageRank state for a PLAIN/WEIGHTED
                              graph, read as symmetric (in-edges = out-edges,
@@ -484,11 +485,15 @@ int og_k_compact_noalloc(const uint32_t *bits, uint32_t v_begin, uint32_t v_end,
 /* A request loop over several resident graphs (no reference counterpart).
  * Requests are queued as they arrive and admitted by worker threads when a
  * query context of their graph is free or a new one fits budget_bytes; the
- * work of concurrent requests overlaps on the GPU.  BFS requests for the same
- * graph that queue up while others run are fused into one og_bfs_batch pass
- * (up to max_batch), and queued PageRank requests for the same graph and
- * iteration count share one computation.  Results are identical to running
- * each request alone. */
+ * work of concurrent requests overlaps on the GPU.  On a graph added with
+ * OG_CFG_SSSP_BATCH(k), k > 1, SSSP requests run in multi-source passes
+ * (og_sssp_batch_*) of up to min(k, max_batch) sources: requests that arrive
+ * while a pass runs join its free slots between rounds, and each is answered
+ * as soon as its own distances are final.  BFS requests for the same graph
+ * that queue up while others run are fused into one og_bfs_batch pass (up to
+ * max_batch), and queued PageRank requests for the same graph and iteration
+ * count share one computation.  Results are identical to running each
+ * request alone. */
 typedef struct og_server og_server;
 
 typedef struct og_server_config {
@@ -517,7 +522,9 @@ typedef struct og_response {
   int32_t graph;
   int32_t algo;
   uint32_t source;
-  uint32_t batch;     /* requests served by the same GPU pass              */
+  uint32_t batch;     /* requests served by the same GPU pass (a
+                         multi-source SSSP pass: those it had answered when
+                         this one finished, this one included)            */
   uint32_t reserved;
   double t_submit_ms; /* server clock (ms since og_server_create)          */
   double t_start_ms;
@@ -529,6 +536,7 @@ typedef struct og_response {
 typedef struct og_server_stats {
   uint64_t submitted, completed, gpu_passes, batched_requests;
   uint64_t contexts_created, used_bytes;
+  uint64_t launches;  /* kernels the server's passes launched */
 } og_server_stats;
 
 int og_server_create(const og_server_config *cfg, og_server **out);

@@ -125,7 +125,7 @@ class Response(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [("submitted", C.c_uint64), ("completed", C.c_uint64), ("gpu_passes", C.c_uint64),
                 ("batched_requests", C.c_uint64), ("contexts_created", C.c_uint64),
-                ("used_bytes", C.c_uint64)]
+                ("used_bytes", C.c_uint64), ("launches", C.c_uint64)]
 
 
 _lib = None
@@ -591,8 +591,11 @@ class Server:
         self._bufs: dict[int, np.ndarray] = {}
 
     def add_graph(self, graph: Graph, budget: int = 0, advisek: float = 0.0, direct: bool = True,
-                  pagerank: bool = False) -> int:
-        cfg = Config(budget, advisek, (CFG_DIRECT if direct else 0) | (CFG_PR if pagerank else 0), 0)
+                  pagerank: bool = False, sssp_batch: int = 0) -> int:
+        """sssp_batch = k > 1 serves the graph's SSSP requests in multi-source
+        passes of up to k sources that requests join and leave while they run."""
+        cfg = Config(budget, advisek, (CFG_DIRECT if direct else 0) | (CFG_PR if pagerank else 0) |
+                     CFG_SSSP_BATCH(sssp_batch), 0)
         gid = C.c_int()
         _check(lib().og_server_add_graph(self._h, graph._h, C.byref(cfg), C.byref(gid)),
                "og_server_add_graph")

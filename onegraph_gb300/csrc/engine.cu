@@ -1597,7 +1597,8 @@ int sb_round(og_engine *e, og_stats &st, Timing &tm, uint32_t *pending, bool *do
     const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
     if (grid) {
       using S = decltype(src);
-      if (e->sb_ks == 8) k_sb_relax<S, 8><<<grid, kThreads, 0, ls>>>(a, src, op);
+      if (e->sb_ks == 4) k_sb_relax<S, 4><<<grid, kThreads, 0, ls>>>(a, src, op);
+      else if (e->sb_ks == 8) k_sb_relax<S, 8><<<grid, kThreads, 0, ls>>>(a, src, op);
       else if (e->sb_ks == 16) k_sb_relax<S, 16><<<grid, kThreads, 0, ls>>>(a, src, op);
       else k_sb_relax<S, 32><<<grid, kThreads, 0, ls>>>(a, src, op);
       e->launches++;
@@ -1611,7 +1612,8 @@ int sb_round(og_engine *e, og_stats &st, Timing &tm, uint32_t *pending, bool *do
     using S0 = decltype(s0);
     using S1 = decltype(s1);
     const unsigned grid = (unsigned)(n0 + n1);
-    if (e->sb_ks == 8) k_sb_relax_pair<S0, S1, 8><<<grid, kThreads, 0, ps>>>(a0, s0, a1, s1, op, n0, n0 + n1);
+    if (e->sb_ks == 4) k_sb_relax_pair<S0, S1, 4><<<grid, kThreads, 0, ps>>>(a0, s0, a1, s1, op, n0, n0 + n1);
+    else if (e->sb_ks == 8) k_sb_relax_pair<S0, S1, 8><<<grid, kThreads, 0, ps>>>(a0, s0, a1, s1, op, n0, n0 + n1);
     else if (e->sb_ks == 16) k_sb_relax_pair<S0, S1, 16><<<grid, kThreads, 0, ps>>>(a0, s0, a1, s1, op, n0, n0 + n1);
     else k_sb_relax_pair<S0, S1, 32><<<grid, kThreads, 0, ps>>>(a0, s0, a1, s1, op, n0, n0 + n1);
     e->launches++;

@@ -84,9 +84,11 @@ inline uint32_t bits_for(uint64_t x) {
   return b;
 }
 
-// Slots of one multi-source SSSP row for k sources: 8, 16 or 32 (a divisor
-// of the warp size, so a warp covers whole rows in the reduction kernels).
-inline uint32_t sb_row_slots(uint32_t k) { return k <= 8 ? 8u : (k <= 16 ? 16u : 32u); }
+// Slots of one multi-source SSSP row for k sources: 4, 8, 16 or 32 (a
+// divisor of the warp size, so a warp covers whole rows in the reduction
+// kernels).  4 slots (16 B) plus the two masks take the 24 B per vertex of the
+// batched BFS masks, so such an engine needs no more memory for both.
+inline uint32_t sb_row_slots(uint32_t k) { return k <= 4 ? 4u : (k <= 8 ? 8u : (k <= 16 ? 16u : 32u)); }
 // Sources per multi-source SSSP pass requested by og_config flags (0: none).
 inline uint32_t sb_sources(uint32_t flags) { return (flags >> 8) & 63u; }
 

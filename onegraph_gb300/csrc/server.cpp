@@ -6,10 +6,18 @@
 // context of the request's graph is free or a new one fits the server's
 // device-memory budget, run them (each context has its own streams, so the
 // work of different requests overlaps on the GPU), and post responses.
-// Continuous batching: when a worker admits a BFS request it also takes the
-// BFS requests for the same graph that queued up meanwhile (up to max_batch)
-// and serves them in one og_bfs_batch pass; queued PageRank requests for the
-// same graph share one computation.  Built on the public C ABI only.
+// Continuous batching:
+//  * SSSP requests of a graph run as one multi-source pass
+//    (og_sssp_batch_begin / _join / _step): the worker that admits one takes
+//    the queued SSSP requests of that graph into free slots, and between
+//    rounds it takes the requests that arrived meanwhile; a request is
+//    answered as soon as its slot has no pending work, and its slot is then
+//    free for the next one.  So requests join and leave a pass in flight.
+//  * when a worker admits a BFS request it also takes the BFS requests for
+//    the same graph that queued up meanwhile (up to max_batch) and serves
+//    them in one og_bfs_batch pass;
+//  * queued PageRank requests for the same graph share one computation.
+// Built on the public C ABI (and the flag helpers of og_internal.hpp).
 // No reference counterpart: the reference runs one query per process run.
 #include <algorithm>
 #include <chrono>
@@ -39,6 +47,7 @@ struct GraphSlot {
   std::vector<og_engine *> idle;     // contexts ready for a request
   std::vector<og_engine *> clones;   // every clone created (destroyed with the server)
   bool batch = false, pagerank = false;
+  uint32_t sssp_slots = 0;  // sources per multi-source SSSP pass (0: one at a time)
 };
 
 double now_ms(std::chrono::steady_clock::time_point t0) {
@@ -72,7 +81,22 @@ struct Job {
   std::vector<Pending> reqs;
   og_engine *ctx = nullptr;
   int graph = -1;
+  bool sssp_pass = false;  // a multi-source SSSP pass that admits requests while it runs
 };
+
+// Moves up to `room` queued SSSP requests of graph g (FIFO) into out.
+// Called with the lock held.
+void take_sssp(og_server *s, int g, size_t room, std::vector<Pending> &out) {
+  for (auto jt = s->queue.begin(); jt != s->queue.end() && room > 0;) {
+    if (jt->r.graph == g && jt->r.algo == OG_ALGO_SSSP) {
+      out.push_back(*jt);
+      jt = s->queue.erase(jt);
+      room--;
+    } else {
+      ++jt;
+    }
+  }
+}
 
 // Takes the first admissible request (FIFO with skipping) and, for BFS, the
 // queued BFS requests of the same graph.  Called with the lock held.
@@ -96,6 +120,13 @@ bool pick(og_server *s, Job &job) {
     if (!ctx) continue;
     job.ctx = ctx;
     job.graph = it->r.graph;
+    if (it->r.algo == OG_ALGO_SSSP && gs.sssp_slots > 1 && s->cfg.max_batch > 1) {
+      job.sssp_pass = true;
+      job.reqs.push_back(*it);
+      s->queue.erase(it);
+      take_sssp(s, job.graph, std::min<size_t>(gs.sssp_slots, s->cfg.max_batch) - 1, job.reqs);
+      return true;
+    }
     job.reqs.push_back(*it);
     const bool bfs_batch = it->r.algo == OG_ALGO_BFS && gs.batch && s->cfg.max_batch > 1 && !it->r.out;
     // PageRank does not depend on a source: queued PR requests for the same
@@ -120,27 +151,138 @@ bool pick(og_server *s, Job &job) {
   return false;
 }
 
-void run_job(og_server *s, Job &job, std::vector<og_response> &out) {
+og_response make_response(const Pending &p, int status, const uint64_t *ck, uint32_t batch, double t_start) {
+  og_response r;
+  memset(&r, 0, sizeof r);
+  r.ticket = p.ticket;
+  r.user = p.r.user;
+  r.status = status;
+  r.graph = p.r.graph;
+  r.algo = p.r.algo;
+  r.source = p.r.source;
+  r.batch = batch;
+  r.t_submit_ms = p.t_submit;
+  r.t_start_ms = t_start;
+  if (ck) {
+    r.checksum[0] = ck[0];
+    r.checksum[1] = ck[1];
+  }
+  return r;
+}
+
+void count_launches(og_server *s, const og_stats &st) {
+  std::lock_guard<std::mutex> lk(s->m);
+  s->st.launches += st.launches;
+}
+
+// Posts finished responses (stamps their completion time).
+void post(og_server *s, std::vector<og_response> &rs) {
+  if (rs.empty()) return;
+  const double t_done = now_ms(s->t0);
+  std::lock_guard<std::mutex> lk(s->m);
+  for (auto &r : rs) {
+    r.t_done_ms = t_done;
+    s->done.push_back(r);
+  }
+  s->in_flight -= rs.size();
+  s->st.completed += rs.size();
+  s->cv_done.notify_all();
+  rs.clear();
+}
+
+// A multi-source SSSP pass on job.ctx: the admitted requests take slots,
+// every round frees the slots whose sources are final (their requests are
+// answered at once) and fills free slots with SSSP requests of the same graph
+// that queued up meanwhile.  Ends when no slot is in use and none is waiting.
+void run_sssp_pass(og_server *s, Job &job) {
+  og_engine *e = job.ctx;
+  const uint32_t k = std::min<uint32_t>(s->graphs[job.graph].sssp_slots, (uint32_t)s->cfg.max_batch);
+  struct Slot {
+    bool used = false;
+    Pending p;
+    double t_start = 0;
+  };
+  std::vector<Slot> slot(k);
+  std::vector<og_response> out;
+  uint32_t served = 0;
+  auto fail_all = [&](int rc) {
+    for (auto &sl : slot)
+      if (sl.used) {
+        out.push_back(make_response(sl.p, rc, nullptr, served, sl.t_start));
+        sl.used = false;
+      }
+    post(s, out);
+  };
+  auto join = [&](std::vector<Pending> &reqs) -> int {
+    std::vector<uint32_t> srcs, ids;
+    const double t = now_ms(s->t0);
+    size_t q = 0;
+    for (uint32_t i = 0; i < k && q < reqs.size(); i++)
+      if (!slot[i].used) {
+        slot[i].used = true;
+        slot[i].p = reqs[q++];
+        slot[i].t_start = t;
+        srcs.push_back(slot[i].p.r.source);
+        ids.push_back(i);
+      }
+    reqs.clear();
+    return og_sssp_batch_join(e, srcs.data(), ids.data(), (int)srcs.size());
+  };
+  int rc = og_sssp_batch_begin(e);
+  if (rc == OG_OK) rc = join(job.reqs);
+  if (rc != OG_OK) return fail_all(rc);
+  for (;;) {
+    uint32_t pending = 0;
+    int done = 0;
+    og_stats st;
+    rc = og_sssp_batch_step(e, &pending, &done, &st);
+    if (rc != OG_OK) return fail_all(rc);
+    count_launches(s, st);
+    uint32_t fin = 0, used = 0;
+    for (uint32_t i = 0; i < k; i++)
+      if (slot[i].used) {
+        used++;
+        if (!((pending >> i) & 1u)) fin |= 1u << i;
+      }
+    if (fin) {
+      uint64_t ck[64];
+      rc = og_sssp_batch_checks(e, fin, ck);
+      for (uint32_t i = 0; i < k; i++) {
+        if (!((fin >> i) & 1u)) continue;
+        int rq = rc;
+        if (rq == OG_OK && slot[i].p.r.out) rq = og_sssp_batch_fetch(e, i, (uint32_t *)slot[i].p.r.out);
+        served++;
+        out.push_back(make_response(slot[i].p, rq, rq == OG_OK ? &ck[2 * i] : nullptr, served, slot[i].t_start));
+        slot[i].used = false;
+        used--;
+      }
+      post(s, out);
+    }
+    // admit the SSSP requests of this graph that arrived meanwhile
+    std::vector<Pending> more;
+    if (used < k) {
+      std::lock_guard<std::mutex> lk(s->m);
+      take_sssp(s, job.graph, k - used, more);
+      if (!more.empty()) s->st.batched_requests += more.size();
+    }
+    if (!more.empty()) {
+      used += (uint32_t)more.size();
+      rc = join(more);
+      if (rc != OG_OK) return fail_all(rc);
+    }
+    if (used == 0) break;
+  }
+}
+
+void run_job(og_server *s, Job &job) {
+  if (job.sssp_pass) return run_sssp_pass(s, job);
   const double t_start = now_ms(s->t0);
   og_engine *e = job.ctx;
   og_stats st;
+  memset(&st, 0, sizeof st);
+  std::vector<og_response> out;
   auto respond = [&](const Pending &p, int status, const uint64_t *ck) {
-    og_response r;
-    memset(&r, 0, sizeof r);
-    r.ticket = p.ticket;
-    r.user = p.r.user;
-    r.status = status;
-    r.graph = p.r.graph;
-    r.algo = p.r.algo;
-    r.source = p.r.source;
-    r.batch = (uint32_t)job.reqs.size();
-    r.t_submit_ms = p.t_submit;
-    r.t_start_ms = t_start;
-    if (ck) {
-      r.checksum[0] = ck[0];
-      r.checksum[1] = ck[1];
-    }
-    out.push_back(r);
+    out.push_back(make_response(p, status, ck, (uint32_t)job.reqs.size(), t_start));
   };
   if (job.reqs.size() > 1 && job.reqs[0].r.algo == OG_ALGO_PR) {
     const Pending &p = job.reqs[0];
@@ -174,8 +316,8 @@ void run_job(og_server *s, Job &job, std::vector<og_response> &out) {
     if (rc == OG_OK) rc = og_result_checksum(e, p.r.algo, ck);
     respond(p, rc, rc == OG_OK ? ck : nullptr);
   }
-  const double t_done = now_ms(s->t0);
-  for (auto &r : out) r.t_done_ms = t_done;
+  count_launches(s, st);
+  post(s, out);
 }
 
 void worker_loop(og_server *s) {
@@ -188,14 +330,9 @@ void worker_loop(og_server *s) {
     s->st.gpu_passes++;
     if (job.reqs.size() > 1) s->st.batched_requests += job.reqs.size();
     lk.unlock();
-    std::vector<og_response> out;
-    run_job(s, job, out);
+    run_job(s, job);  // posts its responses as they finish
     lk.lock();
     s->graphs[job.graph].idle.push_back(job.ctx);
-    for (auto &r : out) s->done.push_back(r);
-    s->in_flight -= out.size();
-    s->st.completed += out.size();
-    s->cv_done.notify_all();
     s->cv_work.notify_all();  // a context came back: something may be admissible
   }
 }
@@ -247,6 +384,7 @@ extern "C" int og_server_add_graph(og_server *s, og_graph *g, const og_config *g
   gs.ctx_bytes = ctx;
   gs.idle.push_back(e);  // the parent is the first context
   gs.batch = (c.flags & OG_CFG_BATCH) != 0;
+  gs.sssp_slots = g->kind == OG_GRAPH_WEIGHTED ? og::sb_sources(c.flags) : 0;
   gs.pagerank = g->kind == OG_GRAPH_PR || (c.flags & OG_CFG_PR);
   s->used_bytes += resident + ctx;
   s->graphs.push_back(std::move(gs));

@@ -9,8 +9,9 @@
 //
 // State (device):
 //   dist[v * ks + s]   distance of vertex v from source slot s (vertex-major,
-//                      ks = 8, 16 or 32 slots per row: the slots of one vertex
-//                      share 32-byte sectors, so a probe of v serves 8 sources)
+//                      ks = 4, 8, 16 or 32 slots per row: the slots of one
+//                      vertex share 32-byte sectors, so a probe of v serves up
+//                      to 8 sources)
 //   pend[v]            slots whose distance at v improved and has not been
 //                      expanded yet
 //   act                bitmap of vertices with pending slots to classify
@@ -291,7 +292,8 @@ struct SbOp {
 
 // One LBS tile of the multi-source relax, a thread per edge position as in
 // lbs_tile.  For each of its U positions a thread loads the edge record,
-// then v's row 8 slots at a time as two 16-byte loads (one 32-byte sector),
+// then v's row 8 slots at a time as two 16-byte loads (one 32-byte sector;
+// a 4-slot row is one 16-byte load),
 // and relaxes u's near slots of that chunk from registers: the slot index is
 // a compile-time loop, so the row never leaves registers.  u's distance is
 // read through L1 (u's row repeats along its adjacency in the tile).  The
@@ -300,7 +302,8 @@ struct SbOp {
 template <class Src, int KS>
 __device__ __forceinline__ void sb_tile(const LbsArgs &a, const Src &src, const SbOp &op,
                                         LbsShared<uint2> &sh, uint64_t k) {
-  static_assert(KS == 8 || KS == 16 || KS == 32, "row width");
+  static_assert(KS == 4 || KS == 8 || KS == 16 || KS == 32, "row width");
+  constexpr int C = KS < 8 ? KS : 8;  // slots per chunk
   constexpr int U = SB_U;  // positions in flight per thread
   const uint64_t pos0 = k * kTile;
   if (pos0 >= a.pos_end) return;
@@ -339,31 +342,38 @@ __device__ __forceinline__ void sb_tile(const LbsArgs &a, const Src &src, const 
         }
       }
     }
+    constexpr uint32_t cmask = (1u << C) - 1u;
 #pragma unroll
-    for (int c = 0; c < KS / 8; c++) {
+    for (int c = 0; c < KS / C; c++) {
       uint4 lo[U], hi[U];
 #pragma unroll
       for (int j = 0; j < U; j++) {
-        if (((okm >> j) & 1u) && ((val[j].x >> (8 * c)) & 0xffu)) {
-          const uint4 *r = (const uint4 *)(op.dist + (uint64_t)edge_dst(ev[j]) * KS + 8 * c);
+        if (((okm >> j) & 1u) && ((val[j].x >> (C * c)) & cmask)) {
+          const uint4 *r = (const uint4 *)(op.dist + (uint64_t)edge_dst(ev[j]) * KS + C * c);
           lo[j] = __ldcg(r);
-          hi[j] = __ldcg(r + 1);
+          if constexpr (C == 8) hi[j] = __ldcg(r + 1);
         }
       }
 #pragma unroll
       for (int j = 0; j < U; j++) {
-        const uint32_t cm = ((okm >> j) & 1u) ? (val[j].x >> (8 * c)) & 0xffu : 0u;
+        const uint32_t cm = ((okm >> j) & 1u) ? (val[j].x >> (C * c)) & cmask : 0u;
         if (!cm) continue;
         const uint32_t v = edge_dst(ev[j]);
         const uint32_t w = edge_w(ev[j]);
-        const uint32_t *ru = op.dist + (uint64_t)val[j].y * KS + 8 * c;
-        uint32_t *rv = op.dist + (uint64_t)v * KS + 8 * c;
-        const uint32_t d[8] = {lo[j].x, lo[j].y, lo[j].z, lo[j].w, hi[j].x, hi[j].y, hi[j].z, hi[j].w};
+        const uint32_t *ru = op.dist + (uint64_t)val[j].y * KS + C * c;
+        uint32_t *rv = op.dist + (uint64_t)v * KS + C * c;
+        uint32_t d[8] = {lo[j].x, lo[j].y, lo[j].z, lo[j].w, 0u, 0u, 0u, 0u};
+        if constexpr (C == 8) {
+          d[4] = hi[j].x;
+          d[5] = hi[j].y;
+          d[6] = hi[j].z;
+          d[7] = hi[j].w;
+        }
 #pragma unroll
-        for (int t = 0; t < 8; t++) {
+        for (int t = 0; t < C; t++) {
           if ((cm >> t) & 1u) {
             const uint32_t cand = ru[t] + w;
-            if (cand < d[t] && cand < atomicMin(rv + t, cand)) nb[j] |= 1u << (8 * c + t);
+            if (cand < d[t] && cand < atomicMin(rv + t, cand)) nb[j] |= 1u << (C * c + t);
           }
         }
       }

@@ -17,6 +17,12 @@ _lib = None
 _P = C.c_void_p
 
 
+class OraGraph(C.Structure):
+    _fields_ = [("V", C.c_uint32), ("weighted", C.c_int), ("E", C.c_uint64),
+                ("off", C.POINTER(C.c_uint64)), ("edges", C.POINTER(C.c_uint32)),
+                ("outdeg", C.POINTER(C.c_uint32))]
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -40,6 +46,17 @@ def lib():
                                    C.POINTER(C.c_double)]
         L.ora_path_certify.argtypes = [u32, _P, _P, u32, C.c_int, _P, u32, u32, C.c_int, _P]
         L.ora_path_certify.restype = u64
+        L.ora_bfs_bounded.argtypes = [u32, _P, _P, u32, u32, u64, _P]
+        L.ora_bfs_bounded.restype = u64
+        L.ora_pr_pull_bounded.argtypes = [u32, _P, _P, u32, u64, _P]
+        L.ora_pr_pull_bounded.restype = u64
+        L.ora_cc_uf_mt.argtypes = [u32, _P, _P, u32, C.c_int, _P]
+        L.ora_cc_uf_mt.restype = u64
+        L.ora_rmat.argtypes = [u32, u32, C.c_double, C.c_double, C.c_double, u64, u64, u32, u32, u32,
+                               C.c_int, C.POINTER(OraGraph)]
+        L.ora_rmat.restype = C.c_int
+        L.ora_graph_free.argtypes = [C.POINTER(OraGraph)]
+        L.ora_graph_free.restype = None
         for f in ("ora_bfs", "ora_cc", "ora_sssp_frontier", "ora_pr_cpu", "ora_pr_onegraph",
                   "ora_pr_l1", "ora_pr_l1_mt"):
             getattr(L, f).restype = C.c_int
@@ -148,3 +165,66 @@ def path_certify_raw(V, off_ptr, edges_ptr, stride, unit, dist, src, unreached, 
     bad = lib().ora_path_certify(V, off_ptr, edges_ptr, stride, 1 if unit else 0, _p(d), src, unreached,
                                  threads, C.byref(fb))
     return int(bad), int(fb.value)
+
+
+def bfs_bounded_raw(V, off_ptr, edges_ptr, stride, src, max_edges, out):
+    """runCPUBFS restatement on pointers, stopped after max_edges edges
+    (0: complete); returns the edges scanned."""
+    return int(lib().ora_bfs_bounded(V, off_ptr, edges_ptr, stride, src, max_edges, out.ctypes.data_as(_P)))
+
+
+def pr_pull_bounded_raw(V, off_ptr, edges_ptr, stride, max_edges, out):
+    """One pr_cal pull iteration on a symmetric graph given by pointers,
+    stopped after max_edges edges; returns the edges read."""
+    return int(lib().ora_pr_pull_bounded(V, off_ptr, edges_ptr, stride, max_edges, out.ctypes.data_as(_P)))
+
+
+def cc_uf_mt_raw(V, off_ptr, edges_ptr, stride, threads, out):
+    """Union-find components of a symmetric graph given by pointers (no
+    copies): out[v] = smallest id of v's component.  Returns the count."""
+    return int(lib().ora_cc_uf_mt(V, off_ptr, edges_ptr, stride, threads, out.ctypes.data_as(_P)))
+
+
+RMAT_SYMMETRIC, RMAT_PERMUTE, RMAT_WEIGHTED, RMAT_PR = 1, 2, 4, 8
+
+
+class RmatGraph:
+    """A seeded R-MAT graph built on the CPU by the oracle (og_oracle_rmat.c):
+    .V, .E, .offsets (V+1 u64), .edges (E u32 columns or (E, 2) {dst, w}
+    pairs), .outdeg (PageRank graphs) as views of C-owned arrays, and the raw
+    pointers off_p / edges_p for the pointer-form oracle calls."""
+
+    def __init__(self, scale, edge_factor=16, seed=1, weight_seed=2, weighted=False, symmetric=True,
+                 permute=True, pagerank=False, wmin=1, wmax=64, abc=(0.57, 0.19, 0.19), threads=0):
+        self._g = OraGraph()
+        flags = ((RMAT_SYMMETRIC if symmetric else 0) | (RMAT_PERMUTE if permute else 0) |
+                 (RMAT_WEIGHTED if weighted else 0) | (RMAT_PR if pagerank else 0))
+        nt = threads or (os.cpu_count() or 1)
+        rc = lib().ora_rmat(scale, edge_factor, abc[0], abc[1], abc[2], seed, weight_seed, wmin, wmax,
+                            flags, nt, C.byref(self._g))
+        if rc != 0:
+            raise MemoryError("ora_rmat failed (%d)" % rc)
+        g = self._g
+        self.V, self.E, self.weighted = g.V, g.E, bool(g.weighted)
+        self.off_p = C.cast(g.off, _P)
+        self.edges_p = C.cast(g.edges, _P)
+        self.offsets = np.ctypeslib.as_array(g.off, (self.V + 1,))
+        n = self.E * (2 if self.weighted else 1)
+        self.edges = np.ctypeslib.as_array(g.edges, (max(n, 1),))[:n]
+        if self.weighted:
+            self.edges = self.edges.reshape(-1, 2)
+        self.outdeg = np.ctypeslib.as_array(g.outdeg, (self.V,)) if g.outdeg else None
+
+    def degrees(self):
+        return np.diff(self.offsets).astype(np.uint32)
+
+    def close(self):
+        if self._g is not None and self._g.off:
+            lib().ora_graph_free(C.byref(self._g))
+        self._g = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

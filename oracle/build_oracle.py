@@ -17,7 +17,9 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 REF_OUT = os.path.join(HERE, "_ref")
-DEFAULT_REF_ROOT = "/root/reference"
+# the reference tree: $OG_REFERENCE_ROOT, else a directory named "reference"
+# beside the repository
+DEFAULT_REF_ROOT = os.path.join(os.path.dirname(os.path.dirname(HERE)), "reference")
 
 LIB = os.path.join(BUILD, "libogoracle.so")
 
@@ -35,16 +37,18 @@ def _run(cmd):
         raise RuntimeError("command failed: %s\n%s%s" % (" ".join(cmd), r.stdout, r.stderr))
 
 
+SOURCES = ["og_oracle.c", "og_oracle_rmat.c"]
+
+
 def build_oracle(force: bool = False) -> str:
-    src = os.path.join(HERE, "og_oracle.c")
-    if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= max(os.path.getmtime(src),
-                                             os.path.getmtime(os.path.join(HERE, "og_oracle.h")))):
+    srcs = [os.path.join(HERE, f) for f in SOURCES]
+    newest = max(os.path.getmtime(f) for f in srcs + [os.path.join(HERE, "og_oracle.h")])
+    if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= newest:
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     tmp = LIB + ".tmp%d" % os.getpid()
-    _run(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", "-o", tmp,
-          src, "-lm", "-lpthread"])
+    _run(["gcc", "-O2", "-std=c11", "-ffp-contract=off", "-fPIC", "-shared", "-Wall", "-o", tmp]
+         + srcs + ["-lm", "-lpthread"])
     os.replace(tmp, LIB)
     return LIB
 

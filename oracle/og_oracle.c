@@ -477,3 +477,151 @@ uint64_t ora_path_certify(uint32_t V, const uint64_t *off, const uint32_t *edges
   if (first_bad) *first_bad = fb;
   return bad;
 }
+
+/* ---------------------------------------------------- union-find components */
+
+typedef struct {
+  uint32_t V, stride;
+  const uint64_t *off;
+  const uint32_t *edges;
+  uint32_t *par;
+  uint32_t v0, v1;
+  int phase;
+  uint64_t roots;
+} UfJob;
+
+static uint32_t uf_find(uint32_t *par, uint32_t x) {
+  for (;;) {
+    const uint32_t p = __atomic_load_n(&par[x], __ATOMIC_RELAXED);
+    if (p == x) return x;
+    const uint32_t gp = __atomic_load_n(&par[p], __ATOMIC_RELAXED);
+    if (gp != p) __atomic_compare_exchange_n(&par[x], (uint32_t *)&p, gp, 0, __ATOMIC_RELAXED, __ATOMIC_RELAXED);
+    x = gp;
+  }
+}
+
+static void *uf_worker(void *arg) {
+  UfJob *j = (UfJob *)arg;
+  if (j->phase == 0) {
+    for (uint32_t u = j->v0; u < j->v1; u++)
+      for (uint64_t e = j->off[u]; e < j->off[u + 1]; e++) {
+        const uint32_t v = j->edges[e * j->stride];
+        if (v <= u) continue; /* each undirected edge once */
+        for (;;) {
+          uint32_t ru = uf_find(j->par, u), rv = uf_find(j->par, v);
+          if (ru == rv) break;
+          if (ru < rv) {
+            const uint32_t t = ru;
+            ru = rv;
+            rv = t;
+          }
+          uint32_t expect = ru; /* link the larger root under the smaller */
+          if (__atomic_compare_exchange_n(&j->par[ru], &expect, rv, 0, __ATOMIC_RELAXED, __ATOMIC_RELAXED))
+            break;
+        }
+      }
+  } else {
+    for (uint32_t v = j->v0; v < j->v1; v++) {  /* no link is left: roots are final */
+      const uint32_t r = uf_find(j->par, v);
+      __atomic_store_n(&j->par[v], r, __ATOMIC_RELAXED);
+      j->roots += (r == v);
+    }
+  }
+  return NULL;
+}
+
+uint64_t ora_cc_uf_mt(uint32_t V, const uint64_t *off, const uint32_t *edges, uint32_t stride,
+                      int threads, uint32_t *out) {
+  if (threads < 1) threads = 1;
+  for (uint32_t v = 0; v < V; v++) out[v] = v;
+  UfJob *jobs = (UfJob *)calloc((size_t)threads, sizeof(UfJob));
+  pthread_t *tid = (pthread_t *)calloc((size_t)threads, sizeof(pthread_t));
+  uint64_t comps = 0;
+  if (!jobs || !tid) goto done;
+  for (int phase = 0; phase < 2; phase++) {
+    for (int t = 0; t < threads; t++) {
+      UfJob *j = &jobs[t];
+      j->V = V;
+      j->stride = stride;
+      j->off = off;
+      j->edges = edges;
+      j->par = out;
+      j->v0 = (uint32_t)((uint64_t)V * t / threads);
+      j->v1 = (uint32_t)((uint64_t)V * (t + 1) / threads);
+      j->phase = phase;
+      j->roots = 0;
+      pthread_create(&tid[t], NULL, uf_worker, j);
+    }
+    for (int t = 0; t < threads; t++) pthread_join(tid[t], NULL);
+  }
+  for (int t = 0; t < threads; t++) comps += jobs[t].roots;
+done:
+  free(jobs);
+  free(tid);
+  return comps;
+}
+
+/* ------------------------------------------------ bounded CPU-baseline samples */
+
+/* runCPUBFS (BFS/cpu_BFS/main.cpp:114-209) on `stride`-spaced columns, stopped
+ * once max_edges edges were scanned (0 = no bound).  Returns the edges scanned;
+ * a timing sample of the reference's CPU BFS on graphs too large to finish. */
+uint64_t ora_bfs_bounded(uint32_t V, const uint64_t *off, const uint32_t *edges, uint32_t stride,
+                         uint32_t src, uint64_t max_edges, uint32_t *out) {
+  unsigned char *active = (unsigned char *)calloc(V ? V : 1, 1);
+  unsigned char *next = (unsigned char *)calloc(V ? V : 1, 1);
+  uint64_t scanned = 0;
+  for (uint32_t i = 0; i < V; i++) out[i] = INF32;
+  if (src < V && active && next) {
+    active[src] = 1;
+    out[src] = 1;
+    for (uint32_t n_active = 1; n_active > 0 && (max_edges == 0 || scanned < max_edges);) {
+      for (uint32_t u = 0; u < V && (max_edges == 0 || scanned < max_edges); u++) {
+        if (!active[u]) continue;
+        const uint32_t cand = out[u] + 1;
+        for (uint64_t e = off[u]; e < off[u + 1]; e++) {
+          const uint32_t v = edges[e * stride];
+          if (cand < out[v]) {
+            out[v] = cand;
+            next[v] = 1;
+          }
+        }
+        scanned += off[u + 1] - off[u];
+      }
+      n_active = 0;
+      for (uint32_t i = 0; i < V; i++) {
+        active[i] = next[i];
+        n_active += next[i];
+        next[i] = 0;
+      }
+    }
+  }
+  free(active);
+  free(next);
+  return scanned;
+}
+
+/* One pull iteration of the reference's CPU PageRank (pr_cal, PR/cpu/pr.cpp:
+ * 126-165: every vertex sums rank / out-degree over its in-neighbours) on a
+ * symmetric graph (in-neighbours = the adjacency, out-degree = its length),
+ * `stride`-spaced columns, ranks initialised to 1/V (pr.cpp:116), stopped once
+ * max_edges edges were read.  Returns the edges read; out receives the sums. */
+uint64_t ora_pr_pull_bounded(uint32_t V, const uint64_t *off, const uint32_t *edges, uint32_t stride,
+                             uint64_t max_edges, double *out) {
+  double *rank = (double *)malloc((V ? V : 1) * sizeof(double));
+  uint64_t scanned = 0;
+  if (!rank) return 0;
+  for (uint32_t i = 0; i < V; i++) rank[i] = 1.0 / V;
+  for (uint32_t v = 0; v < V && (max_edges == 0 || scanned < max_edges); v++) {
+    double sum = 0;
+    for (uint64_t e = off[v]; e < off[v + 1]; e++) {
+      const uint32_t u = edges[e * stride];
+      const uint64_t d = off[u + 1] - off[u];
+      if (d) sum += rank[u] / (double)d;
+    }
+    out[v] = 0.15 + 0.15 * sum;
+    scanned += off[v + 1] - off[v];
+  }
+  free(rank);
+  return scanned;
+}

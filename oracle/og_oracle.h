@@ -101,6 +101,48 @@ uint64_t ora_path_certify(uint32_t V, const uint64_t *off, const uint32_t *edges
                           int unit, const uint32_t *dist, uint32_t src, uint32_t unreached,
                           int threads, uint32_t *first_bad);
 
+/* Components of a symmetric graph by union-find on `threads` host threads:
+ * every edge (u, v) links the roots of u and v, the larger root under the
+ * smaller (compare-and-swap, retried on contention), so every root is the
+ * smallest id of its component; out[v] = root of v.  On a symmetric graph
+ * this is the reference's CC label (the minimum vertex id that reaches v,
+ * CC/serial/serial.cpp:154-213), found without its rounds.  stride as in
+ * ora_path_certify.  Returns the number of components. */
+uint64_t ora_cc_uf_mt(uint32_t V, const uint64_t *off, const uint32_t *edges, uint32_t stride,
+                      int threads, uint32_t *out);
+
+/* Bounded timing samples for the CPU baselines (0 = no bound): runCPUBFS
+ * (BFS/cpu_BFS/main.cpp:114-209) and one pull iteration of pr_cal
+ * (PR/cpu/pr.cpp:126-165) on a symmetric graph, over `stride`-spaced
+ * columns; both return the edges scanned. */
+uint64_t ora_bfs_bounded(uint32_t V, const uint64_t *off, const uint32_t *edges, uint32_t stride,
+                         uint32_t src, uint64_t max_edges, uint32_t *out);
+uint64_t ora_pr_pull_bounded(uint32_t V, const uint64_t *off, const uint32_t *edges, uint32_t stride,
+                             uint64_t max_edges, double *out);
+
+/* A seeded R-MAT graph in CSR (og_oracle_rmat.c): off has V+1 entries,
+ * edges E u32 columns or E {dst, w} pairs (weighted), outdeg V entries for a
+ * PageRank graph (else NULL).  Free with ora_graph_free. */
+typedef struct ora_graph {
+  uint32_t V;
+  int weighted;
+  uint64_t E;
+  uint64_t *off;
+  uint32_t *edges;
+  uint32_t *outdeg;
+} ora_graph;
+
+#define ORA_RMAT_SYMMETRIC 1u
+#define ORA_RMAT_PERMUTE 2u
+#define ORA_RMAT_WEIGHTED 4u
+#define ORA_RMAT_PR 8u
+
+/* Returns 0, -1 for bad parameters, -2 when memory ran out. */
+int ora_rmat(uint32_t scale, uint32_t edge_factor, double a, double b, double c, uint64_t seed,
+             uint64_t weight_seed, uint32_t wmin, uint32_t wmax, uint32_t flags, int threads,
+             ora_graph *out);
+void ora_graph_free(ora_graph *g);
+
 #ifdef __cplusplus
 }
 #endif

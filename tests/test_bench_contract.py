@@ -17,10 +17,41 @@ def _run(*args):
     return json.loads(lines[0])
 
 
-def test_reference_arm_line():
-    d = _run("--impl", "reference", "--scale", "12", "--steps", "2", "--warmup", "1", "--cpu-seconds", "1")
-    for k in ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
-              "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e"):
+KEYS = ("metric", "value", "unit", "n_gpus", "steps", "warmup", "ms_per_step", "higher_is_better",
+        "scaling", "vs_baseline", "dtype", "data", "config", "cpu_baseline", "e2e")
+
+
+def test_reference_arm_serving_line():
+    """The default workload's reference arm: small graphs, CPU only, and the
+    engine's library never mapped into the process."""
+    d = _run("--impl", "reference", "--serving-scales", "10,11,12,13", "--requests", "60", "--steps", "2",
+             "--warmup", "1", "--cpu-seconds", "1")
+    for k in KEYS:
+        assert k in d, k
+    assert d["impl"] == "reference"
+    assert d["metric"] == "served queries/s" and d["unit"] == "queries/s" and d["higher_is_better"] is True
+    assert d["value"] > 0 and d["steps"] == 2 and d["warmup"] == 1
+    assert d["e2e"]["value"] == d["value"] and d["e2e"]["h2d_bytes_per_step"] == 0
+    assert d["config"]["workload"] == "serving-rmat10-11-12-13-24GiB"
+    assert sum(d["config"]["mix"].values()) == 60
+    assert d["cpu_baseline"]["value"] == d["value"] and d["cpu_baseline"]["cores"] >= 1
+
+
+def test_reference_arm_loads_no_engine_library():
+    code = ("import sys, runpy; sys.argv = ['bench.py', '--impl', 'reference', '--serving-scales', '10,11,12,13', "
+            "'--requests', '40', '--steps', '1', '--warmup', '1', '--cpu-seconds', '1']; "
+            "runpy.run_path('bench.py', run_name='__main__'); "
+            "maps = open('/proc/self/maps').read(); "
+            "print('ENGINE_MAPPED' if 'libog.so' in maps else 'ENGINE_NOT_MAPPED')")
+    out = subprocess.run([sys.executable, "-c", code], cwd=ROOT, capture_output=True, text=True, timeout=300)
+    assert out.returncode == 0, out.stderr[-2000:]
+    assert "ENGINE_NOT_MAPPED" in out.stdout
+
+
+def test_reference_arm_sssp_line():
+    d = _run("--impl", "reference", "--workload", "sssp-oom", "--scale", "12", "--steps", "2", "--warmup", "1",
+             "--cpu-seconds", "1")
+    for k in KEYS:
         assert k in d, k
     assert d["impl"] == "reference"
     assert d["metric"] == "queries/s" and d["unit"] == "queries/s" and d["higher_is_better"] is True
@@ -30,6 +61,7 @@ def test_reference_arm_line():
     cb = d["cpu_baseline"]
     assert cb["value"] == d["value"] and cb["kind"] in ("port", "reference") and cb["cores"] >= 1
     assert d["config"]["workload"].startswith("oom-sssp-rmat12")
+    assert d["config"]["sssp_delta"] == 4.0  # the engine's default, as in the GPU arm
 
 
 def test_help_lists_workloads():

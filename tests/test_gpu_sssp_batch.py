@@ -62,7 +62,7 @@ def test_sssp_batch_equals_single_source_and_dijkstra():
         e.close()
 
 
-@pytest.mark.parametrize("k,n", [(8, 5), (16, 16), (20, 7)])
+@pytest.mark.parametrize("k,n", [(4, 4), (8, 5), (16, 16), (20, 7)])
 @pytest.mark.parametrize("delta", [0, 1, 64])
 def test_sssp_batch_widths_and_deltas(k, n, delta):
     """Rows of 8, 16 and 32 slots, partly used; near/far width 0 (every

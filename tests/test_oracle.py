@@ -161,3 +161,63 @@ def test_path_certificate_accepts_exact_and_rejects_planted_errors():
     wrong_src = d.copy()
     wrong_src[s] = 2
     assert oracle.path_certify_raw(g.V, g._off_p, g._edges_p, 2, False, wrong_src, s, 0xFFFFFFFF, 4)[0] > 0
+
+
+def test_union_find_components_match_reference_serial_cc(golden):
+    """ora_cc_uf_mt (the full-size CC checker) gives CC/serial's labels on
+    every symmetric golden graph, on 1 and 8 threads."""
+    for n in golden_names(golden, "cc"):
+        off = np.ascontiguousarray(golden[n + "/off"], np.uint64)
+        col = np.ascontiguousarray(golden[n + "/col"], np.uint32)
+        for threads in (1, 8):
+            lab = np.empty(off.size - 1, np.uint32)
+            comps = oracle.cc_uf_mt_raw(off.size - 1, off.ctypes.data_as(oracle._P),
+                                        col.ctypes.data_as(oracle._P), 1, threads, lab)
+            np.testing.assert_array_equal(lab, golden[n + "/cc"], err_msg="%s/%d" % (n, threads))
+            assert comps == len(np.unique(golden[n + "/cc"]))
+
+
+@pytest.mark.parametrize("scale,kw", [
+    (10, dict(weighted=True)), (12, {}), (11, dict(pagerank=True, symmetric=False)),
+    (13, dict(weighted=True, permute=False)), (9, dict(weighted=True, wmin=5, wmax=70000)),
+    (14, dict(edge_factor=8, seed=7, weight_seed=9, weighted=True)),
+])
+def test_oracle_rmat_equals_the_engine_generator(scale, kw):
+    """The oracle's CPU R-MAT (used where the engine must not be loaded)
+    builds the engine generator's CSR bit for bit."""
+    r = oracle.RmatGraph(scale, **kw)
+    g = og.Graph.rmat(scale, **kw)
+    assert (r.V, r.E) == (g.V, g.E)
+    np.testing.assert_array_equal(r.offsets, g.offsets)
+    np.testing.assert_array_equal(np.asarray(r.edges), np.asarray(g.edges))
+    if kw.get("pagerank"):
+        np.testing.assert_array_equal(r.outdeg, g.outdeg)
+    r.close()
+    g.close()
+
+
+def test_bounded_baseline_samples_agree_with_the_complete_runs(golden):
+    """The bounded BFS sample is runCPUBFS when unbounded (and stops early when
+    bounded); the bounded pull is pr_cal's first iteration sum on a symmetric graph."""
+    for n in golden_names(golden, "bfs")[:4]:
+        off = np.ascontiguousarray(golden[n + "/off"], np.uint64)
+        col = np.ascontiguousarray(golden[n + "/col"], np.uint32)
+        V = off.size - 1
+        s = int(golden[n + "/bfs_src"][0])
+        out = np.empty(V, np.uint32)
+        scanned = oracle.bfs_bounded_raw(V, off.ctypes.data_as(oracle._P), col.ctypes.data_as(oracle._P), 1,
+                                         s, 0, out)
+        np.testing.assert_array_equal(out, golden[n + "/bfs"][0], err_msg=n)
+        assert scanned >= 1 or off[-1] == 0
+        if off[-1] > 8:
+            assert oracle.bfs_bounded_raw(V, off.ctypes.data_as(oracle._P), col.ctypes.data_as(oracle._P), 1,
+                                          s, 1, out) <= scanned
+    g = og.Graph.rmat(10, 16, weighted=True)
+    off, pairs = np.array(g.offsets), np.ascontiguousarray(np.array(g.edges))
+    sums = np.empty(g.V)
+    read = oracle.pr_pull_bounded_raw(g.V, off.ctypes.data_as(oracle._P), pairs.ctypes.data_as(oracle._P), 2, 0, sums)
+    assert read == g.E
+    deg = np.diff(off.astype(np.int64)).astype(np.float64)
+    contrib = np.where(deg > 0, 1.0 / g.V / np.maximum(deg, 1), 0.0)
+    want = np.array([0.15 + 0.15 * contrib[pairs[off[v]:off[v + 1], 0]].sum() for v in range(g.V)])
+    np.testing.assert_allclose(sums, want, rtol=1e-12)
