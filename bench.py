@@ -159,24 +159,23 @@ class ClockSampler:
                 "reasons": sorted(reasons)}
 
 
+LINK_PEAKS: dict = {}
+
+
 def h2d_peak_gbs() -> float:
-    """Page-locked host -> device copy bandwidth (best of 5, 2 GiB)."""
+    """Host-link ceiling for the rooflines: the highest of three probes over a
+    2 GiB page-locked buffer (og_link_probe, best of 3 each): SM loads of the
+    buffer (how the direct-mode kernels read host records), one DMA copy, and
+    two DMA copies at once.  All three are kept in LINK_PEAKS."""
     import torch
-    n = 2 * GIB
-    src = torch.empty(n, dtype=torch.uint8, pin_memory=True)
-    dst = torch.empty(n, dtype=torch.uint8, device="cuda")
-    best = 0.0
-    s = torch.cuda.current_stream()
-    for _ in range(5):
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(s)
-        dst.copy_(src, non_blocking=True)
-        b.record(s)
-        b.synchronize()
-        best = max(best, n / (a.elapsed_time(b) / 1e3) / 1e9)
-    del src, dst
+    import onegraph_gb300 as og
+    src = torch.empty(2 * GIB, dtype=torch.uint8, pin_memory=True)
+    LINK_PEAKS.clear()
+    for mode, name in ((0, "sm_read_gbs"), (1, "dma_copy_gbs"), (2, "dma_copy_2streams_gbs")):
+        LINK_PEAKS[name] = og.link_probe(src, mode, 3)
+    del src
     torch.cuda.empty_cache()
-    return best
+    return max(LINK_PEAKS.values())
 
 
 def measured_peaks() -> dict:
@@ -428,7 +427,7 @@ def run_ours(args, rank, world, local):
     host_static_gbs = ((eb + 4) * st_edges + 20 * st_verts) / (relax_ms / 1e3) / 1e9 if relax_ms else 0.0
     roof_link = {"bound": "host-link", "kernel": kname, "achieved": link_gbs, "peak": h2d, "unit": "GB/s",
                  "frac": link_gbs / h2d if h2d else None, "traffic": None,
-                 "peak_source": "measured pinned H2D copy in this run",
+                 "peak_source": "highest of the link probes measured in this run (og_link_probe)", "link_probes": dict(LINK_PEAKS),
                  "timing": "globaltimer stamps around every relax launch of %d device-driven queries "
                            "(the timed queries' sources, timer on)" % len(tstats)}
     roof_static = {"bound": "hbm", "kernel": kname + ", its HBM side", "achieved": static_gbs,
@@ -837,7 +836,7 @@ def run_cc_oom(args, rank, world, local):
                      "kernel": "k_uf_sample (one record per vertex, random 32-byte sectors over the link)"
                      if method == "union-find" else "k_lbs_pair<SrcP<false>,MinOp<false>> over host-mapped records",
                      "achieved": link_gbs, "peak": h2d, "unit": "GB/s", "frac": link_gbs / h2d if h2d else None,
-                     "traffic": None, "peak_source": "measured pinned H2D copy in this run",
+                     "traffic": None, "peak_source": "highest of the link probes measured in this run (og_link_probe)", "link_probes": dict(LINK_PEAKS),
                      "note": "algorithmic bytes = packed records read; union-find reads one record per "
                              "sampled vertex, a full 32-byte sector each, so it is bound by the link's "
                              "request rate rather than its bandwidth" if method == "union-find" else ""},
@@ -1074,6 +1073,7 @@ def run_serving(args, rank, world, local):
         e.sssp(s0, out=False)
         e.pr_l1(0.85, 0.0, 5, out=False)
     mism = 0
+    pr_dev = 0.0
     plain_lat, plain_svc = [], []
     p0 = time.perf_counter()
     for i in range(n):
@@ -1088,7 +1088,16 @@ def run_serving(args, rank, world, local):
         now = time.perf_counter()
         plain_svc.append((now - q0) * 1e3)
         plain_lat.append(max(0.0, (now - p0) - arrivals[i]) * 1e3)
-        mism += e.checksum(a) != ref_resp[i]["checksum"]
+        ck = e.checksum(a)
+        if a == ALGO_PR:
+            # FP32 pull sums are deterministic for a given plan; the plain
+            # engines (no batch state) plan a larger static region, so their
+            # tiles and summation order differ: equal to FP32 rounding
+            fp = [float(np.array([x], np.uint64).view(np.float64)[0]) for x in (ck[1], ref_resp[i]["checksum"][1])]
+            pr_dev = max(pr_dev, abs(fp[0] - fp[1]) / max(abs(fp[1]), 1e-30))
+            mism += ck[0] != ref_resp[i]["checksum"][0] or pr_dev > 1e-5
+        else:
+            mism += ck != ref_resp[i]["checksum"]
     plain_wall = time.perf_counter() - p0
     for e in engines:
         e.close()
@@ -1134,6 +1143,9 @@ def run_serving(args, rank, world, local):
         "plain_queries_per_s": plain_qps, "plain_p50_ms": float(np.percentile(plain_lat, 50)),
         "plain_p99_ms": float(np.percentile(plain_lat, 99)),
         "speedup_vs_plain": value / plain_qps, "results_identical_to_plain": mism == 0,
+        "results_note": "BFS depths and SSSP distances bit-identical ({reached, sum} per request); PageRank "
+                        "sum of FP32 ranks within 1e-5 relative (max seen %.2e): the plain engines plan a "
+                        "different static region, so their pull tiles differ" % pr_dev,
         "e2e": {"value": e2e_qps, "unit": "queries/s", "h2d_bytes_per_step": 4 * n, "d2h_bytes_per_step":
                 int(d2h * n), "passes": e2e_passes,
                 "note": "a step is one pass of the mix; every request's V results read into page-locked host "
@@ -1171,7 +1183,7 @@ def serving_rooflines(og, g, budget, slots, srcs, gsel, algos, gi, h2d, local):
         ach = st["link_bytes"] / (st["ms_dynamic"] / 1e3) / 1e9 if st["ms_dynamic"] else 0.0
         return {"bound": "host-link", "kernel": kernel, "achieved": ach, "peak": h2d, "unit": "GB/s",
                 "frac": ach / h2d if h2d else None, "traffic": None,
-                "peak_source": "measured pinned H2D copy in this run", "bytes_per_launch_note": unit_note,
+                "peak_source": "highest of the link probes measured in this run (og_link_probe)", "link_probes": dict(LINK_PEAKS), "bytes_per_launch_note": unit_note,
                 "link_gb": st["link_bytes"] / 1e9, "kernel_ms": st["ms_dynamic"]}
     a = roof("k_sb_relax_pair<SrcP<true>,SrcP<true>,%d> (multi-source SSSP relax, R-MAT %d pass of %d sources)"
              % (4 if slots <= 4 else 8, 27, len(ss)), sb, "packed 33-bit records of the dynamic region")

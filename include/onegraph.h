@@ -466,9 +466,11 @@ int og_k_compact(const uint32_t *bits, uint32_t v_begin, uint32_t v_end,
  * loop that cannot pay for the device synchronisation cudaMalloc/cudaFree
  * imply.  Same arguments, results and status as og_k_compact; the caller
  * still passes every input and output buffer.
- * Scratch: a fixed ~0.9 MB array inside libog.so, present on every device
- * that loads the library until the process exits.  Limit: one call covers at
- * most 2^28 vertices (8192 tiles of 32768); larger ranges return OG_E_ARG.
+ * Scratch: a fixed array of 229,700 bytes (28 B per compaction tile for 8192
+ * tiles, plus 324 B) inside libog.so, present on every device that loads the
+ * library until the process exits.  Limit: 8192 tiles of 1024 bitmap words
+ * (32768 vertices) per call, i.e. 2^28 vertices when v_begin is a multiple
+ * of 32 and 2^28 - 32 otherwise; larger ranges return OG_E_ARG.
  * The first call on a device looks up that array's device address, so make it
  * before any stream capture.  Every call shares the array: calls that overlap
  * on the GPU (other streams, other host threads) race and must not be issued;

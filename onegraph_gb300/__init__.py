@@ -128,9 +128,15 @@ class ServerStats(C.Structure):
                 ("used_bytes", C.c_uint64), ("launches", C.c_uint64)]
 
 
+class KRecords(C.Structure):
+    """og_k_records (include/onegraph_kernels.h): packed records in device memory."""
+    _fields_ = [("words", C.c_void_p), ("nrecords", C.c_uint64), ("bpe", C.c_uint32), ("bc", C.c_uint32),
+                ("wmin", C.c_uint32), ("reserved", C.c_uint32)]
+
+
 _lib = None
 
-# (name, restype, argtypes) for every symbol declared in include/onegraph.h
+# (name, restype, argtypes) for every symbol declared in include/*.h
 _P = C.c_void_p
 SIGNATURES = [
     ("og_graph_load", C.c_int, [C.c_char_p, C.c_int, C.POINTER(_P)]),
@@ -180,6 +186,12 @@ SIGNATURES = [
                                C.c_uint64, _P, _P]),
     ("og_k_compact_noalloc", C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P, C.c_uint64, _P,
                                        C.c_uint64, _P, _P]),
+    ("og_k_relax", C.c_int, [C.c_int, _P, _P, _P, C.c_uint32, C.c_uint64, _P, C.POINTER(KRecords), C.c_uint32,
+                             _P, _P, _P, C.c_uint32, _P]),
+    ("og_k_gather", C.c_int, [_P, _P, _P, C.c_uint32, C.c_uint64, _P, C.POINTER(KRecords), C.c_uint64,
+                              C.c_uint64, _P, _P, _P]),
+    ("og_k_wait_check", C.c_int, [C.c_int, C.c_uint32]),
+    ("og_link_probe", C.c_int, [_P, C.c_uint64, C.c_int, C.c_int, C.POINTER(C.c_double)]),
     ("og_server_create", C.c_int, [C.POINTER(ServerConfig), C.POINTER(_P)]),
     ("og_server_add_graph", C.c_int, [_P, _P, C.POINTER(Config), C.POINTER(C.c_int)]),
     ("og_server_submit", C.c_int, [_P, C.POINTER(Request), C.POINTER(C.c_uint64)]),
@@ -690,3 +702,14 @@ def pr_opt(path: str, adviseRate: float = 0.0, budget: int = 0, threshold: float
     st = dict(eng.stats)
     eng.close()
     return r, st
+
+
+def link_probe(host_buffer, mode: int, reps: int = 3) -> float:
+    """og_link_probe on a page-locked host buffer (a pinned torch tensor or an
+    object with data_ptr(), numel(), element_size()): 0 SM reads, 1 one DMA
+    copy, 2 two DMA copies at once; GB/s."""
+    v = C.c_double()
+    nbytes = host_buffer.numel() * host_buffer.element_size() // 16 * 16
+    _check(lib().og_link_probe(C.c_void_p(host_buffer.data_ptr()), nbytes, mode, reps, C.byref(v)),
+           "og_link_probe")
+    return v.value

@@ -74,21 +74,27 @@ struct PersistArgs {
 
 constexpr uint64_t kBatchAlpha = 14, kBatchBeta = 24;
 
-__device__ __forceinline__ bool grid_barrier(unsigned int *bar, uint32_t *err) {
+// Grid-wide barrier of a cooperative launch: the last of `expected` CTAs to
+// arrive (default: the whole grid) releases the others by bumping the
+// generation word.  A wait longer than spin_limit polls sets kErrBarrier and
+// returns false instead of hanging.
+__device__ __forceinline__ bool grid_barrier(unsigned int *bar, uint32_t *err, uint32_t expected = 0,
+                                             uint32_t spin_limit = kSpinLimit) {
   __shared__ int s_ok;
+  if (expected == 0) expected = gridDim.x;
   __syncthreads();
   if (threadIdx.x == 0) {
     int ok = 1;
     const unsigned int gen = ld_acquire((const uint32_t *)&bar[1]);
     __threadfence();
-    if (atomicAdd(&bar[0], 1u) == gridDim.x - 1) {
+    if (atomicAdd(&bar[0], 1u) == expected - 1) {
       bar[0] = 0;
       __threadfence();
       st_release((uint32_t *)&bar[1], gen + 1);
     } else {
       uint32_t spins = 0;
       while (ld_acquire((const uint32_t *)&bar[1]) == gen) {
-        if (++spins > kSpinLimit) {
+        if (++spins > spin_limit) {
           atomicOr(err, kErrBarrier);
           ok = 0;
           break;

@@ -223,9 +223,18 @@ void destroy(og_engine *e) {
 int create_query_state(og_engine *e) {
   const og_plan &P = e->plan;
   const uint64_t V = e->V;
-  CK(cudaStreamCreateWithFlags(&e->s_main, cudaStreamNonBlocking));
-  CK(cudaStreamCreateWithFlags(&e->s_dyn, cudaStreamNonBlocking));
-  CK(cudaStreamCreateWithFlags(&e->s_gat, cudaStreamNonBlocking));
+  // A fully resident graph's queries are short and HBM-bound; an
+  // out-of-memory graph's kernels wait on the host link with many CTAs
+  // resident.  When both share the GPU (several engines, the server), the
+  // resident graph's streams get the highest priority so that the block
+  // scheduler places its CTAs first as SMs free up, instead of behind a
+  // link-bound grid of millions of CTAs.
+  int prio_lo = 0, prio_hi = 0;
+  CK(cudaDeviceGetStreamPriorityRange(&prio_lo, &prio_hi));
+  const int prio = P.dynamic_edges == 0 ? prio_hi : prio_lo;
+  CK(cudaStreamCreateWithPriority(&e->s_main, cudaStreamNonBlocking, prio));
+  CK(cudaStreamCreateWithPriority(&e->s_dyn, cudaStreamNonBlocking, prio));
+  CK(cudaStreamCreateWithPriority(&e->s_gat, cudaStreamNonBlocking, prio));
   cudaEvent_t *evs[] = {&e->ev_round, &e->ev_cs, &e->ev_cd, &e->ev_dyn_done, &e->ev_gat[0],
                         &e->ev_gat[1], &e->ev_rel[0], &e->ev_rel[1], &e->t_s0, &e->t_s1, &e->t_d0};
   for (auto ev : evs) CK(cudaEventCreate(ev));
@@ -2511,9 +2520,10 @@ extern "C" int og_k_compact(const uint32_t *bits, uint32_t v_begin, uint32_t v_e
 //
 // og_k_compact_noalloc runs the same compaction with its look-back scratch in
 // a fixed array that is part of the loaded library instead of memory it asks
-// the CUDA runtime for.  Limit: kNoAllocTiles compaction tiles of 32768 vertices,
-// i.e. a range of at most 2^28 vertices per call.  The array lives on every
-// device that loads the library, for as long as the process runs.
+// the CUDA runtime for.  Limit: kNoAllocTiles compaction tiles of 1024 bitmap
+// words, counted from the word holding v_begin: 2^28 vertices when v_begin is
+// a multiple of 32, 2^28 - 32 otherwise.  The array (229,700 bytes) lives on
+// every device that loads the library, for as long as the process runs.
 
 namespace {
 
@@ -2557,7 +2567,7 @@ extern "C" int og_k_compact_noalloc(const uint32_t *bits, uint32_t v_begin, uint
   if (nt > kNoAllocTiles)
     return fail(OG_E_ARG,
                 "og_k_compact_noalloc: range of %u vertices needs %u scratch tiles, the fixed "
-                "scratch holds %u (at most 2^28 vertices per call)",
+                "scratch holds %u (2^28 vertices per call from a multiple of 32)",
                 v_end - v_begin, nt, kNoAllocTiles);
   void *base = nullptr;
   RC(scratch_address(&base));
@@ -2589,3 +2599,6 @@ extern "C" void og_graph_free(og_graph *g) {
   }
   og::graph_delete(g);
 }
+
+// Kernel-level launchers of include/onegraph_kernels.h (same translation unit).
+#include "kernel_abi.cuh"

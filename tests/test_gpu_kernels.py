@@ -96,3 +96,129 @@ def test_compact_reports_small_capacity():
     assert rc == 10  # OG_E_DEVICE: the kernel's own capacity checks, nothing written past the end
     rc, *_ = run_compact(bits_d, 0, g.V, off_d, g.V, 1)
     assert rc == 10
+
+
+def _records(g):
+    r = g.records()
+    words_d = torch.from_numpy(np.ascontiguousarray(r["words"]).view(np.int32)).cuda()
+    rec = og.KRecords(words_d.data_ptr(), g.E, r["bpe"], r["bc"], r["wmin"], 0)
+    return rec, words_d
+
+
+def _frontier(g, density, seed):
+    """A compacted frontier built by the numpy model (independent of
+    og_k_compact): listed vertices, degree prefix, tile map, on the device."""
+    off = np.array(g.offsets)
+    rng = np.random.default_rng(seed)
+    words = np.packbits(rng.random(((g.V + 31) // 32) * 32) < density, bitorder="little").view(np.uint32)
+    lst, pref, tiles = compact_model(words, 0, g.V, off)
+    dev = [torch.from_numpy(a.view(np.int32 if a.dtype == np.uint32 else np.int64).copy()).cuda()
+           for a in (lst, pref, np.concatenate([tiles, [0]]).astype(np.uint32))]
+    return off, lst, pref, dev
+
+
+def _bits(vs, V):
+    b = np.zeros(((V + 31) // 32) * 32, bool)
+    b[vs] = True
+    return np.packbits(b, bitorder="little").view(np.uint32)
+
+
+@pytest.mark.parametrize("algo", [og.ALGO_BFS, og.ALGO_SSSP, og.ALGO_CC])
+def test_relax_launcher_matches_model(algo):
+    """og_k_relax on a caller-built frontier against a numpy model of one
+    round.  Listed vertices carry values no edge can lower, so the result of
+    the concurrent relax is the same as the sequential model's."""
+    g = og.Graph.rmat(13, 16, weighted=True, seed=5)
+    V = g.V
+    off, lst, pref, (lst_d, pref_d, tile_d) = _frontier(g, 0.05, 3)
+    pairs = np.array(g.edges)
+    rng = np.random.default_rng(11)
+    rec, words_d = _records(g)
+    if algo == og.ALGO_BFS:
+        value = rng.integers(1, 9, V).astype(np.uint32)
+        visited = rng.random(V) < 0.3
+        visited[lst] = True
+    elif algo == og.ALGO_SSSP:
+        value = np.where(rng.random(V) < 0.5, 0xFFFFFFFF, rng.integers(50, 200, V)).astype(np.uint32)
+        value[lst] = 40  # + weight >= 41 > 40: listed values cannot drop
+        visited = None
+    else:
+        value = rng.integers(100, 1000, V).astype(np.uint32)
+        value[lst] = 60
+        visited = None
+    want, nxt = value.copy(), np.zeros(V, bool)
+    vis = None if visited is None else visited.copy()
+    for u in lst:
+        for e in range(int(off[u]), int(off[u + 1])):
+            v, w = int(pairs[e, 0]), int(pairs[e, 1])
+            if algo == og.ALGO_BFS:
+                if not vis[v]:
+                    vis[v] = True
+                    nxt[v] = True
+                    want[v] = 7 + 1
+            else:
+                cand = int(value[u]) + (w if algo == og.ALGO_SSSP else 0)
+                if cand < want[v]:
+                    want[v] = cand
+                    nxt[v] = True
+    value_d = torch.from_numpy(value.view(np.int32).copy()).cuda()
+    next_d = torch.zeros((V + 31) // 32, dtype=torch.int32, device="cuda")
+    vis_d = None if visited is None else torch.from_numpy(_bits(np.nonzero(visited)[0], V).view(np.int32)).cuda()
+    off_d = torch.from_numpy(off.view(np.int64)).cuda()
+    rc = og.lib().og_k_relax(algo, dptr(lst_d), dptr(pref_d), dptr(tile_d), lst.size, int(pref[-1]), dptr(off_d),
+                             C.byref(rec), V, dptr(value_d), dptr(next_d), dptr(vis_d) if vis_d is not None else None,
+                             7, None)
+    assert rc == 0, og.lib().og_last_error()
+    np.testing.assert_array_equal(value_d.cpu().numpy().view(np.uint32), want)
+    np.testing.assert_array_equal(next_d.cpu().numpy().view(np.uint32), _bits(np.nonzero(nxt)[0], V))
+    if vis is not None:
+        np.testing.assert_array_equal(vis_d.cpu().numpy().view(np.uint32), _bits(np.nonzero(vis)[0], V))
+
+
+@pytest.mark.parametrize("weights", [True, False])
+def test_gather_launcher_matches_model(weights):
+    """og_k_gather: the edges at positions [b, e) of a compacted list, in list
+    order, unpacked from the records (the dynamic-region gather)."""
+    g = og.Graph.rmat(13, 16, weighted=True, seed=9)
+    off, lst, pref, (lst_d, pref_d, tile_d) = _frontier(g, 0.2, 4)
+    pairs = np.array(g.edges)
+    order = np.concatenate([np.arange(off[u], off[u + 1]) for u in lst]).astype(np.int64)
+    rec, words_d = _records(g)
+    off_d = torch.from_numpy(off.view(np.int64)).cuda()
+    total = int(pref[-1])
+    assert total > 4096 * 3
+    for b, e in [(0, total), (2048, min(total, 2048 * 5 + 17)), (4096 * 3, total)]:
+        col = torch.zeros(max(e - b, 1), dtype=torch.int32, device="cuda")
+        w = torch.zeros(max(e - b, 1), dtype=torch.int32, device="cuda") if weights else None
+        rc = og.lib().og_k_gather(dptr(lst_d), dptr(pref_d), dptr(tile_d), lst.size, total, dptr(off_d), C.byref(rec),
+                                  b, e, dptr(col), dptr(w) if weights else None, None)
+        assert rc == 0, og.lib().og_last_error()
+        np.testing.assert_array_equal(col.cpu().numpy()[:e - b].view(np.uint32), pairs[order[b:e], 0])
+        if weights:
+            np.testing.assert_array_equal(w.cpu().numpy()[:e - b].view(np.uint32), pairs[order[b:e], 1])
+    col = torch.zeros(8, dtype=torch.int32, device="cuda")
+    assert og.lib().og_k_gather(dptr(lst_d), dptr(pref_d), dptr(tile_d), lst.size, total, dptr(off_d), C.byref(rec),
+                                100, total, dptr(col), None, None) == 1  # start not on a 2048 boundary
+
+
+@pytest.mark.parametrize("which", [0, 1])
+def test_bounded_waits_give_up_and_report_timeout(which):
+    """The compaction look-back (0) and the persistent kernel's grid barrier
+    (1) on a signal nothing gives: the wait ends after its poll limit, the
+    call returns OG_E_TIMEOUT, and the GPU stays usable."""
+    rc = og.lib().og_k_wait_check(which, 2000)
+    assert rc == 6, og.lib().og_last_error()  # OG_E_TIMEOUT
+    assert b"gave up" in og.lib().og_last_error()
+    x = torch.arange(1000, device="cuda").sum().item()  # the context still works
+    assert x == 499500
+
+
+def test_link_probe_modes():
+    """og_link_probe: SM reads, one and two DMA copies of a page-locked buffer
+    all report a positive rate; an unpinned buffer is refused."""
+    buf = torch.empty(64 << 20, dtype=torch.uint8, pin_memory=True)
+    rates = [og.link_probe(buf, m, 2) for m in (0, 1, 2)]
+    assert all(r > 1.0 for r in rates), rates
+    plain = torch.empty(64 << 20, dtype=torch.uint8)
+    with pytest.raises(og.OGError):
+        og.link_probe(plain, 0, 1)

@@ -21,9 +21,12 @@ def _write(path, header, *arrays):
 
 
 def test_abi_exports_every_header_symbol():
-    hdr = open(os.path.join(ROOT, "include", "onegraph.h")).read()
-    declared = set(re.findall(r"^\s*(?:[a-z_ ]+\*?\s*)\b(og_[a-z0-9_]+)\s*\(", hdr, re.M))
+    declared = set()
+    for h in sorted(os.listdir(os.path.join(ROOT, "include"))):
+        hdr = open(os.path.join(ROOT, "include", h)).read()
+        declared |= set(re.findall(r"^\s*(?:[a-z_ ]+\*?\s*)\b(og_[a-z0-9_]+)\s*\(", hdr, re.M))
     assert "og_bfs" in declared and "og_engine_create" in declared
+    assert {"og_sssp_batch", "og_k_relax", "og_k_gather", "og_k_wait_check", "og_link_probe"} <= declared
     lib = og.lib()
     for name in sorted(declared):
         assert hasattr(lib, name), name
@@ -215,6 +218,20 @@ def test_cli_argument_errors(tmp_path):
     r = subprocess.run([_cli("CC_OneGraph"), "-f", str(tmp_path / "nope.csr")], capture_output=True,
                        text=True)
     assert r.returncode == 1 and "og_graph_load" in r.stderr
+
+
+def test_cli_reference_binary_names(tmp_path):
+    """The reference's makefiles name the SSSP and PageRank programs
+    sssp_OneGraph and PR_OneGrpah; both exist and behave as SSSP_OneGraph and
+    PR_OneGraph (a --type of another algorithm is refused the same way)."""
+    g = og.Graph.rmat(6, 4)
+    p = str(tmp_path / "g.csr")
+    g.save(p)
+    for alias, name, other in [("sssp_OneGraph", "SSSP_OneGraph", "bfs"), ("PR_OneGrpah", "PR_OneGraph", "cc")]:
+        assert os.access(_cli(alias), os.X_OK)
+        a = subprocess.run([_cli(alias), "--type", other, "-f", p], capture_output=True, text=True)
+        b = subprocess.run([_cli(name), "--type", other, "-f", p], capture_output=True, text=True)
+        assert a.returncode == b.returncode == 2 and "not this program" in a.stderr
 
 
 def test_bel_export_layout(tmp_path):
