@@ -51,7 +51,8 @@ int og_k_relax(int algo, const uint32_t *list, const uint64_t *pref, const uint3
 /* The dynamic-region gather (fillEdgeArrByMultiThread,
  * BFS/oneGraph_BFS/GraphMeta.h:471-506) on caller buffers: the edges at
  * positions [pos_begin, pos_end) of the compacted list's degree prefix
- * (pos_begin a multiple of 2048, pos_end <= total), unpacked in list order:
+ * (pos_begin a multiple of 2048; pos_end a multiple of 2048 or equal to
+ * total), unpacked in list order:
  * out_col[p - pos_begin] = column, out_w[p - pos_begin] = weight (out_w may
  * be NULL: columns only).  `rec` may point at page-locked host records
  * (a device view from cudaHostGetDevicePointer), as the engine gathers. */

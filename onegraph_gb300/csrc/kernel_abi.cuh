@@ -154,8 +154,11 @@ extern "C" int og_k_gather(const uint32_t *list, const uint64_t *pref, const uin
   int rc = list_args_ok(list, pref, tile, total, off, rec);
   if (rc != OG_OK) return rc;
   if (!out_col) return fail(OG_E_ARG, "null output");
-  if (pos_begin % kTile || pos_begin > pos_end || pos_end > total)
-    return fail(OG_E_ARG, "positions [%llu, %llu) of %llu (the start must be a multiple of %u)",
+  // the kernel finds a tile's last vertex through the tile map, so a range
+  // ends on a tile boundary or at the end of the list, as the engine's
+  // staging chunks do
+  if (pos_begin % kTile || pos_begin > pos_end || pos_end > total || (pos_end % kTile && pos_end != total))
+    return fail(OG_E_ARG, "positions [%llu, %llu) of %llu (both ends multiples of %u, or the end = total)",
                 (unsigned long long)pos_begin, (unsigned long long)pos_end, (unsigned long long)total, kTile);
   cudaGetLastError();
   cudaStream_t s = (cudaStream_t)stream;

@@ -187,7 +187,7 @@ def test_gather_launcher_matches_model(weights):
     off_d = torch.from_numpy(off.view(np.int64)).cuda()
     total = int(pref[-1])
     assert total > 4096 * 3
-    for b, e in [(0, total), (2048, min(total, 2048 * 5 + 17)), (4096 * 3, total)]:
+    for b, e in [(0, total), (2048, 2048 * 5), (4096 * 3, total)]:
         col = torch.zeros(max(e - b, 1), dtype=torch.int32, device="cuda")
         w = torch.zeros(max(e - b, 1), dtype=torch.int32, device="cuda") if weights else None
         rc = og.lib().og_k_gather(dptr(lst_d), dptr(pref_d), dptr(tile_d), lst.size, total, dptr(off_d), C.byref(rec),
@@ -199,6 +199,8 @@ def test_gather_launcher_matches_model(weights):
     col = torch.zeros(8, dtype=torch.int32, device="cuda")
     assert og.lib().og_k_gather(dptr(lst_d), dptr(pref_d), dptr(tile_d), lst.size, total, dptr(off_d), C.byref(rec),
                                 100, total, dptr(col), None, None) == 1  # start not on a 2048 boundary
+    assert og.lib().og_k_gather(dptr(lst_d), dptr(pref_d), dptr(tile_d), lst.size, total, dptr(off_d), C.byref(rec),
+                                0, 2048 + 17, dptr(col), None, None) == 1  # end inside a tile
 
 
 @pytest.mark.parametrize("which", [0, 1])
