@@ -505,6 +505,10 @@ def run_bfs_batch(args, rank, world, local):
                     direct=True, device=local)
     tune = eng.bfs_batch_tune(srcs[:64], reps=1) if args.tune else None
     batches = [srcs[64 * i:64 * (i + 1)] for i in range(4)]
+    # page-locked result buffers for the end-to-end legs, allocated before the
+    # warm-up (large page-locked allocations between queries slow the next ones)
+    host32 = og.pinned_empty((64, g.V), np.uint32)
+    host8 = og.pinned_empty((64, g.V), np.uint8)
     for i in range(args.warmup):
         eng.bfs_batch(batches[i % 4], out=False)
     sampler = ClockSampler(local)
@@ -534,7 +538,16 @@ def run_bfs_batch(args, rank, world, local):
         want = (int(reached.sum()), int(dd[reached].sum(dtype=np.uint64)))
         got = tuple(int(x) for x in cks[0][k])
         exact &= (want == got)
-    e2e_t, _ = timed(lambda k: eng.bfs_batch(batches[k % 4], out=None)[0], 1)
+    # end to end: every depth into page-locked host memory (the first call
+    # allocates the kept device depth matrix and is not timed)
+    eng.bfs_batch(batches[0], out=host32)
+    eng.bfs_batch_u8(batches[0], out=host8)
+    ne2e = max(2, min(args.steps, 4))
+    e2e_t, _ = timed(lambda k: eng.bfs_batch(batches[k % 4], out=host32)[1], ne2e)
+    e2e8_t, cl = timed(lambda k: eng.bfs_batch_u8(batches[k % 4], out=host8)[1], ne2e)
+    # the plain path end to end: one source's depths into page-locked memory
+    host1 = og.pinned_empty(g.V, np.uint32)
+    tpe, _ = timed(lambda k: eng.bfs(int(srcs[k]), out=host1), nplain)
     # the same batches with every level top-down (the bottom-up levels off)
     eng.set_param(og.PARAM_BFS_DIRECTION, og.BFS_TOP_DOWN)
     eng.bfs_batch(batches[0], out=False)  # captures the top-down graph
@@ -567,8 +580,14 @@ def run_bfs_batch(args, rank, world, local):
                           "ms_kernel": sum(x["ms_static"] for x in std) / len(std),
                           "link_gb": sum(x["link_bytes"] for x in std) / len(std) / 1e9,
                           "edges_examined": std[0]["edges_static"] + std[0]["edges_dynamic"]},
-        "e2e": {"value": 64 / e2e_t, "unit": "queries/s",
-                "h2d_bytes_per_step": int(256 + link), "d2h_bytes_per_step": 64 * 4 * g.V},
+        "e2e": {"value": 64 * ne2e / e2e_t, "unit": "queries/s",
+                "h2d_bytes_per_step": int(256 + link), "d2h_bytes_per_step": 64 * 4 * g.V,
+                "note": "u32 depths of every source into page-locked host memory"},
+        "e2e_u8": {"value": 64 * ne2e / e2e8_t, "unit": "queries/s", "d2h_bytes_per_step": 64 * g.V,
+                   "clamped_entries": int(sum(cl)),
+                   "note": "og_bfs_batch_u8: byte depths (0 unreached, 255 for depth >= 255)"},
+        "plain_e2e_queries_per_s": nplain / tpe,
+        "e2e_speedup_vs_plain_e2e": (64 * ne2e / e2e_t) / (nplain / tpe),
         "tune": tune, "clocks": clocks,
         "gpu_launches": sum(x["launches"] for x in stats),
         "setup_s": {"generate": gen_s},
@@ -1014,7 +1033,7 @@ def run_serving(args, rank, world, local):
     # allocated before any query: large page-locked allocations made between
     # queries have slowed the queries after them
     words = [graphs[gi].V for gi in gsel]
-    pool = torch.empty(int(sum(words)), dtype=torch.int32, pin_memory=True).numpy()
+    pool = og.pinned_empty(int(sum(words)), np.uint32)
     outs, o = [], 0
     for i, w in enumerate(words):
         v = pool[o:o + w]

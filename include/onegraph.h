@@ -289,8 +289,8 @@ int og_pr_l1_push(og_engine *e, float *out_rank, double damping, double tol, int
  * those streamed from host memory) serves all sources.  No reference
  * counterpart: the reference runs its sources one after another
  * (CalculateOpt.h:55-209).  Needs OG_CFG_BATCH.  out: n x V depths,
- * source-major, same convention as og_bfs, or NULL (the depth matrix then
- * needs n*V*4 device bytes outside the budget, only when out != NULL);
+ * source-major, same convention as og_bfs, or NULL (with out != NULL the
+ * engine keeps an n x V u32 device depth matrix outside the budget);
  * checks: 2n values, {vertices reached, sum of their depths} per source, or
  * NULL.  Depths are identical to n separate og_bfs calls. */
 int og_bfs_batch(og_engine *e, const uint32_t *srcs, int n, uint32_t *out,
@@ -325,6 +325,23 @@ int og_sssp_batch_join(og_engine *e, const uint32_t *srcs, const uint32_t *slots
 int og_sssp_batch_step(og_engine *e, uint32_t *pending, int *done, og_stats *st);
 int og_sssp_batch_checks(og_engine *e, uint32_t slots, uint64_t *out);
 int og_sssp_batch_fetch(og_engine *e, uint32_t slot, uint32_t *out);
+
+/* og_bfs_batch with byte depths, for hosts that fetch many depth arrays:
+ * out[s*V + v] = the depth when it is at most 254 (the source has 1), 0 when
+ * v is unreached, 255 when the depth is 255 or more (*clamped, when not
+ * NULL, receives the number of such entries; their exact depths come from
+ * og_bfs_batch).  A quarter of og_bfs_batch's bytes to copy to the host.
+ * Both keep their n x V device depth matrix (outside the budget) until the
+ * engine is destroyed, so repeated calls allocate nothing.  No reference
+ * counterpart. */
+int og_bfs_batch_u8(og_engine *e, const uint32_t *srcs, int n, uint8_t *out, uint64_t *clamped,
+                    uint64_t *checks, og_stats *st);
+
+/* Page-locked host memory for result buffers: device-to-host copies of
+ * results into it run at the host link's rate, where pageable memory is
+ * staged by the CUDA driver.  Free with og_host_free. */
+int og_host_alloc(uint64_t bytes, void **out);
+void og_host_free(void *p);
 
 /* og_bfs_batch runs all levels in one persistent cooperative kernel (static
  * edges from HBM, dynamic edges read straight from page-locked host memory);

@@ -174,6 +174,9 @@ SIGNATURES = [
     ("og_sssp_batch_step", C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_int), C.POINTER(Stats)]),
     ("og_sssp_batch_checks", C.c_int, [_P, C.c_uint32, _P]),
     ("og_sssp_batch_fetch", C.c_int, [_P, C.c_uint32, _P]),
+    ("og_bfs_batch_u8", C.c_int, [_P, _P, C.c_int, _P, C.POINTER(C.c_uint64), _P, C.POINTER(Stats)]),
+    ("og_host_alloc", C.c_int, [C.c_uint64, C.POINTER(_P)]),
+    ("og_host_free", None, [_P]),
     ("og_bfs_batch_tune", C.c_int, [_P, _P, C.c_int, C.c_int, C.POINTER(TuneResult)]),
     ("og_bfs_batch_set_config", C.c_int, [_P, C.c_int]),
     ("og_result_fetch", C.c_int, [_P, C.c_int, _P]),
@@ -521,6 +524,21 @@ class Engine:
         _check(lib().og_sssp_batch_fetch(self._h, slot, _ptr(o)), "og_sssp_batch_fetch")
         return o
 
+    def bfs_batch_u8(self, srcs, out=None, checks: bool = True):
+        """og_bfs_batch_u8: byte depths (0 unreached, 255 for depth >= 255).
+        Returns (depths n x V u8, clamped entries, checks or None)."""
+        s = np.ascontiguousarray(srcs, dtype=np.uint32)
+        n = s.size
+        o = np.empty((n, self.graph.V), np.uint8) if out is None else out
+        assert o.dtype == np.uint8 and o.size >= n * self.graph.V and o.flags.c_contiguous
+        ck = np.empty((n, 2), np.uint64) if checks else None
+        cl = C.c_uint64()
+        st = Stats()
+        _check(lib().og_bfs_batch_u8(self._h, _ptr(s), n, _ptr(o), C.byref(cl), _ptr(ck), C.byref(st)),
+               "og_bfs_batch_u8")
+        self.stats = st.as_dict()
+        return o, cl.value, ck
+
     def bfs_batch_tune(self, srcs, reps: int = 2) -> dict:
         s = np.ascontiguousarray(srcs, dtype=np.uint32)
         r = TuneResult()
@@ -713,3 +731,34 @@ def link_probe(host_buffer, mode: int, reps: int = 3) -> float:
     _check(lib().og_link_probe(C.c_void_p(host_buffer.data_ptr()), nbytes, mode, reps, C.byref(v)),
            "og_link_probe")
     return v.value
+
+
+class PinnedArray(np.ndarray):
+    """A numpy array in page-locked host memory from og_host_alloc, released
+    with the last array that views it."""
+
+
+class _PinnedBlock:
+    def __init__(self, nbytes):
+        p = _P()
+        _check(lib().og_host_alloc(max(int(nbytes), 1), C.byref(p)), "og_host_alloc")
+        self.ptr = p.value
+        self.nbytes = nbytes
+
+    def __del__(self):
+        try:
+            lib().og_host_free(C.c_void_p(self.ptr))
+        except Exception:
+            pass
+
+
+def pinned_empty(shape, dtype=np.uint32) -> np.ndarray:
+    """An uninitialised array in page-locked host memory (og_host_alloc), for
+    result buffers: results are copied into it at the host link's rate."""
+    dt = np.dtype(dtype)
+    count = int(np.prod(shape))
+    blk = _PinnedBlock(count * dt.itemsize)
+    raw = np.ctypeslib.as_array(C.cast(blk.ptr, C.POINTER(C.c_uint8)), (max(count * dt.itemsize, 1),))
+    a = raw[:count * dt.itemsize].view(dt).reshape(shape).view(PinnedArray)
+    a._block = blk  # the memory lives as long as any view of it
+    return a

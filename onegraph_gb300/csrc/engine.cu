@@ -122,6 +122,14 @@ struct og_engine {
   int graph_dopt = -1;
   bool graph_broken = false;
 
+  // batched BFS depth matrix (n x V u32, outside the budget), kept between
+  // calls that ask for depths; its byte form for og_bfs_batch_u8
+  uint32_t *depth_d = nullptr;
+  uint64_t depth_cap = 0;  // entries
+  uint8_t *depth8_d = nullptr;
+  uint64_t depth8_cap = 0;
+  unsigned long long *clamp_d = nullptr;
+
   // multi-source SSSP (og_sssp_batch, sssp_batch.cuh): sb_k sources per pass
   // in rows of sb_ks slots; its rows, pending masks and near masks share
   // `arena` with the batched BFS masks
@@ -183,6 +191,9 @@ void destroy(og_engine *e) {
   if (e->s_dyn) cudaStreamSynchronize(e->s_dyn);
   if (e->s_gat) cudaStreamSynchronize(e->s_gat);
   for (void *p : e->dallocs) cudaFree(p);
+  if (e->depth_d) cudaFree(e->depth_d);
+  if (e->depth8_d) cudaFree(e->depth8_d);
+  if (e->clamp_d) cudaFree(e->clamp_d);
   if (e->counts_h) cudaFreeHost(e->counts_h);
   if (e->hist_h) cudaFreeHost(e->hist_h);
   if (e->srcs_h) cudaFreeHost(e->srcs_h);
@@ -1173,6 +1184,21 @@ int run_min_dev(og_engine *e, int algo, uint32_t src, og_stats &st) {
 
 // ------------------------------------------------------------------ batched BFS
 
+// The n x V depth matrix (outside the budget), allocated on first use and
+// kept for later calls; it grows when a call needs more sources.
+int depth_matrix(og_engine *e, uint32_t n, uint32_t **out) {
+  const uint64_t need = (uint64_t)n * e->V;
+  if (need > e->depth_cap) {
+    if (e->depth_d) cudaFree(e->depth_d);
+    e->depth_d = nullptr;
+    e->depth_cap = 0;
+    CK(cudaMalloc(&e->depth_d, 4 * need));
+    e->depth_cap = need;
+  }
+  *out = e->depth_d;
+  return OG_OK;
+}
+
 int run_batch(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *out, uint64_t *checks,
               og_stats &st) {
   const uint64_t V = e->V;
@@ -1180,14 +1206,8 @@ int run_batch(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *out, uin
   unsigned long long *visited = e->bmask[0], *cur = e->bmask[1], *next = e->bmask[2];
   cudaStream_t s = e->s_main;
   uint32_t *depth_d = nullptr;
-  struct Free {
-    uint32_t *&p;
-    ~Free() {
-      if (p) cudaFree(p);
-    }
-  } free_depth{depth_d};
   if (out) {
-    CK(cudaMalloc(&depth_d, 4ull * n * V));
+    RC(depth_matrix(e, n, &depth_d));
     k_fill_u32<<<grid_for(n * V, e->sms), kThreads, 0, s>>>(depth_d, (uint64_t)n * V, (uint32_t)(V + 1));
     e->launches++;
   }
@@ -1393,20 +1413,29 @@ int run_persist_graph(og_engine *e, uint32_t n, int ci, bool *used_graph) {
   return enqueue_persist(e, n, ci, nullptr);
 }
 
-int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *out,
-                      uint64_t *checks, og_stats &st, int ci) {
+// Depths as bytes: depth d <= 254 as d, unreached (V + 1) as 0, d >= 255 as
+// 255 (counted in *clamped).
+__global__ void k_depth_bytes(const uint32_t *d, uint64_t n, uint32_t unreached, uint8_t *out,
+                              unsigned long long *clamped) {
+  unsigned long long c = 0;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
+    const uint32_t x = d[i];
+    out[i] = x == unreached ? 0 : (x >= 255u ? 255 : (uint8_t)x);
+    c += x != unreached && x >= 255u;
+  }
+  c = __reduce_add_sync(0xffffffffu, (uint32_t)c);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(clamped, c);
+}
+
+// out: V u32 depths per source (out_bytes 4) or byte depths (out_bytes 1).
+int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, void *out, int out_bytes,
+                      uint64_t *clamped, uint64_t *checks, og_stats &st, int ci) {
   const uint64_t V = e->V;
   memcpy(e->srcs_h, srcs, 4 * n);
   uint32_t *depth_d = nullptr;
-  struct Free {
-    uint32_t *&p;
-    ~Free() {
-      if (p) cudaFree(p);
-    }
-  } free_depth{depth_d};
   bool graph = false;
   if (out) {
-    CK(cudaMalloc(&depth_d, 4ull * n * V));
+    RC(depth_matrix(e, n, &depth_d));
     k_fill_u32<<<grid_for(n * V, e->sms), kThreads, 0, e->s_main>>>(depth_d, (uint64_t)n * V,
                                                                  (uint32_t)(V + 1));
     e->launches++;
@@ -1445,7 +1474,29 @@ int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *
       checks[2 * i] = r;
       checks[2 * i + 1] = d;
     }
-  if (out) CK(cudaMemcpy(out, depth_d, 4ull * n * V, cudaMemcpyDeviceToHost));
+  if (out && out_bytes == 4) {
+    CK(cudaMemcpyAsync(out, depth_d, 4ull * n * V, cudaMemcpyDeviceToHost, e->s_main));
+  } else if (out) {
+    const uint64_t need = (uint64_t)n * V;
+    if (need > e->depth8_cap) {
+      if (e->depth8_d) cudaFree(e->depth8_d);
+      e->depth8_d = nullptr;
+      e->depth8_cap = 0;
+      CK(cudaMalloc(&e->depth8_d, need));
+      e->depth8_cap = need;
+    }
+    if (!e->clamp_d) CK(cudaMalloc(&e->clamp_d, 8));
+    CK(cudaMemsetAsync(e->clamp_d, 0, 8, e->s_main));
+    k_depth_bytes<<<(unsigned)e->sms * 8, kThreads, 0, e->s_main>>>(depth_d, need, (uint32_t)(V + 1), e->depth8_d,
+                                                                  e->clamp_d);
+    e->launches++;
+    CK(cudaMemcpyAsync(out, e->depth8_d, need, cudaMemcpyDeviceToHost, e->s_main));
+    unsigned long long c = 0;
+    CK(cudaMemcpyAsync(&c, e->clamp_d, 8, cudaMemcpyDeviceToHost, e->s_main));
+    CK(cudaStreamSynchronize(e->s_main));
+    if (clamped) *clamped = c;
+  }
+  CK(cudaStreamSynchronize(e->s_main));
   e->last_algo = -1;
   return OG_OK;
 }
@@ -2228,13 +2279,16 @@ struct BatchCtx {
   uint32_t *out;
   uint64_t *checks;
   int mode;  // 0 persistent (tuned configuration), 1 host-driven levels, 2+k persistent config k
+  uint8_t *out8 = nullptr;  // og_bfs_batch_u8
+  uint64_t *clamped = nullptr;
 };
 
 int batch_body(og_engine *en, og_stats &s, void *cx) {
   const BatchCtx &b = *(BatchCtx *)cx;
   if (b.mode == 1) return run_batch(en, b.srcs, b.n, b.out, b.checks, s);
   const int ci = b.mode >= 2 ? b.mode - 2 : (en->tuned >= 0 ? en->tuned : 0);
-  return run_batch_persist(en, b.srcs, b.n, b.out, b.checks, s, ci);
+  if (b.out8) return run_batch_persist(en, b.srcs, b.n, b.out8, 1, b.clamped, b.checks, s, ci);
+  return run_batch_persist(en, b.srcs, b.n, b.out, 4, nullptr, b.checks, s, ci);
 }
 
 int batch_checks(og_engine *e, const uint32_t *srcs, int n) {
@@ -2252,6 +2306,26 @@ extern "C" int og_bfs_batch(og_engine *e, const uint32_t *srcs, int n, uint32_t 
   RC(batch_checks(e, srcs, n));
   BatchCtx c{srcs, (uint32_t)n, out, checks, (e->cfg.flags & OG_CFG_BATCH_LEVELS) ? 1 : 0};
   return query_common(e, OG_ALGO_BFS, st, nullptr, batch_body, &c);
+}
+
+extern "C" int og_bfs_batch_u8(og_engine *e, const uint32_t *srcs, int n, uint8_t *out, uint64_t *clamped,
+                               uint64_t *checks, og_stats *st) {
+  RC(batch_checks(e, srcs, n));
+  if (!out) return fail(OG_E_ARG, "og_bfs_batch_u8: null output");
+  BatchCtx c{srcs, (uint32_t)n, nullptr, checks, 0, out, clamped};
+  return query_common(e, OG_ALGO_BFS, st, nullptr, batch_body, &c);
+}
+
+extern "C" int og_host_alloc(uint64_t bytes, void **out) {
+  clear_error();
+  if (!out || bytes == 0) return fail(OG_E_ARG, "og_host_alloc: bad argument");
+  *out = nullptr;
+  CK(cudaHostAlloc(out, bytes, cudaHostAllocPortable));
+  return OG_OK;
+}
+
+extern "C" void og_host_free(void *p) {
+  if (p) cudaFreeHost(p);
 }
 
 extern "C" int og_bfs_batch_tune(og_engine *e, const uint32_t *srcs, int n, int reps,

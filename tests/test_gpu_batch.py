@@ -190,3 +190,41 @@ def test_batch_irregular_graph_directions():
         for i in (0, 1, 2):
             np.testing.assert_array_equal(oracle.normalise_bfs(single[i], V), oracle.bfs(off, col, int(srcs[i]))[0])
         e.close()
+
+
+def test_batch_byte_depths_and_pinned_outputs():
+    """og_bfs_batch_u8 equals og_bfs_batch's depths as bytes (0 unreached),
+    on repeated calls that reuse and then grow the kept depth matrix, into
+    pageable and page-locked (og_host_alloc) buffers."""
+    g = og.Graph.rmat(12, 16, seed=4)
+    rng = np.random.default_rng(2)
+    T = max(int(0.3 * g.E), 3 * 2048)
+    e = og.Engine(g, batch=True, direct=True, advisek=0.5, budget=budget_for(g, T, og.CFG_BATCH | og.CFG_DIRECT))
+    for n in (7, 3, 64, 64):
+        srcs = rng.integers(0, g.V, n).astype(np.uint32)
+        want, ck = e.bfs_batch(srcs)
+        pinned = og.pinned_empty((n, g.V), np.uint32)
+        got, ck2 = e.bfs_batch(srcs, out=pinned)
+        np.testing.assert_array_equal(got, want)
+        np.testing.assert_array_equal(ck2, ck)
+        b8, clamped, ck8 = e.bfs_batch_u8(srcs, out=og.pinned_empty((n, g.V), np.uint8))
+        assert clamped == 0
+        np.testing.assert_array_equal(ck8, ck)
+        np.testing.assert_array_equal(b8, np.where(want == g.V + 1, 0, want).astype(np.uint8))
+        b8p, _, _ = e.bfs_batch_u8(srcs)
+        np.testing.assert_array_equal(b8p, b8)
+    e.close()
+
+
+def test_batch_byte_depths_clamp_long_paths():
+    """A path of 300 vertices: depths of 255 and more become 255 and are counted."""
+    V = 300
+    col = np.arange(1, V, dtype=np.uint32)  # 0 -> 1 -> ... -> 299, vertex 299 has no edge
+    off = np.concatenate([np.arange(V, dtype=np.uint64), [V - 1]]).astype(np.uint64)
+    g = og.Graph.from_arrays(off, col)
+    e = og.Engine(g, batch=True, budget=1 << 28)
+    want, _ = e.bfs_batch([0])
+    b8, clamped, _ = e.bfs_batch_u8([0])
+    assert want[0, 299] == 300 and clamped == (want[0] >= 255).sum() == 46
+    np.testing.assert_array_equal(b8[0], np.minimum(want[0], 255).astype(np.uint8))
+    e.close()
