@@ -58,13 +58,18 @@ def parse_args():
     ap.add_argument("--sources", type=int, default=32)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--workload", default="serving",
-                    choices=["serving", "sssp-oom", "cc-oom", "bfs-batch", "bfs-resident", "pr-precision"],
+                    choices=["serving", "sssp-oom", "sssp-batch", "cc-oom", "bfs-batch", "bfs-resident",
+                             "pr-precision"],
                     help="serving (default: the served-queries/s headline), or another measured configuration")
     ap.add_argument("--tune", type=int, default=1, help="bfs-batch: run the autotuner first")
     ap.add_argument("--serving-scales", default="22,24,26,27")
     ap.add_argument("--serving-budget-gib", type=float, default=24.0)
     ap.add_argument("--requests", type=int, default=400)
     ap.add_argument("--rate", type=float, default=2000.0)
+    ap.add_argument("--serving-legs", default="all", choices=["all", "served"],
+                    help="serving: 'served' runs only the warm-up and the timed passes (for launch lists)")
+    ap.add_argument("--sssp-sources", type=int, default=8,
+                    help="sssp-batch: sources per multi-source pass (1..32)")
     ap.add_argument("--workers", type=int, default=4)
     ap.add_argument("--delta", type=float, default=None,
                     help="SSSP near/far split width (default: the engine's, (wmin + wmax) / 16; "
@@ -477,6 +482,75 @@ def run_ours(args, rank, world, local):
     }
     print(json.dumps(line), flush=True)
     eng.close()
+
+
+def run_sssp_batch(args, rank, world, local):
+    """Multi-source SSSP: one step is one og_sssp_batch pass of --sssp-sources
+    seeded sources (seed 3) on the weighted R-MAT graph, against the plain
+    per-query og_sssp on an engine with the same budget and no batch state;
+    per-source distances are checked equal to the plain path's."""
+    import torch
+    import onegraph_gb300 as og
+    torch.cuda.set_device(local)
+    g, gen_s = make_graph(args.scale)
+    k = max(1, min(32, args.sssp_sources))
+    srcs = np.array(pick_sources(g.degrees(), max(k, 32)), np.uint32)
+    budget = int(args.budget_gib * GIB)
+    eng = og.Engine(g, budget=budget, advisek=args.advisek, direct=True, sssp_batch=k, device=local)
+    batches = [srcs[(i * k) % len(srcs):][:k] for i in range(4)]
+    batches = [b if b.size == k else srcs[:k] for b in batches]
+    for i in range(args.warmup):
+        eng.sssp_batch(batches[i % 4], out=False)
+    sampler = ClockSampler(local)
+    sampler.start()
+    stats = []
+
+    def one(i):
+        _, ck = eng.sssp_batch(batches[i % 4], out=False)
+        stats.append(dict(eng.stats))
+        return ck
+    t, cks = timed(one, args.steps)
+    clocks = sampler.stop()
+    value = k * args.steps / t
+    plan = eng.plan
+    eng.close()
+    plain = og.Engine(g, budget=budget, advisek=args.advisek, direct=True, device=local)
+    plain.sssp(int(srcs[0]), out=False)
+    exact = True
+    pst = []
+
+    def p1(i):
+        plain.sssp(int(batches[0][i]), out=False)
+        pst.append(dict(plain.stats))
+        return plain.checksum(og.ALGO_SSSP)
+    tp, pck = timed(p1, k)
+    for i in range(k):
+        exact &= tuple(int(x) for x in cks[0][i]) == pck[i]
+    plain_plan = plain.plan
+    plain.close()
+    link = sum(x["link_bytes"] for x in stats) / len(stats)
+    kms = sum(x["ms_dynamic"] for x in stats) / len(stats)
+    peak = h2d_peak_gbs()
+    ach = link / (kms / 1e3) / 1e9 if kms else 0.0
+    line = {
+        "metric": "queries/s", "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": dict(config_dict(args, g), workload="sssp-batch-rmat%d-%gGiB-%dsrc" % (args.scale,
+                                                                                       args.budget_gib, k)),
+        "plain_queries_per_s": k / tp, "speedup_vs_plain": value / (k / tp), "bit_exact_vs_single_source": exact,
+        "per_pass": {"rounds": stats[0]["iterations"], "link_gb": link / 1e9, "ms_relax": kms,
+                     "ms_compact": sum(x["ms_compact"] for x in stats) / len(stats)},
+        "plain_per_query": {"link_gb": sum(x["link_bytes"] for x in pst) / len(pst) / 1e9},
+        "plan": {"static_edges": plan["static_edges"], "plain_static_edges": plain_plan["static_edges"]},
+        "roofline": {"bound": "host-link", "kernel": "k_sb_relax_pair (multi-source SSSP relax)", "achieved": ach,
+                     "peak": peak, "unit": "GB/s", "frac": ach / peak if peak else None, "traffic": None,
+                     "peak_source": "highest of the link probes measured in this run (og_link_probe)",
+                     "link_probes": dict(LINK_PEAKS)},
+        "clocks": clocks, "gpu_launches": sum(x["launches"] for x in stats), "setup_s": {"generate": gen_s},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 def timed(fn, steps):
@@ -1069,6 +1143,13 @@ def run_serving(args, rank, world, local):
     st1 = srv.stats()
     t_srv = replicas.max_over_ranks(sum(spans) / 1e3, world)
     value = replicas.whole_job_rate(args.steps * n, world, t_srv)
+    if args.serving_legs == "served":
+        srv.close()
+        if rank == 0:
+            print(json.dumps({"metric": "served queries/s", "value": value, "unit": "queries/s", "n_gpus": world,
+                              "steps": args.steps, "warmup": args.warmup, "legs": "served passes only",
+                              "gpu_launches": st1["launches"] - st0["launches"], "clocks": clocks}), flush=True)
+        return
     # end to end: the same passes with every result in page-locked host memory
     e2e_passes = max(1, min(args.steps, 3))
     e2e_spans = []
@@ -1227,6 +1308,8 @@ def main():
         run_bfs_resident(args, rank, world, local)
     elif args.workload == "cc-oom":
         run_cc_oom(args, rank, world, local)
+    elif args.workload == "sssp-batch":
+        run_sssp_batch(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 
