@@ -68,6 +68,9 @@ def parse_args():
     ap.add_argument("--rate", type=float, default=2000.0)
     ap.add_argument("--serving-legs", default="all", choices=["all", "served"],
                     help="serving: 'served' runs only the warm-up and the timed passes (for launch lists)")
+    ap.add_argument("--bfs-direction", default="auto", choices=["auto", "top-down"],
+                    help="bfs-resident: direction of the timed plain queries (top-down: every level "
+                         "from the frontier, the relax kernel on every edge)")
     ap.add_argument("--sssp-sources", type=int, default=8,
                     help="sssp-batch: sources per multi-source pass (1..32)")
     ap.add_argument("--workers", type=int, default=4)
@@ -768,6 +771,8 @@ def run_bfs_resident(args, rank, world, local):
     deg = g.degrees()
     src = int(np.argmax(deg))
     eng = og.Engine(g, budget=int(args.budget_gib * GIB), advisek=1.0, batch=True, device=local)
+    if args.bfs_direction == "top-down":
+        eng.set_param(og.PARAM_BFS_DIRECTION, og.BFS_TOP_DOWN)
     for _ in range(args.warmup):
         eng.bfs(src, out=False)
         eng.bfs_batch([src], out=False)
@@ -808,11 +813,24 @@ def run_bfs_resident(args, rank, world, local):
         eng.bfs(src, out=False)
         tstats.append(dict(eng.stats))
     ttd, _ = timed(topdown, args.steps)
-    eng.set_param(og.PARAM_BFS_DIRECTION, og.BFS_AUTO)
     td_ms = sum(x["ms_static"] + x["ms_dynamic"] for x in tstats)
     td_ex = sum(x["edges_static"] + x["edges_dynamic"] for x in tstats)
     td_fv = sum(x["frontier_sum"] for x in tstats)
     td_gbs = ((eb + 4) * td_ex + 20 * td_fv) / (td_ms / 1e3) / 1e9 if td_ms else 0.0
+    # the relax kernel alone: the same top-down queries with the engine's stamp
+    # timer around every relax launch (og_stats.ms_relax)
+    eng.set_param(og.PARAM_RELAX_TIMER, 1)
+    eng.bfs(src, out=False)
+    rstats = []
+    for _ in range(args.steps):
+        eng.bfs(src, out=False)
+        rstats.append(dict(eng.stats))
+    eng.set_param(og.PARAM_RELAX_TIMER, 0)
+    eng.set_param(og.PARAM_BFS_DIRECTION, og.BFS_AUTO if args.bfs_direction == "auto" else og.BFS_TOP_DOWN)
+    rx_ms = sum(x["ms_relax"] for x in rstats)
+    rx_ex = sum(x["edges_static"] + x["edges_dynamic"] for x in rstats)
+    rx_fv = sum(x["frontier_sum"] for x in rstats)
+    rx_gbs = ((eb + 4) * rx_ex + 20 * rx_fv) / (rx_ms / 1e3) / 1e9 if rx_ms else 0.0
     c0 = time.perf_counter()
     oracle.bfs(np.array(g.offsets), np.array(g.columns), src)
     cpu_s = time.perf_counter() - c0
@@ -829,7 +847,12 @@ def run_bfs_resident(args, rank, world, local):
                           "gteps": comp_edges * args.steps / ttd / 1e9,
                           "edges_examined_per_query": td_ex / args.steps,
                           "achieved_gbs": td_gbs, "frac": td_gbs / peaks["hbm_gbs"],
-                          "graph_vs_l2": "packed records %.0f MB, L2 129 MB" % (g.E * eb / 1e6)},
+                          "graph_vs_l2": "packed records %.0f MB, L2 129 MB" % (g.E * eb / 1e6),
+                          "relax_kernel": {"kernel": "k_lbs_pair_dev<SrcP<false>,SrcP<false>,BfsOp>",
+                                           "ms_per_query": rx_ms / args.steps, "achieved_gbs": rx_gbs,
+                                           "frac": rx_gbs / peaks["hbm_gbs"],
+                                           "timing": "globaltimer stamps around every relax launch"}},
+        "direction": args.bfs_direction,
         "bit_exact_vs_runCPUBFS": exact, "levels": stats[0]["iterations"],
         "edges_examined_per_query": examined / args.steps,
         "roofline": {"bound": "hbm", "kernel": "device-driven level loop (compaction, top-down k_lbs_pair_dev, "
