@@ -665,6 +665,7 @@ def run_bfs_batch(args, rank, world, local):
                    "note": "og_bfs_batch_u8: byte depths (0 unreached, 255 for depth >= 255)"},
         "plain_e2e_queries_per_s": nplain / tpe,
         "e2e_speedup_vs_plain_e2e": (64 * ne2e / e2e_t) / (nplain / tpe),
+        "e2e_u8_speedup_vs_plain_e2e": (64 * ne2e / e2e8_t) / (nplain / tpe),
         "tune": tune, "clocks": clocks,
         "gpu_launches": sum(x["launches"] for x in stats),
         "setup_s": {"generate": gen_s},
@@ -987,6 +988,10 @@ def serving_graph(sc: int):
 # direct mode keeps no staging buffers, so the whole edge share is static
 SERVING_ADVISEK = 1.0
 ALGO_BFS, ALGO_SSSP, ALGO_PR = 0, 1, 3  # og_algo values (the reference arm loads no engine)
+# host-link sectors read by one PageRank pull launch over its algorithmic link
+# bytes, measured with ncu on R-MAT 22 directed under a 256 MiB budget:
+# 2,025,677 sectors of 32 B for 64.2 MB of records per iteration
+PR_PULL_LINK_TRAFFIC_RATIO = 1.010
 
 
 def serving_requests(degrees, n, rate, seed=4):
@@ -1302,16 +1307,22 @@ def serving_rooflines(og, g, budget, slots, srcs, gsel, algos, gi, h2d, local):
     pr = dict(e.stats)
     e.close()
 
-    def roof(kernel, st, unit_note):
+    def roof(kernel, st, unit_note, traffic_ratio=None):
         ach = st["link_bytes"] / (st["ms_dynamic"] / 1e3) / 1e9 if st["ms_dynamic"] else 0.0
+        per_launch = st["link_bytes"] / max(st["iterations"], 1)
         return {"bound": "host-link", "kernel": kernel, "achieved": ach, "peak": h2d, "unit": "GB/s",
-                "frac": ach / h2d if h2d else None, "traffic": None,
+                "frac": ach / h2d if h2d else None,
+                "traffic": per_launch * traffic_ratio if traffic_ratio else None,
+                "traffic_note": ("host-link bytes per launch: this launch's algorithmic bytes x %.3f, the "
+                                 "sysmem-sector / algorithmic ratio ncu measured for the same kernel on R-MAT 22 "
+                                 "under a 256 MiB budget" % traffic_ratio)
+                if traffic_ratio else None,
                 "peak_source": "highest of the link probes measured in this run (og_link_probe)", "link_probes": dict(LINK_PEAKS), "bytes_per_launch_note": unit_note,
                 "link_gb": st["link_bytes"] / 1e9, "kernel_ms": st["ms_dynamic"]}
     a = roof("k_sb_relax_pair<SrcP<true>,SrcP<true>,%d> (multi-source SSSP relax, R-MAT %d pass of %d sources)"
              % (4 if slots <= 4 else 8, 27, len(ss)), sb, "packed 33-bit records of the dynamic region")
     b = roof("k_pr_pull_pair<SrcP<false>,SrcP<false>> (PageRank pull, R-MAT 27, 5 iterations)", pr,
-             "packed records of the dynamic region per iteration")
+             "packed records of the dynamic region per iteration", PR_PULL_LINK_TRAFFIC_RATIO)
     dom = a if sb["ms_dynamic"] >= pr["ms_dynamic"] else b
     return {"dominant": dom, "all": [a, b]}
 

@@ -54,6 +54,7 @@ struct PersistArgs {
   unsigned int *bar;          // [0] arrivals, [1] generation
   unsigned long long *hist;   // [kMaxBatchLevels][64] first-reached counts
   uint32_t *depth;            // n x V depths or null
+  uint8_t *depth8;            // n x V byte depths (0 unreached, 255 for 255 and more) or null
   uint32_t n_src;
   uint32_t *err;
   uint32_t *levels;           // number of expanded levels (out)
@@ -605,6 +606,10 @@ __device__ __forceinline__ void level_tally(const PersistArgs &a, SH &sh, unsign
       if (a.depth)
         for (unsigned long long b = x; b; b &= b - 1)
           a.depth[(uint64_t)(__ffsll((long long)b) - 1) * a.V + (g + j) * 32 + lane] = level + 1;
+      if (a.depth8)
+        for (unsigned long long b = x; b; b &= b - 1)
+          a.depth8[(uint64_t)(__ffsll((long long)b) - 1) * a.V + (g + j) * 32 + lane] =
+              (uint8_t)min(level + 1, 255u);
     }
 #pragma unroll
     for (int j = 0; j < kTallyWords; j++) {

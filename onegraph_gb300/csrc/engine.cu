@@ -128,7 +128,6 @@ struct og_engine {
   uint64_t depth_cap = 0;  // entries
   uint8_t *depth8_d = nullptr;
   uint64_t depth8_cap = 0;
-  unsigned long long *clamp_d = nullptr;
 
   // multi-source SSSP (og_sssp_batch, sssp_batch.cuh): sb_k sources per pass
   // in rows of sb_ks slots; its rows, pending masks and near masks share
@@ -193,7 +192,6 @@ void destroy(og_engine *e) {
   for (void *p : e->dallocs) cudaFree(p);
   if (e->depth_d) cudaFree(e->depth_d);
   if (e->depth8_d) cudaFree(e->depth8_d);
-  if (e->clamp_d) cudaFree(e->clamp_d);
   if (e->counts_h) cudaFreeHost(e->counts_h);
   if (e->hist_h) cudaFreeHost(e->hist_h);
   if (e->srcs_h) cudaFreeHost(e->srcs_h);
@@ -1326,7 +1324,7 @@ uint32_t batch_dopt(const og_engine *e) {
 // Enqueues one whole batch on s_main: clear state, upload the sources from the
 // page-locked buffer, seed, run every level in one cooperative kernel, copy
 // the per-level counts and the status words back to page-locked memory.
-int enqueue_persist(og_engine *e, uint32_t n, int ci, uint32_t *depth_d) {
+int enqueue_persist(og_engine *e, uint32_t n, int ci, uint32_t *depth_d, uint8_t *depth8_d = nullptr) {
   const uint64_t V = e->V;
   cudaStream_t s = e->s_main;
   for (int i = 0; i < 3; i++) CK(cudaMemsetAsync(e->bmask[i], 0, 8 * (V + 1), s));
@@ -1337,7 +1335,7 @@ int enqueue_persist(og_engine *e, uint32_t n, int ci, uint32_t *depth_d) {
   CK(cudaMemsetAsync(e->hist_d, 0, 8ull * kMaxBatchLevels * 64, s));
   CK(cudaMemsetAsync(e->bar_d, 0, 64, s));
   CK(cudaMemcpyAsync(e->srcs_d, e->srcs_h, 4 * n, cudaMemcpyHostToDevice, s));
-  k_batch_init<<<1, 64, 0, s>>>(e->srcs_d, n, e->bmask[0], e->bmask[1], e->bm[0], depth_d, V);
+  k_batch_init<<<1, 64, 0, s>>>(e->srcs_d, n, e->bmask[0], e->bmask[1], e->bm[0], depth_d, V, depth8_d);
   e->launches++;
   PersistArgs a;
   a.V = e->V;
@@ -1362,6 +1360,7 @@ int enqueue_persist(og_engine *e, uint32_t n, int ci, uint32_t *depth_d) {
   a.bar = e->bar_d;
   a.hist = e->hist_d;
   a.depth = depth_d;
+  a.depth8 = depth8_d;
   a.n_src = n;
   a.err = e->bar_d + 2;
   a.levels = e->bar_d + 3;
@@ -1413,37 +1412,35 @@ int run_persist_graph(og_engine *e, uint32_t n, int ci, bool *used_graph) {
   return enqueue_persist(e, n, ci, nullptr);
 }
 
-// Depths as bytes: depth d <= 254 as d, unreached (V + 1) as 0, d >= 255 as
-// 255 (counted in *clamped).
-__global__ void k_depth_bytes(const uint32_t *d, uint64_t n, uint32_t unreached, uint8_t *out,
-                              unsigned long long *clamped) {
-  unsigned long long c = 0;
-  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += (uint64_t)gridDim.x * blockDim.x) {
-    const uint32_t x = d[i];
-    out[i] = x == unreached ? 0 : (x >= 255u ? 255 : (uint8_t)x);
-    c += x != unreached && x >= 255u;
-  }
-  c = __reduce_add_sync(0xffffffffu, (uint32_t)c);
-  if ((threadIdx.x & 31) == 0 && c) atomicAdd(clamped, c);
-}
-
 // out: V u32 depths per source (out_bytes 4) or byte depths (out_bytes 1).
 int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, void *out, int out_bytes,
                       uint64_t *clamped, uint64_t *checks, og_stats &st, int ci) {
   const uint64_t V = e->V;
   memcpy(e->srcs_h, srcs, 4 * n);
   uint32_t *depth_d = nullptr;
+  uint8_t *depth8_d = nullptr;
   bool graph = false;
-  if (out) {
+  if (out && out_bytes == 4) {
     RC(depth_matrix(e, n, &depth_d));
     k_fill_u32<<<grid_for(n * V, e->sms), kThreads, 0, e->s_main>>>(depth_d, (uint64_t)n * V,
                                                                  (uint32_t)(V + 1));
     e->launches++;
+  } else if (out) {  // byte depths, written by the kernel itself (0 = unreached)
+    const uint64_t need = (uint64_t)n * V;
+    if (need > e->depth8_cap) {
+      if (e->depth8_d) cudaFree(e->depth8_d);
+      e->depth8_d = nullptr;
+      e->depth8_cap = 0;
+      CK(cudaMalloc(&e->depth8_d, need));
+      e->depth8_cap = need;
+    }
+    depth8_d = e->depth8_d;
+    CK(cudaMemsetAsync(depth8_d, 0, need, e->s_main));
   }
   // events outside any captured graph: they bracket the whole batch on s_main
   CK(cudaEventRecord(e->t_s0, e->s_main));
   if (out) {
-    RC(enqueue_persist(e, n, ci, depth_d));
+    RC(enqueue_persist(e, n, ci, depth_d, depth8_d));
   } else {
     RC(run_persist_graph(e, n, ci, &graph));
   }
@@ -1477,24 +1474,13 @@ int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, void *out,
   if (out && out_bytes == 4) {
     CK(cudaMemcpyAsync(out, depth_d, 4ull * n * V, cudaMemcpyDeviceToHost, e->s_main));
   } else if (out) {
-    const uint64_t need = (uint64_t)n * V;
-    if (need > e->depth8_cap) {
-      if (e->depth8_d) cudaFree(e->depth8_d);
-      e->depth8_d = nullptr;
-      e->depth8_cap = 0;
-      CK(cudaMalloc(&e->depth8_d, need));
-      e->depth8_cap = need;
+    CK(cudaMemcpyAsync(out, depth8_d, (uint64_t)n * V, cudaMemcpyDeviceToHost, e->s_main));
+    if (clamped) {  // entries at depth L + 1 >= 255, from the per-level counts
+      uint64_t c = 0;
+      for (uint32_t L = 254; L <= levels && L < kMaxBatchLevels; L++)
+        for (uint32_t i = 0; i < n; i++) c += e->hist_h[(uint64_t)L * 64 + i];
+      *clamped = c;
     }
-    if (!e->clamp_d) CK(cudaMalloc(&e->clamp_d, 8));
-    CK(cudaMemsetAsync(e->clamp_d, 0, 8, e->s_main));
-    k_depth_bytes<<<(unsigned)e->sms * 8, kThreads, 0, e->s_main>>>(depth_d, need, (uint32_t)(V + 1), e->depth8_d,
-                                                                  e->clamp_d);
-    e->launches++;
-    CK(cudaMemcpyAsync(out, e->depth8_d, need, cudaMemcpyDeviceToHost, e->s_main));
-    unsigned long long c = 0;
-    CK(cudaMemcpyAsync(&c, e->clamp_d, 8, cudaMemcpyDeviceToHost, e->s_main));
-    CK(cudaStreamSynchronize(e->s_main));
-    if (clamped) *clamped = c;
   }
   CK(cudaStreamSynchronize(e->s_main));
   e->last_algo = -1;

@@ -832,7 +832,7 @@ struct PushOp {
 
 __global__ void k_batch_init(const uint32_t *srcs, uint32_t n, unsigned long long *visited,
                              unsigned long long *cur, uint32_t *cur_any, uint32_t *depth,
-                             uint64_t V) {
+                             uint64_t V, uint8_t *depth8 = nullptr) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const uint32_t v = srcs[i];
@@ -840,6 +840,7 @@ __global__ void k_batch_init(const uint32_t *srcs, uint32_t n, unsigned long lon
   atomicOr(cur + v, 1ull << i);
   atomicOr(cur_any + (v >> 5), 1u << (v & 31));
   if (depth) depth[(uint64_t)i * V + v] = 1u;
+  if (depth8) depth8[(uint64_t)i * V + v] = 1u;
 }
 
 // Per-source count of the vertices first reached at this level (hist[s]),
