@@ -319,7 +319,10 @@ int og_sssp_batch(og_engine *e, const uint32_t *srcs, int n, uint32_t *out, uint
  * left.  og_sssp_batch_checks writes {reached, sum of distances} of every
  * slot in the mask `slots` to out[2 s], out[2 s + 1] (64 values).
  * og_sssp_batch_fetch copies slot `slot`'s V distances to host memory.
- * No reference counterpart. */
+ * Any other query on the engine (og_bfs, og_pr_l1, og_sssp_batch, ...) ends
+ * the session: it reuses the session's state, and the session calls then
+ * return OG_E_STATE until the next og_sssp_batch_begin.  No reference
+ * counterpart. */
 int og_sssp_batch_begin(og_engine *e);
 int og_sssp_batch_join(og_engine *e, const uint32_t *srcs, const uint32_t *slots, int n);
 int og_sssp_batch_step(og_engine *e, uint32_t *pending, int *done, og_stats *st);

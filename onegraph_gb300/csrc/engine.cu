@@ -143,6 +143,7 @@ struct og_engine {
   uint32_t sb_delta = 0;  // OG_PARAM_SSSP_BATCH_DELTA: near/far width of the batch (0: every round)
   bool sb_advance = false;
   uint32_t sb_dirty = 0;  // slots whose distances are not all unreached
+  bool sb_session = false;  // a session is open: no other query ran since og_sssp_batch_begin
 
   og_engine *parent = nullptr;  // set on clones: resident state belongs to the parent
   int clones = 0;               // live clones of this engine
@@ -290,9 +291,14 @@ int create_query_state(og_engine *e) {
       if (e->wbytes) RC(dalloc(e, (char **)&e->stage_w[b], P.chunk_edges * e->wbytes));
     }
   }
+  // PageRank's contributions and sums live in the batch arena when the
+  // engine has one (a context runs one computation at a time)
+  const bool arena = e->batch_enabled || e->sb_k;
   if (e->pr_enabled) {
-    RC(dalloc(e, &e->contrib_d, V + 1));
-    RC(dalloc(e, &e->sum_d, V + 1));
+    if (!arena) {
+      RC(dalloc(e, &e->contrib_d, V + 1));
+      RC(dalloc(e, &e->sum_d, V + 1));
+    }
     e->pr_tiles = e->tile_cap[0] + e->tile_cap[1];
     RC(dalloc(e, &e->cont_d, e->pr_tiles));
     RC(dalloc(e, &e->carry_d, e->pr_tiles));
@@ -301,12 +307,17 @@ int create_query_state(og_engine *e) {
     RC(dalloc(e, &e->part_d, e->part_n));
     RC(dalloc(e, &e->l1_d, 1));
   }
-  if (e->batch_enabled || e->sb_k) {
-    // one arena for the batched BFS masks (24 B per vertex) and the
-    // multi-source SSSP rows (4 sb_ks + 8 B per vertex): a context runs one
-    // at a time
-    const uint64_t per = std::max<uint64_t>(e->batch_enabled ? 24 : 0, e->sb_k ? 4ull * e->sb_ks + 8 : 0);
+  if (arena) {
+    // one arena for the batched BFS masks (24 B per vertex), the
+    // multi-source SSSP rows (4 sb_ks + 8 B per vertex) and PageRank's
+    // contributions and sums (8 B per vertex): a context runs one at a time
+    uint64_t per = std::max<uint64_t>(e->batch_enabled ? 24 : 0, e->sb_k ? 4ull * e->sb_ks + 8 : 0);
+    if (e->pr_enabled) per = std::max<uint64_t>(per, 8);
     RC(dalloc(e, &e->arena, per * (V + 1)));
+    if (e->pr_enabled) {
+      e->contrib_d = (float *)e->arena;
+      e->sum_d = e->contrib_d + (V + 1);
+    }
     if (e->batch_enabled)
       for (int i = 0; i < 3; i++) e->bmask[i] = (unsigned long long *)e->arena + (uint64_t)i * (V + 1);
     if (e->sb_k) {
@@ -1548,6 +1559,7 @@ int sb_reset(og_engine *e) {
   e->sb_far_min = 0xffffffffu;
   e->sb_advance = false;
   e->sb_dirty = 0;
+  e->sb_session = true;
   CK(cudaGetLastError());
   return OG_OK;
 }
@@ -1954,6 +1966,9 @@ int query_common(og_engine *e, int algo, og_stats *st_out, void *out,
     og_stats st;
     memset(&st, 0, sizeof st);
     e->launches = 0;
+    // every query reuses the frontier bitmaps, lists and arena of an open
+    // multi-source SSSP session: the session ends here
+    e->sb_session = false;
     const double t0 = now_ms();
     RC(body(e, st, ctx));
     st.launches = e->launches;
@@ -2383,6 +2398,9 @@ extern "C" int og_sssp_batch_begin(og_engine *e) {
 extern "C" int og_sssp_batch_join(og_engine *e, const uint32_t *srcs, const uint32_t *slots, int n) {
   if (!e || n < 0 || (n && (!srcs || !slots))) return fail(OG_E_ARG, "og_sssp_batch_join: bad argument");
   if (!e->sb_k) return fail(OG_E_STATE, "engine created without OG_CFG_SSSP_BATCH");
+  if (!e->sb_session)
+    return fail(OG_E_STATE, "no open multi-source SSSP session: og_sssp_batch_begin first (any other query on "
+                            "the engine ends a session)");
   return guarded([&]() -> int {
     clear_error();
     CK(cudaSetDevice(e->dev));
@@ -2393,6 +2411,9 @@ extern "C" int og_sssp_batch_join(og_engine *e, const uint32_t *srcs, const uint
 extern "C" int og_sssp_batch_step(og_engine *e, uint32_t *pending, int *done, og_stats *st) {
   if (!e || !pending || !done) return fail(OG_E_ARG, "og_sssp_batch_step: null argument");
   if (!e->sb_k) return fail(OG_E_STATE, "engine created without OG_CFG_SSSP_BATCH");
+  if (!e->sb_session)
+    return fail(OG_E_STATE, "no open multi-source SSSP session: og_sssp_batch_begin first (any other query on "
+                            "the engine ends a session)");
   return guarded([&]() -> int {
     clear_error();
     CK(cudaSetDevice(e->dev));
@@ -2419,6 +2440,9 @@ extern "C" int og_sssp_batch_step(og_engine *e, uint32_t *pending, int *done, og
 extern "C" int og_sssp_batch_checks(og_engine *e, uint32_t slots, uint64_t *out) {
   if (!e || !out) return fail(OG_E_ARG, "og_sssp_batch_checks: null argument");
   if (!e->sb_k) return fail(OG_E_STATE, "engine created without OG_CFG_SSSP_BATCH");
+  if (!e->sb_session)
+    return fail(OG_E_STATE, "no open multi-source SSSP session: og_sssp_batch_begin first (any other query on "
+                            "the engine ends a session)");
   return guarded([&]() -> int {
     clear_error();
     CK(cudaSetDevice(e->dev));
@@ -2429,6 +2453,9 @@ extern "C" int og_sssp_batch_checks(og_engine *e, uint32_t slots, uint64_t *out)
 extern "C" int og_sssp_batch_fetch(og_engine *e, uint32_t slot, uint32_t *out) {
   if (!e || !out) return fail(OG_E_ARG, "og_sssp_batch_fetch: null argument");
   if (!e->sb_k) return fail(OG_E_STATE, "engine created without OG_CFG_SSSP_BATCH");
+  if (!e->sb_session)
+    return fail(OG_E_STATE, "no open multi-source SSSP session: og_sssp_batch_begin first (any other query on "
+                            "the engine ends a session)");
   return guarded([&]() -> int {
     clear_error();
     CK(cudaSetDevice(e->dev));

@@ -183,13 +183,21 @@ uint64_t engine_vertex_bytes(int kind, uint32_t flags) {
   // bitmaps are counted in engine_fixed_bytes.  PageRank adds contrib f32,
   // sum f32 and outdeg u32.
   uint64_t b = 8 + 4 + 4 + 8;
-  if (kind == OG_GRAPH_PR || (flags & OG_CFG_PR)) b += 12;
+  const bool pr = kind == OG_GRAPH_PR || (flags & OG_CFG_PR);
   // batched BFS: visited, frontier, next u64 masks; multi-source SSSP: a row
-  // of distances, a pending-slot mask and a near-slot mask per list entry.
-  // The two share one allocation (a query context runs one at a time).
-  uint64_t batch = (flags & OG_CFG_BATCH) ? 24 : 0;
-  if (sb_sources(flags)) batch = std::max<uint64_t>(batch, 4ull * sb_row_slots(sb_sources(flags)) + 8);
-  return b + batch;
+  // of distances, a pending-slot mask and a near-slot mask per list entry;
+  // PageRank: contributions and sums (f32).  With either batch form they
+  // share one allocation (a query context runs one computation at a time);
+  // PageRank's out-degrees (u32) are resident.
+  const bool arena = (flags & OG_CFG_BATCH) || sb_sources(flags);
+  uint64_t shared = (flags & OG_CFG_BATCH) ? 24 : 0;
+  if (sb_sources(flags)) shared = std::max<uint64_t>(shared, 4ull * sb_row_slots(sb_sources(flags)) + 8);
+  if (pr) {
+    b += 4;
+    if (arena) shared = std::max<uint64_t>(shared, 8);
+    else b += 8;
+  }
+  return b + shared;
 }
 
 uint64_t engine_fixed_bytes(uint32_t V, uint64_t E, uint32_t flags) {

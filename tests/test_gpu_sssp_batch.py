@@ -154,3 +154,35 @@ def test_sssp_batch_rejects_bad_use():
     gu = og.Graph.rmat(9, 8)
     with pytest.raises(og.OGError):
         og.Engine(gu, sssp_batch=4, budget=1 << 30)  # unweighted graph
+
+
+def test_other_queries_end_a_session_and_share_its_memory():
+    """PageRank, batched BFS and multi-source SSSP share one per-vertex
+    allocation on an engine that has them all: each gives its own correct
+    result when they alternate, and a query between the rounds of an open
+    session ends the session (OG_E_STATE) instead of corrupting it."""
+    g = og.Graph.rmat(11, 16, weighted=True, seed=13)
+    off, pairs = np.array(g.offsets), np.array(g.edges)
+    col = np.ascontiguousarray(pairs[:, 0])
+    deg = np.diff(off.astype(np.int64)).astype(np.uint32)
+    T = max(int(0.3 * g.E), 3 * 2048)
+    flags = og.CFG_SSSP_BATCH(8) | og.CFG_BATCH | og.CFG_PR | og.CFG_DIRECT
+    e = og.Engine(g, sssp_batch=8, batch=True, pagerank=True, direct=True, advisek=0.5,
+                  budget=budget_for(g, T, flags))
+    ref, _, _ = oracle.pr_l1(off, col, deg, 0.85, 1e-6, 200)
+    srcs = sources(g, 8, 3)
+    want = np.stack([e.sssp(int(s)) for s in srcs])
+    for _ in range(2):
+        r = e.pr_l1(0.85, 1e-6, 200)
+        assert np.abs(r.astype(np.float64) - ref).max() < 1e-6
+        dist, _ = e.sssp_batch(srcs)
+        np.testing.assert_array_equal(dist, want)
+        depths, _ = e.bfs_batch(srcs)
+        np.testing.assert_array_equal(depths[0], e.bfs(int(srcs[0])))
+    e.sssp_batch_begin()
+    e.sssp_batch_join(srcs[:2], [0, 1])
+    e.sssp_batch_step()
+    e.bfs(int(srcs[0]))
+    with pytest.raises(og.OGError):
+        e.sssp_batch_step()
+    e.close()
