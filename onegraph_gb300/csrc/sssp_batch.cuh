@@ -30,12 +30,14 @@
 namespace og {
 
 constexpr uint32_t kSbMaxSources = 32;
-#ifndef SB_U
-#define SB_U 3
-#endif
-#ifndef SB_MINB
-#define SB_MINB 4
-#endif
+// CTAs per SM of the relax (at most 64 registers at 256 threads) and
+// positions in flight per thread, chosen with -Xptxas -v (no spills) and by
+// measurement on R-MAT 23 and 27: 5 CTAs per SM at 48 registers ran 30-40 %
+// slower, and a 58 % shared-memory carve-out (3 CTAs per SM, more L1) 5-8 %
+// slower, than 4 CTAs per SM with the CUDA driver's carve-out.
+constexpr int kSbMinBlocks = 4;
+template <int KS>
+constexpr int sb_positions_in_flight() { return 3; }
 
 struct SbCompactArgs {
   uint32_t *bits;        // bitmap scanned this round: the active set, or the waiting set
@@ -304,7 +306,7 @@ __device__ __forceinline__ void sb_tile(const LbsArgs &a, const Src &src, const 
                                         LbsShared<uint2> &sh, uint64_t k) {
   static_assert(KS == 4 || KS == 8 || KS == 16 || KS == 32, "row width");
   constexpr int C = KS < 8 ? KS : 8;  // slots per chunk
-  constexpr int U = SB_U;  // positions in flight per thread
+  constexpr int U = sb_positions_in_flight<KS>();  // positions in flight per thread
   const uint64_t pos0 = k * kTile;
   if (pos0 >= a.pos_end) return;
   const uint32_t tlen = (uint32_t)(min(pos0 + kTile, a.pos_end) - pos0);
@@ -390,14 +392,14 @@ __device__ __forceinline__ void sb_tile(const LbsArgs &a, const Src &src, const 
 }
 
 template <class Src, int KS>
-__global__ void __launch_bounds__(kThreads, SB_MINB) k_sb_relax(LbsArgs a, Src src, SbOp op) {
+__global__ void __launch_bounds__(kThreads, kSbMinBlocks) k_sb_relax(LbsArgs a, Src src, SbOp op) {
   __shared__ LbsShared<uint2> sh;
   sb_tile<Src, KS>(a, src, op, sh, a.pos_begin / kTile + blockIdx.x);
 }
 
 // Both regions in one launch, tiles interleaved as in k_lbs_pair.
 template <class Src0, class Src1, int KS>
-__global__ void __launch_bounds__(kThreads, SB_MINB) k_sb_relax_pair(LbsArgs a0, Src0 s0, LbsArgs a1, Src1 s1, SbOp op,
+__global__ void __launch_bounds__(kThreads, kSbMinBlocks) k_sb_relax_pair(LbsArgs a0, Src0 s0, LbsArgs a1, Src1 s1, SbOp op,
                                                             uint64_t n0, uint64_t n) {
   __shared__ LbsShared<uint2> sh;
   const uint64_t b = blockIdx.x;
