@@ -127,14 +127,19 @@ __device__ __forceinline__ void dev_prepare(MinOp<W> &, const uint32_t *) {}
 // control kernel that sets *go), not by a grid stride: a CTA that becomes
 // resident late only finds fewer tiles, so the fixed grid may exceed what
 // fits on the GPU at once without a second wave doing half the work.
+template <class Src>
+constexpr int dev_min_blocks() {  // CTAs per SM the register budget is sized for
+  return std::is_same<Src, SrcP<true>>::value ? 4 : 5;
+}
 template <class Src0, class Src1, class Op>
-__global__ void __launch_bounds__(kThreads) k_lbs_pair_dev(LbsArgs a0, Src0 s0, LbsArgs a1, Src1 s1, Op op,
+__global__ void __launch_bounds__(kThreads, dev_min_blocks<Src0>()) k_lbs_pair_dev(LbsArgs a0, Src0 s0, LbsArgs a1, Src1 s1, Op op,
                                                            const Counts *counts, const uint32_t *go,
                                                            const uint32_t *level, uint32_t *tile_next) {
   static_assert(std::is_same<Src0, Src1>::value, "one tile body for both regions");
   if (*go == 0u) return;
-  __shared__ LbsShared<typename Op::Val> sh;
+  __shared__ LbsSh<Op> sh;
   __shared__ uint32_t s_b[2];
+  __shared__ PairTile s_pt[2];
   // Both regions' arguments live in shared memory and one tile body serves
   // both: kept in registers across the tile loop they cost 98 registers per
   // thread (2 CTAs per SM) against 46 for the one-tile-per-CTA kernel.
@@ -158,16 +163,22 @@ __global__ void __launch_bounds__(kThreads) k_lbs_pair_dev(LbsArgs a0, Src0 s0, 
   __syncthreads();
   const uint64_t n0 = (s_a[0].total + kTile - 1) / kTile, n1 = (s_a[1].total + kTile - 1) / kTile;
   const uint64_t n = n0 + n1;
-  // the next tile's index is fetched while the current tile runs (two slots)
-  if (threadIdx.x == 0) s_b[0] = atomicAdd(tile_next, 1u);
+  // The next tile's ticket (and its region split, by thread 0) is fetched
+  // while the current tile runs (two slots).
+  if (threadIdx.x == 0) {
+    s_b[0] = atomicAdd(tile_next, 1u);
+    s_pt[0] = pair_split(s_b[0], n0, n);
+  }
   __syncthreads();
   for (int slot = 0;; slot ^= 1) {
-    const uint64_t b = s_b[slot];
-    if (b >= n) break;
-    if (threadIdx.x == 0) s_b[slot ^ 1] = atomicAdd(tile_next, 1u);
-    const uint64_t lo = b * n0 / n, hi = (b + 1) * n0 / n;
-    const int r = hi > lo ? 0 : 1;
-    lbs_tile(s_a[r], s_s[r], op, sh, r == 0 ? lo : b - hi);
+    if (s_b[slot] >= n) break;
+    const PairTile pt = s_pt[slot];
+    if (threadIdx.x == 0) {
+      const uint32_t nb = atomicAdd(tile_next, 1u);
+      s_b[slot ^ 1] = nb;
+      if (nb < n) s_pt[slot ^ 1] = pair_split(nb, n0, n);
+    }
+    lbs_tile(s_a[pt.r], s_s[pt.r], op, sh, pt.t);
     __syncthreads();  // the tile tables are rebuilt and the next slot is read after this
   }
 }

@@ -396,10 +396,19 @@ struct LbsArgs {
 // uint8_t / uint16_t / uint32_t).  The static region and the page-locked host
 // copy hold bit-packed records (SrcP).  A source yields one edge as a u32
 // column or a {column, weight} pair; BFS, CC and PageRank read columns only.
+//
+// The LBS tiles address a vertex's edges through a cursor: cur(e) is the
+// cursor of edge index e, at(c, x) the edge x positions after cursor c.
+// Unpacked sources use the edge index itself; packed records use the bit
+// offset, so a position costs a 32-bit multiply and a 64-bit add instead of a
+// 64-bit multiply.  Cursor arithmetic is modulo 2^64 (a vertex that starts
+// after the tile's first position has a "negative" base).
 struct SrcU {
   using Item = uint32_t;
   const uint32_t *col;
   __device__ __forceinline__ Item load(uint64_t i) const { return col[i]; }
+  __device__ __forceinline__ uint64_t cur(uint64_t e) const { return e; }
+  __device__ __forceinline__ Item at(uint64_t c, uint32_t x) const { return col[c + x]; }
 };
 template <class W>
 struct SrcW {
@@ -407,6 +416,8 @@ struct SrcW {
   const uint32_t *col;
   const W *w;
   __device__ __forceinline__ Item load(uint64_t i) const { return make_uint2(col[i], (uint32_t)w[i]); }
+  __device__ __forceinline__ uint64_t cur(uint64_t e) const { return e; }
+  __device__ __forceinline__ Item at(uint64_t c, uint32_t x) const { return load(c + x); }
 };
 // Bit-packed records (the page-locked host copy and the static region):
 // record i holds bits [i*bpe, (i+1)*bpe) of `words`, column in the low bc
@@ -439,6 +450,27 @@ struct SrcP {
       return col;
     }
   }
+  __device__ __forceinline__ uint64_t cur(uint64_t e) const { return e * bpe; }
+  // x below 2^26 / bpe (a tile's positions).  The column is the low bc <= 32
+  // bits of the record, so two words and one funnel shift hold it whatever
+  // bpe is; a weight above it may need a third word.
+  __device__ __forceinline__ Item at(uint64_t c, uint32_t x) const {
+    const uint64_t b = c + x * bpe;
+    const uint32_t *w = words + (b >> 5);
+    const uint32_t r = (uint32_t)b & 31u;
+    const uint32_t lo = w[0], hi = w[1];
+    const uint32_t f = __funnelshift_r(lo, hi, r);
+    const uint32_t col = bc >= 32 ? f : f & ((1u << bc) - 1u);
+    if constexpr (kW) {
+      const uint32_t bw = bpe - bc;
+      uint64_t y = (((uint64_t)hi << 32) | lo) >> r;
+      if (r + bpe > 64) y |= (uint64_t)w[2] << (64 - r);
+      const uint64_t wt = bw == 0 ? 0 : (y >> bc) & ((bw >= 32) ? 0xffffffffull : ((1ull << bw) - 1));
+      return make_uint2(col, (uint32_t)wt + wmin);
+    } else {
+      return col;
+    }
+  }
 };
 
 struct DstU {
@@ -455,12 +487,14 @@ struct DstW {
   }
 };
 
-template <class Val>
+// Per-tile tables.  kVal = false (BFS reads no source value) drops the value
+// table, 8 KB of shared memory per CTA that L1 gets instead.
+template <class Val, bool kVal = true>
 struct LbsShared {
   uint32_t rs[kTile + 2];      // tile-relative start of each local vertex
-  unsigned long long cb[kTile + 1];  // edge index of tile position 0 for the vertex
-  Val val[kTile + 1];          // source value of each local vertex
-  unsigned short map[kTile];   // tile position -> local vertex
+  unsigned long long cb[kTile + 1];  // source cursor of tile position 0 for the vertex
+  Val val[kVal ? kTile + 1 : 1];     // source value of each local vertex
+  alignas(16) unsigned short map[kTile];  // tile position -> local vertex
 };
 
 // Shared tables of a PageRank pull tile, aliased by phase to fit 6 CTAs per
@@ -477,7 +511,7 @@ struct PrShared {
     float tot[kTile + 1];
   };
   uint32_t val[1];  // no source value in PageRank (lbs_setup<false> never writes it)
-  unsigned short map[kTile];
+  alignas(16) unsigned short map[kTile];
 };
 
 // Optional op hooks, detected at compile time:
@@ -494,11 +528,39 @@ struct HasProbeVal : std::false_type {};
 template <class T>
 struct HasProbeVal<T, std::void_t<decltype(T::kProbeVal)>> : std::true_type {};
 
-// Builds the local-vertex tables of tile k; returns the local count (0 on error).
-// Sh is LbsShared<Val> or PrShared.
-template <bool kNeedVal, class Op, class Sh>
-__device__ __forceinline__ uint32_t lbs_setup(const LbsArgs &a, const Op &op, Sh &sh,
+// Block-wide exclusive scan of u32 counts; returns the block total.
+__device__ __forceinline__ uint32_t block_scan_u32(uint32_t cnt, uint32_t &ex) {
+  __shared__ uint32_t s_w[kThreads / 32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  uint32_t ic = cnt;
+#pragma unroll
+  for (int d = 1; d < 32; d <<= 1) {
+    const uint32_t c = __shfl_up_sync(0xffffffffu, ic, d);
+    if (lane >= d) ic += c;
+  }
+  if (lane == 31) s_w[warp] = ic;
+  __syncthreads();
+  uint32_t wp = 0, tot = 0;
+#pragma unroll
+  for (int w = 0; w < kThreads / 32; w++) {
+    const uint32_t x = s_w[w];
+    wp += w < warp ? x : 0u;
+    tot += x;
+  }
+  ex = wp + ic - cnt;
+  return tot;
+}
+
+// Builds the local-vertex tables of tile k; returns the local count (0 on
+// error).  Sh is LbsShared<Val, *> or PrShared.  cb[j] is the source cursor
+// (Src::cur) of tile position 0 for local vertex j, so position x of the tile
+// reads src.at(cb[map[x]], x).  Every local vertex's edge indices in the tile
+// are checked against edge_bound here, once per vertex; a tile with one out
+// of bounds sets kErrEdgeIndex and relaxes nothing.
+template <bool kNeedVal, class Src, class Op, class Sh>
+__device__ __forceinline__ uint32_t lbs_setup(const LbsArgs &a, const Src &src, const Op &op, Sh &sh,
                                               uint64_t k, uint64_t pos0, uint32_t &i0_out) {
+  __shared__ uint32_t s_bad;
   const uint64_t ntiles_total = (a.total + kTile - 1) / kTile;
   const uint32_t i0 = a.tile_first[k];
   const uint32_t i1 = (k + 1 < ntiles_total) ? a.tile_first[k + 1] : a.n - 1;
@@ -507,78 +569,87 @@ __device__ __forceinline__ uint32_t lbs_setup(const LbsArgs &a, const Op &op, Sh
     if (threadIdx.x == 0) atomicOr(a.err, kErrTileMap);
     return 0;
   }
+  const uint64_t pend = min(pos0 + kTile, a.pos_end);
   const uint32_t nl = i1 - i0 + 1;
+  if (threadIdx.x == 0) s_bad = 0;
+  // zero the position map: 2048 u16 = one 16-byte store per thread
+  static_assert(kTile * sizeof(unsigned short) == kThreads * sizeof(uint4), "map zeroing");
+  reinterpret_cast<uint4 *>(sh.map)[threadIdx.x] = make_uint4(0u, 0u, 0u, 0u);
+  __syncthreads();
+  bool bad = false;
+#pragma unroll 1
   for (uint32_t j = threadIdx.x; j < nl; j += kThreads) {
     const uint32_t i = i0 + j;
     const uint32_t v = a.list[i];
-    const uint64_t p = a.pref[i];
-    sh.rs[j] = p > pos0 ? (uint32_t)min(p - pos0, (uint64_t)kTile) : 0u;
-    const uint64_t src = a.off ? a.off[v] - p : (0ull - a.stage_base);
-    sh.cb[j] = src + pos0;
+    const uint64_t p = a.pref[i], pn = a.pref[i + 1];
+    const uint32_t r = p > pos0 ? (uint32_t)min(p - pos0, (uint64_t)kTile) : 0u;
+    sh.rs[j] = r;
+    const uint64_t e0 = (a.off ? a.off[v] - p : (0ull - a.stage_base)) + pos0;  // edge index of position 0
+    sh.cb[j] = src.cur(e0);
+    const uint64_t q1 = min(pn, pend);  // end of the vertex's positions in this tile
+    if (q1 > pos0 + r) {
+      const uint64_t first = e0 + r, last = e0 + (q1 - pos0) - 1;
+      if (pn < p || last < first || last >= a.edge_bound) bad = true;
+    }
     if constexpr (HasListVal<Op>::value) sh.val[j] = op.list_val(v, a.list + i);
     else if constexpr (kNeedVal) sh.val[j] = op.src_val(v);
+    // head flag.  Compacted lists hold no zero-degree vertex, so for j >= 1
+    // the starts are distinct and strictly increasing (rs[0] = 0).
+    if (j >= 1 && r < kTile) sh.map[r] = (unsigned short)1;
   }
-  for (uint32_t x = threadIdx.x; x < kTile; x += kThreads) sh.map[x] = 0;
-  __syncthreads();
-  // Head flags.  Compacted lists hold no zero-degree vertex, so for j >= 1 the
-  // starts rs[j] are distinct and strictly increasing (rs[0] = 0).
-  for (uint32_t j = 1 + threadIdx.x; j < nl; j += kThreads) {
-    const uint32_t r = sh.rs[j];
-    if (r < kTile) sh.map[r] = (unsigned short)1;
+  if (bad) {
+    s_bad = 1;
+    atomicOr(a.err, kErrEdgeIndex);
   }
   __syncthreads();
-  // inclusive scan of the head flags (blocked: thread t owns 8 positions)
+  // inclusive scan of the head flags (blocked: thread t owns positions 8t..8t+7)
   {
-    uint32_t f[kItems];
+    uint4 m = reinterpret_cast<const uint4 *>(sh.map)[threadIdx.x];
+    uint32_t f[kItems] = {m.x & 0xffffu, m.x >> 16, m.y & 0xffffu, m.y >> 16,
+                          m.z & 0xffffu, m.z >> 16, m.w & 0xffffu, m.w >> 16};
     uint32_t s = 0;
 #pragma unroll
-    for (int i = 0; i < (int)kItems; i++) {
-      f[i] = sh.map[threadIdx.x * kItems + i];
-      s += f[i];
-    }
-    uint32_t ex, tot;
-    uint64_t ex64, tot64;
-    block_scan_pair(s, 0, ex, ex64, tot, tot64);
-    uint32_t run = ex;
+    for (int i = 0; i < (int)kItems; i++) s += f[i];
+    uint32_t run;
+    block_scan_u32(s, run);
 #pragma unroll
     for (int i = 0; i < (int)kItems; i++) {
       run += f[i];
-      sh.map[threadIdx.x * kItems + i] = (unsigned short)run;
+      f[i] = run;
     }
+    m = make_uint4(f[0] | (f[1] << 16), f[2] | (f[3] << 16), f[4] | (f[5] << 16), f[6] | (f[7] << 16));
+    reinterpret_cast<uint4 *>(sh.map)[threadIdx.x] = m;
   }
   __syncthreads();
-  return nl;
+  return s_bad ? 0u : nl;
 }
+
+// Shared tables of an LBS relax tile for Op.
+template <class Op>
+using LbsSh = LbsShared<typename Op::Val, Op::kNeedVal || HasListVal<Op>::value>;
 
 // One LBS tile (kTile positions starting at tile k of the list) of a CTA.
 template <class Src, class Op>
-__device__ __forceinline__ void lbs_tile(const LbsArgs &a, const Src &src, const Op &op,
-                                         LbsShared<typename Op::Val> &sh, uint64_t k) {
+__device__ __forceinline__ void lbs_tile(const LbsArgs &a, const Src &src, const Op &op, LbsSh<Op> &sh,
+                                         uint64_t k) {
   const uint64_t pos0 = k * kTile;
   if (pos0 >= a.pos_end) return;
-  const uint64_t pend = min(pos0 + kTile, a.pos_end);
+  const uint32_t tlen = (uint32_t)(min(pos0 + kTile, a.pos_end) - pos0);
   uint32_t i0;
-  const uint32_t nl = lbs_setup<Op::kNeedVal>(a, op, sh, k, pos0, i0);
+  const uint32_t nl = lbs_setup<Op::kNeedVal>(a, src, op, sh, k, pos0, i0);
   if (nl == 0) return;
   // All eight loads are issued before the first relax, so each thread keeps
   // eight edge reads in flight (the host-link gather is latency bound).
   typename Src::Item ev[kItems];
   uint32_t lv[kItems];
-  uint32_t okmask = 0;
 #pragma unroll
   for (int it = 0; it < (int)kItems; it++) {
     const uint32_t x = it * kThreads + threadIdx.x;
     lv[it] = 0;
-    if (pos0 + x < pend) {
+    if (x < tlen) {
       const uint32_t l = sh.map[x];
-      const uint64_t idx = sh.cb[l] + x;
       lv[it] = l;
-      if (idx < a.edge_bound) {
-        ev[it] = src.load(idx);
-        okmask |= 1u << it;
-      } else {
-        atomicOr(a.err, kErrEdgeIndex);
-      }
+      ev[it] = src.at(sh.cb[l], x);
     }
   }
   // Probe phase: every target's current state is read before the first
@@ -589,13 +660,13 @@ __device__ __forceinline__ void lbs_tile(const LbsArgs &a, const Src &src, const
   typename Op::Probe pr[kItems];
 #pragma unroll
   for (int it = 0; it < (int)kItems; it++)
-    if (okmask & (1u << it)) {
+    if (it * kThreads + threadIdx.x < tlen) {
       if constexpr (HasProbeVal<Op>::value) pr[it] = op.probe_v(ev[it], sh.val[lv[it]]);
       else pr[it] = op.probe(ev[it]);
     }
 #pragma unroll
   for (int it = 0; it < (int)kItems; it++) {
-    if (okmask & (1u << it))
+    if (it * kThreads + threadIdx.x < tlen)
       op.relax(ev[it], Op::kNeedVal ? sh.val[lv[it]] : typename Op::Val{},
                pos0 + it * kThreads + threadIdx.x, pr[it]);
   }
@@ -603,7 +674,7 @@ __device__ __forceinline__ void lbs_tile(const LbsArgs &a, const Src &src, const
 
 template <class Src, class Op>
 __global__ void __launch_bounds__(kThreads) k_lbs(LbsArgs a, Src src, Op op) {
-  __shared__ LbsShared<typename Op::Val> sh;
+  __shared__ LbsSh<Op> sh;
   lbs_tile(a, src, op, sh, a.pos_begin / kTile + blockIdx.x);
 }
 
@@ -614,14 +685,32 @@ __global__ void __launch_bounds__(kThreads) k_lbs(LbsArgs a, Src src, Op op) {
 // rest keep the link busy.  CTA b is a static tile iff
 // floor((b + 1) n0 / n) > floor(b n0 / n); its tile index is floor(b n0 / n),
 // else b - floor((b + 1) n0 / n) among the dynamic tiles.
+struct PairTile {
+  unsigned long long t;  // tile index within its region
+  uint32_t r;            // 0: static region, 1: dynamic region
+};
+__device__ __forceinline__ PairTile pair_split(uint64_t b, uint64_t n0, uint64_t n) {
+  if (n0 == n) return PairTile{b, 0u};
+  if (n0 == 0) return PairTile{b, 1u};
+  const uint64_t lo = b * n0 / n, hi = (b + 1) * n0 / n;
+  return hi > lo ? PairTile{lo, 0u} : PairTile{b - hi, 1u};
+}
+// The split of this CTA, computed once: a 64-bit division is a long
+// instruction sequence, so thread 0 runs it and the CTA reads the result.
+__device__ __forceinline__ PairTile pair_split_cta(uint64_t n0, uint64_t n) {
+  __shared__ PairTile s_pt;
+  if (threadIdx.x == 0) s_pt = pair_split(blockIdx.x, n0, n);
+  __syncthreads();
+  return s_pt;
+}
+
 template <class Src0, class Src1, class Op>
 __global__ void __launch_bounds__(kThreads) k_lbs_pair(LbsArgs a0, Src0 s0, LbsArgs a1, Src1 s1, Op op,
                                                        uint64_t n0, uint64_t n) {
-  __shared__ LbsShared<typename Op::Val> sh;
-  const uint64_t b = blockIdx.x;
-  const uint64_t lo = b * n0 / n, hi = (b + 1) * n0 / n;
-  if (hi > lo) lbs_tile(a0, s0, op, sh, a0.pos_begin / kTile + lo);
-  else lbs_tile(a1, s1, op, sh, a1.pos_begin / kTile + (b - hi));
+  __shared__ LbsSh<Op> sh;
+  const PairTile pt = pair_split_cta(n0, n);
+  if (pt.r == 0) lbs_tile(a0, s0, op, sh, a0.pos_begin / kTile + pt.t);
+  else lbs_tile(a1, s1, op, sh, a1.pos_begin / kTile + pt.t);
 }
 
 template <int MULT>
@@ -717,11 +806,15 @@ struct BfsOp {
   uint32_t *visited, *next, *depth, *err;
   uint32_t V, newdepth;
   __device__ uint32_t src_val(uint32_t) const { return 0; }
-  using Probe = uint32_t;  // the target's visited word
+  // The target's visited word, read through L1: bits are only ever set
+  // during a launch (and global data cached in L1 does not outlive the
+  // launch), so a stale word lacks bits at most and costs an extra atomic,
+  // never a wrong result.  Hub vertices' words are read over and over.
+  using Probe = uint32_t;
   template <class Edge>
   __device__ __forceinline__ Probe probe(Edge e) const {
     const uint32_t v = edge_dst(e);
-    return v < V ? __ldcg(visited + (v >> 5)) : 0u;
+    return v < V ? visited[v >> 5] : 0u;
   }
   template <class Edge>
   __device__ __forceinline__ void relax(Edge e, uint32_t, uint64_t, Probe p) const {
@@ -747,11 +840,14 @@ struct MinOp {
   uint32_t *value, *next, *err;
   uint32_t V;
   __device__ uint32_t src_val(uint32_t v) const { return __ldcg(value + v); }
-  using Probe = uint32_t;  // the target's current value
+  // The target's current value, read through L1: values only decrease during
+  // a launch, so a stale value is too large at most and costs an extra
+  // atomicMin, never a wrong result.
+  using Probe = uint32_t;
   template <class Edge>
   __device__ __forceinline__ Probe probe(Edge e) const {
     const uint32_t v = edge_dst(e);
-    return v < V ? __ldcg(value + v) : 0u;
+    return v < V ? value[v] : 0u;
   }
   template <class Edge>
   __device__ __forceinline__ void relax(Edge e, uint32_t sv, uint64_t, Probe p) const {
@@ -782,11 +878,11 @@ struct BatchOp {
   uint32_t *err;
   uint32_t V;
   __device__ Val src_val(uint32_t v) const { return __ldcg(cur + v); }
-  using Probe = unsigned long long;  // the target's visited mask
+  using Probe = unsigned long long;  // the target's visited mask (through L1, as BfsOp)
   template <class Edge>
   __device__ __forceinline__ Probe probe(Edge e) const {
     const uint32_t v = edge_dst(e);
-    return v < V ? __ldcg(visited + v) : ~0ull;
+    return v < V ? visited[v] : ~0ull;
   }
   template <class Edge>
   __device__ __forceinline__ void relax(Edge e, Val m, uint64_t, Probe p) const {
@@ -901,7 +997,7 @@ __device__ __forceinline__ void pr_tile(const LbsArgs &a, const Src &src, const 
     __device__ uint32_t src_val(uint32_t) const { return 0; }
   } nv;
   uint32_t i0;
-  const uint32_t nl = lbs_setup<false>(a, nv, sh, k, pos0, i0);
+  const uint32_t nl = lbs_setup<false>(a, src, nv, sh, k, pos0, i0);
   if (nl == 0) return;
   // three phases, so that a thread keeps all eight record loads and then all
   // eight contribution gathers in flight
@@ -910,11 +1006,7 @@ __device__ __forceinline__ void pr_tile(const LbsArgs &a, const Src &src, const 
   for (int it = 0; it < (int)kItems; it++) {
     const uint32_t x = it * kThreads + threadIdx.x;
     u[it] = 0xffffffffu;  // no edge at this position
-    if (x < tlen) {
-      const uint64_t idx = sh.cb[sh.map[x]] + x;
-      if (idx < a.edge_bound) u[it] = edge_dst(src.load(idx));
-      else atomicOr(a.err, kErrEdgeIndex);
-    }
+    if (x < tlen) u[it] = edge_dst(src.at(sh.cb[sh.map[x]], x));
   }
   float c[kItems];
 #pragma unroll
@@ -1019,10 +1111,9 @@ template <class Src0, class Src1>
 __global__ void __launch_bounds__(kThreads, 6) k_pr_pull_pair(LbsArgs a0, Src0 s0, PrArgs p0, LbsArgs a1,
                                                               Src1 s1, PrArgs p1, uint64_t n0, uint64_t n) {
   __shared__ PrShared sh;
-  const uint64_t b = blockIdx.x;
-  const uint64_t lo = b * n0 / n, hi = (b + 1) * n0 / n;
-  if (hi > lo) pr_tile(a0, s0, p0, sh, a0.pos_begin / kTile + lo);
-  else pr_tile(a1, s1, p1, sh, a1.pos_begin / kTile + (b - hi));
+  const PairTile pt = pair_split_cta(n0, n);
+  if (pt.r == 0) pr_tile(a0, s0, p0, sh, a0.pos_begin / kTile + pt.t);
+  else pr_tile(a1, s1, p1, sh, a1.pos_begin / kTile + pt.t);
 }
 
 // Completes the sums of vertices split over several tiles, in tile order.

@@ -311,7 +311,7 @@ __device__ __forceinline__ void sb_tile(const LbsArgs &a, const Src &src, const 
   if (pos0 >= a.pos_end) return;
   const uint32_t tlen = (uint32_t)(min(pos0 + kTile, a.pos_end) - pos0);
   uint32_t i0;
-  const uint32_t nl = lbs_setup<true>(a, op, sh, k, pos0, i0);
+  const uint32_t nl = lbs_setup<true>(a, src, op, sh, k, pos0, i0);
   if (nl == 0) return;
   for (uint32_t base = 0; base < tlen; base += U * kThreads) {
     typename Src::Item ev[U];
@@ -323,14 +323,9 @@ __device__ __forceinline__ void sb_tile(const LbsArgs &a, const Src &src, const 
       val[j] = make_uint2(0u, 0u);
       if (x < tlen) {
         const uint32_t l = sh.map[x];
-        const uint64_t idx = sh.cb[l] + x;
         val[j] = sh.val[l];
-        if (idx < a.edge_bound) {
-          ev[j] = src.load(idx);
-          okm |= 1u << j;
-        } else {
-          atomicOr(a.err, kErrEdgeIndex);
-        }
+        ev[j] = src.at(sh.cb[l], x);
+        okm |= 1u << j;
       }
     }
     uint32_t nb[U];
@@ -402,12 +397,11 @@ template <class Src0, class Src1, int KS>
 __global__ void __launch_bounds__(kThreads, kSbMinBlocks) k_sb_relax_pair(LbsArgs a0, Src0 s0, LbsArgs a1, Src1 s1, SbOp op,
                                                             uint64_t n0, uint64_t n) {
   __shared__ LbsShared<uint2> sh;
-  const uint64_t b = blockIdx.x;
-  const uint64_t lo = b * n0 / n, hi = (b + 1) * n0 / n;
+  const PairTile pt = pair_split_cta(n0, n);
   static_assert(std::is_same<Src0, Src1>::value, "one tile body for both regions");
   // one inlined tile body for both regions (two would double its registers)
-  const bool st = hi > lo;
-  sb_tile<Src0, KS>(st ? a0 : a1, st ? s0 : s1, op, sh, st ? a0.pos_begin / kTile + lo : a1.pos_begin / kTile + (b - hi));
+  const bool st = pt.r == 0;
+  sb_tile<Src0, KS>(st ? a0 : a1, st ? s0 : s1, op, sh, (st ? a0.pos_begin : a1.pos_begin) / kTile + pt.t);
 }
 
 // Slots in `cols` of every row set to unreached (one thread per row).
