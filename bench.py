@@ -978,7 +978,7 @@ def run_cc_oom(args, rank, world, local):
 # Serving mix: per graph scale, the device budget (GiB) of its resident state
 # and first query context, and the sources of one multi-source SSSP pass.
 # The four budgets hold 22.5 of the 24 GiB; the rest admits extra contexts.
-SERVING_GRAPHS = {22: (1.0, 16), 24: (3.75, 16), 26: (6.75, 8), 27: (11.0, 4)}
+SERVING_GRAPHS = {22: (1.0, 16), 24: (3.75, 16), 26: (6.75, 8), 27: (12.2, 4)}
 
 
 def serving_graph(sc: int):

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define OG_ABI_VERSION 4
+#define OG_ABI_VERSION 5
 
 typedef enum og_status {
   OG_OK = 0,
@@ -329,6 +329,31 @@ int og_sssp_batch_step(og_engine *e, uint32_t *pending, int *done, og_stats *st)
 int og_sssp_batch_checks(og_engine *e, uint32_t slots, uint64_t *out);
 int og_sssp_batch_fetch(og_engine *e, uint32_t slot, uint32_t *out);
 
+/* og_bfs_batch level by level, so that sources can join a batch in flight
+ * (the server's continuous batching of BFS requests).  Needs OG_CFG_BATCH;
+ * slots are 0..63, one bit of the per-vertex masks each.
+ * og_bfs_batch_begin clears every slot; with record_depths != 0 it keeps a
+ * 64 x V u32 device depth matrix (outside the budget) for
+ * og_bfs_batch_fetch.  og_bfs_batch_join seeds slots[i] with source srcs[i]
+ * at the current level boundary: a source that joins at level L has depth 1
+ * there and its vertices get depth (level - L + 1), so its depths and checks
+ * are those of og_bfs from that source.  A slot still in flight cannot be
+ * joined (OG_E_STATE).  og_bfs_batch_step expands one level for every slot in
+ * flight; *pending receives the slots still in flight (a slot that reached no
+ * new vertex has finished: its checks are final and it may be joined again),
+ * *done = 1 once none is.  og_bfs_batch_checks writes {vertices reached, sum
+ * of depths} of every slot in the mask `slots` to out[2 s], out[2 s + 1] (128
+ * values, 0 for slots outside the mask).  og_bfs_batch_fetch copies a
+ * finished slot's V depths (og_bfs's convention) to host memory.  Every level
+ * is expanded top-down.  Any other query on the engine ends the session, as
+ * for og_sssp_batch_begin.  No reference counterpart: the reference runs its
+ * BFS sources one after another (BFS/oneGraph_BFS/CalculateOpt.h:55-209). */
+int og_bfs_batch_begin(og_engine *e, int record_depths);
+int og_bfs_batch_join(og_engine *e, const uint32_t *srcs, const uint32_t *slots, int n);
+int og_bfs_batch_step(og_engine *e, uint64_t *pending, int *done, og_stats *st);
+int og_bfs_batch_checks(og_engine *e, uint64_t slots, uint64_t *out);
+int og_bfs_batch_fetch(og_engine *e, uint32_t slot, uint32_t *out);
+
 /* og_bfs_batch with byte depths, for hosts that fetch many depth arrays:
  * out[s*V + v] = the depth when it is at most 254 (the source has 1), 0 when
  * v is unreached, 255 when the depth is 255 or more (*clamped, when not
@@ -524,8 +549,15 @@ typedef struct og_server_config {
   int32_t workers;       /* host threads driving queries (1..64)           */
   int32_t max_batch;     /* BFS requests per fused pass (1 = no batching)  */
   int32_t device;
-  uint32_t flags;
+  uint32_t flags;        /* OG_SERVER_* below                              */
 } og_server_config;
+
+/* BFS requests of a graph run as a level-by-level pass (og_bfs_batch_begin /
+ * _join / _step) that requests queued meanwhile join at every level
+ * boundary, each answered as soon as its source has finished.  Without it a
+ * BFS pass takes the requests queued at its start (og_bfs_batch, persistent
+ * kernel with a per-source direction choice). */
+#define OG_SERVER_BFS_JOIN 1u
 
 typedef struct og_request {
   int32_t graph;      /* id from og_server_add_graph                       */

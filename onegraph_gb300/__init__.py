@@ -42,6 +42,7 @@ PARAM_LEVEL_LOOP = 4
 LOOP_AUTO, LOOP_HOST = 0, 1
 PARAM_RELAX_TIMER = 5
 PARAM_SSSP_BATCH_DELTA = 6
+SERVER_BFS_JOIN = 1  # og_server_config.flags: BFS requests join level-by-level passes in flight
 # R-MAT quadrant probabilities of the benchmark graphs
 RMAT_ABC = (0.57, 0.19, 0.19)
 
@@ -174,6 +175,11 @@ SIGNATURES = [
     ("og_sssp_batch_step", C.c_int, [_P, C.POINTER(C.c_uint32), C.POINTER(C.c_int), C.POINTER(Stats)]),
     ("og_sssp_batch_checks", C.c_int, [_P, C.c_uint32, _P]),
     ("og_sssp_batch_fetch", C.c_int, [_P, C.c_uint32, _P]),
+    ("og_bfs_batch_begin", C.c_int, [_P, C.c_int]),
+    ("og_bfs_batch_join", C.c_int, [_P, _P, _P, C.c_int]),
+    ("og_bfs_batch_step", C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_int), C.POINTER(Stats)]),
+    ("og_bfs_batch_checks", C.c_int, [_P, C.c_uint64, _P]),
+    ("og_bfs_batch_fetch", C.c_int, [_P, C.c_uint32, _P]),
     ("og_bfs_batch_u8", C.c_int, [_P, _P, C.c_int, _P, C.POINTER(C.c_uint64), _P, C.POINTER(Stats)]),
     ("og_host_alloc", C.c_int, [C.c_uint64, C.POINTER(_P)]),
     ("og_host_free", None, [_P]),
@@ -207,7 +213,7 @@ SIGNATURES = [
 ]
 
 
-ABI_VERSION = 4  # OG_ABI_VERSION of include/onegraph.h these bindings follow
+ABI_VERSION = 5  # OG_ABI_VERSION of include/onegraph.h these bindings follow
 
 
 def lib():
@@ -524,6 +530,33 @@ class Engine:
         _check(lib().og_sssp_batch_fetch(self._h, slot, _ptr(o)), "og_sssp_batch_fetch")
         return o
 
+    # og_bfs_batch level by level (sources may join a batch in flight)
+    def bfs_batch_begin(self, record_depths: bool = False):
+        _check(lib().og_bfs_batch_begin(self._h, 1 if record_depths else 0), "og_bfs_batch_begin")
+
+    def bfs_batch_join(self, srcs, slots):
+        s = np.ascontiguousarray(srcs, dtype=np.uint32)
+        k = np.ascontiguousarray(slots, dtype=np.uint32)
+        assert s.size == k.size
+        _check(lib().og_bfs_batch_join(self._h, _ptr(s), _ptr(k), s.size), "og_bfs_batch_join")
+
+    def bfs_batch_step(self) -> tuple:
+        """One level: (slots still in flight as a 64-bit mask, done)."""
+        p, d, st = C.c_uint64(), C.c_int(), Stats()
+        _check(lib().og_bfs_batch_step(self._h, C.byref(p), C.byref(d), C.byref(st)), "og_bfs_batch_step")
+        self.stats = st.as_dict()
+        return p.value, bool(d.value)
+
+    def bfs_batch_checks(self, slots: int) -> np.ndarray:
+        out = np.zeros((64, 2), np.uint64)
+        _check(lib().og_bfs_batch_checks(self._h, C.c_uint64(slots), _ptr(out)), "og_bfs_batch_checks")
+        return out
+
+    def bfs_batch_fetch(self, slot: int) -> np.ndarray:
+        o = np.empty(self.graph.V, np.uint32)
+        _check(lib().og_bfs_batch_fetch(self._h, slot, _ptr(o)), "og_bfs_batch_fetch")
+        return o
+
     def bfs_batch_u8(self, srcs, out=None, checks: bool = True):
         """og_bfs_batch_u8: byte depths (0 unreached, 255 for depth >= 255).
         Returns (depths n x V u8, clamped entries, checks or None)."""
@@ -612,8 +645,9 @@ class Engine:
 class Server:
     """og_server: resident graphs, pooled query contexts, continuous batching."""
 
-    def __init__(self, budget: int = 0, workers: int = 4, max_batch: int = 64, device: int = 0):
-        cfg = ServerConfig(budget, workers, max_batch, device, 0)
+    def __init__(self, budget: int = 0, workers: int = 4, max_batch: int = 64, device: int = 0,
+                 bfs_join: bool = False):
+        cfg = ServerConfig(budget, workers, max_batch, device, SERVER_BFS_JOIN if bfs_join else 0)
         h = _P()
         _check(lib().og_server_create(C.byref(cfg), C.byref(h)), "og_server_create")
         self._h = h

@@ -145,6 +145,20 @@ struct og_engine {
   uint32_t sb_dirty = 0;  // slots whose distances are not all unreached
   bool sb_session = false;  // a session is open: no other query ran since og_sssp_batch_begin
 
+  // batched BFS level by level (og_bfs_batch_begin ... _fetch): up to 64
+  // slots over the batch masks; a slot's depths are offset by the level it
+  // joined at, and a finished slot's visited bits are cleared when it is
+  // joined again
+  uint32_t *bb_io_d = nullptr, *bb_io_h = nullptr;  // sources [0,64), slots [64,128), depth offsets [128,192)
+  bool bb_session = false;  // no other query ran since og_bfs_batch_begin
+  bool bb_record = false;   // depths recorded in depth_d (64 x V)
+  uint32_t bb_level = 1;    // depth of the frontier the next step expands, for a source at depth 1 at begin
+  uint32_t bb_par = 0;      // frontier parity: cur = bmask[1 + par], cur_any = bm[par]
+  uint64_t bb_used = 0;     // slots joined and not finished
+  uint64_t bb_dirty = 0;    // finished slots whose visited bits are still set
+  uint32_t bb_off[64] = {};
+  uint64_t bb_reached[64] = {}, bb_dsum[64] = {};
+
   og_engine *parent = nullptr;  // set on clones: resident state belongs to the parent
   int clones = 0;               // live clones of this engine
   uint64_t resident_bytes = 0;  // device bytes of the shared resident state
@@ -197,6 +211,7 @@ void destroy(og_engine *e) {
   if (e->hist_h) cudaFreeHost(e->hist_h);
   if (e->srcs_h) cudaFreeHost(e->srcs_h);
   if (e->sb_io_h) cudaFreeHost(e->sb_io_h);
+  if (e->bb_io_h) cudaFreeHost(e->bb_io_h);
   if (e->sb_ck_h) cudaFreeHost(e->sb_ck_h);
   if (e->pmisc_h) cudaFreeHost(e->pmisc_h);
   if (e->graph) cudaGraphExecDestroy(e->graph);
@@ -334,6 +349,8 @@ int create_query_state(og_engine *e) {
   if (e->batch_enabled) {
     RC(dalloc(e, &e->hist_d, (uint64_t)kMaxBatchLevels * 64));
     RC(dalloc(e, &e->srcs_d, 64));
+    RC(dalloc(e, &e->bb_io_d, 192));
+    CK(cudaMallocHost(&e->bb_io_h, 192 * sizeof(uint32_t)));
     e->ptile_cap = e->g->E / 1024 + 8;
     RC(dalloc(e, &e->ptile_d, e->ptile_cap));
     RC(dalloc(e, &e->cta_n, kMaxPersistCtas));
@@ -1285,6 +1302,150 @@ int run_batch(og_engine *e, const uint32_t *srcs, uint32_t n, uint32_t *out, uin
   return OG_OK;
 }
 
+// ------------------------------------------------- batched BFS, level by level
+
+// Opens a session: no slot in use, empty masks and frontier; with `record`
+// the 64 x V depth matrix (outside the budget) is kept for og_bfs_batch_fetch.
+int bb_begin_impl(og_engine *e, bool record) {
+  const uint64_t V = e->V;
+  cudaStream_t s = e->s_main;
+  e->sb_session = false;  // the masks share the arena with the SSSP rows
+  e->bb_session = false;
+  CK(cudaMemsetAsync(e->err_d, 0, 16, s));
+  CK(cudaMemsetAsync(e->bm[0], 0, 4 * e->nwords, s));
+  CK(cudaMemsetAsync(e->bm[1], 0, 4 * e->nwords, s));
+  for (int i = 0; i < 3; i++) CK(cudaMemsetAsync(e->bmask[i], 0, 8 * (V + 1), s));
+  e->bb_record = record;
+  if (record) {
+    uint32_t *d = nullptr;
+    RC(depth_matrix(e, 64, &d));
+    k_fill_u32<<<grid_for(64 * V, e->sms), kThreads, 0, s>>>(d, 64 * V, (uint32_t)(V + 1));
+    e->launches++;
+  }
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  e->bb_level = 1;
+  e->bb_par = 0;
+  e->bb_used = e->bb_dirty = 0;
+  e->bb_session = true;
+  return OG_OK;
+}
+
+// Seeds slots[i] with srcs[i] at the current level boundary.
+int bb_join_impl(og_engine *e, const uint32_t *srcs, const uint32_t *slots, uint32_t n) {
+  if (n == 0) return OG_OK;
+  if (n > 64) return fail(OG_E_ARG, "%u sources joined, a batch holds 64", n);
+  uint64_t cols = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    if (srcs[i] >= e->V) return fail(OG_E_ARG, "source %u >= V %u", srcs[i], e->V);
+    if (slots[i] >= 64) return fail(OG_E_ARG, "slot %u >= 64", slots[i]);
+    const uint64_t b = 1ull << slots[i];
+    if (cols & b) return fail(OG_E_ARG, "slot %u joined twice", slots[i]);
+    if (e->bb_used & b) return fail(OG_E_STATE, "slot %u is still in flight", slots[i]);
+    cols |= b;
+  }
+  const uint64_t V = e->V;
+  cudaStream_t s = e->s_main;
+  if (cols & e->bb_dirty) {
+    k_batch_clear_bits<<<grid_for(V + 1, e->sms), kThreads, 0, s>>>(e->bmask[0], V + 1, cols & e->bb_dirty);
+    e->launches++;
+    e->bb_dirty &= ~cols;
+  }
+  if (e->bb_record)
+    for (uint32_t i = 0; i < n; i++) {
+      k_fill_u32<<<grid_for(V, e->sms), kThreads, 0, s>>>(e->depth_d + (uint64_t)slots[i] * V, V,
+                                                         (uint32_t)(V + 1));
+      e->launches++;
+    }
+  for (uint32_t i = 0; i < n; i++) {
+    e->bb_off[slots[i]] = e->bb_level - 1;
+    e->bb_reached[slots[i]] = 1;  // the source itself, at depth 1
+    e->bb_dsum[slots[i]] = 1;
+  }
+  CK(cudaStreamSynchronize(s));  // the page-locked buffer is rewritten only after the previous upload ran
+  memcpy(e->bb_io_h, srcs, 4 * n);
+  memcpy(e->bb_io_h + 64, slots, 4 * n);
+  memcpy(e->bb_io_h + 128, e->bb_off, 4 * 64);
+  CK(cudaMemcpyAsync(e->bb_io_d, e->bb_io_h, 192 * 4, cudaMemcpyHostToDevice, s));
+  k_batch_init<<<1, 64, 0, s>>>(e->bb_io_d, n, e->bmask[0], e->bmask[1 + e->bb_par], e->bm[e->bb_par],
+                                e->bb_record ? e->depth_d : nullptr, V, nullptr, e->bb_io_d + 64);
+  e->launches++;
+  CK(cudaGetLastError());
+  e->bb_used |= cols;
+  return OG_OK;
+}
+
+// One level: expands the frontier of every slot in flight.  A slot that
+// reached no new vertex has finished: it leaves *pending, its checks are
+// final and it may be joined again.
+int bb_step_impl(og_engine *e, uint64_t *pending, bool *done, og_stats &st, Timing &tm) {
+  const uint64_t V = e->V;
+  cudaStream_t s = e->s_main;
+  const uint32_t par = e->bb_par;
+  uint32_t *cur_any = e->bm[par], *next_any = e->bm[1 - par];
+  unsigned long long *visited = e->bmask[0], *cur = e->bmask[1 + par], *next = e->bmask[2 - par];
+  uint64_t nl = 0;
+  RC(compact_round(e, cur_any, st, tm, &nl));
+  if (nl == 0) {  // nothing in flight
+    e->bb_dirty |= e->bb_used;
+    e->bb_used = 0;
+    *pending = 0;
+    *done = true;
+    return OG_OK;
+  }
+  st.iterations++;
+  st.frontier_sum += nl;
+  st.static_vertices += e->counts_h[0].n;
+  BatchOp op{visited, cur, next, next_any, e->err_d, e->V};
+  auto launch = [&](const LbsArgs &a, auto src, cudaStream_t ls) {
+    const unsigned grid = lbs_grid(a.pos_begin, a.pos_end);
+    if (grid) {
+      k_lbs<decltype(src), BatchOp><<<grid, kThreads, 0, ls>>>(a, src, op);
+      e->launches++;
+    }
+    return (int)OG_OK;
+  };
+  auto sfn = [&](const LbsArgs &a) { return launch(a, EKU::stat(e), s); };
+  auto pfn = [&](const LbsArgs &a0, auto s0, const LbsArgs &a1, auto s1, cudaStream_t ps) {
+    const uint64_t n0 = lbs_grid(a0.pos_begin, a0.pos_end), n1 = lbs_grid(a1.pos_begin, a1.pos_end);
+    if (n0 + n1 > 0x7fffffffull) return fail(OG_E_STATE, "relax grid too large");
+    k_lbs_pair<decltype(s0), decltype(s1), BatchOp><<<(unsigned)(n0 + n1), kThreads, 0, ps>>>(
+        a0, s0, a1, s1, op, n0, n0 + n1);
+    e->launches++;
+    return (int)OG_OK;
+  };
+  RC((run_regions<EKU>(e, st, tm, sfn, launch, pfn)));
+  CK(cudaMemsetAsync(e->hist_d, 0, 64 * 8, s));
+  const uint32_t depth = e->bb_level + 1;  // of the vertices this level reaches, for a source joined at begin
+  k_batch_level<<<grid_for(e->nwords, e->sms), kThreads, 0, s>>>(next_any, next, e->nwords, 64, e->hist_d,
+                                                               e->bb_record ? e->depth_d : nullptr, V, depth,
+                                                               e->bb_io_d + 128);
+  e->launches++;
+  CK(cudaMemcpyAsync(e->hist_h, e->hist_d, 64 * 8, cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamWaitEvent(s, e->ev_cd, 0));
+  CK(cudaMemsetAsync(cur_any, 0, 4 * e->nwords, s));
+  CK(cudaMemsetAsync(cur, 0, 8 * (V + 1), s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  for (uint32_t i = 0; i < 64; i++) {
+    const uint64_t b = 1ull << i;
+    if (!(e->bb_used & b)) continue;
+    const uint64_t c = e->hist_h[i];
+    if (c == 0) {
+      e->bb_used &= ~b;
+      e->bb_dirty |= b;
+    } else {
+      e->bb_reached[i] += c;
+      e->bb_dsum[i] += (uint64_t)(depth - e->bb_off[i]) * c;
+    }
+  }
+  e->bb_par ^= 1u;
+  e->bb_level++;
+  *pending = e->bb_used;
+  *done = e->bb_used == 0;
+  return OG_OK;
+}
+
 // ------------------------------------------------------- persistent batched BFS
 
 struct PersistCfg {
@@ -1560,6 +1721,7 @@ int sb_reset(og_engine *e) {
   e->sb_advance = false;
   e->sb_dirty = 0;
   e->sb_session = true;
+  e->bb_session = false;  // the batch arena now holds SSSP rows
   CK(cudaGetLastError());
   return OG_OK;
 }
@@ -1967,8 +2129,9 @@ int query_common(og_engine *e, int algo, og_stats *st_out, void *out,
     memset(&st, 0, sizeof st);
     e->launches = 0;
     // every query reuses the frontier bitmaps, lists and arena of an open
-    // multi-source SSSP session: the session ends here
+    // multi-source SSSP or batched BFS session: the session ends here
     e->sb_session = false;
+    e->bb_session = false;
     const double t0 = now_ms();
     RC(body(e, st, ctx));
     st.launches = e->launches;
@@ -2460,6 +2623,90 @@ extern "C" int og_sssp_batch_fetch(og_engine *e, uint32_t slot, uint32_t *out) {
     clear_error();
     CK(cudaSetDevice(e->dev));
     return sb_fetch_impl(e, slot, out);
+  });
+}
+
+namespace {
+int bb_session_ok(og_engine *e) {
+  if (!e->batch_enabled) return fail(OG_E_UNSUPPORTED, "engine created without OG_CFG_BATCH");
+  if (!e->bb_session)
+    return fail(OG_E_STATE, "no open batched BFS session: og_bfs_batch_begin first (any other query on the "
+                            "engine ends a session)");
+  return OG_OK;
+}
+}  // namespace
+
+extern "C" int og_bfs_batch_begin(og_engine *e, int record_depths) {
+  if (!e) return fail(OG_E_ARG, "null engine");
+  if (!e->batch_enabled) return fail(OG_E_UNSUPPORTED, "engine created without OG_CFG_BATCH");
+  return guarded([&]() -> int {
+    clear_error();
+    CK(cudaSetDevice(e->dev));
+    cudaGetLastError();
+    e->launches = 0;
+    e->last_algo = -1;
+    return bb_begin_impl(e, record_depths != 0);
+  });
+}
+
+extern "C" int og_bfs_batch_join(og_engine *e, const uint32_t *srcs, const uint32_t *slots, int n) {
+  if (!e || n < 0 || (n && (!srcs || !slots))) return fail(OG_E_ARG, "og_bfs_batch_join: bad argument");
+  RC(bb_session_ok(e));
+  return guarded([&]() -> int {
+    clear_error();
+    CK(cudaSetDevice(e->dev));
+    return bb_join_impl(e, srcs, slots, (uint32_t)n);
+  });
+}
+
+extern "C" int og_bfs_batch_step(og_engine *e, uint64_t *pending, int *done, og_stats *st) {
+  if (!e || !pending || !done) return fail(OG_E_ARG, "og_bfs_batch_step: null argument");
+  RC(bb_session_ok(e));
+  return guarded([&]() -> int {
+    clear_error();
+    CK(cudaSetDevice(e->dev));
+    og_stats s;
+    memset(&s, 0, sizeof s);
+    const uint64_t l0 = e->launches;
+    const double t0 = now_ms();
+    Timing tm;
+    bool d = false;
+    RC(bb_step_impl(e, pending, &d, s, tm));
+    collect_timing(e, tm, &s);
+    CK(cudaMemcpy(e->err_h, e->err_d, 4, cudaMemcpyDeviceToHost));
+    RC(check_device_error(e));
+    s.launches = e->launches - l0;
+    s.ms_total = now_ms() - t0;
+    if (st) *st = s;
+    *done = d ? 1 : 0;
+    e->last_algo = -1;
+    return OG_OK;
+  });
+}
+
+extern "C" int og_bfs_batch_checks(og_engine *e, uint64_t slots, uint64_t *out) {
+  if (!e || !out) return fail(OG_E_ARG, "og_bfs_batch_checks: null argument");
+  RC(bb_session_ok(e));
+  for (uint32_t i = 0; i < 64; i++) {
+    const bool on = (slots >> i) & 1u;
+    out[2 * i] = on ? e->bb_reached[i] : 0;
+    out[2 * i + 1] = on ? e->bb_dsum[i] : 0;
+  }
+  return OG_OK;
+}
+
+extern "C" int og_bfs_batch_fetch(og_engine *e, uint32_t slot, uint32_t *out) {
+  if (!e || !out) return fail(OG_E_ARG, "og_bfs_batch_fetch: null argument");
+  RC(bb_session_ok(e));
+  if (slot >= 64) return fail(OG_E_ARG, "slot %u >= 64", slot);
+  if (!e->bb_record) return fail(OG_E_STATE, "the session was opened without depth recording");
+  if ((e->bb_used >> slot) & 1u) return fail(OG_E_STATE, "slot %u is still in flight", slot);
+  return guarded([&]() -> int {
+    clear_error();
+    CK(cudaSetDevice(e->dev));
+    CK(cudaMemcpyAsync(out, e->depth_d + (uint64_t)slot * e->V, 4ull * e->V, cudaMemcpyDeviceToHost, e->s_main));
+    CK(cudaStreamSynchronize(e->s_main));
+    return OG_OK;
   });
 }
 

@@ -926,27 +926,35 @@ struct PushOp {
   }
 };
 
+// Seeds source i (bit slots[i], or bit i when slots is null) at depth 1.
 __global__ void k_batch_init(const uint32_t *srcs, uint32_t n, unsigned long long *visited,
                              unsigned long long *cur, uint32_t *cur_any, uint32_t *depth,
-                             uint64_t V, uint8_t *depth8 = nullptr) {
+                             uint64_t V, uint8_t *depth8 = nullptr, const uint32_t *slots = nullptr) {
   const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
-  const uint32_t v = srcs[i];
-  atomicOr(visited + v, 1ull << i);
-  atomicOr(cur + v, 1ull << i);
+  const uint32_t v = srcs[i], b = slots ? slots[i] : i;
+  atomicOr(visited + v, 1ull << b);
+  atomicOr(cur + v, 1ull << b);
   atomicOr(cur_any + (v >> 5), 1u << (v & 31));
-  if (depth) depth[(uint64_t)i * V + v] = 1u;
-  if (depth8) depth8[(uint64_t)i * V + v] = 1u;
+  if (depth) depth[(uint64_t)b * V + v] = 1u;
+  if (depth8) depth8[(uint64_t)b * V + v] = 1u;
+}
+
+// Clears the bits `mask` of every vertex's mask (slots released for reuse).
+__global__ void k_batch_clear_bits(unsigned long long *m, uint64_t n, unsigned long long mask) {
+  for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n; v += (uint64_t)gridDim.x * blockDim.x)
+    if (m[v] & mask) m[v] &= ~mask;
 }
 
 // Per-source count of the vertices first reached at this level (hist[s]),
-// and, when depth != nullptr, their depth for the n x V output.
+// and, when depth != nullptr, their depth for the n x V output: level, less
+// doff[s] when doff is not null (a source that joined a pass in flight).
 __global__ void __launch_bounds__(kThreads) k_batch_level(const uint32_t *next_any,
                                                           const unsigned long long *next,
                                                           uint64_t nwords, uint32_t n,
                                                           unsigned long long *hist,
                                                           uint32_t *depth, uint64_t V,
-                                                          uint32_t level) {
+                                                          uint32_t level, const uint32_t *doff = nullptr) {
   __shared__ uint32_t s_cnt[64];
   if (threadIdx.x < 64) s_cnt[threadIdx.x] = 0;
   __syncthreads();
@@ -959,7 +967,7 @@ __global__ void __launch_bounds__(kThreads) k_batch_level(const uint32_t *next_a
         const uint32_t s = __ffsll((long long)m) - 1;
         if (s < n) {
           atomicAdd(&s_cnt[s], 1u);
-          if (depth) depth[(uint64_t)s * V + v] = level;
+          if (depth) depth[(uint64_t)s * V + v] = doff ? level - doff[s] : level;
         }
       }
     }

@@ -15,7 +15,10 @@
 //    free for the next one.  So requests join and leave a pass in flight.
 //  * when a worker admits a BFS request it also takes the BFS requests for
 //    the same graph that queued up meanwhile (up to max_batch) and serves
-//    them in one og_bfs_batch pass;
+//    them in one og_bfs_batch pass; with OG_SERVER_BFS_JOIN the pass runs
+//    level by level (og_bfs_batch_begin / _join / _step) and BFS requests
+//    queued meanwhile join it at every level boundary, as SSSP requests join
+//    SSSP passes;
 //  * queued PageRank requests for the same graph share one computation.
 // Built on the public C ABI (and the flag helpers of og_internal.hpp).
 // No reference counterpart: the reference runs one query per process run.
@@ -82,13 +85,15 @@ struct Job {
   og_engine *ctx = nullptr;
   int graph = -1;
   bool sssp_pass = false;  // a multi-source SSSP pass that admits requests while it runs
+  bool bfs_pass = false;   // a level-by-level BFS pass that admits requests while it runs
 };
 
-// Moves up to `room` queued SSSP requests of graph g (FIFO) into out.
-// Called with the lock held.
-void take_sssp(og_server *s, int g, size_t room, std::vector<Pending> &out) {
+// Moves up to `room` queued requests of graph g for `algo` (FIFO) into out;
+// BFS requests only when they need no result array.  Called with the lock
+// held.
+void take_algo(og_server *s, int g, int algo, size_t room, std::vector<Pending> &out) {
   for (auto jt = s->queue.begin(); jt != s->queue.end() && room > 0;) {
-    if (jt->r.graph == g && jt->r.algo == OG_ALGO_SSSP) {
+    if (jt->r.graph == g && jt->r.algo == algo && (algo != OG_ALGO_BFS || !jt->r.out)) {
       out.push_back(*jt);
       jt = s->queue.erase(jt);
       room--;
@@ -124,7 +129,15 @@ bool pick(og_server *s, Job &job) {
       job.sssp_pass = true;
       job.reqs.push_back(*it);
       s->queue.erase(it);
-      take_sssp(s, job.graph, std::min<size_t>(gs.sssp_slots, s->cfg.max_batch) - 1, job.reqs);
+      take_algo(s, job.graph, OG_ALGO_SSSP, std::min<size_t>(gs.sssp_slots, s->cfg.max_batch) - 1, job.reqs);
+      return true;
+    }
+    if (it->r.algo == OG_ALGO_BFS && gs.batch && s->cfg.max_batch > 1 && !it->r.out &&
+        (s->cfg.flags & OG_SERVER_BFS_JOIN)) {
+      job.bfs_pass = true;
+      job.reqs.push_back(*it);
+      s->queue.erase(it);
+      take_algo(s, job.graph, OG_ALGO_BFS, std::min<size_t>(64, s->cfg.max_batch) - 1, job.reqs);
       return true;
     }
     job.reqs.push_back(*it);
@@ -262,7 +275,90 @@ void run_sssp_pass(og_server *s, Job &job) {
     std::vector<Pending> more;
     if (used < k) {
       std::lock_guard<std::mutex> lk(s->m);
-      take_sssp(s, job.graph, k - used, more);
+      take_algo(s, job.graph, OG_ALGO_SSSP, k - used, more);
+      if (!more.empty()) s->st.batched_requests += more.size();
+    }
+    if (!more.empty()) {
+      used += (uint32_t)more.size();
+      rc = join(more);
+      if (rc != OG_OK) return fail_all(rc);
+    }
+    if (used == 0) break;
+  }
+}
+
+// A level-by-level BFS pass on job.ctx: the admitted requests take slots,
+// every level answers the requests whose sources have finished and seeds
+// the freed slots with BFS requests of the same graph that queued up
+// meanwhile.  Ends when no slot is in use and none is waiting.
+void run_bfs_pass(og_server *s, Job &job) {
+  og_engine *e = job.ctx;
+  const uint32_t k = (uint32_t)std::min(64, s->cfg.max_batch);
+  struct Slot {
+    bool used = false;
+    Pending p;
+    double t_start = 0;
+  };
+  std::vector<Slot> slot(k);
+  std::vector<og_response> out;
+  uint32_t served = 0;
+  auto fail_all = [&](int rc) {
+    for (auto &sl : slot)
+      if (sl.used) {
+        out.push_back(make_response(sl.p, rc, nullptr, served, sl.t_start));
+        sl.used = false;
+      }
+    post(s, out);
+  };
+  auto join = [&](std::vector<Pending> &reqs) -> int {
+    std::vector<uint32_t> srcs, ids;
+    const double t = now_ms(s->t0);
+    size_t q = 0;
+    for (uint32_t i = 0; i < k && q < reqs.size(); i++)
+      if (!slot[i].used) {
+        slot[i].used = true;
+        slot[i].p = reqs[q++];
+        slot[i].t_start = t;
+        srcs.push_back(slot[i].p.r.source);
+        ids.push_back(i);
+      }
+    reqs.clear();
+    return og_bfs_batch_join(e, srcs.data(), ids.data(), (int)srcs.size());
+  };
+  int rc = og_bfs_batch_begin(e, 0);
+  if (rc == OG_OK) rc = join(job.reqs);
+  if (rc != OG_OK) return fail_all(rc);
+  for (;;) {
+    uint64_t pending = 0;
+    int done = 0;
+    og_stats st;
+    rc = og_bfs_batch_step(e, &pending, &done, &st);
+    if (rc != OG_OK) return fail_all(rc);
+    count_launches(s, st);
+    uint64_t fin = 0;
+    uint32_t used = 0;
+    for (uint32_t i = 0; i < k; i++)
+      if (slot[i].used) {
+        used++;
+        if (!((pending >> i) & 1u)) fin |= 1ull << i;
+      }
+    if (fin) {
+      uint64_t ck[128];
+      rc = og_bfs_batch_checks(e, fin, ck);
+      for (uint32_t i = 0; i < k; i++) {
+        if (!((fin >> i) & 1u)) continue;
+        served++;
+        out.push_back(make_response(slot[i].p, rc, rc == OG_OK ? &ck[2 * i] : nullptr, served, slot[i].t_start));
+        slot[i].used = false;
+        used--;
+      }
+      post(s, out);
+    }
+    // admit the BFS requests of this graph that arrived meanwhile
+    std::vector<Pending> more;
+    if (used < k) {
+      std::lock_guard<std::mutex> lk(s->m);
+      take_algo(s, job.graph, OG_ALGO_BFS, k - used, more);
       if (!more.empty()) s->st.batched_requests += more.size();
     }
     if (!more.empty()) {
@@ -276,6 +372,7 @@ void run_sssp_pass(og_server *s, Job &job) {
 
 void run_job(og_server *s, Job &job) {
   if (job.sssp_pass) return run_sssp_pass(s, job);
+  if (job.bfs_pass) return run_bfs_pass(s, job);
   const double t_start = now_ms(s->t0);
   og_engine *e = job.ctx;
   og_stats st;

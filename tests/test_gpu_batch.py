@@ -228,3 +228,82 @@ def test_batch_byte_depths_clamp_long_paths():
     assert want[0, 299] == 300 and clamped == (want[0] >= 255).sum() == 46
     np.testing.assert_array_equal(b8[0], np.minimum(want[0], 255).astype(np.uint8))
     e.close()
+
+
+@pytest.mark.parametrize("layout", ["resident", "oom", "direct"])
+def test_batch_session_sources_join_in_flight(layout):
+    """Level-by-level session: four sources start, four more join after two
+    levels (their depths count from the level they joined at), every slot
+    that leaves the in-flight mask holds final depths and checks equal to a
+    single-source og_bfs, and a new source reuses a finished slot (its
+    visited bits are cleared first)."""
+    g = og.Graph.rmat(12, 16, seed=23)
+    deg = g.degrees()
+    rng = np.random.default_rng(31)
+    srcs = [int(x) for x in rng.integers(0, g.V, 10)]
+    srcs[0] = int(np.argmax(deg))
+    srcs[5] = srcs[4]  # a duplicate source
+    if (deg == 0).any():
+        srcs[6] = int(np.nonzero(deg == 0)[0][0])  # an isolated source
+    kw = dict(batch_configs(g))[layout]
+    e = og.Engine(g, batch=True, **kw)
+    want = {s: e.bfs(s) for s in set(srcs)}
+    e.bfs_batch_begin(record_depths=True)
+    e.bfs_batch_join(srcs[:4], [0, 5, 17, 63])
+    slot_src = {0: srcs[0], 5: srcs[1], 17: srcs[2], 63: srcs[3]}
+    finished, levels, reused, joined_late = [], 0, False, False
+    while True:
+        pending, done = e.bfs_batch_step()
+        levels += 1
+        assert e.stats["launches"] > 0 or done
+        for slot in list(slot_src):
+            if (pending >> slot) & 1:
+                continue
+            w = want[slot_src[slot]]
+            np.testing.assert_array_equal(e.bfs_batch_fetch(slot), w, err_msg="%s slot %d" % (layout, slot))
+            ck = e.bfs_batch_checks(1 << slot)[slot]
+            reached = w != g.V + 1
+            assert ck[0] == reached.sum() and ck[1] == np.where(reached, w, 0).sum(dtype=np.uint64)
+            finished.append(slot_src.pop(slot))
+            if joined_late and not reused:
+                e.bfs_batch_join([srcs[8]], [slot])  # a finished slot takes a new source
+                slot_src[slot] = srcs[8]
+                reused = True
+        if levels == 2:
+            e.bfs_batch_join(srcs[4:8], [1, 2, 40, 41])
+            slot_src.update({1: srcs[4], 2: srcs[5], 40: srcs[6], 41: srcs[7]})
+            joined_late = True
+        if done and not slot_src:
+            break
+        assert levels < 10000
+    assert reused
+    assert sorted(finished) == sorted(srcs[:8] + [srcs[8]])
+    e.close()
+
+
+def test_batch_session_rejects_bad_use():
+    g = og.Graph.rmat(10, 8)
+    plain = og.Engine(g, budget=1 << 30)
+    with pytest.raises(og.OGError):
+        plain.bfs_batch_begin()  # no batch state
+    plain.close()
+    e = og.Engine(g, batch=True, budget=1 << 30)
+    with pytest.raises(og.OGError):
+        e.bfs_batch_step()  # no session yet
+    e.bfs_batch_begin()
+    with pytest.raises(og.OGError):
+        e.bfs_batch_join([1], [64])  # slot out of range
+    with pytest.raises(og.OGError):
+        e.bfs_batch_join([g.V], [0])  # source out of range
+    with pytest.raises(og.OGError):
+        e.bfs_batch_join([1, 2], [3, 3])  # one slot twice
+    e.bfs_batch_join([int(np.argmax(g.degrees()))], [3])
+    with pytest.raises(og.OGError):
+        e.bfs_batch_join([2], [3])  # slot in flight
+    e.bfs_batch_step()
+    with pytest.raises(og.OGError):
+        e.bfs_batch_fetch(0)  # opened without depth recording
+    e.bfs(1)  # another query ends the session
+    with pytest.raises(og.OGError):
+        e.bfs_batch_step()
+    e.close()

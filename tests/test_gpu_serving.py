@@ -167,3 +167,27 @@ def test_clone_shares_the_resident_graph():
     assert resident == 0 and ctx > 0  # a clone holds only per-query state
     c.close()
     e.close()
+
+
+def test_bfs_requests_join_a_pass_in_flight():
+    """With OG_SERVER_BFS_JOIN, one worker and max_batch 8: 24 BFS requests on
+    one graph are answered by passes of at most 8 slots, so a response
+    numbered above 8 took the slot of a finished source while the pass ran;
+    every checksum equals og_bfs's for its source alone."""
+    g = og.Graph.rmat(12, 16, weighted=True, seed=9)
+    srv = og.Server(budget=0, workers=1, max_batch=8, bfs_join=True)
+    srv.add_graph(g, budget=_budget(g), advisek=0.5, direct=True, pagerank=True, sssp_batch=SSSP_SLOTS)
+    deg = g.degrees()
+    rng = np.random.default_rng(12)
+    srcs = [int(x) for x in rng.choice(np.nonzero(deg)[0], 24)]
+    for i, s in enumerate(srcs):
+        srv.submit(0, og.ALGO_BFS, s, user=i)
+    resp = _collect(srv, len(srcs))
+    assert max(r["batch"] for r in resp.values()) > 8
+    e = og.Engine(g, budget=_budget(g), advisek=0.5, direct=True, pagerank=True)
+    for i, s in enumerate(srcs):
+        assert resp[i]["status"] == 0
+        e.bfs(s)
+        assert resp[i]["checksum"] == e.checksum(og.ALGO_BFS), "request %d" % i
+    e.close()
+    srv.close()
