@@ -59,7 +59,7 @@ def parse_args():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--workload", default="serving",
                     choices=["serving", "sssp-oom", "sssp-batch", "cc-oom", "bfs-batch", "bfs-resident",
-                             "pr-precision"],
+                             "pr-precision", "replace"],
                     help="serving (default: the served-queries/s headline), or another measured configuration")
     ap.add_argument("--tune", type=int, default=1, help="bfs-batch: run the autotuner first")
     ap.add_argument("--serving-scales", default="22,24,26,27")
@@ -68,6 +68,11 @@ def parse_args():
     ap.add_argument("--rate", type=float, default=2000.0)
     ap.add_argument("--serving-legs", default="all", choices=["all", "served"],
                     help="serving: 'served' runs only the warm-up and the timed passes (for launch lists)")
+    ap.add_argument("--configs", default="all",
+                    help="serving at N=1: after the serving measurement, run the other measured "
+                         "configurations (resident BFS, out-of-memory SSSP and CC, PageRank precision, "
+                         "batched BFS) each in its own process and embed their lines under 'configs' "
+                         "('all', 'none', or a comma list of workload names)")
     ap.add_argument("--bfs-direction", default="auto", choices=["auto", "top-down"],
                     help="bfs-resident: direction of the timed plain queries (top-down: every level "
                          "from the frontier, the relax kernel on every edge)")
@@ -582,6 +587,7 @@ def run_bfs_batch(args, rank, world, local):
                     direct=True, device=local)
     tune = eng.bfs_batch_tune(srcs[:64], reps=1) if args.tune else None
     batches = [srcs[64 * i:64 * (i + 1)] for i in range(4)]
+    h2d = h2d_peak_gbs()
     # page-locked result buffers for the end-to-end legs, allocated before the
     # warm-up (large page-locked allocations between queries slow the next ones)
     host32 = og.pinned_empty((64, g.V), np.uint32)
@@ -666,6 +672,14 @@ def run_bfs_batch(args, rank, world, local):
         "plain_e2e_queries_per_s": nplain / tpe,
         "e2e_speedup_vs_plain_e2e": (64 * ne2e / e2e_t) / (nplain / tpe),
         "e2e_u8_speedup_vs_plain_e2e": (64 * ne2e / e2e8_t) / (nplain / tpe),
+        "roofline": {"bound": "host-link", "kernel": "k_batch_persistent (one launch per 64-source batch)",
+                     "achieved": link / (kms / 1e3) / 1e9 if kms else 0.0, "peak": h2d, "unit": "GB/s",
+                     "frac": link / (kms / 1e3) / 1e9 / h2d if kms and h2d else None, "traffic": None,
+                     "peak_source": "highest of the link probes measured in this run (og_link_probe)",
+                     "link_probes": dict(LINK_PEAKS), "bytes_per_launch": link,
+                     "note": "packed records read over the host link per batch over the kernel's CUDA-event "
+                             "time; bottom-up levels read a few records per vertex at random, so the kernel is "
+                             "bound by the link's request rate and grid barriers rather than its bandwidth"},
         "tune": tune, "clocks": clocks,
         "gpu_launches": sum(x["launches"] for x in stats),
         "setup_s": {"generate": gen_s},
@@ -693,6 +707,7 @@ def run_pr_precision(args, rank, world, local):
     except og.OGError:
         g = og.Graph.rmat(args.scale, 16, seed=1, pagerank=True, symmetric=False)
     gen_s = time.time() - t0
+    h2d = h2d_peak_gbs()
     eng = og.Engine(g, budget=int(args.budget_gib * GIB), advisek=args.advisek,
                     direct=bool(args.direct), device=local)
     eng.pr_l1(0.85, 1e-6, 3, out=False)  # warm-up
@@ -725,6 +740,29 @@ def run_pr_precision(args, rank, world, local):
     perr = np.abs(push64 - ref)
     iters = max(st["iterations"], 1)
     piters = max(st_push["iterations"], 1)
+    # The pull launches (both regions interleaved) per iteration: HBM side =
+    # the algorithmic bytes of an iteration, V (16 + 4 + 4) + 8 E (offset
+    # pair, rank write, contribution write; column + contribution per edge),
+    # over their CUDA-event time; at 6 GiB most records are static, so HBM is
+    # the bound.  Link side = packed dynamic records per iteration.
+    peaks = measured_peaks()
+    kms = st["ms_dynamic"] / iters
+    hbm_gbs = (24 * g.V + 8 * g.E) / (kms / 1e3) / 1e9 if kms else 0.0
+    roof_hbm = {"bound": "hbm", "kernel": "k_pr_pull_pair<SrcP<false>,SrcP<false>> (every iteration of the run)",
+                "achieved": hbm_gbs, "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": hbm_gbs / peaks["hbm_gbs"], "traffic": None, "peak_source": peaks["source"],
+                "bytes_per_launch": 24 * g.V + 8 * g.E, "kernel_ms_per_iter": kms,
+                "note": "algorithmic bytes V (16 + 4 + 4) + 8 E per iteration over the pull launches' time"}
+    link_gbs = st["link_bytes"] / (st["ms_dynamic"] / 1e3) / 1e9 if st["ms_dynamic"] else 0.0
+    roof = {"bound": "host-link", "kernel": "k_pr_pull_pair<SrcP<false>,SrcP<false>> (every iteration of the run)",
+            "achieved": link_gbs, "peak": h2d, "unit": "GB/s", "frac": link_gbs / h2d if h2d else None,
+            "traffic": st["link_bytes"] / iters * PR_PULL_LINK_TRAFFIC_RATIO,
+            "traffic_note": "host-link bytes per launch: algorithmic bytes x %.3f, the sysmem-sector / "
+                            "algorithmic ratio ncu measured for the same kernel on R-MAT 22 under a 256 MiB "
+                            "budget" % PR_PULL_LINK_TRAFFIC_RATIO,
+            "peak_source": "highest of the link probes measured in this run (og_link_probe)",
+            "link_probes": dict(LINK_PEAKS), "link_gb_per_iter": st["link_bytes"] / iters / 1e9,
+            "kernel_ms_per_iter": st["ms_dynamic"] / iters}
     line = {
         "metric": "pagerank iterations/s", "value": iters / t, "unit": "iterations/s",
         "n_gpus": world, "steps": 1, "warmup": 1, "ms_per_step": t * 1e3 / iters,
@@ -748,6 +786,7 @@ def run_pr_precision(args, rank, world, local):
                  "transpose_s": tr_s},
         "cpu_baseline": {"value": it_ref / cpu_s, "unit": "iterations/s", "cores": threads, "kind": "port",
                          "sample": "FP64 pull PageRank oracle, full run to L1 < 1e-6"},
+        "roofline": roof_hbm, "roofline_link": roof, "gpu_launches": st["launches"],
         "clocks": clocks, "setup_s": {"generate": gen_s},
     }
     if rank == 0:
@@ -868,6 +907,80 @@ def run_bfs_resident(args, rank, world, local):
     if rank == 0:
         print(json.dumps(line), flush=True)
     eng.close()
+
+
+def run_replace(args, rank, world, local):
+    """Static-region replacement (OG_CFG_REPLACE: half of the static region's
+    bytes as fragment slots that the policy refills between rounds) against
+    the same engine without it, on the out-of-memory R-MAT 27 graph (8 GiB,
+    advisek 0.8, direct), both with host-driven rounds: near/far SSSP from
+    the seeded sources, label-propagation CC, top-down BFS.  A step is one
+    SSSP query; the other algorithms' figures sit beside it."""
+    import torch
+    import onegraph_gb300 as og
+    torch.cuda.set_device(local)
+    g, gen_s = make_graph(args.scale)
+    srcs = pick_sources(g.degrees(), args.sources)
+    budget = int(args.budget_gib * GIB)
+    out, checks = {}, {}
+    clocks = None
+    for mode in ("plain", "replace"):
+        eng = og.Engine(g, budget=budget, advisek=args.advisek, direct=True, replace=mode == "replace",
+                        device=local)
+        eng.set_param(og.PARAM_LEVEL_LOOP, og.LOOP_HOST)
+        eng.set_param(og.PARAM_CC_METHOD, og.CC_LABEL_PROPAGATION)
+        for i in range(args.warmup):
+            eng.sssp(srcs[i % len(srcs)], out=False)
+        sampler = ClockSampler(local)
+        sampler.start()
+        r = {}
+        for algo, name, n in ((og.ALGO_SSSP, "sssp", args.steps), (og.ALGO_CC, "cc_label_propagation", 2),
+                              (og.ALGO_BFS, "bfs_top_down", args.steps)):
+            if algo == og.ALGO_BFS:
+                eng.set_param(og.PARAM_BFS_DIRECTION, og.BFS_TOP_DOWN)
+            f0 = eng.fragment_stats() if mode == "replace" else None
+            st, cks = [], []
+
+            def one(k):
+                if algo == og.ALGO_SSSP:
+                    eng.sssp(srcs[(args.warmup + k) % len(srcs)], out=False)
+                elif algo == og.ALGO_CC:
+                    eng.cc(out=False)
+                else:
+                    eng.bfs(srcs[(args.warmup + k) % len(srcs)], out=False)
+                st.append(dict(eng.stats))
+                cks.append(eng.checksum(algo))
+            t, _ = timed(one, n)
+            r[name] = {"ms_per_query": t / n * 1e3, "link_gb_per_query": sum(x["link_bytes"] for x in st) / n / 1e9,
+                       "rounds": statistics.mean(x["iterations"] for x in st)}
+            if f0 is not None:
+                f1 = eng.fragment_stats()
+                dh = f1["records_host"] - f0["records_host"]
+                ds = f1["records_slots"] - f0["records_slots"]
+                r[name].update({"records_from_slots_frac": ds / max(ds + dh, 1),
+                                "swaps_per_query": (f1["swaps"] - f0["swaps"]) / n,
+                                "swap_gb_per_query": (f1["swap_bytes"] - f0["swap_bytes"]) / n / 1e9})
+            checks.setdefault(name, []).append(cks)
+        c = sampler.stop()
+        clocks = clocks or c
+        r["plan"] = {k: eng.plan[k] for k in ("static_vertices", "static_edges", "dynamic_edges", "edge_bits")}
+        if mode == "replace":
+            r["fragments"] = eng.fragment_stats()
+        out[mode] = r
+        eng.close()
+    exact = all(a == b for a, b in checks.values())
+    sp, rp = out["plain"]["sssp"], out["replace"]["sssp"]
+    line = {
+        "metric": "queries/s", "value": 1e3 / rp["ms_per_query"], "unit": "queries/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": rp["ms_per_query"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u32", "data": "synthetic",
+        "config": dict(config_dict(args, g), workload="replace-rmat%d-%gGiB" % (args.scale, args.budget_gib),
+                       level_loop="host"),
+        "plain_queries_per_s": 1e3 / sp["ms_per_query"], "results_identical": exact,
+        "replace": out["replace"], "plain": out["plain"], "clocks": clocks, "setup_s": {"generate": gen_s},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
 
 
 def run_cc_oom(args, rank, world, local):
@@ -1283,8 +1396,69 @@ def run_serving(args, rank, world, local):
         "server": {k: st1[k] - st0.get(k, 0) if k != "used_bytes" else st1[k] for k in st1},
         "breakdown": breakdown, "setup_s": {"generate": gen_s},
     }
+    if rank == 0 and world == 1 and args.configs != "none":
+        # release this process's page-locked buffers and graphs first: every
+        # configuration builds its own inputs in its own process
+        pool = outs = None
+        for g in graphs:
+            g.close()
+        graphs = []
+        import gc
+        gc.collect()
+        torch.cuda.empty_cache()
+        line["configs"] = run_config_legs(args)
     if rank == 0:
         print(json.dumps(line), flush=True)
+
+
+# The other measured configurations, run after the serving measurement of the
+# default line (one process each, so that each starts from an empty device):
+# (key, bench.py arguments).  Graph, budget, sources and seeds are each
+# workload's defaults: R-MAT 20 resident BFS from the highest-degree vertex;
+# R-MAT 27 weighted, 8 GiB, advisek 0.8, 32 seeded SSSP sources; the same
+# graph's CC; R-MAT 26 directed PageRank to L1 < 1e-6 under 6 GiB; 256 BFS
+# sources as four 64-source batches on the R-MAT 27 graph.
+CONFIG_LEGS = (
+    ("bfs-resident", ["--workload", "bfs-resident", "--steps", "20"]),
+    ("sssp-oom", ["--workload", "sssp-oom", "--steps", "8", "--cpu-seconds", "4"]),
+    ("cc-oom", ["--workload", "cc-oom", "--steps", "4", "--cpu-seconds", "4"]),
+    ("pr-precision", ["--workload", "pr-precision"]),
+    ("bfs-batch", ["--workload", "bfs-batch", "--steps", "4"]),
+)
+CONFIG_LEGS_DEADLINE_S = 900.0
+
+
+def run_config_legs(args) -> dict:
+    """Runs the CONFIG_LEGS selected by --configs, each as `python bench.py
+    --workload ...` with this run's warm-up count, and returns their JSON
+    lines by workload.  A leg that fails or runs out of the shared deadline is
+    recorded with its reason instead of a line."""
+    want = None if args.configs == "all" else set(args.configs.split(","))
+    out = {}
+    t_end = time.time() + CONFIG_LEGS_DEADLINE_S
+    for key, argv in CONFIG_LEGS:
+        if want is not None and key not in want:
+            continue
+        left = t_end - time.time()
+        if left < 60:
+            out[key] = {"error": "not run: the configurations' %.0f s deadline was reached" % CONFIG_LEGS_DEADLINE_S}
+            continue
+        cmd = [sys.executable, os.path.abspath(__file__), *argv, "--warmup", str(max(3, args.warmup)),
+               "--configs", "none"]
+        t0 = time.time()
+        try:
+            p = subprocess.run(cmd, cwd=ROOT, capture_output=True, text=True, timeout=left)
+            lines = [x for x in p.stdout.splitlines() if x.startswith("{")]
+            if p.returncode == 0 and lines:
+                out[key] = json.loads(lines[-1])
+            else:
+                out[key] = {"error": "exit %d: %s" % (p.returncode, (p.stderr or p.stdout)[-400:])}
+        except subprocess.TimeoutExpired:
+            out[key] = {"error": "killed after %.0f s (deadline)" % left}
+        except Exception as ex:  # a leg never takes the headline line down
+            out[key] = {"error": repr(ex)[:400]}
+        out[key]["wall_s"] = time.time() - t0
+    return out
 
 
 def serving_rooflines(og, g, budget, slots, srcs, gsel, algos, gi, h2d, local):
@@ -1344,6 +1518,8 @@ def main():
         run_cc_oom(args, rank, world, local)
     elif args.workload == "sssp-batch":
         run_sssp_batch(args, rank, world, local)
+    elif args.workload == "replace":
+        run_replace(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)
 

@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define OG_ABI_VERSION 5
+#define OG_ABI_VERSION 6
 
 typedef enum og_status {
   OG_OK = 0,
@@ -222,6 +222,22 @@ typedef struct og_config {
 #define OG_CFG_PR 4u      /* also hold PageRank state for a PLAIN/WEIGHTED
                              graph, read as symmetric (in-edges = out-edges,
                              outDegree = degree); implied for OG_GRAPH_PR    */
+/* Static-region replacement (Ascetic's fragment swap, which the reference
+ * declares and never defines: bfs_kernelStaticSwap, recordFragmentVisit,
+ * setFragmentData in BFS/oneGraph_BFS/gpu_kernels.h:46-66,153-176 and
+ * FragmentData in globals.h:22-33).  Half of the static region's device
+ * bytes become slots for fragments of the dynamic region (the packed record
+ * stream cut into fragments of OG_PARAM_FRAGMENT_WORDS words), first filled
+ * with the fragments that follow the static prefix.  The relax counts the
+ * records it lists per fragment; after every round the host replaces slots
+ * whose fragments were read least with the most-read fragments that have
+ * none, copying at most a quarter of the round's host-link bytes, and a slot
+ * holds its fragment across rounds and queries.  Reads of a fragment with a
+ * slot come from device memory, the others from the host copy, so results
+ * are identical to an engine without it.  Needs OG_CFG_DIRECT and a static
+ * region; og_bfs, og_sssp and label-propagation og_cc run host-driven rounds
+ * through the slots; other queries read the host copy; no clones. */
+#define OG_CFG_REPLACE 64u
 
 /* Per-query counters (what CalculateOpt.h:193-208 prints, plus rooflines). */
 typedef struct og_stats {
@@ -459,12 +475,32 @@ int og_engine_clone(og_engine *parent, og_engine **out);
  *   re-expansions per source, less sharing).  Distances are exact for every
  *   value.  Clones inherit it. */
 #define OG_PARAM_SSSP_BATCH_DELTA 6
+/* OG_PARAM_FRAGMENT_WORDS: words per fragment of an OG_CFG_REPLACE engine,
+ *   a power of two in [2^8, 2^20].  Default: the power of two nearest
+ *   packed words / 4096, clamped to [2^8, 2^14].  Setting it lays the slots
+ *   out again (same device bytes) and refills them as at creation. */
+#define OG_PARAM_FRAGMENT_WORDS 7
 int og_engine_set_param(og_engine *e, int param, double value);
 int og_engine_get_param(const og_engine *e, int param, double *value);
 
 /* Device bytes of the shared resident graph (0 for a clone) and of one
  * query context. */
 int og_engine_bytes(const og_engine *e, uint64_t *resident, uint64_t *context);
+
+/* Counters of an OG_CFG_REPLACE engine since its creation (or the last
+ * OG_PARAM_FRAGMENT_WORDS change).  The reference declares the fragment
+ * records (recordFragmentVisit, BFS/oneGraph_BFS/gpu_kernels.h:168-170) but
+ * reports nothing. */
+typedef struct og_fragment_stats {
+  uint64_t fragments;       /* fragments of the record stream               */
+  uint32_t slots;           /* device slots                                 */
+  uint32_t fragment_words;  /* words per fragment                           */
+  uint64_t swaps;           /* fragments copied into a slot after creation  */
+  uint64_t swap_bytes;      /* bytes those copies read over the host link   */
+  uint64_t records_slots;   /* dynamic-region records read from slots       */
+  uint64_t records_host;    /* dynamic-region records read from host memory */
+} og_fragment_stats;
+int og_engine_fragment_stats(const og_engine *e, og_fragment_stats *out);
 
 /* Checksum of the last result on the device, reduced in a fixed order:
  * BFS/SSSP {vertices reached, sum of their values}; CC {components, sum of

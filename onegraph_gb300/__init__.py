@@ -26,6 +26,7 @@ PLAIN, WEIGHTED, PR = 0, 1, 2
 ALGO_BFS, ALGO_SSSP, ALGO_CC, ALGO_PR = 0, 1, 2, 3
 RMAT_SYMMETRIC, RMAT_PERMUTE, RMAT_WEIGHTED, RMAT_PR, RMAT_ON_GPU = 1, 2, 4, 8, 16
 CFG_DIRECT, CFG_NO_PIN, CFG_PR, CFG_BATCH, CFG_BATCH_LEVELS, CFG_NO_STATIC = 1, 2, 4, 8, 16, 32
+CFG_REPLACE = 64  # fragment slots: Ascetic's static-region replacement
 
 
 def CFG_SSSP_BATCH(k: int) -> int:
@@ -42,6 +43,7 @@ PARAM_LEVEL_LOOP = 4
 LOOP_AUTO, LOOP_HOST = 0, 1
 PARAM_RELAX_TIMER = 5
 PARAM_SSSP_BATCH_DELTA = 6
+PARAM_FRAGMENT_WORDS = 7
 SERVER_BFS_JOIN = 1  # og_server_config.flags: BFS requests join level-by-level passes in flight
 # R-MAT quadrant probabilities of the benchmark graphs
 RMAT_ABC = (0.57, 0.19, 0.19)
@@ -129,6 +131,15 @@ class ServerStats(C.Structure):
                 ("used_bytes", C.c_uint64), ("launches", C.c_uint64)]
 
 
+class FragmentStats(C.Structure):
+    _fields_ = [("fragments", C.c_uint64), ("slots", C.c_uint32), ("fragment_words", C.c_uint32),
+                ("swaps", C.c_uint64), ("swap_bytes", C.c_uint64), ("records_slots", C.c_uint64),
+                ("records_host", C.c_uint64)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class KRecords(C.Structure):
     """og_k_records (include/onegraph_kernels.h): packed records in device memory."""
     _fields_ = [("words", C.c_void_p), ("nrecords", C.c_uint64), ("bpe", C.c_uint32), ("bc", C.c_uint32),
@@ -191,6 +202,7 @@ SIGNATURES = [
     ("og_engine_bytes", C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_uint64)]),
     ("og_engine_set_param", C.c_int, [_P, C.c_int, C.c_double]),
     ("og_engine_get_param", C.c_int, [_P, C.c_int, C.POINTER(C.c_double)]),
+    ("og_engine_fragment_stats", C.c_int, [_P, C.POINTER(FragmentStats)]),
     ("og_k_compact", C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P, C.c_uint64, _P,
                                C.c_uint64, _P, _P]),
     ("og_k_compact_noalloc", C.c_int, [_P, C.c_uint32, C.c_uint32, _P, _P, _P, C.c_uint64, _P,
@@ -213,7 +225,7 @@ SIGNATURES = [
 ]
 
 
-ABI_VERSION = 5  # OG_ABI_VERSION of include/onegraph.h these bindings follow
+ABI_VERSION = 6  # OG_ABI_VERSION of include/onegraph.h these bindings follow
 
 
 def lib():
@@ -406,12 +418,13 @@ class Engine:
     def __init__(self, graph: Graph, budget: int = 0, advisek: float = 0.0, direct: bool = False,
                  pagerank: bool = False, no_pin: bool = False, batch: bool = False,
                  batch_levels: bool = False, no_static: bool = False, sssp_batch: int = 0,
-                 device: int = 0):
+                 replace: bool = False, device: int = 0):
         self.graph = graph
         cfg = Config(budget, advisek, (CFG_DIRECT if direct else 0) | (CFG_PR if pagerank else 0) |
                      (CFG_NO_PIN if no_pin else 0) | (CFG_BATCH if batch or batch_levels else 0) |
                      (CFG_BATCH_LEVELS if batch_levels else 0) |
-                     (CFG_NO_STATIC if no_static else 0) | CFG_SSSP_BATCH(sssp_batch), device)
+                     (CFG_NO_STATIC if no_static else 0) | CFG_SSSP_BATCH(sssp_batch) |
+                     (CFG_REPLACE if replace else 0), device)
         h = _P()
         _check(lib().og_engine_create(graph._h, C.byref(cfg), C.byref(h)), "og_engine_create")
         self._h = h
@@ -420,6 +433,12 @@ class Engine:
         _check(lib().og_engine_plan(h, C.byref(p)), "og_engine_plan")
         self.plan = p.as_dict()
         self.stats: dict = {}
+
+    def fragment_stats(self) -> dict:
+        """og_engine_fragment_stats of an engine created with replace=True."""
+        fs = FragmentStats()
+        _check(lib().og_engine_fragment_stats(self._h, C.byref(fs)), "og_engine_fragment_stats")
+        return fs.as_dict()
 
     def _out(self, out, dtype):
         if out is False:

@@ -11,6 +11,7 @@
 //    previous buffer is relaxed and the static region is relaxed on the main
 //    stream (CalculateOpt.h:75-188, GraphMeta.h:471-557).
 #include <algorithm>
+#include <cmath>
 #include <type_traits>
 #include <chrono>
 #include <cstring>
@@ -39,6 +40,31 @@ using namespace og;
     int r_ = (x);                \
     if (r_ != OG_OK) return r_;  \
   } while (0)
+
+// Fragment slots of an OG_CFG_REPLACE engine (SrcF, kernels.cuh): the slot
+// memory, the device slot table and its host mirror, and the policy state.
+struct FragState {
+  uint32_t fs = 0;          // log2 words per fragment
+  uint64_t nfrag = 0;       // fragments of the packed record stream
+  uint32_t nslots = 0;
+  uint64_t bytes = 0;       // device bytes for slots, tables and update lists
+  uint32_t *slots_d = nullptr;
+  int32_t *slot_of_d = nullptr;
+  uint32_t *visits_d = nullptr;  // records listed per fragment since the last step
+  uint2 *pairs_d = nullptr;      // one update: (fragment, slot)
+  uint32_t *evict_d = nullptr;   // one update: the fragment each slot held before
+  uint32_t max_pairs = 0;
+  uint32_t *visits_h = nullptr;  // page-locked
+  uint2 *pairs_h = nullptr;      // page-locked
+  uint32_t *evict_h = nullptr;   // page-locked
+  cudaEvent_t ev_ready = nullptr;  // slot updates done (the dynamic stream waits on it)
+  std::vector<int32_t> slot_of;  // host mirror of slot_of_d
+  std::vector<uint32_t> owner;   // fragment held by each slot (UINT32_MAX: none)
+  std::vector<float> score;      // records listed per fragment, halved every step
+  std::vector<void *> dallocs, hallocs;
+  uint64_t dalloc_bytes = 0;
+  og_fragment_stats st{};
+};
 
 struct og_engine {
   og_graph *g = nullptr;
@@ -159,6 +185,8 @@ struct og_engine {
   uint32_t bb_off[64] = {};
   uint64_t bb_reached[64] = {}, bb_dsum[64] = {};
 
+  FragState *frag = nullptr;  // OG_CFG_REPLACE: fragment slots of the dynamic region
+
   og_engine *parent = nullptr;  // set on clones: resident state belongs to the parent
   int clones = 0;               // live clones of this engine
   uint64_t resident_bytes = 0;  // device bytes of the shared resident state
@@ -198,12 +226,219 @@ int grid_for(uint64_t n, int sms) {
   return (int)std::max<uint64_t>(1, std::min<uint64_t>(g, (uint64_t)sms * 8));
 }
 
+// ------------------------------------------------------- fragment slots
+//
+// Static-region replacement (OG_CFG_REPLACE).  The reference declares its
+// pieces and never defines them: recordFragmentVisit (per-fragment visit
+// records), setFragmentData / setStaticFragmentData (which static fragments
+// may be swapped) and bfs_kernelStaticSwap (BFS/oneGraph_BFS/gpu_kernels.h:
+// 46-66,153-176, FragmentData in globals.h:22-33).  Here the swappable part
+// is a set of slots carved from the static region's bytes; the relax counts
+// the records it lists per fragment (SrcF::note) and frag_step, after every
+// round, moves the most-read fragments without a slot into the slots whose
+// fragments were read least.
+
+void frag_release(og_engine *e) {
+  FragState &F = *e->frag;
+  for (void *p : F.dallocs) cudaFree(p);
+  for (void *p : F.hallocs) cudaFreeHost(p);
+  F.dallocs.clear();
+  F.hallocs.clear();
+  e->dbytes -= F.dalloc_bytes;
+  if (!e->parent) e->resident_bytes -= std::min(e->resident_bytes, F.dalloc_bytes);
+  F.dalloc_bytes = 0;
+  F.slots_d = nullptr;
+  F.slot_of_d = nullptr;
+  F.visits_d = nullptr;
+  F.pairs_d = nullptr;
+  F.evict_d = nullptr;
+  F.visits_h = nullptr;
+  F.pairs_h = nullptr;
+  F.evict_h = nullptr;
+}
+
+template <class T>
+int frag_dalloc(og_engine *e, T **p, uint64_t count) {
+  const uint64_t bytes = std::max<uint64_t>(count * sizeof(T), 256);
+  void *q = nullptr;
+  CK(cudaMalloc(&q, bytes));
+  e->frag->dallocs.push_back(q);
+  e->frag->dalloc_bytes += bytes;
+  e->dbytes += bytes;
+  *p = (T *)q;
+  return OG_OK;
+}
+
+template <class T>
+int frag_halloc(og_engine *e, T **p, uint64_t count) {
+  void *q = nullptr;
+  CK(cudaHostAlloc(&q, std::max<uint64_t>(count * sizeof(T), 64), cudaHostAllocDefault));
+  e->frag->hallocs.push_back(q);
+  *p = (T *)q;
+  return OG_OK;
+}
+
+// Default fragment size: the power of two nearest packed words / 4096,
+// clamped to [2^8, 2^14] words.
+uint32_t frag_default_shift(uint64_t packed_words) {
+  const double x = std::log2(std::max<double>(1.0, (double)packed_words / 4096.0));
+  return (uint32_t)std::min(14.0, std::max(8.0, std::floor(x + 0.5)));
+}
+
+// Lays out slots of 2^fs + kFragPad words, the slot table, the visit counts
+// and the update lists inside F.bytes of device memory.
+int frag_layout(og_engine *e, uint32_t fs) {
+  FragState &F = *e->frag;
+  frag_release(e);
+  const og_graph *g = e->g;
+  F.fs = fs;
+  F.nfrag = (g->packed_words + (1ull << fs) - 1) >> fs;
+  const uint64_t slot_words = (1ull << fs) + kFragPad;
+  // one step moves at most a quarter of the slots (and 4096)
+  F.max_pairs = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(4096, F.bytes / (4 * slot_words) / 4));
+  const uint64_t fixed = F.nfrag * 8 + (uint64_t)F.max_pairs * 12 + 5 * 256;
+  if (F.bytes < fixed + 4 * slot_words)
+    return fail(OG_E_BUDGET, "fragment slots: %llu B of static region cannot hold one %llu-word slot and the "
+                "%llu-fragment tables", (unsigned long long)F.bytes, (unsigned long long)slot_words,
+                (unsigned long long)F.nfrag);
+  const uint64_t ns = std::min<uint64_t>((F.bytes - fixed) / (4 * slot_words), std::min<uint64_t>(F.nfrag, 0x7fffffffull));
+  F.nslots = (uint32_t)ns;
+  RC(frag_dalloc(e, &F.slots_d, ns * slot_words));
+  RC(frag_dalloc(e, &F.slot_of_d, F.nfrag));
+  RC(frag_dalloc(e, &F.visits_d, F.nfrag));
+  RC(frag_dalloc(e, &F.pairs_d, F.max_pairs));
+  RC(frag_dalloc(e, &F.evict_d, F.max_pairs));
+  if (!e->parent) e->resident_bytes += F.dalloc_bytes;
+  RC(frag_halloc(e, &F.visits_h, F.nfrag));
+  RC(frag_halloc(e, &F.pairs_h, F.max_pairs));
+  RC(frag_halloc(e, &F.evict_h, F.max_pairs));
+  F.slot_of.assign(F.nfrag, -1);
+  F.owner.assign(F.nslots, 0xffffffffu);
+  F.score.assign(F.nfrag, 0.0f);
+  F.st = og_fragment_stats{};
+  F.st.fragments = F.nfrag;
+  F.st.slots = F.nslots;
+  F.st.fragment_words = 1u << fs;
+  return OG_OK;
+}
+
+// Copies n (fragment, slot) pairs from F.pairs_h / F.evict_h into the slots
+// and the table on stream s.
+int frag_apply(og_engine *e, uint32_t n, cudaStream_t s) {
+  FragState &F = *e->frag;
+  if (n == 0) return OG_OK;
+  CK(cudaMemcpyAsync(F.pairs_d, F.pairs_h, 8ull * n, cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(F.evict_d, F.evict_h, 4ull * n, cudaMemcpyHostToDevice, s));
+  k_frag_fill<<<n, kThreads, 0, s>>>(e->hpk_d, e->g->packed_words, F.slots_d, F.pairs_d, n, F.fs);
+  k_frag_table<<<(n + 255) / 256, 256, 0, s>>>(F.slot_of_d, F.pairs_d, F.evict_d, n);
+  e->launches += 2;
+  CK(cudaGetLastError());
+  return OG_OK;
+}
+
+// Empties the slots, then fills them with the fragments that follow the
+// static prefix (the records a larger static prefix would hold).
+int frag_reset(og_engine *e) {
+  FragState &F = *e->frag;
+  cudaStream_t s = e->s_main;
+  CK(cudaMemsetAsync(F.slot_of_d, 0xff, 4 * F.nfrag, s));
+  CK(cudaMemsetAsync(F.visits_d, 0, 4 * F.nfrag, s));
+  const uint64_t f0 = (e->plan.static_edges * e->bpe >> 5) >> F.fs;
+  uint32_t filled = 0;
+  while (filled < F.nslots && f0 + filled < F.nfrag) {
+    uint32_t n = 0;
+    for (; n < F.max_pairs && filled < F.nslots && f0 + filled < F.nfrag; n++, filled++) {
+      const uint32_t f = (uint32_t)(f0 + filled);
+      F.pairs_h[n] = make_uint2(f, filled);
+      F.evict_h[n] = 0xffffffffu;
+      F.slot_of[f] = (int32_t)filled;
+      F.owner[filled] = f;
+    }
+    RC(frag_apply(e, n, s));
+    CK(cudaStreamSynchronize(s));  // the page-locked lists are reused
+  }
+  if (!F.ev_ready) CK(cudaEventCreateWithFlags(&F.ev_ready, cudaEventDisableTiming));
+  return OG_OK;
+}
+
+// After a compaction (the previous round's relax has finished): reads the
+// round's visit counts, moves the records served from slots out of the
+// host-link bytes, and replaces slots.  Ascetic's rule: fragments read in
+// this round that have no slot take the slots of fragments that were read
+// least; scores are records listed, halved every step; a fragment comes in
+// only if its score is at least a quarter of its records and above twice the
+// evicted one's; the copies of one step read at most a quarter of the
+// round's host-link bytes.  The dynamic stream waits for the updates.
+int frag_step(og_engine *e, og_stats &st) {
+  FragState &F = *e->frag;
+  cudaStream_t s = e->s_main;
+  CK(cudaMemcpyAsync(F.visits_h, F.visits_d, 4 * F.nfrag, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemsetAsync(F.visits_d, 0, 4 * F.nfrag, s));
+  CK(cudaStreamSynchronize(s));
+  uint64_t in_slots = 0, in_host = 0;
+  std::vector<uint32_t> cand;
+  const float min_score = (float)((double)(1ull << F.fs) * 32.0 / e->bpe / 4.0);
+  for (uint64_t f = 0; f < F.nfrag; f++) {
+    const uint32_t v = F.visits_h[f];
+    F.score[f] = 0.5f * F.score[f] + (float)v;
+    if (!v) continue;
+    if (F.slot_of[f] >= 0) {
+      in_slots += v;
+    } else {
+      in_host += v;
+      if (F.score[f] >= min_score) cand.push_back((uint32_t)f);
+    }
+  }
+  F.st.records_slots += in_slots;
+  F.st.records_host += in_host;
+  const uint64_t slot_link = (in_slots * e->bpe) / 8;
+  st.link_bytes -= std::min(st.link_bytes, slot_link);
+  const uint64_t frag_bytes = 4ull * ((1ull << F.fs) + kFragPad);
+  const uint64_t cap = (in_host * e->bpe / 8) / 4 / frag_bytes;
+  uint32_t n = (uint32_t)std::min<uint64_t>({cap, (uint64_t)F.max_pairs, (uint64_t)F.nslots, (uint64_t)cand.size()});
+  if (n == 0) return OG_OK;
+  auto hot = [&](uint32_t a, uint32_t b) { return F.score[a] > F.score[b] || (F.score[a] == F.score[b] && a < b); };
+  std::partial_sort(cand.begin(), cand.begin() + n, cand.end(), hot);
+  std::vector<uint32_t> vict(F.nslots);
+  for (uint32_t i = 0; i < F.nslots; i++) vict[i] = i;
+  auto vscore = [&](uint32_t sl) { return F.owner[sl] == 0xffffffffu ? -1.0f : F.score[F.owner[sl]]; };
+  std::partial_sort(vict.begin(), vict.begin() + n, vict.end(), [&](uint32_t a, uint32_t b) {
+    return vscore(a) < vscore(b) || (vscore(a) == vscore(b) && a < b);
+  });
+  uint32_t m = 0;
+  for (uint32_t i = 0; i < n; i++) {
+    const uint32_t f = cand[i], sl = vict[i];
+    if (F.score[f] <= 2.0f * vscore(sl) + 1.0f) break;
+    const uint32_t old = F.owner[sl];
+    F.pairs_h[m] = make_uint2(f, sl);
+    F.evict_h[m] = old;
+    if (old != 0xffffffffu) F.slot_of[old] = -1;
+    F.slot_of[f] = (int32_t)sl;
+    F.owner[sl] = f;
+    m++;
+  }
+  if (m == 0) return OG_OK;
+  RC(frag_apply(e, m, s));
+  CK(cudaEventRecord(F.ev_ready, s));
+  CK(cudaStreamWaitEvent(e->s_dyn, F.ev_ready, 0));
+  F.st.swaps += m;
+  F.st.swap_bytes += m * frag_bytes;
+  st.link_bytes += m * frag_bytes;
+  return OG_OK;
+}
+
 void destroy(og_engine *e) {
   if (!e) return;
   cudaSetDevice(e->dev);
   if (e->s_main) cudaStreamSynchronize(e->s_main);
   if (e->s_dyn) cudaStreamSynchronize(e->s_dyn);
   if (e->s_gat) cudaStreamSynchronize(e->s_gat);
+  if (e->frag) {
+    frag_release(e);
+    if (e->frag->ev_ready) cudaEventDestroy(e->frag->ev_ready);
+    delete e->frag;
+    e->frag = nullptr;
+  }
   for (void *p : e->dallocs) cudaFree(p);
   if (e->depth_d) cudaFree(e->depth_d);
   if (e->depth8_d) cudaFree(e->depth8_d);
@@ -389,6 +624,24 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
   e->wmin = g->wmin;
   RC(plan_compute(g->V, g->E, g->off, g->kind, cfg->budget_bytes, cfg->advisek, cfg->flags, &e->plan,
                   g->bpe, 4 + g->wbytes));
+  if (cfg->flags & OG_CFG_REPLACE) {
+    // half of the static prefix's bytes become fragment slots: the prefix
+    // shrinks to the largest vertex prefix within half of its edges
+    if (!(cfg->flags & OG_CFG_DIRECT) || (cfg->flags & (OG_CFG_NO_PIN | OG_CFG_NO_STATIC)))
+      return fail(OG_E_ARG, "OG_CFG_REPLACE needs OG_CFG_DIRECT, a page-locked host copy and a static region");
+    og_plan &Q = e->plan;
+    if (Q.static_edges == 0 || Q.dynamic_edges == 0)
+      return fail(OG_E_BUDGET, "OG_CFG_REPLACE: the plan has no %s region to share",
+                  Q.static_edges == 0 ? "static" : "dynamic");
+    const uint64_t old_words = g->packed_words_for(Q.static_edges);
+    const uint64_t half = Q.static_edges / 2;
+    const uint32_t vs = (uint32_t)(std::upper_bound(g->off, g->off + (uint64_t)g->V + 1, half) - g->off - 1);
+    Q.static_vertices = vs;
+    Q.static_edges = g->off[vs];
+    Q.dynamic_edges = g->E - Q.static_edges;
+    e->frag = new FragState;
+    e->frag->bytes = 4 * (old_words - (Q.static_edges ? g->packed_words_for(Q.static_edges) : 0));
+  }
   const og_plan &P = e->plan;
   size_t free_b = 0, total_b = 0;
   CK(cudaMemGetInfo(&free_b, &total_b));
@@ -452,6 +705,7 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
   if (P.static_edges) RC(dalloc(e, &e->spk_d, g->packed_words_for(P.static_edges)));
   if (e->pr_enabled) RC(dalloc(e, &e->outdeg_d, V + 1));
   e->resident_bytes = e->dbytes;
+  if (e->frag) RC(frag_layout(e, frag_default_shift(g->packed_words)));
   RC(create_query_state(e));
   if (e->dbytes > P.budget_bytes)
     return fail(OG_E_BUDGET, "engine allocated %llu B, above the %llu B budget",
@@ -470,6 +724,7 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
       e->launches++;
     }
   }
+  if (e->frag) RC(frag_reset(e));
   CK(cudaStreamSynchronize(e->s_main));
   CK(cudaGetLastError());
   return OG_OK;
@@ -597,6 +852,7 @@ int check_device_error(og_engine *e) {
 // buffers hold unpacked edges (Src / Dst).
 template <class W>
 struct EK {
+  static constexpr bool kFrag = false;
   using PSrc = SrcP<true>;
   using Src = SrcW<W>;
   using Dst = DstW<W>;
@@ -607,6 +863,7 @@ struct EK {
 };
 template <>
 struct EK<void> {
+  static constexpr bool kFrag = false;
   using PSrc = SrcP<false>;
   using Src = SrcU;
   using Dst = DstU;
@@ -616,6 +873,25 @@ struct EK<void> {
   static Dst stage_dst(const og_engine *e, int b) { return Dst{e->stage_col[b]}; }
 };
 using EKU = EK<void>;
+// An OG_CFG_REPLACE engine's views: the dynamic region is read through the
+// fragment slots (direct mode only: there are no staging buffers).
+template <class W>
+struct EKF : EK<W> {
+  static constexpr bool kFrag = true;
+  using HSrc = SrcF<!std::is_void<W>::value>;
+  static HSrc host(const og_engine *e) {
+    HSrc h;
+    h.words = e->hpk_d;
+    h.bpe = e->bpe;
+    h.bc = e->bc;
+    h.wmin = e->wmin;
+    h.slots = e->frag->slots_d;
+    h.slot_of = e->frag->slot_of_d;
+    h.visits = e->frag->visits_d;
+    h.fs = e->frag->fs;
+    return h;
+  }
+};
 
 // Relax op factory per algorithm; `level` is the BFS depth of the frontier.
 struct RoundOps {
@@ -738,10 +1014,10 @@ int run_regions(og_engine *e, og_stats &st, Timing &tm, StaticFn static_fn, DynF
   }
   if (cd.n) {
     CK(cudaEventRecord(e->t_d0, e->s_dyn));
-    if (e->cfg.flags & OG_CFG_DIRECT) {
+    if (K::kFrag || (e->cfg.flags & OG_CFG_DIRECT)) {
       RC(dyn_fn(lbs_args(e, 1, 0, cd.total, true, e->g->E), K::host(e), e->s_dyn));
       st.chunks += 1;
-    } else {
+    } else if constexpr (!K::kFrag) {
       const uint64_t C = e->plan.chunk_edges;
       const uint64_t nch = (cd.total + C - 1) / C;
       for (uint64_t c = 0; c < nch; c++) {
@@ -898,6 +1174,7 @@ int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
     sp.clear_bits = split ? waiting : nullptr;
     sp.far_bits = split && !advance ? waiting : nullptr;
     RC(compact_round(e, advance ? waiting : cur, st, tm, &n, sp));
+    if constexpr (K::kFrag) RC(frag_step(e, st));
     if (split) {
       const uint32_t fm = std::min(far_of(e, 0), far_of(e, 1));
       far_min = advance ? fm : std::min(far_min, fm);
@@ -2171,6 +2448,7 @@ extern "C" int og_engine_clone(og_engine *parent, og_engine **out) {
   clear_error();
   if (!parent || !out) return fail(OG_E_ARG, "og_engine_clone: null argument");
   if (parent->parent) return fail(OG_E_ARG, "og_engine_clone: clone a parent engine, not a clone");
+  if (parent->frag) return fail(OG_E_UNSUPPORTED, "og_engine_clone: an OG_CFG_REPLACE engine has no clones");
   *out = nullptr;
   return guarded([&]() -> int {
     og_engine *e = new og_engine;
@@ -2218,6 +2496,21 @@ extern "C" int og_engine_set_param(og_engine *e, int param, double value) {
     e->sb_delta = (uint32_t)value;
     return OG_OK;
   }
+  if (param == OG_PARAM_FRAGMENT_WORDS) {
+    if (!e->frag) return fail(OG_E_STATE, "fragment words: the engine was created without OG_CFG_REPLACE");
+    uint32_t fs = 8;
+    while (fs <= 20 && (double)(1u << fs) != value) fs++;
+    if (fs > 20) return fail(OG_E_ARG, "fragment words must be a power of two in [2^8, 2^20], not %g", value);
+    return guarded([&]() -> int {
+      CK(cudaSetDevice(e->dev));
+      CK(cudaStreamSynchronize(e->s_main));
+      CK(cudaStreamSynchronize(e->s_dyn));
+      RC(frag_layout(e, fs));
+      RC(frag_reset(e));
+      CK(cudaStreamSynchronize(e->s_main));
+      return (int)OG_OK;
+    });
+  }
   return fail(OG_E_ARG, "unknown parameter %d", param);
 }
 
@@ -2247,7 +2540,19 @@ extern "C" int og_engine_get_param(const og_engine *e, int param, double *value)
     *value = e->sb_delta;
     return OG_OK;
   }
+  if (param == OG_PARAM_FRAGMENT_WORDS) {
+    if (!e->frag) return fail(OG_E_STATE, "fragment words: the engine was created without OG_CFG_REPLACE");
+    *value = (double)(1u << e->frag->fs);
+    return OG_OK;
+  }
   return fail(OG_E_ARG, "unknown parameter %d", param);
+}
+
+extern "C" int og_engine_fragment_stats(const og_engine *e, og_fragment_stats *out) {
+  if (!e || !out) return fail(OG_E_ARG, "og_engine_fragment_stats: null argument");
+  if (!e->frag) return fail(OG_E_STATE, "the engine was created without OG_CFG_REPLACE");
+  *out = e->frag->st;
+  return OG_OK;
 }
 
 extern "C" int og_engine_bytes(const og_engine *e, uint64_t *resident, uint64_t *context) {
@@ -2269,6 +2574,7 @@ extern "C" int og_bfs(og_engine *e, uint32_t src, uint32_t *out_depth, og_stats 
   if (e && src >= e->V) return fail(OG_E_ARG, "source %u >= V %u", src, e->V);
   return query_common(e, OG_ALGO_BFS, st, out_depth, [](og_engine *en, og_stats &s, void *c) {
     const uint32_t src_ = *(uint32_t *)c;
+    if (en->frag) return run_frontier<EKF<void>>(en, OG_ALGO_BFS, src_, s);
     // the device-driven loop needs no staging pipeline: direct mode or a
     // fully resident graph
     const bool dev = en->level_loop == OG_LOOP_AUTO &&
@@ -2282,6 +2588,7 @@ extern "C" int og_sssp(og_engine *e, uint32_t src, uint32_t *out_dist, og_stats 
   if (e && e->g->kind != OG_GRAPH_WEIGHTED) return fail(OG_E_UNSUPPORTED, "SSSP needs a weighted graph");
   return query_common(e, OG_ALGO_SSSP, st, out_dist, [](og_engine *en, og_stats &s, void *c) {
     const uint32_t src_ = *(uint32_t *)c;
+    if (en->frag) return run_frontier<EKF<uint8_t>>(en, OG_ALGO_SSSP, src_, s);
     if (en->level_loop == OG_LOOP_AUTO && (en->plan.dynamic_edges == 0 || (en->cfg.flags & OG_CFG_DIRECT)))
       return run_min_dev(en, OG_ALGO_SSSP, src_, s);
     if (en->wbytes == 1) return run_frontier<EK<uint8_t>>(en, OG_ALGO_SSSP, src_, s);
@@ -2392,6 +2699,7 @@ extern "C" int og_cc(og_engine *e, uint32_t *out_label, og_stats *st) {
     if (en->cc_method == OG_CC_UNION_FIND && en->g->symmetric != 1)
       return fail(OG_E_ARG, "union-find CC needs a graph known to be symmetric (og_graph_symmetric)");
     if (uf) return run_cc_uf(en, s);
+    if (en->frag) return run_frontier<EKF<void>>(en, OG_ALGO_CC, 0, s);
     if (en->level_loop == OG_LOOP_AUTO && (en->plan.dynamic_edges == 0 || (en->cfg.flags & OG_CFG_DIRECT)))
       return run_min_dev(en, OG_ALGO_CC, 0, s);
     return run_frontier<EKU>(en, OG_ALGO_CC, 0, s);

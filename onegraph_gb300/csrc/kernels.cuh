@@ -456,8 +456,10 @@ struct SrcP {
   // bpe is; a weight above it may need a third word.
   __device__ __forceinline__ Item at(uint64_t c, uint32_t x) const {
     const uint64_t b = c + x * bpe;
-    const uint32_t *w = words + (b >> 5);
-    const uint32_t r = (uint32_t)b & 31u;
+    return decode(words + (b >> 5), (uint32_t)b & 31u);
+  }
+  // The record starting at bit r of w[0] (w[1], w[2] hold its rest).
+  __device__ __forceinline__ Item decode(const uint32_t *w, uint32_t r) const {
     const uint32_t lo = w[0], hi = w[1];
     const uint32_t f = __funnelshift_r(lo, hi, r);
     const uint32_t col = bc >= 32 ? f : f & ((1u << bc) - 1u);
@@ -472,6 +474,76 @@ struct SrcP {
     }
   }
 };
+
+// Dynamic-region records with fragment slots (the static-region replacement
+// the reference declares as bfs_kernelStaticSwap / recordFragmentVisit,
+// BFS/oneGraph_BFS/gpu_kernels.h:46-66,153-176): the page-locked record
+// stream is cut into fragments of 2^fs words, and slot_of[f] >= 0 names a
+// device slot holding a copy of fragment f followed by the stream's next
+// words (a slot is 2^fs + kFragPad words), so a record whose first word lies
+// in the fragment is read whole from the slot.  Other records are read from
+// the host stream, which holds every record: slots only redirect reads, and
+// results never depend on which fragments hold one.  note() counts, per
+// fragment, the records a tile lists (by their first word); the host's
+// replacement policy reads the counts between rounds.  The slot table only
+// changes between launches.
+constexpr uint32_t kFragPad = 4;  // words after a fragment's copy (keeps slots 16-byte aligned)
+template <bool kW>
+struct SrcF : SrcP<kW> {
+  using Item = typename SrcP<kW>::Item;
+  const uint32_t *slots;
+  const int32_t *slot_of;
+  uint32_t *visits;
+  uint32_t fs;
+  __device__ __forceinline__ const uint32_t *word_ptr(uint64_t q) const {
+    const int32_t s = __ldg(slot_of + (q >> fs));
+    return s >= 0 ? slots + (uint64_t)s * ((1ull << fs) + kFragPad) + (q & ((1ull << fs) - 1)) : this->words + q;
+  }
+  __device__ __forceinline__ Item at(uint64_t c, uint32_t x) const {
+    const uint64_t b = c + x * this->bpe;
+    return this->decode(word_ptr(b >> 5), (uint32_t)b & 31u);
+  }
+  // cnt records from edge index e on: one visit count per fragment they start in.
+  __device__ __forceinline__ void note(uint64_t e, uint32_t cnt) const {
+    uint64_t b = e * this->bpe;
+    while (cnt) {
+      const uint64_t f = b >> (5 + fs);
+      const uint32_t left = (uint32_t)(((f + 1) << (5 + fs)) - b);  // bits to the next fragment, < 2^25
+      const uint32_t n = min(cnt, (left + this->bpe - 1) / this->bpe);
+      atomicAdd(visits + f, n);
+      cnt -= n;
+      b += (uint64_t)n * this->bpe;
+    }
+  }
+};
+
+// Copies fragment pairs[i].x of the record stream `words` (nwords words,
+// padding included) into slot pairs[i].y: one CTA per pair.
+__global__ void __launch_bounds__(kThreads) k_frag_fill(const uint32_t *words, uint64_t nwords, uint32_t *slots,
+                                                        const uint2 *pairs, uint32_t n, uint32_t fs) {
+  if (blockIdx.x >= n) return;
+  const uint2 p = pairs[blockIdx.x];
+  const uint64_t q0 = (uint64_t)p.x << fs;
+  const uint64_t len = min((uint64_t)(1ull << fs) + kFragPad, nwords - min(nwords, q0));
+  uint32_t *dst = slots + (uint64_t)p.y * ((1ull << fs) + kFragPad);
+  // fragment starts are multiples of 2^fs >= 256 words and slots are
+  // 16-byte aligned: whole uint4s first, then the tail
+  const uint64_t n4 = len / 4;
+  const uint4 *s4 = reinterpret_cast<const uint4 *>(words + q0);
+  uint4 *d4 = reinterpret_cast<uint4 *>(dst);
+  for (uint64_t i = threadIdx.x; i < n4; i += kThreads) d4[i] = s4[i];
+  for (uint64_t i = n4 * 4 + threadIdx.x; i < len; i += kThreads) dst[i] = words[q0 + i];
+}
+
+// Slot table update after k_frag_fill: pairs[i] = (fragment, slot), and
+// evict[i] the fragment that slot held before (UINT32_MAX: none).
+__global__ void k_frag_table(int32_t *slot_of, const uint2 *pairs, const uint32_t *evict, uint32_t n) {
+  const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  // a fragment is never both evicted and filled in one update
+  if (evict[i] != 0xffffffffu) slot_of[evict[i]] = -1;
+  slot_of[pairs[i].x] = (int32_t)pairs[i].y;
+}
 
 struct DstU {
   uint32_t *col;
@@ -518,11 +590,17 @@ struct PrShared {
 //  list_val(v, e)   the source value belongs to the list entry at address e
 //                   (an array parallel to the compacted list) instead of
 //                   src_val(v);
-//  probe_v(e, val)  the probe also sees the source value.
+//  probe_v(e, val)  the probe also sees the source value;
+// and a source hook:
+//  note(e, n)       the tile lists n records from edge index e on (SrcF).
 template <class T, class = void>
 struct HasListVal : std::false_type {};
 template <class T>
 struct HasListVal<T, std::void_t<decltype(&T::list_val)>> : std::true_type {};
+template <class T, class = void>
+struct HasNote : std::false_type {};
+template <class T>
+struct HasNote<T, std::void_t<decltype(&T::note)>> : std::true_type {};
 template <class T, class = void>
 struct HasProbeVal : std::false_type {};
 template <class T>
@@ -590,6 +668,7 @@ __device__ __forceinline__ uint32_t lbs_setup(const LbsArgs &a, const Src &src, 
     if (q1 > pos0 + r) {
       const uint64_t first = e0 + r, last = e0 + (q1 - pos0) - 1;
       if (pn < p || last < first || last >= a.edge_bound) bad = true;
+      else if constexpr (HasNote<Src>::value) src.note(first, (uint32_t)(last - first + 1));
     }
     if constexpr (HasListVal<Op>::value) sh.val[j] = op.list_val(v, a.list + i);
     else if constexpr (kNeedVal) sh.val[j] = op.src_val(v);

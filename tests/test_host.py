@@ -32,7 +32,7 @@ def test_abi_exports_every_header_symbol():
         assert hasattr(lib, name), name
     bound = {n for n, _, _ in og.SIGNATURES}
     assert declared <= bound, declared - bound
-    assert lib.og_abi_version() == og.ABI_VERSION == 5
+    assert lib.og_abi_version() == og.ABI_VERSION == 6
 
 
 def test_csr_roundtrip_all_kinds(tmp_path):
