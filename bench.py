@@ -995,6 +995,10 @@ def run_cc_oom(args, rank, world, local):
     g, gen_s = make_graph(args.scale)
     eng = og.Engine(g, budget=int(args.budget_gib * GIB), advisek=args.advisek,
                     direct=bool(args.direct), device=local)
+    # page-locked result buffer and link probe before the warm-up (a large
+    # page-locked allocation between queries slows the queries after it)
+    host = torch.empty(g.V, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
+    h2d = h2d_peak_gbs()
     for _ in range(args.warmup):
         eng.cc(out=False)
     sampler = ClockSampler(local)
@@ -1020,7 +1024,6 @@ def run_cc_oom(args, rank, world, local):
     same = eng.checksum(og.ALGO_CC) == check
     eng.set_param(og.PARAM_CC_METHOD, og.CC_AUTO)
     eng.cc(out=False)
-    host = torch.empty(g.V, dtype=torch.int32, pin_memory=True).numpy().view(np.uint32)
     e0 = time.perf_counter()
     for _ in range(args.steps):
         eng.cc(out=host)
@@ -1032,7 +1035,6 @@ def run_cc_oom(args, rank, world, local):
     lp_visits = lp_stats["edges_static"] + lp_stats["edges_dynamic"]
     dyn_ms = sum(x["ms_dynamic"] for x in stats)
     dyn_bytes = sum(x["link_bytes"] for x in stats)
-    h2d = h2d_peak_gbs()
     link_gbs = dyn_bytes / (dyn_ms / 1e3) / 1e9 if dyn_ms else 0.0
     # CPU: the serial label propagation's first round over the same graph,
     # bounded, as an edge-visit rate; the full run is extrapolated by the edge

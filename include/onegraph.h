@@ -311,6 +311,16 @@ int og_pr_l1_push(og_engine *e, float *out_rank, double damping, double tol, int
  * NULL.  Depths are identical to n separate og_bfs calls. */
 int og_bfs_batch(og_engine *e, const uint32_t *srcs, int n, uint32_t *out,
                  uint64_t *checks, og_stats *st);
+
+/* og_bfs_batch with source i's V depths copied to outs[i] (n host arrays of
+ * V u32 each, page-locked for the copies to run at link speed) instead of one
+ * contiguous n x V array: callers whose requests each own a result buffer
+ * (the server's BFS requests) share one pass.  Same device depth matrix,
+ * checks and results as og_bfs_batch; needs the persistent kernel (not
+ * OG_CFG_BATCH_LEVELS).  No reference counterpart (CalculateOpt.h:55-209
+ * runs sources one by one). */
+int og_bfs_batch_to(og_engine *e, const uint32_t *srcs, int n, uint32_t *const *outs,
+                    uint64_t *checks, og_stats *st);
 /* Multi-source SSSP: up to k sources (the engine's OG_CFG_SSSP_BATCH(k)) in
  * one pass.  Every round compacts the vertices whose distance from some
  * source improved, and one edge-balanced relax serves every source active at

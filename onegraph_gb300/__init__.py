@@ -191,6 +191,7 @@ SIGNATURES = [
     ("og_bfs_batch_step", C.c_int, [_P, C.POINTER(C.c_uint64), C.POINTER(C.c_int), C.POINTER(Stats)]),
     ("og_bfs_batch_checks", C.c_int, [_P, C.c_uint64, _P]),
     ("og_bfs_batch_fetch", C.c_int, [_P, C.c_uint32, _P]),
+    ("og_bfs_batch_to", C.c_int, [_P, _P, C.c_int, _P, _P, C.POINTER(Stats)]),
     ("og_bfs_batch_u8", C.c_int, [_P, _P, C.c_int, _P, C.POINTER(C.c_uint64), _P, C.POINTER(Stats)]),
     ("og_host_alloc", C.c_int, [C.c_uint64, C.POINTER(_P)]),
     ("og_host_free", None, [_P]),
@@ -507,6 +508,22 @@ class Engine:
                "og_bfs_batch")
         self.stats = st.as_dict()
         return o, ck
+
+    def bfs_batch_to(self, srcs, outs):
+        """og_bfs_batch_to: source i's depths into outs[i] (one V-array each).
+        Returns the n x 2 checks."""
+        s = np.ascontiguousarray(srcs, dtype=np.uint32)
+        n = s.size
+        assert len(outs) == n
+        for o in outs:
+            assert o.dtype == np.uint32 and o.size >= self.graph.V and o.flags.c_contiguous
+        ptrs = (C.c_void_p * n)(*[o.ctypes.data for o in outs])
+        ck = np.empty((n, 2), np.uint64)
+        st = Stats()
+        _check(lib().og_bfs_batch_to(self._h, _ptr(s), n, C.cast(ptrs, C.c_void_p), _ptr(ck), C.byref(st)),
+               "og_bfs_batch_to")
+        self.stats = st.as_dict()
+        return ck
 
     def sssp_batch(self, srcs, out=None, checks: bool = True):
         """Up to k SSSP sources (Engine(sssp_batch=k)) in one pass.  Returns

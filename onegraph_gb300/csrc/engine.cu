@@ -1862,14 +1862,16 @@ int run_persist_graph(og_engine *e, uint32_t n, int ci, bool *used_graph) {
 }
 
 // out: V u32 depths per source (out_bytes 4) or byte depths (out_bytes 1).
+// outs (og_bfs_batch_to): source i's V u32 depths go to outs[i] instead.
 int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, void *out, int out_bytes,
-                      uint64_t *clamped, uint64_t *checks, og_stats &st, int ci) {
+                      uint64_t *clamped, uint64_t *checks, og_stats &st, int ci,
+                      uint32_t *const *outs = nullptr) {
   const uint64_t V = e->V;
   memcpy(e->srcs_h, srcs, 4 * n);
   uint32_t *depth_d = nullptr;
   uint8_t *depth8_d = nullptr;
   bool graph = false;
-  if (out && out_bytes == 4) {
+  if ((out && out_bytes == 4) || outs) {
     RC(depth_matrix(e, n, &depth_d));
     k_fill_u32<<<grid_for(n * V, e->sms), kThreads, 0, e->s_main>>>(depth_d, (uint64_t)n * V,
                                                                  (uint32_t)(V + 1));
@@ -1888,7 +1890,7 @@ int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, void *out,
   }
   // events outside any captured graph: they bracket the whole batch on s_main
   CK(cudaEventRecord(e->t_s0, e->s_main));
-  if (out) {
+  if (out || outs) {
     RC(enqueue_persist(e, n, ci, depth_d, depth8_d));
   } else {
     RC(run_persist_graph(e, n, ci, &graph));
@@ -1920,7 +1922,10 @@ int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, void *out,
       checks[2 * i] = r;
       checks[2 * i + 1] = d;
     }
-  if (out && out_bytes == 4) {
+  if (outs) {
+    for (uint32_t i = 0; i < n; i++)
+      CK(cudaMemcpyAsync(outs[i], depth_d + (uint64_t)i * V, 4ull * V, cudaMemcpyDeviceToHost, e->s_main));
+  } else if (out && out_bytes == 4) {
     CK(cudaMemcpyAsync(out, depth_d, 4ull * n * V, cudaMemcpyDeviceToHost, e->s_main));
   } else if (out) {
     CK(cudaMemcpyAsync(out, depth8_d, (uint64_t)n * V, cudaMemcpyDeviceToHost, e->s_main));
@@ -2753,6 +2758,7 @@ struct BatchCtx {
   int mode;  // 0 persistent (tuned configuration), 1 host-driven levels, 2+k persistent config k
   uint8_t *out8 = nullptr;  // og_bfs_batch_u8
   uint64_t *clamped = nullptr;
+  uint32_t *const *outs = nullptr;  // og_bfs_batch_to
 };
 
 int batch_body(og_engine *en, og_stats &s, void *cx) {
@@ -2760,7 +2766,7 @@ int batch_body(og_engine *en, og_stats &s, void *cx) {
   if (b.mode == 1) return run_batch(en, b.srcs, b.n, b.out, b.checks, s);
   const int ci = b.mode >= 2 ? b.mode - 2 : (en->tuned >= 0 ? en->tuned : 0);
   if (b.out8) return run_batch_persist(en, b.srcs, b.n, b.out8, 1, b.clamped, b.checks, s, ci);
-  return run_batch_persist(en, b.srcs, b.n, b.out, 4, nullptr, b.checks, s, ci);
+  return run_batch_persist(en, b.srcs, b.n, b.out, 4, nullptr, b.checks, s, ci, b.outs);
 }
 
 int batch_checks(og_engine *e, const uint32_t *srcs, int n) {
@@ -2777,6 +2783,19 @@ extern "C" int og_bfs_batch(og_engine *e, const uint32_t *srcs, int n, uint32_t 
                             uint64_t *checks, og_stats *st) {
   RC(batch_checks(e, srcs, n));
   BatchCtx c{srcs, (uint32_t)n, out, checks, (e->cfg.flags & OG_CFG_BATCH_LEVELS) ? 1 : 0};
+  return query_common(e, OG_ALGO_BFS, st, nullptr, batch_body, &c);
+}
+
+extern "C" int og_bfs_batch_to(og_engine *e, const uint32_t *srcs, int n, uint32_t *const *outs,
+                               uint64_t *checks, og_stats *st) {
+  RC(batch_checks(e, srcs, n));
+  if (!outs) return fail(OG_E_ARG, "og_bfs_batch_to: null output list");
+  for (int i = 0; i < n; i++)
+    if (!outs[i]) return fail(OG_E_ARG, "og_bfs_batch_to: output %d is null", i);
+  if (e->cfg.flags & OG_CFG_BATCH_LEVELS)
+    return fail(OG_E_UNSUPPORTED, "og_bfs_batch_to runs the persistent kernel (engine has OG_CFG_BATCH_LEVELS)");
+  BatchCtx c{srcs, (uint32_t)n, nullptr, checks, 0};
+  c.outs = outs;
   return query_common(e, OG_ALGO_BFS, st, nullptr, batch_body, &c);
 }
 

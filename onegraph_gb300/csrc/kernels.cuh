@@ -904,8 +904,11 @@ struct BfsOp {
     }
     const uint32_t w = v >> 5, bit = 1u << (v & 31);
     if (p & bit) return;
-    const uint32_t old = atomicOr(visited + w, bit);
-    if (old & bit) return;
+    // The probe holds every bit set before this launch, so v is reached at
+    // this level, by this thread or another one of the launch: every writer
+    // stores the same depth and sets the same bits.  No atomic's old value
+    // is needed, so none is waited for (the atomics compile to reductions).
+    atomicOr(visited + w, bit);
     depth[v] = newdepth;
     atomicOr(next + w, bit);
   }
@@ -937,8 +940,11 @@ struct MinOp {
     }
     const uint32_t cand = kWeighted ? sv + edge_w(e) : sv;
     if (cand >= p) return;
-    const uint32_t old = atomicMin(value + v, cand);
-    if (cand < old) atomicOr(next + (v >> 5), 1u << (v & 31));
+    // cand < p: v's value drops in this launch, to cand here or lower by
+    // another thread that marks v as well, so v is in the next frontier
+    // either way.  The atomics' old values are not needed (reductions).
+    atomicMin(value + v, cand);
+    atomicOr(next + (v >> 5), 1u << (v & 31));
   }
 };
 

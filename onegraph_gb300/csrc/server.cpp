@@ -15,7 +15,8 @@
 //    free for the next one.  So requests join and leave a pass in flight.
 //  * when a worker admits a BFS request it also takes the BFS requests for
 //    the same graph that queued up meanwhile (up to max_batch) and serves
-//    them in one og_bfs_batch pass; with OG_SERVER_BFS_JOIN the pass runs
+//    them in one og_bfs_batch pass (og_bfs_batch_to when the requests carry
+//    result buffers, at most 8 GiB of depths per pass); with OG_SERVER_BFS_JOIN the pass runs
 //    level by level (og_bfs_batch_begin / _join / _step) and BFS requests
 //    queued meanwhile join it at every level boundary, as SSSP requests join
 //    SSSP passes;
@@ -80,6 +81,10 @@ namespace {
 
 using og::fail;
 
+// Device bytes of the depth matrix of one batched pass of BFS requests that
+// carry result buffers (outside the server's budget, like og_bfs_batch's).
+constexpr uint64_t kBfsOutMatrixBytes = 8ull << 30;
+
 struct Job {
   std::vector<Pending> reqs;
   og_engine *ctx = nullptr;
@@ -141,15 +146,20 @@ bool pick(og_server *s, Job &job) {
       return true;
     }
     job.reqs.push_back(*it);
-    const bool bfs_batch = it->r.algo == OG_ALGO_BFS && gs.batch && s->cfg.max_batch > 1 && !it->r.out;
+    // BFS requests with result buffers share a pass too (og_bfs_batch_to);
+    // its n x V depth matrix is kept within kBfsOutMatrixBytes
+    const bool with_out = it->r.out != nullptr;
+    const int bfs_cap = with_out ? (int)std::min<uint64_t>(64, kBfsOutMatrixBytes / (4ull * gs.g->V)) : 64;
+    const bool bfs_batch = it->r.algo == OG_ALGO_BFS && gs.batch && s->cfg.max_batch > 1 && bfs_cap > 1;
     // PageRank does not depend on a source: queued PR requests for the same
     // graph and iteration count are answered by one computation
     const bool pr_share = it->r.algo == OG_ALGO_PR && s->cfg.max_batch > 1;
     const int iters = it->r.iterations;
+    const int limit = bfs_batch ? std::min(s->cfg.max_batch, bfs_cap) : s->cfg.max_batch;
     it = s->queue.erase(it);
     if (bfs_batch || pr_share) {
-      for (auto jt = s->queue.begin(); jt != s->queue.end() && (int)job.reqs.size() < s->cfg.max_batch;) {
-        const bool same_bfs = bfs_batch && jt->r.algo == OG_ALGO_BFS && !jt->r.out;
+      for (auto jt = s->queue.begin(); jt != s->queue.end() && (int)job.reqs.size() < limit;) {
+        const bool same_bfs = bfs_batch && jt->r.algo == OG_ALGO_BFS && (jt->r.out != nullptr) == with_out;
         const bool same_pr = pr_share && jt->r.algo == OG_ALGO_PR && jt->r.iterations == iters;
         if (jt->r.graph == job.graph && (same_bfs || same_pr)) {
           job.reqs.push_back(*jt);
@@ -393,9 +403,14 @@ void run_job(og_server *s, Job &job) {
     }
   } else if (job.reqs.size() > 1) {
     std::vector<uint32_t> srcs;
-    for (auto &p : job.reqs) srcs.push_back(p.r.source);
+    std::vector<uint32_t *> outs;
+    for (auto &p : job.reqs) {
+      srcs.push_back(p.r.source);
+      outs.push_back((uint32_t *)p.r.out);
+    }
     std::vector<uint64_t> checks(2 * srcs.size());
-    const int rc = og_bfs_batch(e, srcs.data(), (int)srcs.size(), nullptr, checks.data(), &st);
+    const int rc = outs[0] ? og_bfs_batch_to(e, srcs.data(), (int)srcs.size(), outs.data(), checks.data(), &st)
+                           : og_bfs_batch(e, srcs.data(), (int)srcs.size(), nullptr, checks.data(), &st);
     for (size_t i = 0; i < job.reqs.size(); i++) respond(job.reqs[i], rc, rc == OG_OK ? &checks[2 * i] : nullptr);
   } else {
     const Pending &p = job.reqs[0];

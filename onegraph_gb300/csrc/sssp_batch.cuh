@@ -277,13 +277,19 @@ struct SbOp {
     {
       const uint32_t s = __ffs(m) - 1;
       const uint32_t cand = ru[s] + w;
-      if (cand < p && cand < atomicMin(rv + s, cand)) nb |= 1u << s;
+      if (cand < p) {
+        atomicMin(rv + s, cand);
+        nb |= 1u << s;
+      }
       m &= m - 1;
     }
     for (; m; m &= m - 1) {
       const uint32_t s = __ffs(m) - 1;
       const uint32_t cand = ru[s] + w;
-      if (cand < __ldcg(rv + s) && cand < atomicMin(rv + s, cand)) nb |= 1u << s;
+      if (cand < __ldcg(rv + s)) {
+        atomicMin(rv + s, cand);
+        nb |= 1u << s;
+      }
     }
     if (nb) {
       atomicOr(pend + v, nb);
@@ -370,7 +376,13 @@ __device__ __forceinline__ void sb_tile(const LbsArgs &a, const Src &src, const 
         for (int t = 0; t < C; t++) {
           if ((cm >> t) & 1u) {
             const uint32_t cand = ru[t] + w;
-            if (cand < d[t] && cand < atomicMin(rv + t, cand)) nb[j] |= 1u << (C * c + t);
+            // distances only fall during a launch: cand < d[t] means the
+            // pair improves in this launch (here, or lower by another
+            // thread that marks it pending too), so no old value is waited for
+            if (cand < d[t]) {
+              atomicMin(rv + t, cand);
+              nb[j] |= 1u << (C * c + t);
+            }
           }
         }
       }

@@ -46,6 +46,31 @@ def test_batch_equals_single_source(weighted):
         e.close()
 
 
+def test_batch_to_separate_buffers_equals_single_source():
+    """og_bfs_batch_to: each source's depths land in its own host array
+    (page-locked and pageable), equal to og_bfs and to og_bfs_batch's rows;
+    a host-driven-levels engine refuses it."""
+    g = og.Graph.rmat(12, 16, seed=11)
+    rng = np.random.default_rng(2)
+    srcs = rng.integers(0, g.V, 9).astype(np.uint32)
+    for cname, kw in batch_configs(g):
+        e = og.Engine(g, batch=True, **kw)
+        want = np.stack([e.bfs(int(s)) for s in srcs])
+        outs = [og.pinned_empty(g.V, np.uint32) if i % 2 else np.full(g.V, 7, np.uint32)
+                for i in range(srcs.size)]
+        ck = e.bfs_batch_to(srcs, outs)
+        for i in range(srcs.size):
+            np.testing.assert_array_equal(outs[i], want[i], err_msg="%s source %d" % (cname, i))
+        _, ck2 = e.bfs_batch(srcs, out=False)
+        np.testing.assert_array_equal(ck, ck2)
+        e.close()
+    lv = og.Engine(g, batch_levels=True, budget=1 << 30, advisek=1.0)
+    with pytest.raises(og.OGError) as ex:
+        lv.bfs_batch_to(srcs[:2], [np.empty(g.V, np.uint32) for _ in range(2)])
+    assert ex.value.status == 9
+    lv.close()
+
+
 def test_persistent_graph_levels_and_all_configs_agree():
     """The persistent kernel (direct launch or CUDA-graph replay), the
     host-driven level loop and every autotuner candidate give the same depths."""
