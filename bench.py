@@ -64,6 +64,9 @@ def parse_args():
     ap.add_argument("--tune", type=int, default=1, help="bfs-batch: run the autotuner first")
     ap.add_argument("--serving-scales", default="22,24,26,27")
     ap.add_argument("--serving-budget-gib", type=float, default=24.0)
+    ap.add_argument("--serving-slots", default=None,
+                    help="serving: SSSP sources per multi-source pass for each graph (comma list, one per "
+                         "--serving-scales entry); default per scale: 16 (22, 24), 8 (26), 4 (27)")
     ap.add_argument("--requests", type=int, default=400)
     ap.add_argument("--rate", type=float, default=2000.0)
     ap.add_argument("--serving-legs", default="all", choices=["all", "served"],
@@ -90,6 +93,9 @@ def parse_args():
         a.scale = {"pr-precision": 26, "bfs-resident": 20}.get(a.workload, 27)
     if a.workload == "serving":
         a.steps = max(1, a.steps)
+    if a.serving_slots:
+        SERVING_SLOTS.update(zip((int(x) for x in a.serving_scales.split(",")),
+                                 (int(x) for x in a.serving_slots.split(","))))
     if a.budget_gib is None:
         a.budget_gib = 6.0 if a.workload == "pr-precision" else 8.0
     return a
@@ -1096,10 +1102,14 @@ def run_cc_oom(args, rank, world, local):
 SERVING_GRAPHS = {22: (1.0, 16), 24: (3.75, 16), 26: (6.75, 8), 27: (12.2, 4)}
 
 
+SERVING_SLOTS: dict = {}  # --serving-slots overrides by scale
+
+
 def serving_graph(sc: int):
     """(budget GiB, SSSP sources per pass) of a serving graph; smaller test
     graphs get 1 GiB and 8 sources."""
-    return SERVING_GRAPHS.get(sc, (1.0, 8))
+    b, k = SERVING_GRAPHS.get(sc, (1.0, 8))
+    return b, SERVING_SLOTS.get(sc, k)
 # direct mode keeps no staging buffers, so the whole edge share is static
 SERVING_ADVISEK = 1.0
 ALGO_BFS, ALGO_SSSP, ALGO_PR = 0, 1, 3  # og_algo values (the reference arm loads no engine)
