@@ -63,6 +63,8 @@ struct FragState {
   std::vector<float> score;      // records listed per fragment, halved every step
   std::vector<void *> dallocs, hallocs;
   uint64_t dalloc_bytes = 0;
+  uint64_t since = 0;      // dynamic records listed since the last policy step
+  uint64_t step_min = 0;   // records between policy steps (an eighth of the slots' records)
   og_fragment_stats st{};
 };
 
@@ -315,6 +317,8 @@ int frag_layout(og_engine *e, uint32_t fs) {
   F.slot_of.assign(F.nfrag, -1);
   F.owner.assign(F.nslots, 0xffffffffu);
   F.score.assign(F.nfrag, 0.0f);
+  F.since = 0;
+  F.step_min = (uint64_t)((double)F.nslots * (double)(1ull << fs) * 32.0 / e->bpe / 8.0);
   F.st = og_fragment_stats{};
   F.st.fragments = F.nfrag;
   F.st.slots = F.nslots;
@@ -361,16 +365,20 @@ int frag_reset(og_engine *e) {
   return OG_OK;
 }
 
-// After a compaction (the previous round's relax has finished): reads the
-// round's visit counts, moves the records served from slots out of the
+// After a compaction (the previous round's relax has finished), once an
+// eighth of the slots' records have been listed since the last step or when
+// `force` (a compaction that lists nothing, e.g. the query's last): reads
+// the visit counts, moves the records served from slots out of the
 // host-link bytes, and replaces slots.  Ascetic's rule: fragments read in
 // this round that have no slot take the slots of fragments that were read
 // least; scores are records listed, halved every step; a fragment comes in
 // only if its score is at least a quarter of its records and above twice the
 // evicted one's; the copies of one step read at most a quarter of the
 // round's host-link bytes.  The dynamic stream waits for the updates.
-int frag_step(og_engine *e, og_stats &st) {
+int frag_step(og_engine *e, og_stats &st, bool force) {
   FragState &F = *e->frag;
+  if (!force && F.since < F.step_min) return OG_OK;  // counts keep adding up on the device
+  F.since = 0;
   cudaStream_t s = e->s_main;
   CK(cudaMemcpyAsync(F.visits_h, F.visits_d, 4 * F.nfrag, cudaMemcpyDeviceToHost, s));
   CK(cudaMemsetAsync(F.visits_d, 0, 4 * F.nfrag, s));
@@ -1174,7 +1182,7 @@ int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
     sp.clear_bits = split ? waiting : nullptr;
     sp.far_bits = split && !advance ? waiting : nullptr;
     RC(compact_round(e, advance ? waiting : cur, st, tm, &n, sp));
-    if constexpr (K::kFrag) RC(frag_step(e, st));
+    if constexpr (K::kFrag) RC(frag_step(e, st, n == 0));
     if (split) {
       const uint32_t fm = std::min(far_of(e, 0), far_of(e, 1));
       far_min = advance ? fm : std::min(far_min, fm);
@@ -1208,6 +1216,7 @@ int run_frontier(og_engine *e, int algo, uint32_t src, og_stats &st) {
       return launch_relax_pair(e, ro, a0, s0, a1, s1, next, ps);
     };
     RC((run_regions<K>(e, st, tm, sfn, dfn, pfn)));
+    if constexpr (K::kFrag) e->frag->since += e->counts_h[1].total;
     CK(cudaStreamWaitEvent(e->s_main, e->ev_cd, 0));
     CK(cudaMemsetAsync(cur, 0, 4 * e->nwords, e->s_main));
     std::swap(cur, next);
