@@ -444,8 +444,14 @@ def run_ours(args, rank, world, local):
     static_gbs = (eb + 4) * static_dev / (relax_dev_ms / 1e3) / 1e9 if relax_dev_ms else 0.0
     host_link_gbs = dyn_bytes / (relax_ms / 1e3) / 1e9 if relax_ms else 0.0
     host_static_gbs = ((eb + 4) * st_edges + 20 * st_verts) / (relax_ms / 1e3) / 1e9 if relax_ms else 0.0
+    rounds_dev = statistics.mean(s["iterations"] for s in tstats)
     roof_link = {"bound": "host-link", "kernel": kname, "achieved": link_gbs, "peak": h2d, "unit": "GB/s",
-                 "frac": link_gbs / h2d if h2d else None, "traffic": None,
+                 "frac": link_gbs / h2d if h2d else None,
+                 "traffic": link_dev / max(rounds_dev, 1) * SSSP_RELAX_LINK_TRAFFIC_RATIO,
+                 "traffic_note": "host-link bytes per relax launch: this query's algorithmic link bytes per round "
+                                 "x %.3f, the sysmem-sector / algorithmic ratio ncu measured for the same relax's "
+                                 "largest dynamic launch on R-MAT 22 under a 256 MiB budget"
+                                 % SSSP_RELAX_LINK_TRAFFIC_RATIO,
                  "peak_source": "highest of the link probes measured in this run (og_link_probe)", "link_probes": dict(LINK_PEAKS),
                  "timing": "globaltimer stamps around every relax launch of %d device-driven queries "
                            "(the timed queries' sources, timer on)" % len(tstats)}
@@ -1117,6 +1123,9 @@ ALGO_BFS, ALGO_SSSP, ALGO_PR = 0, 1, 3  # og_algo values (the reference arm load
 # bytes, measured with ncu on R-MAT 22 directed under a 256 MiB budget:
 # 2,025,677 sectors of 32 B for 64.2 MB of records per iteration
 PR_PULL_LINK_TRAFFIC_RATIO = 1.010
+# the same for the single-source SSSP relax's largest dynamic launch on R-MAT
+# 22 weighted, 256 MiB: 96.6 MB of sysmem sectors for 94.8 MB of records
+SSSP_RELAX_LINK_TRAFFIC_RATIO = 1.019
 
 
 def serving_requests(degrees, n, rate, seed=4):
