@@ -314,13 +314,16 @@ int og_pr_l1_push(og_engine *e, float *out_rank, double damping, double tol, int
 int og_bfs_batch(og_engine *e, const uint32_t *srcs, int n, uint32_t *out,
                  uint64_t *checks, og_stats *st);
 
-/* og_bfs_batch with source i's V depths copied to outs[i] (n host arrays of
- * V u32 each, page-locked for the copies to run at link speed) instead of one
- * contiguous n x V array: callers whose requests each own a result buffer
- * (the server's BFS requests) share one pass.  Same device depth matrix,
- * checks and results as og_bfs_batch; needs the persistent kernel (not
- * OG_CFG_BATCH_LEVELS).  No reference counterpart (CalculateOpt.h:55-209
- * runs sources one by one). */
+/* og_bfs_batch with source i's V depths written to outs[i] (n host arrays
+ * of V u32 each) instead of one contiguous n x V array: callers whose
+ * requests each own a result buffer (the server's BFS requests) share one
+ * pass.  The persistent kernel writes byte depths (an n x V byte device
+ * matrix kept between calls, outside the budget), and each row is widened
+ * in a V-entry device buffer and copied to its output (page-locked outputs
+ * copy at the link's rate).  If some depth reaches 255 the
+ * outputs are filled by single-source runs instead.  Checks and depths equal
+ * og_bfs_batch's; needs the persistent kernel (not OG_CFG_BATCH_LEVELS).
+ * No reference counterpart (CalculateOpt.h:55-209 runs sources one by one). */
 int og_bfs_batch_to(og_engine *e, const uint32_t *srcs, int n, uint32_t *const *outs,
                     uint64_t *checks, og_stats *st);
 /* Multi-source SSSP: up to k sources (the engine's OG_CFG_SSSP_BATCH(k)) in

@@ -1872,6 +1872,9 @@ int run_persist_graph(og_engine *e, uint32_t n, int ci, bool *used_graph) {
 
 // out: V u32 depths per source (out_bytes 4) or byte depths (out_bytes 1).
 // outs (og_bfs_batch_to): source i's V u32 depths go to outs[i] instead.
+// The kernel then writes byte depths (an n x V byte matrix, a quarter of the
+// u32 one) and each row is widened into its output; if some depth reaches
+// 255, the outputs are filled by single-source runs instead.
 int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, void *out, int out_bytes,
                       uint64_t *clamped, uint64_t *checks, og_stats &st, int ci,
                       uint32_t *const *outs = nullptr) {
@@ -1880,12 +1883,12 @@ int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, void *out,
   uint32_t *depth_d = nullptr;
   uint8_t *depth8_d = nullptr;
   bool graph = false;
-  if ((out && out_bytes == 4) || outs) {
+  if (out && out_bytes == 4) {
     RC(depth_matrix(e, n, &depth_d));
     k_fill_u32<<<grid_for(n * V, e->sms), kThreads, 0, e->s_main>>>(depth_d, (uint64_t)n * V,
                                                                  (uint32_t)(V + 1));
     e->launches++;
-  } else if (out) {  // byte depths, written by the kernel itself (0 = unreached)
+  } else if (out || outs) {  // byte depths, written by the kernel itself (0 = unreached)
     const uint64_t need = (uint64_t)n * V;
     if (need > e->depth8_cap) {
       if (e->depth8_d) cudaFree(e->depth8_d);
@@ -1932,8 +1935,34 @@ int run_batch_persist(og_engine *e, const uint32_t *srcs, uint32_t n, void *out,
       checks[2 * i + 1] = d;
     }
   if (outs) {
-    for (uint32_t i = 0; i < n; i++)
-      CK(cudaMemcpyAsync(outs[i], depth_d + (uint64_t)i * V, 4ull * V, cudaMemcpyDeviceToHost, e->s_main));
+    // entries at depth >= 255 do not fit a byte: single-source runs fill the
+    // outputs (no n x V u32 matrix is needed for that)
+    uint64_t c = 0;
+    for (uint32_t L = 254; L <= levels && L < kMaxBatchLevels; L++)
+      for (uint32_t i = 0; i < n; i++) c += e->hist_h[(uint64_t)L * 64 + i];
+    if (c) {
+      for (uint32_t i = 0; i < n; i++) {
+        og_stats one;
+        memset(&one, 0, sizeof one);
+        RC(run_frontier<EKU>(e, OG_ALGO_BFS, srcs[i], one));
+        CK(cudaMemcpyAsync(outs[i], e->value_d, 4ull * V, cudaMemcpyDeviceToHost, e->s_main));
+        CK(cudaStreamSynchronize(e->s_main));
+      }
+      e->last_algo = -1;
+      return OG_OK;
+    }
+    // widened into a V-entry device buffer, then one DMA copy per source
+    // (kernel stores straight into page-locked memory measured several
+    // times slower than the copy engine)
+    uint32_t *stage = nullptr;
+    RC(depth_matrix(e, 1, &stage));
+    for (uint32_t i = 0; i < n; i++) {
+      k_depth_expand<<<grid_for((V + 3) / 4, e->sms), kThreads, 0, e->s_main>>>(depth8_d + (uint64_t)i * V, V,
+                                                                                (uint32_t)(V + 1), stage);
+      e->launches++;
+      CK(cudaMemcpyAsync(outs[i], stage, 4ull * V, cudaMemcpyDeviceToHost, e->s_main));
+    }
+    CK(cudaGetLastError());
   } else if (out && out_bytes == 4) {
     CK(cudaMemcpyAsync(out, depth_d, 4ull * n * V, cudaMemcpyDeviceToHost, e->s_main));
   } else if (out) {

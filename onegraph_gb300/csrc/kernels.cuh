@@ -1384,6 +1384,33 @@ __global__ void k_fill_u32(uint32_t *p, uint64_t n, uint32_t v) {
     p[i] = v;
 }
 
+// Byte depths of one source (0 unreached, 1 the source, at most 254 here)
+// as u32 depths with `unreached` for 0, written to dst (device memory, or
+// page-locked host memory through its device pointer).  Four vertices per
+// thread, one 4-byte load each, when b is 4-byte aligned (rows of a matrix
+// with V not a multiple of 4 are not); else one vertex per thread.
+__global__ void k_depth_expand(const uint8_t *b, uint64_t n, uint32_t unreached, uint32_t *dst) {
+  if (reinterpret_cast<uintptr_t>(b) & 3u) {
+    for (uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < n;
+         v += (uint64_t)gridDim.x * blockDim.x)
+      dst[v] = b[v] ? b[v] : unreached;
+    return;
+  }
+  const uint64_t n4 = n / 4;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n4;
+       i += (uint64_t)gridDim.x * blockDim.x) {
+    const uchar4 q = reinterpret_cast<const uchar4 *>(b)[i];
+    dst[4 * i] = q.x ? q.x : unreached;
+    dst[4 * i + 1] = q.y ? q.y : unreached;
+    dst[4 * i + 2] = q.z ? q.z : unreached;
+    dst[4 * i + 3] = q.w ? q.w : unreached;
+  }
+  if (blockIdx.x == 0 && threadIdx.x < n - 4 * n4) {
+    const uint64_t v = 4 * n4 + threadIdx.x;
+    dst[v] = b[v] ? b[v] : unreached;
+  }
+}
+
 // ---------------------------------------------------------- bottom-up BFS
 //
 // One bottom-up level of a direction-optimizing BFS (Beamer et al., 2012)

@@ -81,8 +81,9 @@ namespace {
 
 using og::fail;
 
-// Device bytes of the depth matrix of one batched pass of BFS requests that
-// carry result buffers (outside the server's budget, like og_bfs_batch's).
+// Device bytes of the byte-depth matrix of one batched pass of BFS requests
+// that carry result buffers (og_bfs_batch_to; outside the server's budget,
+// like og_bfs_batch's): 64 sources of 2^27 vertices.
 constexpr uint64_t kBfsOutMatrixBytes = 8ull << 30;
 
 struct Job {
@@ -149,7 +150,7 @@ bool pick(og_server *s, Job &job) {
     // BFS requests with result buffers share a pass too (og_bfs_batch_to);
     // its n x V depth matrix is kept within kBfsOutMatrixBytes
     const bool with_out = it->r.out != nullptr;
-    const int bfs_cap = with_out ? (int)std::min<uint64_t>(64, kBfsOutMatrixBytes / (4ull * gs.g->V)) : 64;
+    const int bfs_cap = with_out ? (int)std::min<uint64_t>(64, kBfsOutMatrixBytes / (uint64_t)gs.g->V) : 64;
     const bool bfs_batch = it->r.algo == OG_ALGO_BFS && gs.batch && s->cfg.max_batch > 1 && bfs_cap > 1;
     // PageRank does not depend on a source: queued PR requests for the same
     // graph and iteration count are answered by one computation

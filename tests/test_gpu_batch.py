@@ -71,6 +71,45 @@ def test_batch_to_separate_buffers_equals_single_source():
     lv.close()
 
 
+def test_batch_to_depths_beyond_a_byte():
+    """A path of 601 vertices (depths up to 601, beyond the byte matrix),
+    a separate R-MAT part and two isolated vertices, V = 1627 (rows of the
+    byte matrix not 4-byte aligned): a batch with a deep source falls back
+    to single-source runs, a shallow batch takes the byte path, and both
+    equal og_bfs."""
+    L = 601
+    r = og.Graph.rmat(10, 8, seed=4)
+    ro, rc = np.array(r.offsets), np.array(r.columns)
+    V = L + r.V + 2
+    adj = [[] for _ in range(V)]
+    for i in range(L - 1):
+        adj[i].append(i + 1)
+        adj[i + 1].append(i)
+    for u in range(r.V):
+        adj[L + u].extend(int(c) + L for c in rc[ro[u]:ro[u + 1]])
+    adj = [sorted(set(a)) for a in adj]
+    off = np.concatenate([[0], np.cumsum([len(a) for a in adj])]).astype(np.uint64)
+    col = np.array([c for a in adj for c in a], np.uint32)
+    g = og.Graph.from_arrays(off, col)
+    assert g.V % 4 != 0
+    srcs = np.array([0, L // 2, L + 5, V - 1], np.uint32)
+    for kw in (dict(budget=1 << 30, advisek=1.0), dict(budget=budget_for(g, g.E // 3, og.CFG_BATCH | og.CFG_DIRECT),
+                                                       advisek=0.5, direct=True)):
+        e = og.Engine(g, batch=True, **kw)
+        want = [e.bfs(int(s)) for s in srcs]
+        assert want[0].max() > 255
+        outs = [og.pinned_empty(g.V, np.uint32) for _ in srcs]
+        e.bfs_batch_to(srcs, outs)
+        for i in range(srcs.size):
+            np.testing.assert_array_equal(outs[i], want[i])
+        # a batch whose depths all fit a byte takes the byte path
+        outs2 = [np.zeros(g.V, np.uint32) for _ in range(2)]
+        e.bfs_batch_to(srcs[2:], outs2)
+        np.testing.assert_array_equal(outs2[0], want[2])
+        np.testing.assert_array_equal(outs2[1], want[3])
+        e.close()
+
+
 def test_persistent_graph_levels_and_all_configs_agree():
     """The persistent kernel (direct launch or CUDA-graph replay), the
     host-driven level loop and every autotuner candidate give the same depths."""
