@@ -63,6 +63,7 @@ struct FragState {
   std::vector<float> score;      // records listed per fragment, halved every step
   std::vector<void *> dallocs, hallocs;
   uint64_t dalloc_bytes = 0;
+  bool broken = false;     // a layout failed: queries through the slots are refused
   uint64_t since = 0;      // dynamic records listed since the last policy step
   uint64_t step_min = 0;   // records between policy steps (an eighth of the slots' records)
   og_fragment_stats st{};
@@ -289,20 +290,37 @@ uint32_t frag_default_shift(uint64_t packed_words) {
 
 // Lays out slots of 2^fs + kFragPad words, the slot table, the visit counts
 // and the update lists inside F.bytes of device memory.
+// Device bytes of the tables and update lists for fragments of 2^fs words,
+// and the most pairs one step moves (a quarter of the slots, at most 4096).
+uint64_t frag_fixed_bytes(const FragState &F, uint64_t nfrag, uint32_t fs, uint32_t *max_pairs) {
+  const uint64_t slot_words = (1ull << fs) + kFragPad;
+  *max_pairs = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(4096, F.bytes / (4 * slot_words) / 4));
+  return nfrag * 8 + (uint64_t)*max_pairs * 12 + 5 * 256;
+}
+
+// 0 when slots of 2^fs words fit F.bytes (checked before anything is freed).
+int frag_fits(const og_engine *e, uint32_t fs) {
+  const FragState &F = *e->frag;
+  const uint64_t nfrag = (e->g->packed_words + (1ull << fs) - 1) >> fs;
+  uint32_t mp;
+  const uint64_t slot_words = (1ull << fs) + kFragPad;
+  if (F.bytes < frag_fixed_bytes(F, nfrag, fs, &mp) + 4 * slot_words)
+    return fail(OG_E_BUDGET, "fragment slots: %llu B of static region cannot hold one %llu-word slot and the "
+                "%llu-fragment tables", (unsigned long long)F.bytes, (unsigned long long)slot_words,
+                (unsigned long long)nfrag);
+  return OG_OK;
+}
+
 int frag_layout(og_engine *e, uint32_t fs) {
   FragState &F = *e->frag;
+  RC(frag_fits(e, fs));
   frag_release(e);
+  F.broken = true;  // until the layout below completes
   const og_graph *g = e->g;
   F.fs = fs;
   F.nfrag = (g->packed_words + (1ull << fs) - 1) >> fs;
   const uint64_t slot_words = (1ull << fs) + kFragPad;
-  // one step moves at most a quarter of the slots (and 4096)
-  F.max_pairs = (uint32_t)std::max<uint64_t>(1, std::min<uint64_t>(4096, F.bytes / (4 * slot_words) / 4));
-  const uint64_t fixed = F.nfrag * 8 + (uint64_t)F.max_pairs * 12 + 5 * 256;
-  if (F.bytes < fixed + 4 * slot_words)
-    return fail(OG_E_BUDGET, "fragment slots: %llu B of static region cannot hold one %llu-word slot and the "
-                "%llu-fragment tables", (unsigned long long)F.bytes, (unsigned long long)slot_words,
-                (unsigned long long)F.nfrag);
+  const uint64_t fixed = frag_fixed_bytes(F, F.nfrag, fs, &F.max_pairs);
   const uint64_t ns = std::min<uint64_t>((F.bytes - fixed) / (4 * slot_words), std::min<uint64_t>(F.nfrag, 0x7fffffffull));
   F.nslots = (uint32_t)ns;
   RC(frag_dalloc(e, &F.slots_d, ns * slot_words));
@@ -323,6 +341,7 @@ int frag_layout(og_engine *e, uint32_t fs) {
   F.st.fragments = F.nfrag;
   F.st.slots = F.nslots;
   F.st.fragment_words = 1u << fs;
+  F.broken = false;
   return OG_OK;
 }
 
@@ -345,6 +364,7 @@ int frag_apply(og_engine *e, uint32_t n, cudaStream_t s) {
 int frag_reset(og_engine *e) {
   FragState &F = *e->frag;
   cudaStream_t s = e->s_main;
+  F.broken = true;  // until every fill below is queued
   CK(cudaMemsetAsync(F.slot_of_d, 0xff, 4 * F.nfrag, s));
   CK(cudaMemsetAsync(F.visits_d, 0, 4 * F.nfrag, s));
   const uint64_t f0 = (e->plan.static_edges * e->bpe >> 5) >> F.fs;
@@ -362,6 +382,7 @@ int frag_reset(og_engine *e) {
     CK(cudaStreamSynchronize(s));  // the page-locked lists are reused
   }
   if (!F.ev_ready) CK(cudaEventCreateWithFlags(&F.ev_ready, cudaEventDisableTiming));
+  F.broken = false;
   return OG_OK;
 }
 
@@ -2548,7 +2569,7 @@ extern "C" int og_engine_set_param(og_engine *e, int param, double value) {
       CK(cudaSetDevice(e->dev));
       CK(cudaStreamSynchronize(e->s_main));
       CK(cudaStreamSynchronize(e->s_dyn));
-      RC(frag_layout(e, fs));
+      RC(frag_layout(e, fs));  // checks the fit before releasing the old layout
       RC(frag_reset(e));
       CK(cudaStreamSynchronize(e->s_main));
       return (int)OG_OK;
@@ -2617,6 +2638,8 @@ extern "C" int og_bfs(og_engine *e, uint32_t src, uint32_t *out_depth, og_stats 
   if (e && src >= e->V) return fail(OG_E_ARG, "source %u >= V %u", src, e->V);
   return query_common(e, OG_ALGO_BFS, st, out_depth, [](og_engine *en, og_stats &s, void *c) {
     const uint32_t src_ = *(uint32_t *)c;
+    if (en->frag && en->frag->broken)
+      return fail(OG_E_STATE, "the fragment slots were not laid out (a failed OG_PARAM_FRAGMENT_WORDS change)");
     if (en->frag) return run_frontier<EKF<void>>(en, OG_ALGO_BFS, src_, s);
     // the device-driven loop needs no staging pipeline: direct mode or a
     // fully resident graph
@@ -2631,6 +2654,8 @@ extern "C" int og_sssp(og_engine *e, uint32_t src, uint32_t *out_dist, og_stats 
   if (e && e->g->kind != OG_GRAPH_WEIGHTED) return fail(OG_E_UNSUPPORTED, "SSSP needs a weighted graph");
   return query_common(e, OG_ALGO_SSSP, st, out_dist, [](og_engine *en, og_stats &s, void *c) {
     const uint32_t src_ = *(uint32_t *)c;
+    if (en->frag && en->frag->broken)
+      return fail(OG_E_STATE, "the fragment slots were not laid out (a failed OG_PARAM_FRAGMENT_WORDS change)");
     if (en->frag) return run_frontier<EKF<uint8_t>>(en, OG_ALGO_SSSP, src_, s);
     if (en->level_loop == OG_LOOP_AUTO && (en->plan.dynamic_edges == 0 || (en->cfg.flags & OG_CFG_DIRECT)))
       return run_min_dev(en, OG_ALGO_SSSP, src_, s);
@@ -2742,6 +2767,8 @@ extern "C" int og_cc(og_engine *e, uint32_t *out_label, og_stats *st) {
     if (en->cc_method == OG_CC_UNION_FIND && en->g->symmetric != 1)
       return fail(OG_E_ARG, "union-find CC needs a graph known to be symmetric (og_graph_symmetric)");
     if (uf) return run_cc_uf(en, s);
+    if (en->frag && en->frag->broken)
+      return fail(OG_E_STATE, "the fragment slots were not laid out (a failed OG_PARAM_FRAGMENT_WORDS change)");
     if (en->frag) return run_frontier<EKF<void>>(en, OG_ALGO_CC, 0, s);
     if (en->level_loop == OG_LOOP_AUTO && (en->plan.dynamic_edges == 0 || (en->cfg.flags & OG_CFG_DIRECT)))
       return run_min_dev(en, OG_ALGO_CC, 0, s);

@@ -109,6 +109,15 @@ def test_replace_argument_checks():
         with pytest.raises(og.OGError) as ex:
             e.set_param(og.PARAM_FRAGMENT_WORDS, bad)
         assert ex.value.status == 1
+    # a size whose one slot does not fit the slot bytes is refused before the
+    # current layout is released: the engine keeps answering through it
+    words = e.get_param(og.PARAM_FRAGMENT_WORDS)
+    with pytest.raises(og.OGError) as ex:
+        e.set_param(og.PARAM_FRAGMENT_WORDS, 1 << 20)
+    assert ex.value.status == 4
+    assert e.get_param(og.PARAM_FRAGMENT_WORDS) == words
+    s = int(np.argmax(g.degrees()))
+    np.testing.assert_array_equal(e.sssp(s), oracle.sssp_dijkstra(np.array(g.offsets), np.array(g.edges), s))
     with pytest.raises(og.OGError) as ex:
         e.clone()
     assert ex.value.status == 9
