@@ -51,6 +51,8 @@ struct FragState {
   uint32_t *slots_d = nullptr;
   int32_t *slot_of_d = nullptr;
   uint32_t *visits_d = nullptr;  // records listed per fragment since the last step
+  unsigned long long *miss_d = nullptr;  // of those, records of slotted fragments read from the host
+  unsigned long long *miss_h = nullptr;  // page-locked
   uint2 *pairs_d = nullptr;      // one update: (fragment, slot)
   uint32_t *evict_d = nullptr;   // one update: the fragment each slot held before
   uint32_t max_pairs = 0;
@@ -253,6 +255,8 @@ void frag_release(og_engine *e) {
   F.slots_d = nullptr;
   F.slot_of_d = nullptr;
   F.visits_d = nullptr;
+  F.miss_d = nullptr;
+  F.miss_h = nullptr;
   F.pairs_d = nullptr;
   F.evict_d = nullptr;
   F.visits_h = nullptr;
@@ -326,10 +330,12 @@ int frag_layout(og_engine *e, uint32_t fs) {
   RC(frag_dalloc(e, &F.slots_d, ns * slot_words));
   RC(frag_dalloc(e, &F.slot_of_d, F.nfrag));
   RC(frag_dalloc(e, &F.visits_d, F.nfrag));
+  RC(frag_dalloc(e, &F.miss_d, 1));
   RC(frag_dalloc(e, &F.pairs_d, F.max_pairs));
   RC(frag_dalloc(e, &F.evict_d, F.max_pairs));
   if (!e->parent) e->resident_bytes += F.dalloc_bytes;
   RC(frag_halloc(e, &F.visits_h, F.nfrag));
+  RC(frag_halloc(e, &F.miss_h, 1));
   RC(frag_halloc(e, &F.pairs_h, F.max_pairs));
   RC(frag_halloc(e, &F.evict_h, F.max_pairs));
   F.slot_of.assign(F.nfrag, -1);
@@ -367,6 +373,7 @@ int frag_reset(og_engine *e) {
   F.broken = true;  // until every fill below is queued
   CK(cudaMemsetAsync(F.slot_of_d, 0xff, 4 * F.nfrag, s));
   CK(cudaMemsetAsync(F.visits_d, 0, 4 * F.nfrag, s));
+  CK(cudaMemsetAsync(F.miss_d, 0, 8, s));
   const uint64_t f0 = (e->plan.static_edges * e->bpe >> 5) >> F.fs;
   uint32_t filled = 0;
   while (filled < F.nslots && f0 + filled < F.nfrag) {
@@ -402,7 +409,9 @@ int frag_step(og_engine *e, og_stats &st, bool force) {
   F.since = 0;
   cudaStream_t s = e->s_main;
   CK(cudaMemcpyAsync(F.visits_h, F.visits_d, 4 * F.nfrag, cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(F.miss_h, F.miss_d, 8, cudaMemcpyDeviceToHost, s));
   CK(cudaMemsetAsync(F.visits_d, 0, 4 * F.nfrag, s));
+  CK(cudaMemsetAsync(F.miss_d, 0, 8, s));
   CK(cudaStreamSynchronize(s));
   uint64_t in_slots = 0, in_host = 0;
   std::vector<uint32_t> cand;
@@ -418,6 +427,10 @@ int frag_step(og_engine *e, og_stats &st, bool force) {
       if (F.score[f] >= min_score) cand.push_back((uint32_t)f);
     }
   }
+  // records of slotted fragments that a range over a fragment end read from the host
+  const uint64_t miss = std::min<uint64_t>(*F.miss_h, in_slots);
+  in_slots -= miss;
+  in_host += miss;
   F.st.records_slots += in_slots;
   F.st.records_host += in_host;
   const uint64_t slot_link = (in_slots * e->bpe) / 8;
@@ -917,6 +930,7 @@ struct EKF : EK<W> {
     h.slots = e->frag->slots_d;
     h.slot_of = e->frag->slot_of_d;
     h.visits = e->frag->visits_d;
+    h.miss = e->frag->miss_d;
     h.fs = e->frag->fs;
     return h;
   }

@@ -483,10 +483,11 @@ struct SrcP {
 // words (a slot is 2^fs + kFragPad words), so a record whose first word lies
 // in the fragment is read whole from the slot.  Other records are read from
 // the host stream, which holds every record: slots only redirect reads, and
-// results never depend on which fragments hold one.  note() counts, per
-// fragment, the records a tile lists (by their first word); the host's
-// replacement policy reads the counts between rounds.  The slot table only
-// changes between launches.
+// results never depend on which fragments hold one.  The tile setup picks
+// each vertex's source once (cur_range); note() counts, per fragment, the
+// records a tile lists (by their first word); the host's replacement policy
+// reads the counts between rounds.  The slot table only changes between
+// launches.
 constexpr uint32_t kFragPad = 4;  // words after a fragment's copy (keeps slots 16-byte aligned)
 template <bool kW>
 struct SrcF : SrcP<kW> {
@@ -494,23 +495,46 @@ struct SrcF : SrcP<kW> {
   const uint32_t *slots;
   const int32_t *slot_of;
   uint32_t *visits;
+  unsigned long long *miss;  // records of fragments with a slot that were read from the host copy
   uint32_t fs;
-  __device__ __forceinline__ const uint32_t *word_ptr(uint64_t q) const {
-    const int32_t s = __ldg(slot_of + (q >> fs));
-    return s >= 0 ? slots + (uint64_t)s * ((1ull << fs) + kFragPad) + (q & ((1ull << fs) - 1)) : this->words + q;
+  // Cursors are absolute bit addresses (byte address x 8 + bit), so a
+  // vertex's cursor points into its fragment's slot or into the host copy
+  // and a record read needs no table lookup.  Device and host-mapped
+  // addresses stay below 2^61, and a slot starts 16-byte aligned, so a
+  // record's bit within its word is the same in both.
+  __device__ __forceinline__ uint64_t cur(uint64_t e) const {
+    return ((uint64_t)reinterpret_cast<uintptr_t>(this->words) << 3) + e * this->bpe;
+  }
+  // The cursor of edge index e for a vertex whose records in this tile are
+  // [first, last]: into the slot when they all start in one fragment that
+  // has one, else into the host copy.
+  __device__ __forceinline__ uint64_t cur_range(uint64_t e, uint64_t first, uint64_t last) const {
+    const uint64_t f = (first * this->bpe) >> (5 + fs);
+    if (((last * this->bpe) >> (5 + fs)) == f) {
+      const int32_t s = __ldg(slot_of + f);
+      if (s >= 0) {
+        const uint32_t *base = slots + (uint64_t)s * ((1ull << fs) + kFragPad);
+        return ((uint64_t)reinterpret_cast<uintptr_t>(base) << 3) - (f << (5 + fs)) + e * this->bpe;
+      }
+    }
+    return cur(e);
   }
   __device__ __forceinline__ Item at(uint64_t c, uint32_t x) const {
     const uint64_t b = c + x * this->bpe;
-    return this->decode(word_ptr(b >> 5), (uint32_t)b & 31u);
+    return this->decode(reinterpret_cast<const uint32_t *>((uintptr_t)((b >> 5) << 2)), (uint32_t)b & 31u);
   }
-  // cnt records from edge index e on: one visit count per fragment they start in.
+  // cnt records from edge index e on: one visit count per fragment they start
+  // in; a range over two fragments was read from the host copy, and its
+  // records in fragments that have a slot are counted in *miss as well.
   __device__ __forceinline__ void note(uint64_t e, uint32_t cnt) const {
     uint64_t b = e * this->bpe;
+    const bool split = (b >> (5 + fs)) != (((e + cnt - 1) * this->bpe) >> (5 + fs));
     while (cnt) {
       const uint64_t f = b >> (5 + fs);
-      const uint32_t left = (uint32_t)(((f + 1) << (5 + fs)) - b);  // bits to the next fragment, < 2^25
+      const uint32_t left = (uint32_t)(((f + 1) << (5 + fs)) - b);  // bits to the next fragment, < 2^26
       const uint32_t n = min(cnt, (left + this->bpe - 1) / this->bpe);
       atomicAdd(visits + f, n);
+      if (split && __ldg(slot_of + f) >= 0) atomicAdd(miss, (unsigned long long)n);
       cnt -= n;
       b += (uint64_t)n * this->bpe;
     }
@@ -591,8 +615,10 @@ struct PrShared {
 //                   (an array parallel to the compacted list) instead of
 //                   src_val(v);
 //  probe_v(e, val)  the probe also sees the source value;
-// and a source hook:
-//  note(e, n)       the tile lists n records from edge index e on (SrcF).
+// and source hooks (SrcF):
+//  cur_range(e, first, last)  the cursor of a vertex whose records in the
+//                             tile are [first, last];
+//  note(e, n)                 the tile lists n records from edge index e on.
 template <class T, class = void>
 struct HasListVal : std::false_type {};
 template <class T>
@@ -601,6 +627,10 @@ template <class T, class = void>
 struct HasNote : std::false_type {};
 template <class T>
 struct HasNote<T, std::void_t<decltype(&T::note)>> : std::true_type {};
+template <class T, class = void>
+struct HasCurRange : std::false_type {};
+template <class T>
+struct HasCurRange<T, std::void_t<decltype(&T::cur_range)>> : std::true_type {};
 template <class T, class = void>
 struct HasProbeVal : std::false_type {};
 template <class T>
@@ -663,12 +693,26 @@ __device__ __forceinline__ uint32_t lbs_setup(const LbsArgs &a, const Src &src, 
     const uint32_t r = p > pos0 ? (uint32_t)min(p - pos0, (uint64_t)kTile) : 0u;
     sh.rs[j] = r;
     const uint64_t e0 = (a.off ? a.off[v] - p : (0ull - a.stage_base)) + pos0;  // edge index of position 0
-    sh.cb[j] = src.cur(e0);
-    const uint64_t q1 = min(pn, pend);  // end of the vertex's positions in this tile
-    if (q1 > pos0 + r) {
-      const uint64_t first = e0 + r, last = e0 + (q1 - pos0) - 1;
-      if (pn < p || last < first || last >= a.edge_bound) bad = true;
-      else if constexpr (HasNote<Src>::value) src.note(first, (uint32_t)(last - first + 1));
+    if constexpr (HasCurRange<Src>::value) {
+      uint64_t cb = src.cur(e0);
+      const uint64_t q1 = min(pn, pend);  // end of the vertex's positions in this tile
+      if (q1 > pos0 + r) {
+        const uint64_t first = e0 + r, last = e0 + (q1 - pos0) - 1;
+        if (pn < p || last < first || last >= a.edge_bound) {
+          bad = true;
+        } else {
+          cb = src.cur_range(e0, first, last);
+          if constexpr (HasNote<Src>::value) src.note(first, (uint32_t)(last - first + 1));
+        }
+      }
+      sh.cb[j] = cb;
+    } else {
+      sh.cb[j] = src.cur(e0);
+      const uint64_t q1 = min(pn, pend);  // end of the vertex's positions in this tile
+      if (q1 > pos0 + r) {
+        const uint64_t first = e0 + r, last = e0 + (q1 - pos0) - 1;
+        if (pn < p || last < first || last >= a.edge_bound) bad = true;
+      }
     }
     if constexpr (HasListVal<Op>::value) sh.val[j] = op.list_val(v, a.list + i);
     else if constexpr (kNeedVal) sh.val[j] = op.src_val(v);
