@@ -229,9 +229,9 @@ typedef struct og_config {
  * bytes become slots for fragments of the dynamic region (the packed record
  * stream cut into fragments of OG_PARAM_FRAGMENT_WORDS words), first filled
  * with the fragments that follow the static prefix.  The relax counts the
- * records it lists per fragment; between rounds, once an eighth of the
- * slots' records have been listed since the last step and at the end of
- * every query, the host replaces slots whose fragments were read least with
+ * records it lists per fragment; between rounds, once as many records as the
+ * slots hold have been listed since the last step and at the end of every
+ * query, the host replaces slots whose fragments were read least with
  * the most-read fragments that have none, copying at most a quarter of the
  * host-link bytes read since the last step, and a slot holds its fragment
  * across rounds and queries.  Reads of a fragment with a

@@ -67,7 +67,7 @@ struct FragState {
   uint64_t dalloc_bytes = 0;
   bool broken = false;     // a layout failed: queries through the slots are refused
   uint64_t since = 0;      // dynamic records listed since the last policy step
-  uint64_t step_min = 0;   // records between policy steps (an eighth of the slots' records)
+  uint64_t step_min = 0;   // records between policy steps (as many as the slots hold)
   og_fragment_stats st{};
 };
 
@@ -342,7 +342,7 @@ int frag_layout(og_engine *e, uint32_t fs) {
   F.owner.assign(F.nslots, 0xffffffffu);
   F.score.assign(F.nfrag, 0.0f);
   F.since = 0;
-  F.step_min = (uint64_t)((double)F.nslots * (double)(1ull << fs) * 32.0 / e->bpe / 8.0);
+  F.step_min = (uint64_t)((double)F.nslots * (double)(1ull << fs) * 32.0 / e->bpe);
   F.st = og_fragment_stats{};
   F.st.fragments = F.nfrag;
   F.st.slots = F.nslots;
@@ -393,8 +393,8 @@ int frag_reset(og_engine *e) {
   return OG_OK;
 }
 
-// After a compaction (the previous round's relax has finished), once an
-// eighth of the slots' records have been listed since the last step or when
+// After a compaction (the previous round's relax has finished), once as many
+// records as the slots hold have been listed since the last step, or when
 // `force` (a compaction that lists nothing, e.g. the query's last): reads
 // the visit counts, moves the records served from slots out of the
 // host-link bytes, and replaces slots.  Ascetic's rule: fragments read in
@@ -712,6 +712,11 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
                           cudaFuncAttributePreferredSharedMemoryCarveout, 58));
   CK(cudaFuncSetAttribute(k_lbs_pair_dev<SrcP<true>, SrcP<true>, MinOp<true>>,
                           cudaFuncAttributePreferredSharedMemoryCarveout, 58));
+  if (cfg->flags & OG_CFG_REPLACE) {  // the same relax reading fragment slots
+    CK(cudaFuncSetAttribute(k_lbs_pair<SrcP<true>, SrcF<true>, MinOp<true>>,
+                            cudaFuncAttributePreferredSharedMemoryCarveout, 58));
+    CK(cudaFuncSetAttribute(k_lbs<SrcF<true>, MinOp<true>>, cudaFuncAttributePreferredSharedMemoryCarveout, 58));
+  }
   // Same for the PageRank pull (29 KB tiles: 4 CTAs per SM at 58 %).  R-MAT 26
   // directed: 58.5 iterations/s with the CUDA driver's choice, 69.6 at 58 %,
   // 68.4 at 44 %, 63.2 at 30 %, 34.0 at 86 %.
