@@ -595,15 +595,17 @@ def run_bfs_batch(args, rank, world, local):
     g, gen_s = make_graph(args.scale)
     deg = g.degrees()
     srcs = np.array(pick_sources(deg, 256), np.uint32)
+    # page-locked result buffers for the end-to-end legs (43 GB at R-MAT 27)
+    # and the link probe come first, before the engine page-locks the graph
+    # and before any query: large page-locked allocations between queries
+    # have slowed the queries after them
+    host32 = og.pinned_empty((64, g.V), np.uint32)
+    host8 = og.pinned_empty((64, g.V), np.uint8)
+    h2d = h2d_peak_gbs()
     eng = og.Engine(g, budget=int(args.budget_gib * GIB), advisek=args.advisek, batch=True,
                     direct=True, device=local)
     tune = eng.bfs_batch_tune(srcs[:64], reps=1) if args.tune else None
     batches = [srcs[64 * i:64 * (i + 1)] for i in range(4)]
-    h2d = h2d_peak_gbs()
-    # page-locked result buffers for the end-to-end legs, allocated before the
-    # warm-up (large page-locked allocations between queries slow the next ones)
-    host32 = og.pinned_empty((64, g.V), np.uint32)
-    host8 = og.pinned_empty((64, g.V), np.uint8)
     for i in range(args.warmup):
         eng.bfs_batch(batches[i % 4], out=False)
     sampler = ClockSampler(local)
