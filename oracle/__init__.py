@@ -1,8 +1,8 @@
 """ctypes binding of the CPU oracle (og_oracle.c) — test infrastructure only.
 
 Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg import
-this package, and only as the checker or the timed CPU baseline; libog.so
-never calls it.
+this package, and only as the oracle that results are compared with or as
+the timed CPU baseline; libog.so never calls it.
 """
 from __future__ import annotations
 

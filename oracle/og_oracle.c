@@ -1,6 +1,7 @@
 /*
  * og_oracle.c — CPU restatement of OneGraph's BFS / SSSP / CC / PageRank
- * (test infrastructure only: the checker for libog.so, never the product).
+ * (test infrastructure only: the oracle libog.so's results are compared
+ * with, never the product).
  * Each function cites the reference lines it restates; declarations and the
  * parity pins are described in og_oracle.h.
  *

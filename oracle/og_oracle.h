@@ -1,7 +1,7 @@
 /*
  * og_oracle.h — CPU restatement of OneGraph's BFS / SSSP / CC / PageRank paths.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker that the CUDA engine
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle that the CUDA engine
  * (libog.so) is compared against; it is never linked into the product.  Only
  * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg load it.
  *

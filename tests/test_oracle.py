@@ -164,7 +164,7 @@ def test_path_certificate_accepts_exact_and_rejects_planted_errors():
 
 
 def test_union_find_components_match_reference_serial_cc(golden):
-    """ora_cc_uf_mt (the full-size CC checker) gives CC/serial's labels on
+    """ora_cc_uf_mt (the full-size CC oracle) gives CC/serial's labels on
     every symmetric golden graph, on 1 and 8 threads."""
     for n in golden_names(golden, "cc"):
         off = np.ascontiguousarray(golden[n + "/off"], np.uint64)
