@@ -667,22 +667,12 @@ int create(og_graph *g, const og_config *cfg, og_engine *e) {
   RC(plan_compute(g->V, g->E, g->off, g->kind, cfg->budget_bytes, cfg->advisek, cfg->flags, &e->plan,
                   g->bpe, 4 + g->wbytes));
   if (cfg->flags & OG_CFG_REPLACE) {
-    // half of the static prefix's bytes become fragment slots: the prefix
-    // shrinks to the largest vertex prefix within half of its edges
-    if (!(cfg->flags & OG_CFG_DIRECT) || (cfg->flags & (OG_CFG_NO_PIN | OG_CFG_NO_STATIC)))
-      return fail(OG_E_ARG, "OG_CFG_REPLACE needs OG_CFG_DIRECT, a page-locked host copy and a static region");
-    og_plan &Q = e->plan;
-    if (Q.static_edges == 0 || Q.dynamic_edges == 0)
-      return fail(OG_E_BUDGET, "OG_CFG_REPLACE: the plan has no %s region to share",
-                  Q.static_edges == 0 ? "static" : "dynamic");
-    const uint64_t old_words = g->packed_words_for(Q.static_edges);
-    const uint64_t half = Q.static_edges / 2;
-    const uint32_t vs = (uint32_t)(std::upper_bound(g->off, g->off + (uint64_t)g->V + 1, half) - g->off - 1);
-    Q.static_vertices = vs;
-    Q.static_edges = g->off[vs];
-    Q.dynamic_edges = g->E - Q.static_edges;
+    // half of the static prefix's bytes become fragment slots (the same split
+    // og_graph_plan reports)
+    uint64_t slot_bytes = 0;
+    RC(plan_replace_split(g, cfg->flags, &e->plan, &slot_bytes));
     e->frag = new FragState;
-    e->frag->bytes = 4 * (old_words - (Q.static_edges ? g->packed_words_for(Q.static_edges) : 0));
+    e->frag->bytes = slot_bytes;
   }
   const og_plan &P = e->plan;
   size_t free_b = 0, total_b = 0;

@@ -645,11 +645,32 @@ extern "C" int og_plan_compute(uint64_t V, uint64_t E, const uint64_t *offsets, 
                       w ? 8 : 4);
 }
 
+int og::plan_replace_split(const og_graph *g, uint32_t flags, og_plan *p, uint64_t *slot_bytes) {
+  if (!(flags & OG_CFG_DIRECT) || (flags & (OG_CFG_NO_PIN | OG_CFG_NO_STATIC)))
+    return fail(OG_E_ARG, "OG_CFG_REPLACE needs OG_CFG_DIRECT, a page-locked host copy and a static region");
+  if (p->static_edges == 0 || p->dynamic_edges == 0)
+    return fail(OG_E_BUDGET, "OG_CFG_REPLACE: the plan has no %s region to share",
+                p->static_edges == 0 ? "static" : "dynamic");
+  const uint64_t old_words = g->packed_words_for(p->static_edges);
+  const uint64_t half = p->static_edges / 2;
+  const uint32_t vs = (uint32_t)(std::upper_bound(g->off, g->off + (uint64_t)g->V + 1, half) - g->off - 1);
+  p->static_vertices = vs;
+  p->static_edges = g->off[vs];
+  p->dynamic_edges = g->E - p->static_edges;
+  *slot_bytes = 4 * (old_words - (p->static_edges ? g->packed_words_for(p->static_edges) : 0));
+  return OG_OK;
+}
+
 extern "C" int og_graph_plan(og_graph *g, uint64_t budget_bytes, double advisek, uint32_t flags,
                              og_plan *out) {
   clear_error();
   if (!g) return fail(OG_E_ARG, "og_graph_plan: null graph");
   RC_HOST(graph_prepare(g));
-  return plan_compute(g->V, g->E, g->off, g->kind, budget_bytes, advisek, flags, out, g->bpe,
-                      4 + g->wbytes);
+  RC_HOST(plan_compute(g->V, g->E, g->off, g->kind, budget_bytes, advisek, flags, out, g->bpe,
+                       4 + g->wbytes));
+  if (flags & OG_CFG_REPLACE) {
+    uint64_t slot_bytes = 0;
+    RC_HOST(plan_replace_split(g, flags, out, &slot_bytes));
+  }
+  return OG_OK;
 }

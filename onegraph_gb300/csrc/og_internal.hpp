@@ -74,6 +74,13 @@ int plan_compute(uint32_t V, uint64_t E, const uint64_t *off, int kind,
                  uint64_t budget, double advisek, uint32_t flags, og_plan *out,
                  uint32_t edge_bits, uint32_t stage_bytes);
 
+// OG_CFG_REPLACE on a plan made by plan_compute: the static prefix shrinks to
+// the largest vertex prefix within half of its edges, and *slot_bytes gets
+// the device bytes that frees for fragment slots.  OG_E_ARG for flags the
+// mode cannot run with, OG_E_BUDGET for a plan without a static or a dynamic
+// region.
+int plan_replace_split(const og_graph *g, uint32_t flags, og_plan *p, uint64_t *slot_bytes);
+
 // Bits needed to hold values 0..x (0 for x == 0).
 inline uint32_t bits_for(uint64_t x) {
   uint32_t b = 0;

@@ -13,7 +13,9 @@ pytestmark = pytest.mark.gpu
 
 
 def budget_for(g, edge_slots, flags):
-    p = g.plan(budget=1 << 40, flags=flags)
+    # per-vertex and fixed bytes do not depend on the replacement mode (whose
+    # split needs a dynamic region, which a 1 TiB plan does not have)
+    p = g.plan(budget=1 << 40, flags=flags & ~og.CFG_REPLACE)
     return p["vertex_bytes"] + p["fixed_bytes"] + int(edge_slots) * p["stage_edge_bytes"]
 
 
@@ -27,8 +29,10 @@ def test_replace_results_equal_oracle(words):
     change between and within them."""
     g = og.Graph.rmat(12, 16, weighted=True)
     off, pairs, col = np.array(g.offsets), np.array(g.edges), np.array(g.columns)
-    e = og.Engine(g, budget=budget_for(g, int(0.4 * g.E), FLAGS), advisek=0.6, direct=True, replace=True)
+    b = budget_for(g, int(0.4 * g.E), FLAGS)
+    e = og.Engine(g, budget=b, advisek=0.6, direct=True, replace=True)
     assert 0 < e.plan["static_edges"] < g.E
+    assert e.plan == g.plan(budget=b, advisek=0.6, flags=FLAGS)  # the planner reports the same split
     e.set_param(og.PARAM_FRAGMENT_WORDS, words)
     assert e.get_param(og.PARAM_FRAGMENT_WORDS) == words
     fs = e.fragment_stats()

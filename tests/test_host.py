@@ -325,6 +325,31 @@ def test_graph_plan_uses_packed_width():
     assert u.plan(budget=1 << 40)["edge_bits"] == 10
 
 
+def test_graph_plan_replace_split():
+    """OG_CFG_REPLACE: the static prefix becomes the largest vertex prefix
+    within half of the plain plan's static edges (the slots take the rest);
+    the mode needs direct mode and both regions."""
+    g = og.Graph.rmat(12, 16, weighted=True, seed=2)
+    off = np.array(g.offsets)
+    pg = g.plan(budget=1 << 40)
+    b = pg["vertex_bytes"] + pg["fixed_bytes"] + int(0.4 * g.E * pg["edge_bits"] / 8)
+    plain = g.plan(budget=b, advisek=0.6, flags=og.CFG_DIRECT)
+    rep = g.plan(budget=b, advisek=0.6, flags=og.CFG_DIRECT | og.CFG_REPLACE)
+    assert 0 < plain["static_edges"] < g.E
+    vs = int(np.searchsorted(off, plain["static_edges"] // 2, side="right")) - 1
+    assert rep["static_vertices"] == vs
+    assert rep["static_edges"] == int(off[vs]) <= plain["static_edges"] // 2
+    assert rep["dynamic_edges"] == g.E - rep["static_edges"]
+    for k in ("budget_bytes", "vertex_bytes", "fixed_bytes", "edge_capacity", "edge_bits"):
+        assert rep[k] == plain[k], k
+    with pytest.raises(og.OGError) as ex:  # staged mode
+        g.plan(budget=b, advisek=0.6, flags=og.CFG_REPLACE)
+    assert ex.value.status == 1
+    with pytest.raises(og.OGError) as ex:  # fully resident: no dynamic region
+        g.plan(budget=1 << 40, advisek=1.0, flags=og.CFG_DIRECT | og.CFG_REPLACE)
+    assert ex.value.status == 4
+
+
 def test_graph_plan_staged_budget():
     """Staged mode: static records + two staging buffers of unpacked edges fit
     the budget's edge share."""
