@@ -180,7 +180,8 @@ int og_plan_compute(uint64_t V, uint64_t E, const uint64_t *offsets, int kind,
  * [1, 64]) in the page-locked host copy and the static region; staging
  * buffers hold unpacked edges (u32 column + 1, 2 or 4 weight bytes).
  * og_plan_compute, which has no graph, charges the reference's sizeof(Edge)
- * (4 or 8 bytes) per edge. */
+ * (4 or 8 bytes) per edge.  With OG_CFG_REPLACE in flags the plan is the one
+ * such an engine runs: the static prefix halved as described there. */
 int og_graph_plan(og_graph *g, uint64_t budget_bytes, double advisek, uint32_t flags,
                   og_plan *out);
 
