@@ -70,3 +70,23 @@ def test_help_lists_workloads():
     assert out.returncode == 0
     for w in ("sssp-oom", "cc-oom", "bfs-batch", "bfs-resident", "pr-precision", "serving"):
         assert w in out.stdout
+
+
+def test_config_legs_parse():
+    """Every configuration the default line runs after the serving passes is
+    a valid bench.py command line (a renamed workload would drop a leg)."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    keys = set()
+    for key, argv in bench.CONFIG_LEGS:
+        old = sys.argv
+        try:
+            sys.argv = ["bench.py", *argv, "--warmup", "3", "--configs", "none"]
+            a = bench.parse_args()
+        finally:
+            sys.argv = old
+        assert a.workload == key and a.warmup == 3 and a.configs == "none"
+        keys.add(key)
+    assert keys == {"bfs-resident", "sssp-oom", "cc-oom", "pr-precision", "bfs-batch"}
